@@ -1,0 +1,107 @@
+"""ctypes binding of libafqmc_gb300.so, the C ABI declared in include/afqmc_gb300.h.
+
+The shared library is the product: there is no CPU or PyTorch fallback. Loading fails
+loudly when the library has not been built (``python -c "import __graft_entry__ as g;
+g.build()"``) or when no CUDA device is present at call time.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libafqmc_gb300.so")
+
+AFQ_WALKERS_RESTRICTED, AFQ_WALKERS_UNRESTRICTED = 0, 1
+AFQ_TRIAL_RHF, AFQ_TRIAL_UHF = 0, 1
+AFQ_PREC_FP64, AFQ_PREC_MIXED = 0, 1
+AFQ_S_E_ESTIMATE, AFQ_S_POP_CONTROL_SHIFT, AFQ_S_N_KILLED = 0, 1, 2
+AFQ_S_BLOCK_ENERGY, AFQ_S_BLOCK_WEIGHT, AFQ_S_STATUS = 3, 4, 5
+AFQ_NSCALARS = 8
+
+_vp = ctypes.c_void_p
+
+
+class Dims(ctypes.Structure):
+    _fields_ = [
+        ("norb", ctypes.c_int32), ("n_up", ctypes.c_int32), ("n_dn", ctypes.c_int32),
+        ("nchol", ctypes.c_int32), ("n_walkers", ctypes.c_int32),
+        ("walker_type", ctypes.c_int32), ("trial_type", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("n_exp_terms", ctypes.c_int32),
+        ("n_batch", ctypes.c_int32), ("dt", ctypes.c_double),
+    ]
+
+
+class Hamiltonian(ctypes.Structure):
+    _fields_ = [
+        ("h0", ctypes.c_double), ("h0_prop_re", ctypes.c_double), ("h0_prop_im", ctypes.c_double),
+        ("trial_up", _vp), ("trial_dn", _vp), ("chol", _vp),
+        ("rot_chol_up", _vp), ("rot_chol_dn", _vp), ("rot_h1_up", _vp), ("rot_h1_dn", _vp),
+        ("exp_h1_up", _vp), ("exp_h1_dn", _vp), ("mf_shifts", _vp),
+    ]
+
+
+class WalkerState(ctypes.Structure):
+    _fields_ = [("walkers_up", _vp), ("walkers_dn", _vp), ("weights", _vp),
+                ("overlaps", _vp), ("scalars", _vp)]
+
+
+_SIGS = {
+    "afq_abi_version": (ctypes.c_int, []),
+    "afq_last_error": (ctypes.c_char_p, []),
+    "afq_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(Dims)]),
+    "afq_ctx_create": (ctypes.c_int, [ctypes.POINTER(Dims), ctypes.POINTER(Hamiltonian), _vp,
+                                      ctypes.c_size_t, _vp, ctypes.POINTER(_vp)]),
+    "afq_ctx_destroy": (None, [_vp]),
+    "afq_calc_overlap": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "afq_calc_force_bias": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "afq_calc_energy": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "afq_propagate": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp]),
+    "afq_orthonormalize_walkers": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp]),
+    "afq_stochastic_reconfiguration": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp]),
+    "afq_propagate_phaseless": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp,
+                                               ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                               _vp, _vp, _vp, _vp]),
+    "afq_block_end": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp]),
+    "afq_fill_normal": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, _vp]),
+    "afq_fill_uniform": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, _vp]),
+}
+
+EXPORTED = tuple(_SIGS)
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+class AfqError(RuntimeError):
+    pass
+
+
+def load(path: Optional[str] = None) -> ctypes.CDLL:
+    """Load (once) and return the library; raises AfqError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise AfqError(
+            f"{path} not found: build it with `python -c \"import __graft_entry__ as g; g.build()\"`"
+        )
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = load().afq_last_error().decode(errors="replace")
+        raise AfqError(f"{what} failed (rc={rc}): {msg}")
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args), name)

@@ -1,0 +1,449 @@
+// C ABI of the AFQMC hot path: context creation, workspace layout and the stream-ordered
+// orchestration of the kernels (one propagation step, QR, SR, measurements, and the
+// sampler's block loop). See include/afqmc_gb300.h for the contract of each entry point.
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "afq_common.cuh"
+#include "afq_kernels.cuh"
+#include "afq_tc.cuh"
+
+static thread_local char g_err[512] = "";
+
+void afq_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+struct afq_ctx {
+  afq_dims d;
+  afq_hamiltonian h;
+  afq_ctx_dev dev;
+  int nw_chunk;
+  int e_chunks, e_gchunk;
+  size_t welem;  // bytes per walker element (16 complex128, 8 complex64)
+  // workspace views
+  char* ws;
+  size_t ws_bytes;
+  double2* green;
+  double2* fb;
+  double2* xt;
+  double2* shift;
+  double2* fbt;
+  double2* vhs;
+  double2* ovl_new;
+  double2* ene;
+  double2* epart;
+  double* rccat;
+  void* wcopy;
+  int32_t* sr_idx;
+  double* cum;
+  afq::TcState tc;  // tensor-core (mixed precision) operands and plans
+};
+
+namespace {
+
+struct Layout {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  }
+};
+
+struct Sizes {
+  size_t green, fb, xt, shift, fbt, vhs, ovl_new, ene, epart, rccat, wcopy, sr_idx, cum, tc, total;
+};
+
+int derive(const afq_dims* d, afq_ctx_dev* c, int* nw_chunk, int* e_chunks, int* e_gchunk,
+           size_t* welem) {
+  if (!d) { afq_set_error("dims is NULL"); return -1; }
+  if (d->norb < 1 || d->n_up < 1 || d->n_dn < 0 || d->nchol < 1 || d->n_walkers < 1) {
+    afq_set_error("bad sizes norb=%d n_up=%d n_dn=%d nchol=%d n_walkers=%d", d->norb, d->n_up,
+                  d->n_dn, d->nchol, d->n_walkers);
+    return -1;
+  }
+  if (d->n_up > d->norb || d->n_dn > d->norb) { afq_set_error("more electrons than orbitals"); return -1; }
+  if (d->precision != AFQ_PREC_FP64 && d->precision != AFQ_PREC_MIXED) {
+    afq_set_error("unknown precision %d", d->precision); return -1;
+  }
+  if (d->walker_type != AFQ_WALKERS_RESTRICTED && d->walker_type != AFQ_WALKERS_UNRESTRICTED) {
+    afq_set_error("unknown walker_type %d", d->walker_type); return -1;
+  }
+  if (d->trial_type != AFQ_TRIAL_RHF && d->trial_type != AFQ_TRIAL_UHF) {
+    afq_set_error("unknown trial_type %d", d->trial_type); return -1;
+  }
+  if (d->trial_type == AFQ_TRIAL_RHF && d->n_up != d->n_dn) {
+    afq_set_error("RHF requires equal number of up and down electrons"); return -1;
+  }
+  if (d->walker_type == AFQ_WALKERS_RESTRICTED && d->trial_type != AFQ_TRIAL_RHF) {
+    afq_set_error("restricted walkers are supported with the RHF trial only"); return -1;
+  }
+  if (d->walker_type == AFQ_WALKERS_UNRESTRICTED && d->n_dn < 1) {
+    afq_set_error("unrestricted walkers need n_dn >= 1"); return -1;
+  }
+  if (d->n_exp_terms < 1 || d->n_exp_terms > 32) { afq_set_error("n_exp_terms out of range"); return -1; }
+  if (!(d->dt > 0.0)) { afq_set_error("dt must be positive"); return -1; }
+  int nb = d->n_batch < 1 ? 1 : d->n_batch;
+  if (d->n_walkers % nb != 0) { afq_set_error("n_batch must divide n_walkers"); return -1; }
+  memset(c, 0, sizeof(*c));
+  c->norb = d->norb;
+  c->nchol = d->nchol;
+  c->nw = d->n_walkers;
+  c->n_exp_terms = d->n_exp_terms;
+  c->dt = d->dt;
+  if (d->walker_type == AFQ_WALKERS_RESTRICTED) {
+    c->nslab = 1;
+    c->kslab[0] = c->nocc_slab[0] = d->n_up;
+    c->restricted_square = 1;
+  } else {
+    c->nslab = 2;
+    c->kslab[0] = c->nocc_slab[0] = d->n_up;
+    c->kslab[1] = c->nocc_slab[1] = d->n_dn;
+  }
+  c->kmax = c->kslab[0] > c->kslab[1] ? c->kslab[0] : c->kslab[1];
+  if (d->trial_type == AFQ_TRIAL_RHF) {
+    c->nspin_g = 1;
+    c->gocc[0] = d->n_up;
+    c->ktot = d->n_up * d->norb;
+    c->energy_mode = (c->nslab == 1) ? 0 : 1;
+  } else {
+    c->nspin_g = 2;
+    c->gocc[0] = d->n_up;
+    c->gocc[1] = d->n_dn;
+    c->ktot = (d->n_up + d->n_dn) * d->norb;
+    c->energy_mode = 2;
+  }
+  // kernel resource limits
+  if (c->kmax > 64) { afq_set_error("at most 64 electrons per spin are supported"); return -1; }
+  if ((size_t)d->norb * c->kmax > 7000) { afq_set_error("norb * nocc too large (<= 7000)"); return -1; }
+  *nw_chunk = d->n_walkers / nb;
+  *e_gchunk = 16;
+  *e_chunks = (d->nchol + *e_gchunk - 1) / *e_gchunk;
+  *welem = d->precision == AFQ_PREC_FP64 ? 16 : 8;
+  return 0;
+}
+
+Sizes sizes_for(const afq_dims* d, const afq_ctx_dev& c, int nw_chunk, int e_chunks, size_t welem,
+                Layout* L) {
+  Sizes s;
+  const size_t nw = c.nw, C16 = sizeof(double2);
+  s.green = L->take(nw * c.ktot * C16);
+  s.fb = L->take(nw * c.nchol * C16);
+  s.xt = L->take(nw * c.nchol * C16);
+  s.shift = L->take(nw * C16);
+  s.fbt = L->take(nw * C16);
+  s.vhs = L->take(d->precision == AFQ_PREC_FP64 ? (size_t)nw_chunk * c.norb * c.norb * C16 : 256);
+  s.ovl_new = L->take(nw * C16);
+  s.ene = L->take(nw * C16);
+  s.epart = L->take(nw * e_chunks * 5 * C16);
+  s.rccat = L->take(c.nspin_g == 2 ? (size_t)c.nchol * c.ktot * sizeof(double) : 256);
+  s.wcopy = L->take(nw * c.norb * (c.kslab[0] + c.kslab[1]) * welem);
+  s.sr_idx = L->take(nw * sizeof(int32_t));
+  s.cum = L->take(nw * sizeof(double));
+  s.tc = L->take(d->precision == AFQ_PREC_MIXED ? afq::tc_workspace_bytes(c, nw_chunk) : 256);
+  s.total = L->off;
+  return s;
+}
+
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define CHECK(x)            \
+  do {                      \
+    int _e = (x);           \
+    if (_e) return _e;      \
+  } while (0)
+
+bool is_fp64(const afq_ctx* c) { return c->d.precision == AFQ_PREC_FP64; }
+
+int green(afq_ctx* c, const void* wu, const void* wd, double2* g, double2* ovl, bool wg, cudaStream_t st) {
+  if (is_fp64(c)) return afq::launch_green<double>(c->dev, wu, wd, g, ovl, wg, st);
+  return afq::launch_green<float>(c->dev, wu, wd, g, ovl, wg, st);
+}
+
+int force_bias_from_green(afq_ctx* c, double2* out, cudaStream_t st) {
+  const afq_ctx_dev& d = c->dev;
+  double2 alpha = c2(d.energy_mode == 0 ? 2.0 : 1.0, 0.0);
+  const double* B = d.nspin_g == 2 ? c->rccat : d.rot_chol[0];
+  if (!is_fp64(c)) return afq::tc_force_bias(c->tc, d, c->green, out, alpha.x, st);
+  return afq::launch_gemm_cr(false, d.nw, d.nchol, d.ktot, c->green, d.ktot, B, d.ktot, out, d.nchol,
+                             alpha, st);
+}
+
+int energy_from_green(afq_ctx* c, double2* out, cudaStream_t st) {
+  if (!is_fp64(c)) return afq::tc_energy(c->tc, c->dev, c->green, c->epart, out, st);
+  return afq::launch_energy_f64(c->dev, c->e_chunks, c->e_gchunk, c->green, c->epart, out, st);
+}
+
+int check_walkers(const afq_ctx* c, const void* wu, const void* wd) {
+  if (!wu) { afq_set_error("walkers_up is NULL"); return -1; }
+  if (c->dev.nslab == 2 && !wd) { afq_set_error("unrestricted walkers need walkers_dn"); return -1; }
+  return 0;
+}
+
+int check_state(const afq_ctx* c, const afq_walker_state* s) {
+  if (!s) { afq_set_error("state is NULL"); return -1; }
+  CHECK(check_walkers(c, s->walkers_up, s->walkers_dn));
+  if (!s->weights || !s->overlaps || !s->scalars) { afq_set_error("state has NULL arrays"); return -1; }
+  return 0;
+}
+
+int propagate_impl(afq_ctx* c, afq_walker_state* s, const double* fields, cudaStream_t st) {
+  const afq_ctx_dev& d = c->dev;
+  CHECK(green(c, s->walkers_up, s->walkers_dn, c->green, nullptr, true, st));
+  CHECK(force_bias_from_green(c, c->fb, st));
+  CHECK(afq::launch_field_shifts(d, fields, c->fb, c->xt, c->shift, c->fbt, st));
+  const int nb = d.nw / c->nw_chunk;
+  for (int b = 0; b < nb; ++b) {
+    const int w0 = b * c->nw_chunk;
+    if (is_fp64(c)) {
+      double sq = sqrt(d.dt);
+      CHECK(afq::launch_gemm_cr(true, c->nw_chunk, d.norb * d.norb, d.nchol, c->xt + (size_t)w0 * d.nchol,
+                                d.nchol, c->h.chol, (long)d.norb * d.norb, c->vhs, (long)d.norb * d.norb,
+                                c2(0.0, sq), st));
+      CHECK(afq::launch_taylor_f64<double>(d, w0, c->nw_chunk, c->vhs, s->walkers_up, s->walkers_dn, st));
+    } else {
+      CHECK(afq::tc_propagate_chunk(c->tc, d, w0, c->nw_chunk, c->xt, s->walkers_up, s->walkers_dn, st));
+    }
+  }
+  CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, c->ovl_new, false, st));
+  return afq::launch_weights(d, c->shift, c->fbt, c->ovl_new, reinterpret_cast<double2*>(s->overlaps),
+                             s->weights, s->scalars, st);
+}
+
+int qr_impl(afq_ctx* c, afq_walker_state* s, cudaStream_t st) {
+  if (is_fp64(c)) return afq::launch_qr<double>(c->dev, s->walkers_up, s->walkers_dn, st);
+  return afq::tc_orthonormalize(c->tc, c->dev, s->walkers_up, s->walkers_dn, st);
+}
+
+int sr_impl(afq_ctx* c, afq_walker_state* s, const double* zeta, int32_t* indices, cudaStream_t st) {
+  if (is_fp64(c))
+    CHECK(afq::launch_sr<double>(c->dev, zeta, s->weights, c->cum, c->sr_idx, s->walkers_up,
+                                 s->walkers_dn, c->wcopy, st));
+  else
+    CHECK(afq::launch_sr<float>(c->dev, zeta, s->weights, c->cum, c->sr_idx, s->walkers_up,
+                                s->walkers_dn, c->wcopy, st));
+  if (indices) {
+    cudaError_t e = cudaMemcpyAsync(indices, c->sr_idx, sizeof(int32_t) * c->dev.nw,
+                                    cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) { afq_set_error("sr index copy: %s", cudaGetErrorString(e)); return (int)e; }
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int afq_abi_version(void) { return AFQ_ABI_VERSION; }
+
+const char* afq_last_error(void) { return g_err; }
+
+size_t afq_workspace_size(const afq_dims* dims) {
+  afq_ctx_dev c;
+  int nwc, ec, eg;
+  size_t we;
+  if (derive(dims, &c, &nwc, &ec, &eg, &we)) return 0;
+  Layout L;
+  return sizes_for(dims, c, nwc, ec, we, &L).total;
+}
+
+int afq_ctx_create(const afq_dims* dims, const afq_hamiltonian* ham, void* workspace,
+                   size_t workspace_bytes, void* stream, afq_ctx** out) {
+  if (!out) { afq_set_error("out is NULL"); return -1; }
+  *out = nullptr;
+  afq_ctx_dev dev;
+  int nwc, ec, eg;
+  size_t we;
+  CHECK(derive(dims, &dev, &nwc, &ec, &eg, &we));
+  if (!ham) { afq_set_error("hamiltonian is NULL"); return -1; }
+  const bool uhf = dims->trial_type == AFQ_TRIAL_UHF;
+  const bool unres = dims->walker_type == AFQ_WALKERS_UNRESTRICTED;
+  if (!ham->trial_up || !ham->chol || !ham->rot_chol_up || !ham->rot_h1_up || !ham->exp_h1_up ||
+      !ham->mf_shifts || (uhf && (!ham->trial_dn || !ham->rot_chol_dn || !ham->rot_h1_dn)) ||
+      (unres && !ham->exp_h1_dn)) {
+    afq_set_error("hamiltonian has NULL arrays");
+    return -1;
+  }
+  Layout L;
+  Sizes sz = sizes_for(dims, dev, nwc, ec, we, &L);
+  if (!workspace || workspace_bytes < sz.total) {
+    afq_set_error("workspace too small: need %zu bytes, got %zu", sz.total, workspace_bytes);
+    return -1;
+  }
+  if (reinterpret_cast<uintptr_t>(workspace) & 255) { afq_set_error("workspace must be 256-byte aligned"); return -1; }
+  afq_ctx* c = new (std::nothrow) afq_ctx();
+  if (!c) { afq_set_error("out of host memory"); return -1; }
+  c->d = *dims;
+  if (c->d.n_batch < 1) c->d.n_batch = 1;
+  c->h = *ham;
+  c->nw_chunk = nwc;
+  c->e_chunks = ec;
+  c->e_gchunk = eg;
+  c->welem = we;
+  dev.h0 = ham->h0;
+  dev.h0_prop_re = ham->h0_prop_re;
+  dev.h0_prop_im = ham->h0_prop_im;
+  dev.trial[0] = ham->trial_up;
+  dev.trial[1] = uhf ? ham->trial_dn : ham->trial_up;
+  dev.exp_h1[0] = ham->exp_h1_up;
+  dev.exp_h1[1] = unres ? ham->exp_h1_dn : ham->exp_h1_up;
+  dev.rot_chol[0] = ham->rot_chol_up;
+  dev.rot_chol[1] = uhf ? ham->rot_chol_dn : ham->rot_chol_up;
+  dev.rot_h1[0] = ham->rot_h1_up;
+  dev.rot_h1[1] = uhf ? ham->rot_h1_dn : ham->rot_h1_up;
+  dev.mf = reinterpret_cast<const double2*>(ham->mf_shifts);
+  c->dev = dev;
+  char* ws = static_cast<char*>(workspace);
+  c->ws = ws;
+  c->ws_bytes = workspace_bytes;
+  c->green = reinterpret_cast<double2*>(ws + sz.green);
+  c->fb = reinterpret_cast<double2*>(ws + sz.fb);
+  c->xt = reinterpret_cast<double2*>(ws + sz.xt);
+  c->shift = reinterpret_cast<double2*>(ws + sz.shift);
+  c->fbt = reinterpret_cast<double2*>(ws + sz.fbt);
+  c->vhs = reinterpret_cast<double2*>(ws + sz.vhs);
+  c->ovl_new = reinterpret_cast<double2*>(ws + sz.ovl_new);
+  c->ene = reinterpret_cast<double2*>(ws + sz.ene);
+  c->epart = reinterpret_cast<double2*>(ws + sz.epart);
+  c->rccat = reinterpret_cast<double*>(ws + sz.rccat);
+  c->wcopy = ws + sz.wcopy;
+  c->sr_idx = reinterpret_cast<int32_t*>(ws + sz.sr_idx);
+  c->cum = reinterpret_cast<double*>(ws + sz.cum);
+  cudaStream_t st = S(stream);
+  if (uhf) {
+    // rccat[g] = [rot_chol_up[g] | rot_chol_dn[g]]
+    const size_t a = (size_t)dims->n_up * dims->norb, b = (size_t)dims->n_dn * dims->norb;
+    cudaError_t e = cudaMemcpy2DAsync(c->rccat, dev.ktot * sizeof(double), ham->rot_chol_up, a * sizeof(double),
+                                      a * sizeof(double), dims->nchol, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(c->rccat + a, dev.ktot * sizeof(double), ham->rot_chol_dn, b * sizeof(double),
+                            b * sizeof(double), dims->nchol, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+      afq_set_error("rot_chol concat: %s", cudaGetErrorString(e));
+      delete c;
+      return (int)e;
+    }
+  }
+  if (dims->precision == AFQ_PREC_MIXED) {
+    int e = afq::tc_init(&c->tc, c->dev, *ham, c->rccat, nwc, ws + sz.tc, st);
+    if (e) {
+      delete c;
+      return e;
+    }
+  }
+  *out = c;
+  return 0;
+}
+
+void afq_ctx_destroy(afq_ctx* ctx) { delete ctx; }
+
+int afq_calc_overlap(afq_ctx* ctx, const void* walkers_up, const void* walkers_dn, double* overlaps,
+                     void* stream) {
+  if (!ctx || !overlaps) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_walkers(ctx, walkers_up, walkers_dn));
+  return green(ctx, walkers_up, walkers_dn, nullptr, reinterpret_cast<double2*>(overlaps), false, S(stream));
+}
+
+int afq_calc_force_bias(afq_ctx* ctx, const void* walkers_up, const void* walkers_dn,
+                        double* force_bias, void* stream) {
+  if (!ctx || !force_bias) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_walkers(ctx, walkers_up, walkers_dn));
+  CHECK(green(ctx, walkers_up, walkers_dn, ctx->green, nullptr, true, S(stream)));
+  return force_bias_from_green(ctx, reinterpret_cast<double2*>(force_bias), S(stream));
+}
+
+int afq_calc_energy(afq_ctx* ctx, const void* walkers_up, const void* walkers_dn, double* energies,
+                    void* stream) {
+  if (!ctx || !energies) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_walkers(ctx, walkers_up, walkers_dn));
+  CHECK(green(ctx, walkers_up, walkers_dn, ctx->green, nullptr, true, S(stream)));
+  return energy_from_green(ctx, reinterpret_cast<double2*>(energies), S(stream));
+}
+
+int afq_propagate(afq_ctx* ctx, afq_walker_state* state, const double* fields, void* stream) {
+  if (!ctx || !fields) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_state(ctx, state));
+  return propagate_impl(ctx, state, fields, S(stream));
+}
+
+int afq_orthonormalize_walkers(afq_ctx* ctx, afq_walker_state* state, void* stream) {
+  if (!ctx) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_state(ctx, state));
+  return qr_impl(ctx, state, S(stream));
+}
+
+int afq_stochastic_reconfiguration(afq_ctx* ctx, afq_walker_state* state, const double* zeta,
+                                   int32_t* indices, void* stream) {
+  if (!ctx || !zeta) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_state(ctx, state));
+  return sr_impl(ctx, state, zeta, indices, S(stream));
+}
+
+int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double* fields,
+                            const double* zetas, int32_t n_prop_steps, int32_t n_ene_blocks,
+                            int32_t n_sr_blocks, double* block_energy, double* block_weight,
+                            double* energy, void* stream) {
+  if (!ctx || !fields || !zetas || !block_energy || !block_weight || !energy) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (n_prop_steps < 1 || n_ene_blocks < 1 || n_sr_blocks < 1) {
+    afq_set_error("block counts must be >= 1");
+    return -1;
+  }
+  CHECK(check_state(ctx, state));
+  cudaStream_t st = S(stream);
+  const afq_ctx_dev& d = ctx->dev;
+  double2* ovl = reinterpret_cast<double2*>(state->overlaps);
+  CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+  CHECK(afq::launch_phaseless_begin(state->scalars, st));
+  const size_t step_elems = (size_t)d.nw * d.nchol;
+  int blk = 0;
+  for (int sr = 0; sr < n_sr_blocks; ++sr) {
+    for (int eb = 0; eb < n_ene_blocks; ++eb, ++blk) {
+      for (int p = 0; p < n_prop_steps; ++p) {
+        const double* f = fields + ((size_t)blk * n_prop_steps + p) * step_elems;
+        CHECK(propagate_impl(ctx, state, f, st));
+      }
+      CHECK(qr_impl(ctx, state, st));
+      CHECK(green(ctx, state->walkers_up, state->walkers_dn, ctx->green, ovl, true, st));
+      CHECK(energy_from_green(ctx, ctx->ene, st));
+      CHECK(afq::launch_block_stats(d, ctx->ene, state->weights, state->scalars, block_energy + blk,
+                                    block_weight + blk, st));
+    }
+    CHECK(sr_impl(ctx, state, zetas + sr, nullptr, st));
+    CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+  }
+  return afq::launch_phaseless_end(blk, (double)n_sr_blocks * n_ene_blocks * d.nw, block_energy,
+                                   block_weight, state->scalars, energy, st);
+}
+
+int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, const double* zeta,
+                  double* block_weight, void* stream) {
+  if (!ctx || !energy || !zeta || !block_weight) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_state(ctx, state));
+  cudaStream_t st = S(stream);
+  CHECK(afq::launch_driver_update(ctx->dev, state->weights, energy, state->scalars, block_weight, st));
+  CHECK(qr_impl(ctx, state, st));
+  return sr_impl(ctx, state, zeta, nullptr, st);
+}
+
+int afq_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream) {
+  if (!out && n > 0) { afq_set_error("NULL argument"); return -1; }
+  return afq::launch_fill_normal(out, n, seed, offset, S(stream));
+}
+
+int afq_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream) {
+  if (!out && n > 0) { afq_set_error("NULL argument"); return -1; }
+  return afq::launch_fill_uniform(out, n, seed, offset, S(stream));
+}
+
+}  // extern "C"

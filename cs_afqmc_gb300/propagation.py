@@ -1,0 +1,246 @@
+"""Phaseless-AFQMC propagators with the reference's API, evaluated by GB300 kernels.
+
+Mirrors ad_afqmc/propagation.py: ``propagator_restricted`` (201-328) and
+``propagator_unrestricted`` (331-512) with ``init_prop_data``, ``propagate``,
+``orthonormalize_walkers``, ``stochastic_reconfiguration_local`` /
+``stochastic_reconfiguration_global`` and ``_build_propagation_intermediates``.
+
+``prop_data`` is a :class:`PropData` dict. Walkers, weights and overlaps are CUDA tensors;
+the scalars ``e_estimate``, ``pop_control_ene_shift`` and ``n_killed_walkers`` live in a
+device array and read back as 0-d CUDA tensors, so nothing synchronises with the host.
+``prop_data["key"]`` is an :class:`RngKey` (seed and Philox offsets), standing in for the
+JAX PRNG key.
+
+``precision`` selects the walker dtype: "fp64" -> complex128 walkers and FP64 kernels;
+"mixed" -> complex64 walkers and BF16 tensor-core contractions.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+from typing import Any, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _engine, _lib
+from ._engine import as_dev, device, stream_ptr
+
+_SCALAR_KEYS = {"e_estimate": _lib.AFQ_S_E_ESTIMATE,
+                "pop_control_ene_shift": _lib.AFQ_S_POP_CONTROL_SHIFT,
+                "n_killed_walkers": _lib.AFQ_S_N_KILLED}
+
+
+class RngKey:
+    """Counter-based key: draws are a pure function of (seed, offset)."""
+
+    def __init__(self, seed: int, offset: int = 0):
+        self.seed = int(seed) & ((1 << 64) - 1)
+        self.offset = int(offset)
+
+    def take(self, n: int) -> int:
+        """Reserve n draws and return their starting offset (kept even)."""
+        o = self.offset
+        self.offset += n + (n & 1)
+        return o
+
+    def __repr__(self):
+        return f"RngKey(seed={self.seed}, offset={self.offset})"
+
+
+class PropData(dict):
+    """prop_data dict whose scalar entries are views of a device array."""
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+        if "_scalars" not in self:
+            dict.__setitem__(self, "_scalars",
+                             torch.zeros(_lib.AFQ_NSCALARS, dtype=torch.float64, device=device()))
+
+    def __getitem__(self, k):
+        if k in _SCALAR_KEYS:
+            return dict.__getitem__(self, "_scalars")[_SCALAR_KEYS[k]]
+        return dict.__getitem__(self, k)
+
+    def __setitem__(self, k, v):
+        if k in _SCALAR_KEYS:
+            s = dict.__getitem__(self, "_scalars")
+            if isinstance(v, torch.Tensor):
+                s[_SCALAR_KEYS[k]].copy_(v.reshape(()).to(torch.float64).real
+                                         if v.is_complex() else v.reshape(()))
+            else:
+                s[_SCALAR_KEYS[k]] = float(np.real(v))
+            return
+        dict.__setitem__(self, k, v)
+
+    def __contains__(self, k):
+        return k in _SCALAR_KEYS or dict.__contains__(self, k)
+
+    def state(self, eng: _engine.Engine) -> _lib.WalkerState:
+        wu, wd = eng.walkers(self["walkers"])
+        w, o = self["weights"], self["overlaps"]
+        if w.dtype != torch.float64 or not w.is_contiguous() or w.numel() != eng.nw:
+            raise _lib.AfqError("weights must be contiguous float64 [nw]")
+        if o.dtype != torch.complex128 or not o.is_contiguous() or o.numel() != eng.nw:
+            raise _lib.AfqError("overlaps must be contiguous complex128 [nw]")
+        return _lib.WalkerState(walkers_up=wu, walkers_dn=wd, weights=w.data_ptr(),
+                                overlaps=o.data_ptr(), scalars=self["_scalars"].data_ptr())
+
+
+@dataclass
+class propagator_restricted:
+    """Propagator for walkers with the same alpha and beta dets (propagation.py:201-328)."""
+
+    dt: float = 0.01
+    n_walkers: int = 50
+    n_exp_terms: int = 6
+    n_batch: int = 1
+    precision: str = "fp64"
+
+    restricted = True
+
+    @property
+    def walker_dtype(self) -> torch.dtype:
+        return torch.complex128 if self.precision == "fp64" else torch.complex64
+
+    def _engine(self, trial, ham_data, wave_data, walkers) -> _engine.Engine:
+        return _engine.engine_for(trial, ham_data, wave_data, walkers, dt=self.dt,
+                                  n_exp_terms=self.n_exp_terms, n_batch=self.n_batch,
+                                  need_propagation=True)
+
+    def _cast_walkers(self, walkers):
+        if isinstance(walkers, (list, tuple)):
+            return [as_dev(w, self.walker_dtype) for w in walkers]
+        return as_dev(walkers, self.walker_dtype)
+
+    # ---- state ----------------------------------------------------------------------
+    def init_prop_data(self, trial, wave_data: dict, ham_data: dict,
+                       init_walkers=None) -> PropData:
+        """weights 1, walkers, e_estimate = mean real energy, overlaps
+        (propagation.py:210-232, 333-357)."""
+        pd = PropData()
+        pd["weights"] = torch.ones(self.n_walkers, dtype=torch.float64, device=device())
+        if init_walkers is not None:
+            pd["walkers"] = self._cast_walkers(init_walkers)
+        else:
+            pd["walkers"] = trial.get_init_walkers(wave_data, self.n_walkers,
+                                                   restricted=self.restricted,
+                                                   dtype=self.walker_dtype)
+        e = trial.calc_energy(pd["walkers"], ham_data, wave_data).real
+        pd["e_estimate"] = e.sum() / self.n_walkers
+        pd["pop_control_ene_shift"] = pd["e_estimate"]
+        pd["overlaps"] = trial.calc_overlap(pd["walkers"], wave_data)
+        if not self.restricted:
+            pd["normed_overlaps"] = pd["overlaps"]
+            pd["norms"] = torch.ones(self.n_walkers, dtype=torch.complex128, device=device())
+        pd["n_killed_walkers"] = 0.0
+        if "exp_h1" in ham_data:
+            bind(self, trial, ham_data, wave_data, pd)
+        return pd
+
+    # ---- propagation ----------------------------------------------------------------
+    def propagate(self, trial, ham_data: dict, prop_data: PropData, fields,
+                  wave_data: dict) -> PropData:
+        """One phaseless step with auxiliary fields [nw, nchol] (propagation.py:100-165)."""
+        eng = self._engine(trial, ham_data, wave_data, prop_data["walkers"])
+        f = as_dev(fields)
+        if tuple(f.shape) != (eng.nw, eng.nchol):
+            raise _lib.AfqError(f"fields must be [{eng.nw}, {eng.nchol}], got {tuple(f.shape)}")
+        dict.__setitem__(prop_data, "_engine", eng)
+        st = prop_data.state(eng)
+        _lib.call("afq_propagate", eng.ctx, ctypes.byref(st), f.data_ptr(), stream_ptr())
+        return prop_data
+
+    def orthonormalize_walkers(self, prop_data: PropData, trial=None, ham_data=None,
+                               wave_data=None) -> PropData:
+        """Q of the reduced QR of every walker (propagation.py:251-253, 422-424)."""
+        eng = _any_engine(prop_data, trial, ham_data, wave_data, self)
+        st = prop_data.state(eng)
+        _lib.call("afq_orthonormalize_walkers", eng.ctx, ctypes.byref(st), stream_ptr())
+        return prop_data
+
+    def stochastic_reconfiguration_local(self, prop_data: PropData, trial=None, ham_data=None,
+                                         wave_data=None, zeta=None) -> PropData:
+        """Comb resampling with a uniform zeta drawn from prop_data["key"] (or given)
+        (propagation.py:234-240 -> sr.py:24-47)."""
+        eng = _any_engine(prop_data, trial, ham_data, wave_data, self)
+        if zeta is None:
+            z = torch.empty(1, dtype=torch.float64, device=device())
+            key: RngKey = prop_data["key"]
+            _lib.call("afq_fill_uniform", z.data_ptr(), 1, key.seed, key.take(1), stream_ptr())
+        else:
+            z = as_dev(zeta).reshape(1)
+        st = prop_data.state(eng)
+        idx = torch.empty(eng.nw, dtype=torch.int32, device=device())
+        _lib.call("afq_stochastic_reconfiguration", eng.ctx, ctypes.byref(st), z.data_ptr(),
+                  idx.data_ptr(), stream_ptr())
+        dict.__setitem__(prop_data, "sr_indices", idx)
+        return prop_data
+
+    def stochastic_reconfiguration_global(self, prop_data: PropData, comm: Any = None,
+                                          **kw) -> PropData:
+        """One GPU, one rank: the global comb equals the local one (sr.py:66-106 with a
+        single rank)."""
+        if comm is not None and getattr(comm, "Get_size", lambda: 1)() != 1:
+            raise NotImplementedError("multi-rank SR: run independent replicas per GPU")
+        return self.stochastic_reconfiguration_local(prop_data, **kw)
+
+    # ---- intermediates --------------------------------------------------------------
+    def _build_propagation_intermediates(self, ham_data: dict, trial, wave_data: dict) -> dict:
+        """mf_shifts, h0_prop, exp_h1 = expm(-dt h1_mod/2) (propagation.py:292-325)."""
+        norb = trial.norb
+        rdm1 = trial.get_rdm1(wave_data)
+        rho = rdm1[0] + rdm1[1]
+        chol = as_dev(ham_data["chol"]).reshape(-1, norb, norb)
+        mf = 1.0j * torch.einsum("gij,ij->g", chol, rho).to(torch.complex128)
+        ham_data["mf_shifts"] = mf
+        h0 = float(np.real(_engine._scalar(ham_data["h0"])))
+        ham_data["h0_prop"] = -h0 - torch.sum(mf * mf).item() / 2.0
+        v0 = 0.5 * torch.einsum("gik,gjk->ij", chol, chol)
+        v1 = torch.real(1.0j * torch.einsum("g,gik->ik", mf, chol.to(torch.complex128)))
+        h1 = as_dev(ham_data["h1"])
+        ham_data["exp_h1"] = self._exp_h1(h1, v0, v1)
+        return ham_data
+
+    def _exp_h1(self, h1, v0, v1):
+        h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
+        return torch.linalg.matrix_exp(-self.dt * h1_mod / 2.0).contiguous()
+
+    def __hash__(self) -> int:
+        return hash((type(self).__name__, self.dt, self.n_walkers, self.n_exp_terms,
+                     self.n_batch, self.precision))
+
+
+@dataclass
+class propagator_unrestricted(propagator_restricted):
+    """Two-slab walkers, one exp_h1 per spin (propagation.py:331-512)."""
+
+    restricted = False
+
+    def _exp_h1(self, h1, v0, v1):
+        return torch.stack([torch.linalg.matrix_exp(-self.dt * (h1[0] - v0 - v1) / 2.0),
+                            torch.linalg.matrix_exp(-self.dt * (h1[1] - v0 - v1) / 2.0)]).contiguous()
+
+    def __hash__(self) -> int:
+        return super().__hash__()
+
+
+def _any_engine(prop_data, trial, ham_data, wave_data, prop):
+    """QR and SR need only sizes: reuse the engine that last propagated these walkers."""
+    eng = prop_data.get("_engine") if isinstance(prop_data, dict) else None
+    if trial is not None and ham_data is not None:
+        eng = prop._engine(trial, ham_data, wave_data, prop_data["walkers"])
+    if eng is None:
+        raise _lib.AfqError("no engine bound to prop_data: call bind(trial, ham_data, wave_data) "
+                            "through init_prop_data first")
+    return eng
+
+
+def bind(prop, trial, ham_data, wave_data, prop_data: PropData) -> PropData:
+    """Remember the engine of (prop, trial, ham_data) in prop_data so that QR and SR can be
+    called with the reference's one-argument signatures."""
+    dict.__setitem__(prop_data, "_engine", prop._engine(trial, ham_data, wave_data,
+                                                        prop_data["walkers"]))
+    return prop_data

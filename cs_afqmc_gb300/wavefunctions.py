@@ -1,0 +1,168 @@
+"""Trial wave functions with the reference's measurement API, evaluated by GB300 kernels.
+
+Mirrors ad_afqmc/wavefunctions.py: ``rhf`` (453-635) and ``uhf`` (638-844) with
+``calc_overlap``, ``calc_force_bias``, ``calc_energy`` dispatched on the walker container
+(one array = restricted walkers, a 2-list = unrestricted walkers, wavefunctions.py:45-241),
+``get_rdm1``, ``get_init_walkers`` and ``_build_measurement_intermediates``.
+
+Walkers are CUDA tensors. Their dtype selects the arithmetic: complex128 runs the FP64
+kernels, complex64 runs the mixed-precision (BF16 tensor-core) kernels. Results are
+complex128 CUDA tensors, as the reference returns complex arrays.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Any, List, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _engine, _lib
+from ._engine import as_dev, device, stream_ptr
+
+
+def _out(shape) -> torch.Tensor:
+    return torch.empty(shape, dtype=torch.complex128, device=device())
+
+
+@dataclass
+class wave_function:
+    norb: int
+    nelec: Tuple[int, int]
+    n_batch: int = 1
+    kind = "base"
+
+    # ---- measurements ---------------------------------------------------------------
+    def calc_overlap(self, walkers, wave_data: dict) -> torch.Tensor:
+        """<psi_T|walker> per walker (wavefunctions.py:45-96)."""
+        eng = _engine.engine_for(self, None, wave_data, walkers)
+        wu, wd = eng.walkers(walkers)
+        out = _out(eng.nw)
+        _lib.call("afq_calc_overlap", eng.ctx, wu, wd, out.data_ptr(), stream_ptr())
+        return out
+
+    def calc_force_bias(self, walkers, ham_data: dict, wave_data: dict) -> torch.Tensor:
+        """<psi_T|L_g|walker>/<psi_T|walker>, [nw, nchol] (wavefunctions.py:111-165)."""
+        eng = _engine.engine_for(self, ham_data, wave_data, walkers)
+        wu, wd = eng.walkers(walkers)
+        out = _out((eng.nw, eng.nchol))
+        _lib.call("afq_calc_force_bias", eng.ctx, wu, wd, out.data_ptr(), stream_ptr())
+        return out
+
+    def calc_energy(self, walkers, ham_data: dict, wave_data: dict) -> torch.Tensor:
+        """Mixed local energy per walker (wavefunctions.py:186-241)."""
+        eng = _engine.engine_for(self, ham_data, wave_data, walkers)
+        wu, wd = eng.walkers(walkers)
+        out = _out(eng.nw)
+        _lib.call("afq_calc_energy", eng.ctx, wu, wd, out.data_ptr(), stream_ptr())
+        return out
+
+    # ---- trial data -----------------------------------------------------------------
+    def get_rdm1(self, wave_data: dict) -> torch.Tensor:
+        """wave_data["rdm1"] if present, else the trial's own (wavefunctions.py:254-270)."""
+        if "rdm1" in wave_data:
+            return as_dev(wave_data["rdm1"])
+        return self._calc_rdm1(wave_data)
+
+    def _calc_rdm1(self, wave_data: dict) -> torch.Tensor:
+        raise NotImplementedError(
+            "One-body spin RDM not found in wave_data and not implemented for this trial.")
+
+    def get_init_walkers(self, wave_data: dict, n_walkers: int, restricted: bool = False,
+                         dtype=torch.complex128):
+        """Walkers from the natural orbitals of rdm1 (wavefunctions.py:298-355). The
+        equal-spin restricted case and the unrestricted case are supported."""
+        rdm1 = self.get_rdm1(wave_data).cpu().numpy()
+        nat_up = np.linalg.eigh(rdm1[0])[1][:, ::-1][:, : self.nelec[0]]
+        nat_dn = np.linalg.eigh(rdm1[1])[1][:, ::-1][:, : self.nelec[1]]
+        dev = device()
+        if restricted:
+            if self.nelec[0] != self.nelec[1]:
+                raise NotImplementedError("restricted walkers need equal spin counts here")
+            det_overlap = np.linalg.det(nat_up.T @ nat_dn)
+            if abs(det_overlap) <= 1e-3:
+                raise ValueError("Cannot find a set of RHF orbitals with good trial overlap.")
+            w = torch.as_tensor(np.ascontiguousarray(nat_up), dtype=dtype, device=dev)
+            return w.unsqueeze(0).repeat(n_walkers, 1, 1).contiguous()
+        return [torch.as_tensor(np.ascontiguousarray(nat_up), dtype=dtype, device=dev)
+                .unsqueeze(0).repeat(n_walkers, 1, 1).contiguous(),
+                torch.as_tensor(np.ascontiguousarray(nat_dn), dtype=dtype, device=dev)
+                .unsqueeze(0).repeat(n_walkers, 1, 1).contiguous()]
+
+    def optimize(self, ham_data: dict, wave_data: dict) -> dict:
+        return wave_data
+
+    def __hash__(self) -> int:
+        return hash((self.kind, self.norb, tuple(self.nelec), self.n_batch))
+
+
+def _sym(h1: torch.Tensor) -> torch.Tensor:
+    return torch.stack([(h1[0] + h1[0].T) / 2.0, (h1[1] + h1[1].T) / 2.0])
+
+
+@dataclass
+class rhf(wave_function):
+    """Restricted Hartree-Fock trial; wave_data["mo_coeff"] is [norb, nocc], real
+    (wavefunctions.py:453-635)."""
+
+    norb: int
+    nelec: Tuple[int, int]
+    n_opt_iter: int = 30
+    n_batch: int = 1
+    kind = "rhf"
+
+    def __post_init__(self):
+        assert self.nelec[0] == self.nelec[1], "RHF requires equal number of up and down electrons."
+
+    def _calc_rdm1(self, wave_data: dict) -> torch.Tensor:
+        # mo @ mo.T without conjugation, as wavefunctions.py:563-565
+        mo = as_dev(wave_data["mo_coeff"])
+        return torch.stack([mo @ mo.T, mo @ mo.T])
+
+    def _build_measurement_intermediates(self, ham_data: dict, wave_data: dict) -> dict:
+        """h1 <- (h1 + h1^T)/2 per spin; rot_h1 = C^H (h1_a + h1_b)/2; rot_chol_g = C^H L_g
+        (wavefunctions.py:602-619)."""
+        mo = as_dev(wave_data["mo_coeff"])
+        h1 = _sym(as_dev(ham_data["h1"]))
+        ham_data["h1"] = h1
+        ham_data["rot_h1"] = (mo.T @ ((h1[0] + h1[1]) / 2.0)).contiguous()
+        chol = as_dev(ham_data["chol"]).reshape(-1, self.norb, self.norb)
+        ham_data["rot_chol"] = torch.einsum("pi,gij->gpj", mo.T, chol).contiguous()
+        return ham_data
+
+    def __hash__(self) -> int:
+        return super().__hash__()
+
+
+@dataclass
+class uhf(wave_function):
+    """Unrestricted Hartree-Fock trial; wave_data["mo_coeff"] = [C_a [norb, n_a],
+    C_b [norb, n_b]], real (wavefunctions.py:638-844)."""
+
+    norb: int
+    nelec: Tuple[int, int]
+    n_opt_iter: int = 30
+    n_batch: int = 1
+    kind = "uhf"
+
+    def _calc_rdm1(self, wave_data: dict) -> torch.Tensor:
+        mo = wave_data["mo_coeff"]
+        a, b = as_dev(mo[0]), as_dev(mo[1])
+        return torch.stack([a @ a.T, b @ b.T])
+
+    def _build_measurement_intermediates(self, ham_data: dict, wave_data: dict) -> dict:
+        """(wavefunctions.py:817-841)."""
+        mo = wave_data["mo_coeff"]
+        a, b = as_dev(mo[0]), as_dev(mo[1])
+        h1 = _sym(as_dev(ham_data["h1"]))
+        ham_data["h1"] = h1
+        ham_data["rot_h1"] = [(a.T @ h1[0]).contiguous(), (b.T @ h1[1]).contiguous()]
+        chol = as_dev(ham_data["chol"]).reshape(-1, self.norb, self.norb)
+        ham_data["rot_chol"] = [torch.einsum("pi,gij->gpj", a.T, chol).contiguous(),
+                                torch.einsum("pi,gij->gpj", b.T, chol).contiguous()]
+        return ham_data
+
+    def __hash__(self) -> int:
+        return super().__hash__()

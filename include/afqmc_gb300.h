@@ -1,0 +1,192 @@
+/*
+ * afqmc_gb300.h - C ABI of the GB300-native phaseless-AFQMC hot path.
+ *
+ * The reference (zh-yichi/cs_afqmc, package ad_afqmc) is pure Python on JAX and has no
+ * foreign-function layer of its own: its hot path is a set of jitted Python methods. Each
+ * entry point below replaces one of those methods, cited as file:line inside ad_afqmc/.
+ * A Python host (cs_afqmc_gb300, via ctypes) or any C caller binds them.
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers owned by the caller, row-major, with complex
+ *    numbers stored interleaved (re, im). No function allocates device memory except where
+ *    stated; scratch lives in the caller-provided workspace (afq_workspace_size).
+ *  - Every call is stream-ordered on the caller's cudaStream_t (passed as void*), performs
+ *    no host synchronisation and is capturable into a CUDA graph.
+ *  - Return value: 0 on success; negative on a host-side error (bad shape, pointer or
+ *    unsupported option: nothing was launched); positive on a CUDA launch error.
+ *    afq_last_error() returns a message for the last failure on the calling thread.
+ *  - A context is not thread-safe; several contexts may share one device.
+ *
+ * Walker containers mirror the reference (wavefunctions.py:15-43):
+ *  - restricted walkers: one slab [nw, norb, max(n_up, n_dn)];
+ *  - unrestricted walkers: two slabs [nw, norb, n_up] and [nw, norb, n_dn].
+ * Walker element type: complex128 when precision == AFQ_PREC_FP64, complex64 when
+ * precision == AFQ_PREC_MIXED.
+ */
+#ifndef AFQMC_GB300_H
+#define AFQMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AFQ_ABI_VERSION 1
+
+enum afq_walker_type { AFQ_WALKERS_RESTRICTED = 0, AFQ_WALKERS_UNRESTRICTED = 1 };
+enum afq_trial_type { AFQ_TRIAL_RHF = 0, AFQ_TRIAL_UHF = 1 };
+enum afq_precision {
+  AFQ_PREC_FP64 = 0,  /* every contraction in FP64 (the reference's arithmetic) */
+  AFQ_PREC_MIXED = 1  /* BF16 tensor-core contractions with split-BF16 correction, FP32
+                         walkers, FP64 determinants / weights / energy accumulation */
+};
+
+/* Sizes and options. Mirrors the static fields of the reference's dataclasses:
+ * propagator_restricted(dt, n_walkers, n_exp_terms, n_batch) (propagation.py:201-212) and
+ * rhf/uhf(norb, nelec) (wavefunctions.py:453-476, 638-660). */
+typedef struct afq_dims {
+  int32_t norb;
+  int32_t n_up;
+  int32_t n_dn;
+  int32_t nchol;
+  int32_t n_walkers;
+  int32_t walker_type;  /* afq_walker_type */
+  int32_t trial_type;   /* afq_trial_type */
+  int32_t precision;    /* afq_precision */
+  int32_t n_exp_terms;  /* Taylor terms of exp(vhs), reference default 6 */
+  int32_t n_batch;      /* walker chunks for the vhs workspace (>= 1, divides n_walkers) */
+  double dt;
+} afq_dims;
+
+/* Hamiltonian and trial intermediates built by hamiltonian.build_measurement_intermediates
+ * and build_propagation_intermediates (hamiltonian.py:49-81 -> wavefunctions.py:602-619,
+ * 817-841; propagation.py:292-325, 464-509). Device pointers; the caller keeps them alive
+ * for the context's lifetime. The trial must be real (float64 mo_coeff). */
+typedef struct afq_hamiltonian {
+  double h0;
+  double h0_prop_re, h0_prop_im;  /* -h0 - sum(mf_shifts^2)/2 */
+  const double* trial_up;         /* [norb, n_up] mo_coeff (spin up; RHF: the only one) */
+  const double* trial_dn;         /* [norb, n_dn] (UHF); NULL for RHF */
+  const double* chol;             /* [nchol, norb*norb] */
+  const double* rot_chol_up;      /* [nchol, n_up, norb]  C_up^H L_g */
+  const double* rot_chol_dn;      /* [nchol, n_dn, norb]  (UHF); NULL for RHF */
+  const double* rot_h1_up;        /* [n_up, norb] */
+  const double* rot_h1_dn;        /* [n_dn, norb] (UHF); NULL for RHF */
+  const double* exp_h1_up;        /* [norb, norb] expm(-dt h1_mod/2) */
+  const double* exp_h1_dn;        /* [norb, norb] (unrestricted walkers); NULL otherwise */
+  const double* mf_shifts;        /* [nchol] complex128 */
+} afq_hamiltonian;
+
+/* Propagation state, the device-resident part of the reference's prop_data dict
+ * (propagation.py:210-232). scalars[] indices below. */
+typedef struct afq_walker_state {
+  void* walkers_up;   /* restricted: the only slab */
+  void* walkers_dn;   /* unrestricted only */
+  double* weights;    /* [nw] */
+  double* overlaps;   /* [nw] complex128 */
+  double* scalars;    /* [AFQ_NSCALARS] */
+} afq_walker_state;
+
+enum afq_scalar_index {
+  AFQ_S_E_ESTIMATE = 0,        /* prop_data["e_estimate"] */
+  AFQ_S_POP_CONTROL_SHIFT = 1, /* prop_data["pop_control_ene_shift"] */
+  AFQ_S_N_KILLED = 2,          /* prop_data["n_killed_walkers"] */
+  AFQ_S_BLOCK_ENERGY = 3,      /* last block's weighted energy */
+  AFQ_S_BLOCK_WEIGHT = 4,      /* last block's total weight */
+  AFQ_S_STATUS = 5,            /* device-side guard word (0 = ok) */
+  AFQ_NSCALARS = 8
+};
+
+typedef struct afq_ctx afq_ctx;
+
+/* ---- context ------------------------------------------------------------------------ */
+
+/* Bytes of device workspace a context with these sizes needs. Returns 0 on bad sizes. */
+size_t afq_workspace_size(const afq_dims* dims);
+
+/* Create a context. `workspace` must hold afq_workspace_size(dims) bytes (256-B aligned)
+ * and stays owned by the caller. Converts and caches precision-specific copies of the
+ * Hamiltonian inside the workspace (stream-ordered on `stream`). */
+int afq_ctx_create(const afq_dims* dims, const afq_hamiltonian* ham, void* workspace,
+                   size_t workspace_bytes, void* stream, afq_ctx** out);
+void afq_ctx_destroy(afq_ctx* ctx);
+const char* afq_last_error(void);
+int afq_abi_version(void);
+
+/* ---- trial measurements (wave_function.calc_*) --------------------------------------- */
+
+/* Overlap <psi_T|walker> per walker, complex128 [nw].
+ * Replaces wave_function.calc_overlap, wavefunctions.py:45-96 (rhf 478-488, uhf 658-667). */
+int afq_calc_overlap(afq_ctx* ctx, const void* walkers_up, const void* walkers_dn,
+                     double* overlaps, void* stream);
+
+/* Force bias <psi_T|L_g|walker>/<psi_T|walker>, complex128 [nw, nchol].
+ * Replaces wave_function.calc_force_bias, wavefunctions.py:111-165 (rhf 503-527,
+ * uhf 694-709). */
+int afq_calc_force_bias(afq_ctx* ctx, const void* walkers_up, const void* walkers_dn,
+                        double* force_bias, void* stream);
+
+/* Mixed local energy, complex128 [nw].
+ * Replaces wave_function.calc_energy, wavefunctions.py:186-241 (rhf 529-561,
+ * uhf 711-743). */
+int afq_calc_energy(afq_ctx* ctx, const void* walkers_up, const void* walkers_dn,
+                    double* energies, void* stream);
+
+/* ---- propagator ---------------------------------------------------------------------- */
+
+/* One phaseless step with the given fields (float64 [nw, nchol]): force bias, shifted
+ * fields, exp(vhs) by Taylor series between two exp_h1 half steps, new overlaps,
+ * phaseless importance function and clamps, weights and pop_control_ene_shift.
+ * Replaces propagator.propagate, propagation.py:100-165 (+ _apply_trotprop 255-290,
+ * 359-400 and _apply_trotprop_det 67-92). */
+int afq_propagate(afq_ctx* ctx, afq_walker_state* state, const double* fields, void* stream);
+
+/* Q of the reduced QR of every walker slab (LAPACK Householder convention in FP64 mode).
+ * Replaces propagator.orthonormalize_walkers, propagation.py:251-253, 422-424
+ * (linalg_utils.py:51-65). */
+int afq_orthonormalize_walkers(afq_ctx* ctx, afq_walker_state* state, void* stream);
+
+/* Comb stochastic reconfiguration with uniform *zeta (device pointer). Writes the chosen
+ * source index per walker to `indices` (int32 [nw], may be NULL).
+ * Replaces sr.stochastic_reconfiguration(_uhf), sr.py:24-47, as called by
+ * propagator.stochastic_reconfiguration_local, propagation.py:234-240, 402-408. */
+int afq_stochastic_reconfiguration(afq_ctx* ctx, afq_walker_state* state, const double* zeta,
+                                   int32_t* indices, void* stream);
+
+/* ---- sampler ------------------------------------------------------------------------- */
+
+/* sampler.propagate_phaseless, sampling.py:319-341 (with _sr_block_scan 126-144 and
+ * _block_scan 50-92): n_sr_blocks x [n_ene_blocks x [n_prop_steps propagate, QR,
+ * overlaps, clamped energies, block energy/weight, pop-control update], local SR].
+ * fields: float64 [n_sr_blocks, n_ene_blocks, n_prop_steps, nw, nchol];
+ * zetas: float64 [n_sr_blocks]; block_energy / block_weight: float64
+ * [n_sr_blocks * n_ene_blocks]; energy: float64 [1] = sum(E_b w_b)/sum(w_b).
+ * All on the device; no host synchronisation. */
+int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double* fields,
+                            const double* zetas, int32_t n_prop_steps, int32_t n_ene_blocks,
+                            int32_t n_sr_blocks, double* block_energy, double* block_weight,
+                            double* energy, void* stream);
+
+/* Per-block driver bookkeeping for one rank (driver.py:250-308, non-AD branch):
+ * *block_weight = sum(weights) (before QR/SR), e_estimate <- 0.9 e_estimate + 0.1 *energy,
+ * QR of every walker, then the comb SR with uniform *zeta (the single-rank
+ * stochastic_reconfiguration_global, sr.py:66-106). energy, zeta, block_weight are device
+ * pointers to one double each. */
+int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, const double* zeta,
+                  double* block_weight, void* stream);
+
+/* Standard normal draws (Philox4x32-10 + Box-Muller), float64 [n], counter-based:
+ * element i depends only on (seed, offset + i). Stands in for jax.random.normal in
+ * sampling.py:61-69. */
+int afq_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream);
+
+/* Uniform [0,1) draws, same generator. Stands in for jax.random.uniform in
+ * propagation.py:236-237. */
+int afq_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFQMC_GB300_H */

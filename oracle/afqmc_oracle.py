@@ -1,0 +1,489 @@
+"""FP64 NumPy oracle for the phaseless-AFQMC walker-propagation and local-energy path.
+
+This module is TEST INFRASTRUCTURE. Only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it, and only as the
+checker or as the timed CPU restatement of the reference. The product path
+(``cs_afqmc_gb300``) never calls it.
+
+It restates, in plain NumPy at float64/complex128, the reference package ``ad_afqmc``
+(zh-yichi/cs_afqmc, pure Python on JAX), line by line, for:
+
+* RHF / UHF trial measurements: overlap, half Green's function, force bias, mixed local
+  energy, half-rotated intermediates (ad_afqmc/wavefunctions.py)
+* propagation intermediates and the phaseless propagation step
+  (ad_afqmc/propagation.py)
+* QR orthonormalisation (ad_afqmc/linalg_utils.py) and comb stochastic reconfiguration
+  (ad_afqmc/sr.py)
+* the sampler's block loop and the driver's per-block bookkeeping
+  (ad_afqmc/sampling.py, ad_afqmc/driver.py)
+
+Parity pin: the RHF/UHF known-answer values of tests/test_wavefunctions.py:127-183 in the
+reference (overlap, Green's-function sum, force-bias sum, energy at the seed-102 fixture)
+are reproduced by this module; ``tests/test_oracle_golden.py`` checks them. The functions
+beyond those (propagate, QR, SR, block loop) are pinned by restatement only: the
+reference's own tests check them by output shape (tests/test_propagation.py:88-127).
+
+Random inputs are never drawn here: auxiliary fields and the SR uniforms are arguments, so
+the oracle and the GPU path consume identical draws. JAX's PRNG streams are not reproduced.
+
+Walker containers follow the reference: restricted walkers are one array
+``[nw, norb, max(n_up, n_dn)]``; unrestricted walkers are a 2-list ``[up, dn]`` with shapes
+``[nw, norb, n_up]`` and ``[nw, norb, n_dn]``.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional, Sequence, Tuple
+
+import numpy as np
+import scipy.linalg
+
+# ----------------------------------------------------------------------------------------
+# small batched helpers
+# ----------------------------------------------------------------------------------------
+
+
+def _h(a: np.ndarray) -> np.ndarray:
+    """Conjugate transpose of the last two axes."""
+    return np.conj(np.swapaxes(a, -1, -2))
+
+
+def _t(a: np.ndarray) -> np.ndarray:
+    return np.swapaxes(a, -1, -2)
+
+
+# ----------------------------------------------------------------------------------------
+# RHF trial  (wavefunctions.py:453-635)
+# ----------------------------------------------------------------------------------------
+
+
+def rhf_overlap_restricted(walkers: np.ndarray, mo: np.ndarray) -> np.ndarray:
+    """det(C^H W)^2 per walker (wavefunctions.py:478-480). walkers [nw,norb,nocc]."""
+    return np.linalg.det(_h(mo) @ walkers) ** 2
+
+
+def rhf_overlap(walkers_up, walkers_dn, mo) -> np.ndarray:
+    """det(C^H W_up) det(C^H W_dn) (wavefunctions.py:482-488)."""
+    return np.linalg.det(_h(mo) @ walkers_up) * np.linalg.det(_h(mo) @ walkers_dn)
+
+
+def rhf_green(walkers: np.ndarray, mo: np.ndarray) -> np.ndarray:
+    """Half Green's function (W (C^H W)^-1)^T, shape [nw, nocc, norb]
+    (wavefunctions.py:490-501)."""
+    return _t(walkers @ np.linalg.inv(_h(mo) @ walkers))
+
+
+def rhf_force_bias_restricted(walkers, rot_chol, mo) -> np.ndarray:
+    """2 sum_ij rot_chol[g,i,j] G[i,j] (wavefunctions.py:503-511)."""
+    g = rhf_green(walkers, mo)
+    return 2.0 * np.einsum("gij,wij->wg", rot_chol, g)
+
+
+def rhf_force_bias(walkers_up, walkers_dn, rot_chol, mo) -> np.ndarray:
+    """Two-slab walkers, G_up + G_dn contracted once (wavefunctions.py:513-527)."""
+    g = rhf_green(walkers_up, mo) + rhf_green(walkers_dn, mo)
+    return np.einsum("gij,wij->wg", rot_chol, g)
+
+
+def _exchange_coulomb(rot_chol: np.ndarray, green: np.ndarray):
+    """f_g = rot_chol_g G^T per walker; returns (c [nw,G], exc [nw]) with c_g = tr f_g and
+    exc = sum_g sum_ik f_g[i,k] f_g[k,i] (wavefunctions.py:537-539)."""
+    f = np.einsum("gij,wkj->wgik", rot_chol, green)
+    c = np.einsum("wgii->wg", f)
+    exc = np.einsum("wgik,wgki->w", f, f)
+    return c, exc
+
+
+def rhf_energy_restricted(walkers, h0, rot_h1, rot_chol, mo) -> np.ndarray:
+    """Mixed local energy, RHF restricted walkers (wavefunctions.py:529-541):
+    h0 + 2 sum G*rot_h1 + 2 sum_g c_g^2 - exc."""
+    g = rhf_green(walkers, mo)
+    ene1 = 2.0 * np.einsum("wij,ij->w", g, rot_h1)
+    c, exc = _exchange_coulomb(rot_chol, g)
+    ene2 = 2.0 * np.sum(c * c, axis=1) - exc
+    return ene2 + ene1 + h0
+
+
+def rhf_energy(walkers_up, walkers_dn, h0, rot_h1, rot_chol, mo) -> np.ndarray:
+    """Two-slab walkers with the RHF trial (wavefunctions.py:543-561)."""
+    g = rhf_green(walkers_up, mo) + rhf_green(walkers_dn, mo)
+    ene1 = np.einsum("wij,ij->w", g, rot_h1)
+    c, exc = _exchange_coulomb(rot_chol, g)
+    return np.sum(c * c, axis=1) - exc + ene1 + h0
+
+
+def rhf_build_measurement_intermediates(ham_data: dict, mo: np.ndarray, norb: int) -> dict:
+    """Symmetrise h1 per spin with (h + h^T)/2 (not Hermitian), rot_h1 = C^H (h1_a+h1_b)/2,
+    rot_chol_g = C^H L_g (wavefunctions.py:602-619)."""
+    h1 = np.array(ham_data["h1"])
+    h1 = np.stack([(h1[0] + h1[0].T) / 2.0, (h1[1] + h1[1].T) / 2.0])
+    ham_data["h1"] = h1
+    ham_data["rot_h1"] = _h(mo) @ ((h1[0] + h1[1]) / 2.0)
+    ham_data["rot_chol"] = np.einsum(
+        "pi,gij->gpj", _h(mo), np.asarray(ham_data["chol"]).reshape(-1, norb, norb)
+    )
+    return ham_data
+
+
+# ----------------------------------------------------------------------------------------
+# UHF trial  (wavefunctions.py:638-844)
+# ----------------------------------------------------------------------------------------
+
+
+def uhf_overlap(walkers_up, walkers_dn, mo: Sequence[np.ndarray]) -> np.ndarray:
+    """det(C_a^H W_up) det(C_b^H W_dn) (wavefunctions.py:658-667)."""
+    return np.linalg.det(_h(mo[0]) @ walkers_up) * np.linalg.det(_h(mo[1]) @ walkers_dn)
+
+
+def uhf_green(walkers_up, walkers_dn, mo) -> List[np.ndarray]:
+    """[G_up [nw,n_up,norb], G_dn [nw,n_dn,norb]] (wavefunctions.py:669-692)."""
+    return [rhf_green(walkers_up, mo[0]), rhf_green(walkers_dn, mo[1])]
+
+
+def uhf_force_bias(walkers_up, walkers_dn, rot_chol, mo) -> np.ndarray:
+    """sum over spins of rot_chol[s]:G[s] (wavefunctions.py:694-709)."""
+    g = uhf_green(walkers_up, walkers_dn, mo)
+    return np.einsum("gij,wij->wg", rot_chol[0], g[0]) + np.einsum(
+        "gij,wij->wg", rot_chol[1], g[1]
+    )
+
+
+def uhf_energy(walkers_up, walkers_dn, h0, rot_h1, rot_chol, mo) -> np.ndarray:
+    """(sum c_up^2 + sum c_dn^2 + 2 sum c_up c_dn - exc_up - exc_dn)/2 + ene1 + h0
+    (wavefunctions.py:711-743)."""
+    g = uhf_green(walkers_up, walkers_dn, mo)
+    ene1 = np.einsum("wij,ij->w", g[0], rot_h1[0]) + np.einsum("wij,ij->w", g[1], rot_h1[1])
+    c_up, exc_up = _exchange_coulomb(rot_chol[0], g[0])
+    c_dn, exc_dn = _exchange_coulomb(rot_chol[1], g[1])
+    ene2 = (
+        np.sum(c_up * c_up, 1) + np.sum(c_dn * c_dn, 1) + 2.0 * np.sum(c_up * c_dn, 1)
+        - exc_up - exc_dn
+    ) / 2.0
+    return ene2 + ene1 + h0
+
+
+def uhf_build_measurement_intermediates(ham_data: dict, mo, norb: int) -> dict:
+    """(wavefunctions.py:817-841)."""
+    h1 = np.array(ham_data["h1"])
+    h1 = np.stack([(h1[0] + h1[0].T) / 2.0, (h1[1] + h1[1].T) / 2.0])
+    ham_data["h1"] = h1
+    ham_data["rot_h1"] = [_h(mo[0]) @ h1[0], _h(mo[1]) @ h1[1]]
+    chol = np.asarray(ham_data["chol"]).reshape(-1, norb, norb)
+    ham_data["rot_chol"] = [
+        np.einsum("pi,gij->gpj", _h(mo[0]), chol),
+        np.einsum("pi,gij->gpj", _h(mo[1]), chol),
+    ]
+    return ham_data
+
+
+# ----------------------------------------------------------------------------------------
+# Trial dispatch (the singledispatch of wavefunctions.py:45-241)
+# ----------------------------------------------------------------------------------------
+
+
+@dataclass
+class Trial:
+    """kind 'rhf' (wave_data mo [norb,nocc]) or 'uhf' (mo = [C_a, C_b])."""
+
+    kind: str
+    norb: int
+    nelec: Tuple[int, int]
+
+    def overlap(self, walkers, mo):
+        if isinstance(walkers, list):
+            if self.kind == "rhf":
+                return rhf_overlap(walkers[0], walkers[1], mo)
+            return uhf_overlap(walkers[0], walkers[1], mo)
+        if self.kind == "rhf":
+            return rhf_overlap_restricted(walkers, mo)
+        # base-class restricted dispatch: slice the single slab (wavefunctions.py:98-104)
+        return uhf_overlap(walkers[:, :, : self.nelec[0]], walkers[:, :, : self.nelec[1]], mo)
+
+    def force_bias(self, walkers, ham_data, mo):
+        rc = ham_data["rot_chol"]
+        if isinstance(walkers, list):
+            if self.kind == "rhf":
+                return rhf_force_bias(walkers[0], walkers[1], rc, mo)
+            return uhf_force_bias(walkers[0], walkers[1], rc, mo)
+        if self.kind == "rhf":
+            return rhf_force_bias_restricted(walkers, rc, mo)
+        return uhf_force_bias(walkers[:, :, : self.nelec[0]], walkers[:, :, : self.nelec[1]], rc, mo)
+
+    def energy(self, walkers, ham_data, mo):
+        h0, rh1, rc = ham_data["h0"], ham_data["rot_h1"], ham_data["rot_chol"]
+        if isinstance(walkers, list):
+            if self.kind == "rhf":
+                return rhf_energy(walkers[0], walkers[1], h0, rh1, rc, mo)
+            return uhf_energy(walkers[0], walkers[1], h0, rh1, rc, mo)
+        if self.kind == "rhf":
+            return rhf_energy_restricted(walkers, h0, rh1, rc, mo)
+        return uhf_energy(
+            walkers[:, :, : self.nelec[0]], walkers[:, :, : self.nelec[1]], h0, rh1, rc, mo
+        )
+
+    def build_measurement_intermediates(self, ham_data, mo):
+        if self.kind == "rhf":
+            return rhf_build_measurement_intermediates(ham_data, mo, self.norb)
+        return uhf_build_measurement_intermediates(ham_data, mo, self.norb)
+
+
+# ----------------------------------------------------------------------------------------
+# Propagation intermediates  (propagation.py:292-325 restricted, 464-509 unrestricted)
+# ----------------------------------------------------------------------------------------
+
+
+def build_propagation_intermediates(
+    ham_data: dict, rdm1: np.ndarray, norb: int, nelec, dt: float, restricted: bool
+) -> dict:
+    """mf_shifts_g = i sum L_g*(rho_a+rho_b); h0_prop = -h0 - sum mf^2/2;
+    v0 = 1/2 sum_g L_g L_g^T; h1_mod = h1 - v0 - Re(i sum_g mf_g L_g); exp_h1 = expm(-dt h1_mod/2).
+
+    The restricted propagator averages the two spin blocks of h1 (propagation.py:315); the
+    unrestricted one keeps one exp_h1 per spin (propagation.py:497-508).
+    """
+    chol = np.asarray(ham_data["chol"]).reshape(-1, norb, norb)
+    rho = rdm1[0] + rdm1[1]
+    mf = 1.0j * np.einsum("gij,ij->g", chol, rho)
+    ham_data["mf_shifts"] = mf
+    ham_data["h0_prop"] = -ham_data["h0"] - np.sum(mf**2) / 2.0
+    v0 = 0.5 * np.einsum("gik,gjk->ij", chol, chol)
+    v1 = np.real(1.0j * np.einsum("g,gik->ik", mf, chol))
+    h1 = np.asarray(ham_data["h1"])
+    if restricted:
+        h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
+        ham_data["exp_h1"] = scipy.linalg.expm(-dt * h1_mod / 2.0)
+    else:
+        ham_data["exp_h1"] = np.stack(
+            [
+                scipy.linalg.expm(-dt * (h1[0] - v0 - v1) / 2.0),
+                scipy.linalg.expm(-dt * (h1[1] - v0 - v1) / 2.0),
+            ]
+        )
+    return ham_data
+
+
+# ----------------------------------------------------------------------------------------
+# Propagator  (propagation.py:67-165, 201-290, 331-400)
+# ----------------------------------------------------------------------------------------
+
+
+def apply_trotprop_det(exp_h1: np.ndarray, vhs: np.ndarray, walkers: np.ndarray, n_exp_terms: int):
+    """Batched W <- e^{h1/2} (W + sum_{m=1}^{n_exp_terms-1} V^m W / m!) with W = e^{h1/2} W
+    first (propagation.py:67-92). vhs [nw,norb,norb], walkers [nw,norb,k]."""
+    w = exp_h1 @ walkers
+    carry = w
+    terms = []
+    for _ in range(1, n_exp_terms):
+        carry = vhs @ carry
+        terms.append(carry)
+    acc = np.zeros_like(w)
+    for m, t in enumerate(terms):
+        acc = acc + t / math.factorial(m + 1)
+    w = w + acc
+    return exp_h1 @ w
+
+
+def make_vhs(shifted_fields: np.ndarray, chol: np.ndarray, dt: float, norb: int) -> np.ndarray:
+    """vhs = i sqrt(dt) fields . chol, reshaped [nw, norb, norb] (propagation.py:265-271)."""
+    return (1.0j * math.sqrt(dt) * (shifted_fields @ chol.reshape(chol.shape[0], -1))).reshape(
+        -1, norb, norb
+    )
+
+
+def apply_trotprop(ham_data, walkers, shifted_fields, dt, norb, n_exp_terms):
+    vhs = make_vhs(shifted_fields, np.asarray(ham_data["chol"]), dt, norb)
+    if isinstance(walkers, list):
+        e = ham_data["exp_h1"]
+        return [
+            apply_trotprop_det(e[0], vhs, walkers[0], n_exp_terms),
+            apply_trotprop_det(e[1], vhs, walkers[1], n_exp_terms),
+        ]
+    return apply_trotprop_det(ham_data["exp_h1"], vhs, walkers, n_exp_terms)
+
+
+@dataclass
+class Propagator:
+    dt: float = 0.01
+    n_walkers: int = 50
+    n_exp_terms: int = 6
+
+    def propagate(self, trial: Trial, ham_data: dict, prop_data: dict, fields: np.ndarray, mo):
+        """One phaseless step (propagation.py:100-165). Mutates and returns prop_data."""
+        dt = self.dt
+        sdt = math.sqrt(dt)
+        mf = ham_data["mf_shifts"]
+        force_bias = trial.force_bias(prop_data["walkers"], ham_data, mo)
+        field_shifts = -sdt * (1.0j * force_bias - mf)
+        shifted_fields = fields - field_shifts
+        shift_term = np.sum(shifted_fields * mf, axis=1)
+        fb_term = np.sum(fields * field_shifts - field_shifts * field_shifts / 2.0, axis=1)
+        prop_data["walkers"] = apply_trotprop(
+            ham_data, prop_data["walkers"], shifted_fields, dt, trial.norb, self.n_exp_terms
+        )
+        overlaps_new = trial.overlap(prop_data["walkers"], mo)
+        ratio = overlaps_new / prop_data["overlaps"]
+        with np.errstate(all="ignore"):
+            imp_fun = (
+                np.exp(
+                    -sdt * shift_term
+                    + fb_term
+                    + dt * (prop_data["pop_control_ene_shift"] + ham_data["h0_prop"])
+                )
+                * ratio
+            )
+            theta = np.angle(np.exp(-sdt * shift_term) * ratio)
+            imp = np.abs(imp_fun) * np.cos(theta)
+        imp = np.where(np.isnan(imp), 0.0, imp)
+        imp = np.where(imp < 1.0e-3, 0.0, imp)
+        imp = np.where(imp > 100.0, 0.0, imp)
+        w = imp * prop_data["weights"]
+        w = np.where(w > 100, 0.0, w)
+        prop_data["weights"] = w
+        prop_data["pop_control_ene_shift"] = prop_data["e_estimate"] - 0.1 * np.log(
+            np.sum(w) / self.n_walkers
+        ) / dt
+        prop_data["overlaps"] = overlaps_new
+        return prop_data
+
+    def orthonormalize_walkers(self, prop_data: dict) -> dict:
+        """Q of the reduced QR of each walker (propagation.py:251-253, 422-424 ->
+        linalg_utils.py:51-65). LAPACK Householder convention, as jnp.linalg.qr."""
+        w = prop_data["walkers"]
+        if isinstance(w, list):
+            prop_data["walkers"] = [np.linalg.qr(w[0])[0], np.linalg.qr(w[1])[0]]
+        else:
+            prop_data["walkers"] = np.linalg.qr(w)[0]
+        return prop_data
+
+    def stochastic_reconfiguration(self, prop_data: dict, zeta: float) -> dict:
+        """Comb resampling (sr.py:24-47): z = W (i + zeta)/nw, idx = searchsorted(cumsum|w|, z)
+        (left side), walkers gathered, weights set to the mean."""
+        weights = prop_data["weights"]
+        nw = weights.shape[0]
+        cw = np.cumsum(np.abs(weights))
+        tw = cw[-1]
+        z = tw * (np.arange(nw) + zeta) / nw
+        idx = np.searchsorted(cw, z)
+        idx = np.minimum(idx, nw - 1)  # JAX clamps out-of-range gathers
+        w = prop_data["walkers"]
+        if isinstance(w, list):
+            prop_data["walkers"] = [w[0][idx], w[1][idx]]
+        else:
+            prop_data["walkers"] = w[idx]
+        prop_data["weights"] = np.ones(nw) * (tw / nw)
+        prop_data["sr_indices"] = idx
+        return prop_data
+
+
+def init_prop_data(prop: Propagator, trial: Trial, ham_data: dict, mo, walkers) -> dict:
+    """weights 1, e_estimate = mean real energy, overlaps (propagation.py:210-232, 333-357)."""
+    pd = {"weights": np.ones(prop.n_walkers), "walkers": walkers}
+    e = np.real(trial.energy(walkers, ham_data, mo))
+    pd["e_estimate"] = np.sum(e) / prop.n_walkers
+    pd["pop_control_ene_shift"] = pd["e_estimate"]
+    pd["overlaps"] = trial.overlap(walkers, mo)
+    return pd
+
+
+# ----------------------------------------------------------------------------------------
+# Sampler  (sampling.py:22-144, 319-341) and driver bookkeeping (driver.py:207-308)
+# ----------------------------------------------------------------------------------------
+
+
+@dataclass
+class Sampler:
+    n_prop_steps: int = 50
+    n_ene_blocks: int = 50
+    n_sr_blocks: int = 1
+    n_blocks: int = 50
+
+    def block_scan(self, prop, trial, ham_data, prop_data, mo, fields):
+        """fields [n_prop_steps, nw, G] (sampling.py:50-92)."""
+        for s in range(self.n_prop_steps):
+            prop_data = prop.propagate(trial, ham_data, prop_data, fields[s], mo)
+        prop_data["n_killed_walkers"] += prop_data["weights"].size - np.count_nonzero(
+            prop_data["weights"]
+        )
+        prop_data = prop.orthonormalize_walkers(prop_data)
+        prop_data["overlaps"] = trial.overlap(prop_data["walkers"], mo)
+        e = np.real(trial.energy(prop_data["walkers"], ham_data, mo))
+        e = np.where(np.abs(e - prop_data["e_estimate"]) > np.sqrt(2.0 / prop.dt), prop_data["e_estimate"], e)
+        bw = np.sum(prop_data["weights"])
+        be = np.sum(e * prop_data["weights"]) / bw
+        prop_data["pop_control_ene_shift"] = 0.9 * prop_data["pop_control_ene_shift"] + 0.1 * be
+        return prop_data, be, bw
+
+    def propagate_phaseless(self, prop, trial, ham_data, prop_data, mo, fields, zetas):
+        """fields [n_sr_blocks, n_ene_blocks, n_prop_steps, nw, G]; zetas [n_sr_blocks]
+        (sampling.py:126-144, 319-341). Returns (energy, prop_data, block_e, block_w)."""
+        prop_data["overlaps"] = trial.overlap(prop_data["walkers"], mo)
+        prop_data["n_killed_walkers"] = 0
+        prop_data["pop_control_ene_shift"] = prop_data["e_estimate"]
+        be_all, bw_all = [], []
+        for s in range(self.n_sr_blocks):
+            for b in range(self.n_ene_blocks):
+                prop_data, be, bw = self.block_scan(prop, trial, ham_data, prop_data, mo, fields[s, b])
+                be_all.append(be)
+                bw_all.append(bw)
+            prop_data = prop.stochastic_reconfiguration(prop_data, zetas[s])
+            prop_data["overlaps"] = trial.overlap(prop_data["walkers"], mo)
+        prop_data["n_killed_walkers"] /= self.n_sr_blocks * self.n_ene_blocks * prop.n_walkers
+        be_all, bw_all = np.array(be_all), np.array(bw_all)
+        return np.sum(be_all * bw_all) / np.sum(bw_all), prop_data, be_all, bw_all
+
+
+def run_blocks(
+    sampler: Sampler,
+    prop: Propagator,
+    trial: Trial,
+    ham_data: dict,
+    prop_data: dict,
+    mo,
+    draw_fields: Callable[[int], np.ndarray],
+    draw_zetas: Callable[[int], np.ndarray],
+    n_blocks: int,
+):
+    """Single-rank driver loop without AD (driver.py:207-308): per block
+    propagate_phaseless, record (energy, sum of weights), QR, global SR (one rank: the same
+    comb), e_estimate <- 0.9 e_estimate + 0.1 E_block.
+
+    draw_fields(n) -> fields for block n, shape [n_sr, n_ene, n_prop, nw, G];
+    draw_zetas(n) -> [n_sr + 1] uniforms (n_sr local SRs, then the driver's global SR).
+    """
+    energies, weights = [], []
+    for n in range(n_blocks):
+        f = draw_fields(n)
+        z = draw_zetas(n)
+        e, prop_data, _, _ = sampler.propagate_phaseless(prop, trial, ham_data, prop_data, mo, f, z[:-1])
+        energies.append(e)
+        weights.append(np.sum(prop_data["weights"]))
+        prop_data = prop.orthonormalize_walkers(prop_data)
+        prop_data = prop.stochastic_reconfiguration(prop_data, z[-1])
+        prop_data["e_estimate"] = 0.9 * prop_data["e_estimate"] + 0.1 * e
+    return np.array(energies), np.array(weights), prop_data
+
+
+def blocking_analysis(weights: np.ndarray, energies: np.ndarray, neql: int = 0):
+    """Weighted mean and plateau error of blocked samples (stat_utils.py:8-52), computed in
+    float64 throughout (the reference's blocked arrays are float32)."""
+    weights = np.asarray(weights, dtype=np.float64)[neql:]
+    energies = np.asarray(energies, dtype=np.float64)[neql:]
+    n = weights.shape[0]
+    we = weights * energies
+    mean = we.sum() / weights.sum()
+    prev, plateau = 0.0, None
+    for i in range(1, n + 1):
+        if not i < n / 2.0:
+            break
+        nb = n // i
+        bw = np.array([weights[j * i:(j + 1) * i].sum() for j in range(nb)])
+        be = np.array([we[j * i:(j + 1) * i].sum() for j in range(nb)]) / bw
+        v1, v2 = bw.sum(), (bw**2).sum()
+        m = (bw * be).sum() / v1
+        err = ((bw * (be - m) ** 2).sum() / (v1 - v2 / v1) / (nb - 1)) ** 0.5
+        if err <= 1.05 * prev and plateau is None:
+            plateau = max(err, prev)
+        prev = err
+    return mean, plateau
