@@ -71,6 +71,14 @@ _SIGS = {
 
 EXPORTED = tuple(_SIGS)
 
+# include/afqmc_gb300_testing.h: single-kernel hooks for the numerics tests
+_TEST_SIGS = {
+    "afq_test_gemm_f16": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_long, ctypes.c_long, _vp,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+}
+_SIGS.update(_TEST_SIGS)
+
 _lib: Optional[ctypes.CDLL] = None
 
 

@@ -1,0 +1,168 @@
+// Warp-specialised tcgen05 GEMM core: D[M x N] (fp32, TMEM) = sum_t A_t[M x K] * B_t[N x K]^T
+// over up to three (A_t, B_t) operand pairs (the split-precision hi/lo terms), 16-bit inputs
+// (bf16 or fp16), both operands K-major in global memory, loaded by TMA with the 128-byte
+// swizzle. One 128 x BN output tile per CTA.
+//
+// Warp roles (192 threads): warp 0 lane 0 issues TMA loads into a STAGES-deep ring;
+// warp 1 owns the TMEM allocation and lane 0 issues the MMAs; warps 2..5 run the epilogue
+// (warp w reads TMEM lanes 32*(w%4) .. 32*(w%4)+31). Every wait is bounded: on a timeout the
+// CTA records a nonzero word in *status and still frees its TMEM.
+#pragma once
+#include "afq_ptx.cuh"
+
+namespace afq {
+
+struct GemmMaps {
+  CUtensorMap a[3];
+  CUtensorMap b[3];
+};
+
+constexpr int kGemmThreads = 192;
+
+__host__ __device__ constexpr int gemm_tmem_cols(int bn) {
+  return bn <= 32 ? 32 : bn <= 64 ? 64 : bn <= 128 ? 128 : bn <= 256 ? 256 : 512;
+}
+
+template <int BN, int STAGES>
+__host__ __device__ constexpr int gemm_pipe_bytes() {
+  return STAGES * (128 * 128 + BN * 128);
+}
+
+// Dynamic shared memory for the core: pipeline + 256 B of barriers + epilogue scratch,
+// plus 1 KB of alignment slack.
+template <int BN, int STAGES, class Epi>
+__host__ __device__ constexpr int gemm_smem_bytes() {
+  return 1024 + gemm_pipe_bytes<BN, STAGES>() + 256 + Epi::kSmemBytes;
+}
+
+template <int BN, int STAGES, class Epi>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_gemm_tc(const __grid_constant__ GemmMaps maps, int nterms, int k_tiles, uint32_t idesc,
+              const __grid_constant__ typename Epi::Params ep, int* status) {
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "BN");
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr int A_BYTES = 128 * 128;  // 128 rows x 64 x 16-bit
+  constexpr int B_BYTES = BN * 128;
+  constexpr int STAGE = A_BYTES + B_BYTES;
+  constexpr uint32_t TMEM_COLS = gemm_tmem_cols(BN);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accb = empty + STAGES;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(accb + 1);
+  unsigned char* epi_smem = smem + STAGES * STAGE + 256;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
+  const int total = nterms * k_tiles;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full[s], 1);
+      ptx::mbar_init(&empty[s], 1);
+    }
+    ptx::mbar_init(accb, 1);
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(tmem_holder, TMEM_COLS);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  bool ok = true;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int t = 0; t < nterms; ++t) {
+        ptx::prefetch_tmap(&maps.a[t]);
+        ptx::prefetch_tmap(&maps.b[t]);
+      }
+      int issued = 0;
+      for (int it = 0; it < total; ++it) {
+        const int s = it % STAGES, r = it / STAGES;
+        if (r > 0 && !ptx::mbar_wait(&empty[s], (r - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        const int t = it / k_tiles, kt = it % k_tiles;
+        unsigned char* sa = smem + s * STAGE;
+        ptx::mbar_expect_tx(&full[s], STAGE);
+        ptx::tma_load_2d(sa, &maps.a[t], &full[s], kt * 64, m0);
+        ptx::tma_load_2d(sa + A_BYTES, &maps.b[t], &full[s], kt * 64, n0);
+        ++issued;
+      }
+      // never leave a copy in flight: wait for the last round issued on each stage
+      for (int it = issued - 1; it >= 0 && it >= issued - STAGES; --it)
+        if (!ptx::mbar_wait(&full[it % STAGES], (it / STAGES) & 1)) ok = false;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      for (int it = 0; it < total; ++it) {
+        const int s = it % STAGES, r = it / STAGES;
+        if (!ptx::mbar_wait(&full[s], r & 1)) {
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        const uint32_t sa = ptx::smem_u32(smem + s * STAGE), sb = sa + A_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          ptx::mma_f16(tmem, ptx::desc_kmajor_sw128(sa + kk * 32), ptx::desc_kmajor_sw128(sb + kk * 32),
+                       idesc, (it > 0 || kk > 0) ? 1u : 0u);
+        }
+        ptx::mma_commit(&empty[s]);
+      }
+      ptx::mma_commit(accb);
+    }
+  } else {
+    const int q = warp & 3;
+    const bool got = ptx::mbar_wait(accb, 0);
+    ptx::tc_fence_after();
+    if (!got) ok = false;
+    Epi::template run<BN>(ep, m0, n0, tmem, q, lane, epi_smem, got);
+  }
+  if (!ok) atomicOr(status, 1);
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// Plain epilogue: D (fp32, row-major, ldd) = accumulator, clipped to M x N. Used by tests.
+struct EpiStoreF32 {
+  struct Params {
+    float* d;
+    int M, N;
+    long ldd;
+  };
+  static constexpr int kSmemBytes = 0;
+  template <int BN>
+  __device__ static void run(const Params& p, int m0, int n0, uint32_t tmem, int q, int lane,
+                             unsigned char*, bool) {
+    const int row = m0 + q * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 16) {
+      float v[16];
+      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c, v);
+      ptx::tmem_ld_wait();
+      if (row < p.M) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (n0 + c + j < p.N) p.d[(long)row * p.ldd + n0 + c + j] = v[j];
+      }
+    }
+  }
+};
+
+// Host: tensor map for a row-major 16-bit matrix [rows][cols] (row stride ld elements),
+// box = 64 columns x box_rows rows, 128-byte swizzle, zero fill out of bounds.
+int make_tmap_16(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld,
+                 uint32_t box_rows, bool bf16);
+
+}  // namespace afq

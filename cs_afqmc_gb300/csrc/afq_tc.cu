@@ -1,7 +1,81 @@
-// Mixed-precision (BF16 tcgen05) path.
+// Mixed-precision (16-bit tcgen05) path: tensor maps, GEMM launchers, test hooks.
+#include <stdio.h>
+#include <string.h>
+
+#include "afq_gemm.cuh"
 #include "afq_tc.cuh"
 
 namespace afq {
+
+// ---- tensor maps ----------------------------------------------------------------------
+
+typedef CUresult (*PFN_tmapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                         const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                         const cuuint32_t*, CUtensorMapInterleave,
+                                         CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                         CUtensorMapFloatOOBfill);
+
+static PFN_tmapEncodeTiled encode_fn() {
+  static PFN_tmapEncodeTiled fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_tmapEncodeTiled>(p);
+  }
+  return fn;
+}
+
+int make_tmap_16(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld,
+                 uint32_t box_rows, bool bf16) {
+  PFN_tmapEncodeTiled enc = encode_fn();
+  if (!enc) {
+    afq_set_error("cuTensorMapEncodeTiled unavailable");
+    return -3;
+  }
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld * 2) % 16 || box_rows < 1 || box_rows > 256) {
+    afq_set_error("tensor map: base/stride must be 16-byte aligned, box rows in [1,256]");
+    return -1;
+  }
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {ld * 2};
+  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                   const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    afq_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return -3;
+  }
+  return 0;
+}
+
+static int launch_check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    afq_set_error("%s: %s", what, cudaGetErrorString(e));
+    return (int)e;
+  }
+  return 0;
+}
+
+template <int BN, int STAGES, class Epi>
+static int launch_gemm(const GemmMaps& maps, int nterms, int k_tiles, int m_tiles, int n_tiles,
+                       bool bf16, const typename Epi::Params& ep, int* status, cudaStream_t st) {
+  constexpr int smem = gemm_smem_bytes<BN, STAGES, Epi>();
+  auto kfn = k_gemm_tc<BN, STAGES, Epi>;
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  kfn<<<dim3(n_tiles, m_tiles), kGemmThreads, smem, st>>>(maps, nterms, k_tiles,
+                                                          ptx::idesc_f16(128, BN, bf16 ? 1 : 0), ep,
+                                                          status);
+  return launch_check("gemm_tc");
+}
+
+// ---- mixed-precision path (filled in below) -------------------------------------------
 
 static int not_ready() {
   afq_set_error("mixed precision path is not built yet");
@@ -20,3 +94,37 @@ int tc_propagate_chunk(TcState&, const afq_ctx_dev&, int, int, const double2*, v
 int tc_orthonormalize(TcState&, const afq_ctx_dev&, void*, void*, cudaStream_t) { return not_ready(); }
 
 }  // namespace afq
+
+// ---- test hooks (include/afqmc_gb300_testing.h) ---------------------------------------
+
+extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stride,
+                                 long b_term_stride, float* d, int M, int N, int K, int lda,
+                                 int ldb, int bf16, int bn, int* status, void* stream) {
+  using namespace afq;
+  if (!a || !b || !d || !status || M < 1 || N < 1 || K < 1 || nterms < 1 || nterms > 3) {
+    afq_set_error("afq_test_gemm_f16: bad arguments");
+    return -1;
+  }
+  if (bn != 64 && bn != 128 && bn != 240 && bn != 256) {
+    afq_set_error("afq_test_gemm_f16: bn must be 64, 128, 240 or 256");
+    return -1;
+  }
+  GemmMaps maps;
+  memset(&maps, 0, sizeof(maps));
+  for (int t = 0; t < nterms; ++t) {
+    const char* at = static_cast<const char*>(a) + (size_t)t * a_term_stride * 2;
+    const char* bt = static_cast<const char*>(b) + (size_t)t * b_term_stride * 2;
+    int e = make_tmap_16(&maps.a[t], at, M, K, lda, 128, bf16 != 0);
+    if (!e) e = make_tmap_16(&maps.b[t], bt, N, K, ldb, bn, bf16 != 0);
+    if (e) return e;
+  }
+  EpiStoreF32::Params ep{d, M, N, (long)N};
+  const int kt = (K + 63) / 64, mt = (M + 127) / 128, nt = (N + bn - 1) / bn;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  switch (bn) {
+    case 64: return launch_gemm<64, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
+    case 128: return launch_gemm<128, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
+    case 240: return launch_gemm<240, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
+    default: return launch_gemm<256, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
+  }
+}

@@ -1,0 +1,30 @@
+/*
+ * afqmc_gb300_testing.h - test hooks of libafqmc_gb300.so.
+ *
+ * These entry points have no counterpart in the reference: they expose single kernels of
+ * the mixed-precision path so that tests can compare each one with a PyTorch FP32
+ * computation of the same operation. Same conventions as afqmc_gb300.h (device pointers,
+ * stream-ordered, 0 on success, afq_last_error() on failure).
+ */
+#ifndef AFQMC_GB300_TESTING_H
+#define AFQMC_GB300_TESTING_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* D[M,N] (fp32, row-major) = sum_{t < nterms} A_t[M,K] * B_t[N,K]^T on the tcgen05 tensor
+ * cores. A_t = a + t*a_term_stride, B_t = b + t*b_term_stride (elements); rows of A and B
+ * are K-major with leading dimensions lda/ldb (multiples of 8). bf16 != 0: bfloat16 inputs,
+ * else float16. bn: output tile width (64, 128, 240 or 256). *status (device int) becomes
+ * nonzero if a pipeline wait timed out. */
+int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stride,
+                      long b_term_stride, float* d, int M, int N, int K, int lda, int ldb,
+                      int bf16, int bn, int* status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
