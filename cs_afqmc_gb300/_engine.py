@@ -84,7 +84,7 @@ class Engine:
 
     def __init__(self, *, norb: int, nelec, nchol: int, n_walkers: int, restricted: bool,
                  uhf: bool, precision: int, dt: float, n_exp_terms: int, n_batch: int,
-                 arrays: dict, h0: float, h0_prop: complex):
+                 arrays: dict, h0: float, h0_prop: complex, mixed_config: int = 0):
         self.lib = _lib.load()
         self.norb, self.nelec, self.nchol, self.nw = norb, tuple(nelec), nchol, n_walkers
         self.restricted, self.uhf, self.precision = restricted, uhf, precision
@@ -92,7 +92,8 @@ class Engine:
         d = _lib.Dims(norb=norb, n_up=nelec[0], n_dn=nelec[1], nchol=nchol, n_walkers=n_walkers,
                       walker_type=_lib.AFQ_WALKERS_RESTRICTED if restricted else _lib.AFQ_WALKERS_UNRESTRICTED,
                       trial_type=_lib.AFQ_TRIAL_UHF if uhf else _lib.AFQ_TRIAL_RHF,
-                      precision=precision, n_exp_terms=n_exp_terms, n_batch=n_batch, dt=dt)
+                      precision=precision, n_exp_terms=n_exp_terms, n_batch=n_batch,
+                      mixed_config=int(mixed_config), dt=dt)
         self.dims = d
         nbytes = self.lib.afq_workspace_size(ctypes.byref(d))
         if nbytes == 0:
@@ -132,7 +133,8 @@ def _zeros(n, dtype=torch.float64):
 
 
 def engine_for(trial, ham_data: Optional[dict], wave_data: dict, walkers, *, dt: float = 1.0,
-               n_exp_terms: int = 6, n_batch: int = 1, need_propagation: bool = False) -> Engine:
+               n_exp_terms: int = 6, n_batch: int = 1, need_propagation: bool = False,
+               mixed_config: int = 0) -> Engine:
     """Find or build the engine for these walkers (shape, dtype) and intermediates."""
     restricted = not isinstance(walkers, (list, tuple))
     w0 = walkers if restricted else walkers[0]
@@ -160,6 +162,7 @@ def engine_for(trial, ham_data: Optional[dict], wave_data: dict, walkers, *, dt:
         return (id(x), x.data_ptr() if isinstance(x, torch.Tensor) else None)
 
     key = (nw, restricted, prec, float(dt) if have_prop else None, n_exp_terms, n_batch,
+           int(mixed_config),
            ident(mo),
            ident(ham_data.get("rot_chol")) if ham_data is not None else None,
            ident(ham_data.get("exp_h1")) if have_prop else None,
@@ -212,7 +215,7 @@ def engine_for(trial, ham_data: Optional[dict], wave_data: dict, walkers, *, dt:
         a.pop("exp_h1_dn", None)
     eng = Engine(norb=norb, nelec=nelec, nchol=nchol, n_walkers=nw, restricted=restricted, uhf=uhf,
                  precision=prec, dt=dt, n_exp_terms=n_exp_terms, n_batch=n_batch, arrays=a, h0=h0,
-                 h0_prop=h0p)
+                 h0_prop=h0p, mixed_config=mixed_config)
     cache[key] = eng
     return eng
 

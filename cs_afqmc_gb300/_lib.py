@@ -30,7 +30,7 @@ class Dims(ctypes.Structure):
         ("nchol", ctypes.c_int32), ("n_walkers", ctypes.c_int32),
         ("walker_type", ctypes.c_int32), ("trial_type", ctypes.c_int32),
         ("precision", ctypes.c_int32), ("n_exp_terms", ctypes.c_int32),
-        ("n_batch", ctypes.c_int32), ("dt", ctypes.c_double),
+        ("n_batch", ctypes.c_int32), ("mixed_config", ctypes.c_int32), ("dt", ctypes.c_double),
     ]
 
 
@@ -69,8 +69,6 @@ _SIGS = {
     "afq_fill_uniform": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, _vp]),
 }
 
-EXPORTED = tuple(_SIGS)
-
 # include/afqmc_gb300_testing.h: single-kernel hooks for the numerics tests
 _TEST_SIGS = {
     "afq_test_gemm_f16": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_long, ctypes.c_long, _vp,
@@ -78,6 +76,8 @@ _TEST_SIGS = {
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]),
 }
 _SIGS.update(_TEST_SIGS)
+
+EXPORTED = tuple(_SIGS)
 
 _lib: Optional[ctypes.CDLL] = None
 

@@ -148,7 +148,8 @@ Sizes sizes_for(const afq_dims* d, const afq_ctx_dev& c, int nw_chunk, int e_chu
   s.wcopy = L->take(nw * c.norb * (c.kslab[0] + c.kslab[1]) * welem);
   s.sr_idx = L->take(nw * sizeof(int32_t));
   s.cum = L->take(nw * sizeof(double));
-  s.tc = L->take(d->precision == AFQ_PREC_MIXED ? afq::tc_workspace_bytes(c, nw_chunk) : 256);
+  s.tc = L->take(d->precision == AFQ_PREC_MIXED ? afq::tc_workspace_bytes(c, nw_chunk, d->mixed_config)
+                                                : 256);
   s.total = L->off;
   return s;
 }
@@ -163,22 +164,24 @@ inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 bool is_fp64(const afq_ctx* c) { return c->d.precision == AFQ_PREC_FP64; }
 
+// Green's function + overlap. FP64: G into c->green. Mixed: the 16-bit operands of the
+// force-bias, energy and exp_h1 contractions (wg) and/or the overlap.
 int green(afq_ctx* c, const void* wu, const void* wd, double2* g, double2* ovl, bool wg, cudaStream_t st) {
   if (is_fp64(c)) return afq::launch_green<double>(c->dev, wu, wd, g, ovl, wg, st);
-  return afq::launch_green<float>(c->dev, wu, wd, g, ovl, wg, st);
+  return afq::tc_green(c->tc, c->dev, wu, wd, ovl, wg, st);
 }
 
 int force_bias_from_green(afq_ctx* c, double2* out, cudaStream_t st) {
   const afq_ctx_dev& d = c->dev;
   double2 alpha = c2(d.energy_mode == 0 ? 2.0 : 1.0, 0.0);
   const double* B = d.nspin_g == 2 ? c->rccat : d.rot_chol[0];
-  if (!is_fp64(c)) return afq::tc_force_bias(c->tc, d, c->green, out, alpha.x, st);
+  if (!is_fp64(c)) return afq::tc_force_bias(c->tc, d, out, st);
   return afq::launch_gemm_cr(false, d.nw, d.nchol, d.ktot, c->green, d.ktot, B, d.ktot, out, d.nchol,
                              alpha, st);
 }
 
 int energy_from_green(afq_ctx* c, double2* out, cudaStream_t st) {
-  if (!is_fp64(c)) return afq::tc_energy(c->tc, c->dev, c->green, c->epart, out, st);
+  if (!is_fp64(c)) return afq::tc_energy(c->tc, c->dev, out, st);
   return afq::launch_energy_f64(c->dev, c->e_chunks, c->e_gchunk, c->green, c->epart, out, st);
 }
 
@@ -197,24 +200,29 @@ int check_state(const afq_ctx* c, const afq_walker_state* s) {
 
 int propagate_impl(afq_ctx* c, afq_walker_state* s, const double* fields, cudaStream_t st) {
   const afq_ctx_dev& d = c->dev;
+  if (!is_fp64(c)) {
+    // mixed: operands -> fused force bias / field shifts -> exp_h1, vhs + Taylor, exp_h1
+    CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, nullptr, true, st));
+    CHECK(afq::tc_field_shifts(c->tc, d, fields, st));
+    CHECK(afq::tc_propagate_walkers(c->tc, d, s->walkers_up, s->walkers_dn, st));
+    CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, c->ovl_new, false, st));
+    return afq::tc_weights(c->tc, d, c->ovl_new, reinterpret_cast<double2*>(s->overlaps), s->weights,
+                           s->scalars, st);
+  }
   CHECK(green(c, s->walkers_up, s->walkers_dn, c->green, nullptr, true, st));
   CHECK(force_bias_from_green(c, c->fb, st));
   CHECK(afq::launch_field_shifts(d, fields, c->fb, c->xt, c->shift, c->fbt, st));
   const int nb = d.nw / c->nw_chunk;
   for (int b = 0; b < nb; ++b) {
     const int w0 = b * c->nw_chunk;
-    if (is_fp64(c)) {
-      double sq = sqrt(d.dt);
-      CHECK(afq::launch_gemm_cr(true, c->nw_chunk, d.norb * d.norb, d.nchol, c->xt + (size_t)w0 * d.nchol,
-                                d.nchol, c->h.chol, (long)d.norb * d.norb, c->vhs, (long)d.norb * d.norb,
-                                c2(0.0, sq), st));
-      CHECK(afq::launch_taylor_f64<double>(d, w0, c->nw_chunk, c->vhs, s->walkers_up, s->walkers_dn, st));
-    } else {
-      CHECK(afq::tc_propagate_chunk(c->tc, d, w0, c->nw_chunk, c->xt, s->walkers_up, s->walkers_dn, st));
-    }
+    double sq = sqrt(d.dt);
+    CHECK(afq::launch_gemm_cr(true, c->nw_chunk, d.norb * d.norb, d.nchol, c->xt + (size_t)w0 * d.nchol,
+                              d.nchol, c->h.chol, (long)d.norb * d.norb, c->vhs, (long)d.norb * d.norb,
+                              c2(0.0, sq), st));
+    CHECK(afq::launch_taylor_f64<double>(d, w0, c->nw_chunk, c->vhs, s->walkers_up, s->walkers_dn, st));
   }
   CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, c->ovl_new, false, st));
-  return afq::launch_weights(d, c->shift, c->fbt, c->ovl_new, reinterpret_cast<double2*>(s->overlaps),
+  return afq::launch_weights(d, c->shift, c->fbt, 1, c->ovl_new, reinterpret_cast<double2*>(s->overlaps),
                              s->weights, s->scalars, st);
 }
 
@@ -333,7 +341,7 @@ int afq_ctx_create(const afq_dims* dims, const afq_hamiltonian* ham, void* works
     }
   }
   if (dims->precision == AFQ_PREC_MIXED) {
-    int e = afq::tc_init(&c->tc, c->dev, *ham, c->rccat, nwc, ws + sz.tc, st);
+    int e = afq::tc_init(&c->tc, c->dev, *ham, c->rccat, nwc, dims->mixed_config, ws + sz.tc, st);
     if (e) {
       delete c;
       return e;

@@ -40,6 +40,27 @@ AFQ_HD double2 cexp_(double2 a) {
   return make_double2(e * cos(a.y), e * sin(a.y));
 }
 
+// float2 complex arithmetic (mixed-precision kernels)
+AFQ_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+AFQ_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+AFQ_HD float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+AFQ_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+AFQ_HD float2 cmulc(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+AFQ_HD float cabs2(float2 a) { return a.x * a.x + a.y * a.y; }
+AFQ_HD float2 cdiv(float2 a, float2 b) {
+  if (fabsf(b.x) >= fabsf(b.y)) {
+    float r = b.y / b.x, den = b.x + b.y * r;
+    return make_float2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+  } else {
+    float r = b.x / b.y, den = b.x * r + b.y;
+    return make_float2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+  }
+}
+
 // walker storage <-> double2
 AFQ_D double2 ld_c(const double2* p) { return *p; }
 AFQ_D double2 ld_c(const float2* p) {

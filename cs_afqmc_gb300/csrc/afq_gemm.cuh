@@ -1,7 +1,11 @@
 // Warp-specialised tcgen05 GEMM core: D[M x N] (fp32, TMEM) = sum_t A_t[M x K] * B_t[N x K]^T
 // over up to three (A_t, B_t) operand pairs (the split-precision hi/lo terms), 16-bit inputs
 // (bf16 or fp16), both operands K-major in global memory, loaded by TMA with the 128-byte
-// swizzle. One 128 x BN output tile per CTA.
+// swizzle. One 128 x bn output tile per CTA; bn (runtime, multiple of 16, <= BNMAX) sets the
+// MMA N, the B box and the epilogue width; BNMAX sizes the shared-memory ring.
+//
+// The A rows of the tile start at a_row0 + 128 * blockIdx.y (a_row0 selects a walker chunk);
+// the epilogue sees the tile origin without a_row0.
 //
 // Warp roles (192 threads): warp 0 lane 0 issues TMA loads into a STAGES-deep ring;
 // warp 1 owns the TMEM allocation and lane 0 issues the MMAs; warps 2..5 run the epilogue
@@ -23,30 +27,30 @@ __host__ __device__ constexpr int gemm_tmem_cols(int bn) {
   return bn <= 32 ? 32 : bn <= 64 ? 64 : bn <= 128 ? 128 : bn <= 256 ? 256 : 512;
 }
 
-template <int BN, int STAGES>
+template <int BNMAX, int STAGES>
 __host__ __device__ constexpr int gemm_pipe_bytes() {
-  return STAGES * (128 * 128 + BN * 128);
+  return STAGES * (128 * 128 + BNMAX * 128);
 }
 
 // Dynamic shared memory for the core: pipeline + 256 B of barriers + epilogue scratch,
 // plus 1 KB of alignment slack.
-template <int BN, int STAGES, class Epi>
+template <int BNMAX, int STAGES, class Epi>
 __host__ __device__ constexpr int gemm_smem_bytes() {
-  return 1024 + gemm_pipe_bytes<BN, STAGES>() + 256 + Epi::kSmemBytes;
+  return 1024 + gemm_pipe_bytes<BNMAX, STAGES>() + 256 + Epi::kSmemBytes;
 }
 
-template <int BN, int STAGES, class Epi>
+template <int BNMAX, int STAGES, class Epi>
 __global__ void __launch_bounds__(kGemmThreads, 1)
-    k_gemm_tc(const __grid_constant__ GemmMaps maps, int nterms, int k_tiles, uint32_t idesc,
-              const __grid_constant__ typename Epi::Params ep, int* status) {
-  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "BN");
+    k_gemm_tc(const __grid_constant__ GemmMaps maps, int nterms, int k_tiles, int bn, int a_row0,
+              uint32_t idesc, const __grid_constant__ typename Epi::Params ep, int* status) {
+  static_assert(BNMAX % 16 == 0 && BNMAX >= 16 && BNMAX <= 256, "BNMAX");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr int A_BYTES = 128 * 128;  // 128 rows x 64 x 16-bit
-  constexpr int B_BYTES = BN * 128;
-  constexpr int STAGE = A_BYTES + B_BYTES;
-  constexpr uint32_t TMEM_COLS = gemm_tmem_cols(BN);
+  constexpr int STAGE = A_BYTES + BNMAX * 128;
+  const uint32_t TMEM_COLS = gemm_tmem_cols(bn);
+  const uint32_t tx_bytes = A_BYTES + bn * 128;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
   uint64_t* empty = full + STAGES;
   uint64_t* accb = empty + STAGES;
@@ -54,7 +58,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   unsigned char* epi_smem = smem + STAGES * STAGE + 256;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * bn;
   const int total = nterms * k_tiles;
 
   if (threadIdx.x == 0) {
@@ -90,8 +94,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
         const int t = it / k_tiles, kt = it % k_tiles;
         unsigned char* sa = smem + s * STAGE;
-        ptx::mbar_expect_tx(&full[s], STAGE);
-        ptx::tma_load_2d(sa, &maps.a[t], &full[s], kt * 64, m0);
+        ptx::mbar_expect_tx(&full[s], tx_bytes);
+        ptx::tma_load_2d(sa, &maps.a[t], &full[s], kt * 64, a_row0 + m0);
         ptx::tma_load_2d(sa + A_BYTES, &maps.b[t], &full[s], kt * 64, n0);
         ++issued;
       }
@@ -123,7 +127,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     const bool got = ptx::mbar_wait(accb, 0);
     ptx::tc_fence_after();
     if (!got) ok = false;
-    Epi::template run<BN>(ep, m0, n0, tmem, q, lane, epi_smem, got);
+    Epi::run(ep, m0, n0, bn, tmem, q, lane, epi_smem, got);
   }
   if (!ok) atomicOr(status, 1);
   ptx::tc_fence_before();
@@ -142,12 +146,11 @@ struct EpiStoreF32 {
     long ldd;
   };
   static constexpr int kSmemBytes = 0;
-  template <int BN>
-  __device__ static void run(const Params& p, int m0, int n0, uint32_t tmem, int q, int lane,
-                             unsigned char*, bool) {
+  __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q,
+                             int lane, unsigned char*, bool) {
     const int row = m0 + q * 32 + lane;
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 16) {
+    for (int c = 0; c < bn; c += 16) {
       float v[16];
       ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c, v);
       ptx::tmem_ld_wait();

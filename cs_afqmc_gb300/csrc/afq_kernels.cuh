@@ -33,7 +33,8 @@ int launch_field_shifts(const afq_ctx_dev& c, const double* fields, const double
 template <typename WT>
 int launch_taylor_f64(const afq_ctx_dev& c, int w0, int nwc, const double2* vhs, void* wu, void* wd,
                       cudaStream_t st);
-int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt,
+// shift / fbt: per-walker partial sums [nw][ntiles] (summed here)
+int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt, int ntiles,
                    const double2* ovl_new, double2* ovl, double* weights, double* scalars,
                    cudaStream_t st);
 int launch_energy_f64(const afq_ctx_dev& c, int nchunks, int gchunk, const double2* green,

@@ -1,0 +1,488 @@
+// Device code of the mixed-precision path: 16-bit operand packing, the Green's function /
+// overlap kernel (FP32 Gauss-Jordan, FP64 log-determinant), GEMM epilogues (fused field
+// shifts, vhs scatter into the Taylor layout, exp_h1 products, exchange/Coulomb energy),
+// the per-walker tcgen05 Taylor kernel, and one-time operand preparation.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "afq_tc.cuh"
+
+namespace afq {
+
+// ---- 16-bit helpers -------------------------------------------------------------------
+
+__device__ __forceinline__ uint16_t f2h(float x, bool bf) {
+  return bf ? __bfloat16_as_ushort(__float2bfloat16_rn(x)) : __half_as_ushort(__float2half_rn(x));
+}
+__device__ __forceinline__ float h2f(uint16_t h, bool bf) {
+  return bf ? __bfloat162float(__ushort_as_bfloat16(h)) : __half2float(__ushort_as_half(h));
+}
+// x ~ hi + lo with both parts 16-bit
+__device__ __forceinline__ void split16(float x, bool bf, uint16_t& hi, uint16_t& lo) {
+  hi = f2h(x, bf);
+  lo = f2h(x - h2f(hi, bf), bf);
+}
+// byte offset of (row r, column k < 64) inside a [rows x 64] 16-bit tile, 128-byte swizzle
+__device__ __forceinline__ uint32_t sw128(int r, int k) {
+  return (uint32_t)(r * 128 + ((((k >> 3) ^ (r & 7)) << 4) | ((k & 7) << 1)));
+}
+// exact power of two 2^-e with 2^-e * amax in (0.5, 1]; 1 for amax == 0
+__device__ __forceinline__ float pow2_scale(float amax) {
+  if (!(amax > 0.0f) || !isfinite(amax)) return 1.0f;
+  int e;
+  frexpf(amax, &e);  // amax = m * 2^e, m in [0.5, 1)
+  return ldexpf(1.0f, -e);
+}
+
+// Plain-data view of the mixed state passed to kernels.
+struct MixedDev {
+  int n, nq, nk, ldfb, ldg, nw, nchol, nslab, nblk, kfb, restricted_square, energy_mode;
+  int o_slab[2], R[2], o_blk[2], Rb[2];
+  int bf16;
+  double h0;
+  const float* trial32[2];
+  const float* rh1_32[2];
+  uint16_t* g_fb[2];
+  uint16_t* gen[2][2];
+  uint16_t* wt[2][2];
+  float* g_inv;
+  double2* ene1;
+};
+
+// ======================================================================================
+// Green's function, overlap and operand packing. One CTA per walker.
+// S_s = C_s^T W_s (FP32), Gauss-Jordan on [S | I] in FP32 with partial pivoting, the
+// determinant kept as FP64 log-modulus and phase. G_s = (W_s S_s^-1)^T (FP32).
+// wavefunctions.py:478-501 (rhf), 658-692 (uhf).
+// ======================================================================================
+
+__global__ void __launch_bounds__(256) k_green_mixed(const MixedDev md, const float2* __restrict__ wu,
+                                                     const float2* __restrict__ wd,
+                                                     double2* __restrict__ ovl, int write_ops) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int w = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, n = md.n;
+  const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
+  const int gtot = md.o_blk[0] + md.o_blk[1];
+  float2* Ws = reinterpret_cast<float2*>(sm);       // [n][omax]
+  float2* Gs = Ws + (size_t)n * omax;                // [gtot][n]
+  float2* Aug = Gs + (size_t)gtot * n;               // [omax][2 omax]
+  float* Cs = reinterpret_cast<float*>(Aug + (size_t)omax * 2 * omax);  // [n][omax]
+  __shared__ double red[32];
+  __shared__ int piv_sh;
+  __shared__ float gmax_sh[32];
+  __shared__ float2 colj[64];
+  double logabs = 0.0;          // thread 0 only
+  double2 phase = c2(1.0, 0.0);  // thread 0 only
+  const bool bf = md.bf16 != 0;
+
+  for (int s = 0; s < md.nslab; ++s) {
+    const int o = md.o_slab[s];
+    const float2* W = (s == 0 ? wu : wd) + (size_t)w * n * o;
+    const float* C = md.trial32[s];
+    for (int i = tid; i < n * o; i += nt) {
+      Ws[i] = W[i];
+      Cs[i] = C[i];
+    }
+    __syncthreads();
+    if (write_ops) {
+      // walker operand for the exp_h1 products: row (w, 2k + c), column p
+      const int R = md.R[s];
+      uint16_t* hi = md.wt[s][0] + (size_t)w * R * md.nk;
+      uint16_t* lo = md.wt[s][1] + (size_t)w * R * md.nk;
+      for (int e = tid; e < 2 * o * n; e += nt) {
+        const int rr = e / n, p = e % n;
+        const float2 v = Ws[p * o + (rr >> 1)];
+        uint16_t h, l;
+        split16((rr & 1) ? v.y : v.x, bf, h, l);
+        hi[(size_t)rr * md.nk + p] = h;
+        lo[(size_t)rr * md.nk + p] = l;
+      }
+    }
+    for (int e = tid; e < o * o; e += nt) {
+      const int i = e / o, k = e % o;
+      float2 a = make_float2(0.f, 0.f);
+      for (int p = 0; p < n; ++p) {
+        const float cv = Cs[p * o + i];
+        const float2 wv = Ws[p * o + k];
+        a.x = fmaf(cv, wv.x, a.x);
+        a.y = fmaf(cv, wv.y, a.y);
+      }
+      Aug[i * 2 * o + k] = a;
+      Aug[i * 2 * o + o + k] = make_float2(i == k ? 1.f : 0.f, 0.f);
+    }
+    __syncthreads();
+    for (int j = 0; j < o; ++j) {
+      if (tid < 32) {
+        float best = -1.f;
+        int bi = j;
+        for (int r = j + tid; r < o; r += 32) {
+          const float2 v = Aug[r * 2 * o + j];
+          const float m = fabsf(v.x) + fabsf(v.y);
+          if (m > best) { best = m; bi = r; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+          const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (tid == 0) piv_sh = bi;
+      }
+      __syncthreads();
+      const int pr = piv_sh;
+      if (pr != j)
+        for (int e = tid; e < 2 * o; e += nt) {
+          const float2 t = Aug[j * 2 * o + e];
+          Aug[j * 2 * o + e] = Aug[pr * 2 * o + e];
+          Aug[pr * 2 * o + e] = t;
+        }
+      __syncthreads();
+      const float2 pv = Aug[j * 2 * o + j];
+      if (tid == 0) {
+        const double m = hypot((double)pv.x, (double)pv.y);
+        logabs += log(m);
+        double2 u = c2(pv.x / m, pv.y / m);
+        if (pr != j) u = c2(-u.x, -u.y);
+        phase = cmul(phase, u);
+      }
+      const float2 inv = cdiv(make_float2(1.f, 0.f), pv);
+      __syncthreads();
+      for (int e = tid; e < 2 * o; e += nt) Aug[j * 2 * o + e] = cmul(Aug[j * 2 * o + e], inv);
+      // snapshot the multipliers (column j) before any thread overwrites them
+      for (int r = tid; r < o; r += nt) colj[r] = Aug[r * 2 * o + j];
+      __syncthreads();
+      for (int e = tid; e < o * 2 * o; e += nt) {
+        const int r = e / (2 * o), col = e % (2 * o);
+        if (r == j) continue;
+        Aug[e] = csub(Aug[e], cmul(colj[r], Aug[j * 2 * o + col]));
+      }
+      __syncthreads();
+    }
+    if (write_ops) {
+      const int b = md.nblk == 2 ? s : 0;
+      float2* Gb = Gs + (size_t)(b == 0 ? 0 : md.o_blk[0]) * n;
+      for (int e = tid; e < o * n; e += nt) {
+        const int i = e / n, p = e % n;
+        float2 a = make_float2(0.f, 0.f);
+        for (int k = 0; k < o; ++k) a = cadd(a, cmul(Ws[p * o + k], Aug[k * 2 * o + o + i]));
+        if (md.nblk == 1 && s == 1) a = cadd(a, Gb[e]);  // RHF two slabs: G_up + G_dn
+        Gb[e] = a;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && ovl) {
+    double la = logabs;
+    double2 ph = phase;
+    if (md.restricted_square) {
+      la *= 2.0;
+      ph = cmul(ph, ph);
+    }
+    const double m = exp(la);
+    ovl[w] = c2(m * ph.x, m * ph.y);
+  }
+  if (!write_ops) return;
+  // ---- scale, pack, ene1
+  float mx = 0.f;
+  for (int e = tid; e < gtot * n; e += nt) mx = fmaxf(mx, fmaxf(fabsf(Gs[e].x), fabsf(Gs[e].y)));
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((tid & 31) == 0) gmax_sh[tid >> 5] = mx;
+  __syncthreads();
+  if (tid < 32) {
+    float v = tid < (nt >> 5) ? gmax_sh[tid] : 0.f;
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (tid == 0) gmax_sh[0] = v;
+  }
+  __syncthreads();
+  const float scl = pow2_scale(gmax_sh[0]);
+  if (tid == 0) md.g_inv[w] = 1.0f / scl;
+  double e1x = 0.0, e1y = 0.0;
+  for (int e = tid; e < gtot * n; e += nt) {
+    const float2 g = Gs[e];
+    // force-bias operand: rows (2w, 2w+1), column e
+    uint16_t h, l;
+    split16(g.x * scl, bf, h, l);
+    md.g_fb[0][(size_t)(2 * w) * md.ldfb + e] = h;
+    md.g_fb[1][(size_t)(2 * w) * md.ldfb + e] = l;
+    split16(g.y * scl, bf, h, l);
+    md.g_fb[0][(size_t)(2 * w + 1) * md.ldfb + e] = h;
+    md.g_fb[1][(size_t)(2 * w + 1) * md.ldfb + e] = l;
+    // energy operand of block b: row (w, 2k + c), column p
+    const int b = (md.nblk == 2 && e >= md.o_blk[0] * n) ? 1 : 0;
+    const int eb = e - b * md.o_blk[0] * n;
+    const int k = eb / n, p = eb % n;
+    const size_t row = (size_t)w * md.Rb[b] + 2 * k;
+    split16(g.x * scl, bf, h, l);
+    md.gen[b][0][row * md.nk + p] = h;
+    md.gen[b][1][row * md.nk + p] = l;
+    split16(g.y * scl, bf, h, l);
+    md.gen[b][0][(row + 1) * md.nk + p] = h;
+    md.gen[b][1][(row + 1) * md.nk + p] = l;
+    const float r1 = md.rh1_32[b][eb];
+    e1x += (double)(g.x * r1);
+    e1y += (double)(g.y * r1);
+  }
+  e1x = block_sum(e1x, red);
+  e1y = block_sum(e1y, red);
+  if (tid == 0) md.ene1[w] = c2(e1x, e1y);
+}
+
+// ======================================================================================
+// Force-bias GEMM epilogue: rows (w, re/im) of fb = alpha * G . rot_chol^T, fused with the
+// field shifts of propagation.py:121-127 (writes the shifted-field operand and per-tile
+// partial sums of shift_term and fb_term), or, for calc_force_bias, the plain force bias.
+// ======================================================================================
+
+struct EpiFB {
+  struct Params {
+    const double* fields;
+    const double2* mf;
+    const float* rc_inv;
+    const float* g_inv;
+    float alpha, sqdt;
+    int nw, nchol, ldg, ntiles, bf16;
+    uint16_t* xt_hi;
+    uint16_t* xt_lo;
+    double2* part_shift;
+    double2* part_fbt;
+    double2* fb_out;  // non-null: write the force bias instead
+  };
+  static constexpr int kSmemBytes = 0;
+  __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
+                             unsigned char*, bool) {
+    const int R = m0 + q * 32 + lane, w = R >> 1, c = R & 1;
+    const bool valid = w < p.nw;
+    const float gi = valid ? p.g_inv[w] : 0.f;
+    const bool bf = p.bf16 != 0;
+    float shx = 0.f, shy = 0.f, fbx = 0.f, fby = 0.f;
+#pragma unroll 1
+    for (int c0 = 0; c0 < bn; c0 += 16) {
+      float v[16];
+      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
+      ptx::tmem_ld_wait();
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int g = n0 + c0 + j;
+        const bool gv = g < p.nchol;
+        const float val = v[j] * p.alpha * gi * (gv ? p.rc_inv[g] : 0.f);
+        const float other = __shfl_xor_sync(0xffffffffu, val, 1);
+        if (!valid || !gv) continue;
+        const float fr = c ? other : val, fi = c ? val : other;
+        if (p.fb_out) {
+          if (c == 0) p.fb_out[(size_t)w * p.nchol + g] = c2(fr, fi);
+          continue;
+        }
+        const double2 mfd = p.mf[g];
+        const float mfr = (float)mfd.x, mfi = (float)mfd.y;
+        const float sr = -p.sqdt * (-fi - mfr), si = -p.sqdt * (fr - mfi);
+        const float x = (float)p.fields[(size_t)w * p.nchol + g];
+        const float xtr = x - sr, xti = -si;
+        uint16_t h, l;
+        split16(c ? xti : xtr, bf, h, l);
+        p.xt_hi[(size_t)R * p.ldg + g] = h;
+        p.xt_lo[(size_t)R * p.ldg + g] = l;
+        if (c == 0) {
+          shx += xtr * mfr - xti * mfi;
+          shy += xtr * mfi + xti * mfr;
+          fbx += x * sr - 0.5f * (sr * sr - si * si);
+          fby += x * si - sr * si;
+        }
+      }
+    }
+    if (valid && c == 0 && !p.fb_out) {
+      p.part_shift[(size_t)w * p.ntiles + blockIdx.x] = c2(shx, shy);
+      p.part_fbt[(size_t)w * p.ntiles + blockIdx.x] = c2(fbx, fby);
+    }
+  }
+};
+
+// ======================================================================================
+// vhs GEMM epilogue (propagation.py:265-271): rows (w, re/im) of xt . chol give
+// V = i sqrt(dt) xt . chol = sqrt(dt) (-(xt_i.L) + i (xt_r.L)); write the Taylor A operand
+// [Vr | Vi] (hi and lo) for each walker of the chunk. Columns are (p, q) with q padded to nq.
+// ======================================================================================
+
+struct EpiVHS {
+  struct Params {
+    uint16_t* v_hi;
+    uint16_t* v_lo;
+    int n, nq, rows, bf16, want_lo;
+    float sqdt;
+  };
+  static constexpr int kSmemBytes = 0;
+  __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
+                             unsigned char*, bool) {
+    const int R = m0 + q * 32 + lane, wl = R >> 1, c = R & 1;
+    const bool bf = p.bf16 != 0;
+    const float scale = c == 0 ? p.sqdt : -p.sqdt;
+#pragma unroll 1
+    for (int c0 = 0; c0 < bn; c0 += 16) {
+      float v[16];
+      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
+      ptx::tmem_ld_wait();
+      const int col = n0 + c0, pr = col / p.nq, q0 = col % p.nq;
+      if (R >= p.rows || pr >= p.n) continue;
+      const size_t off = ((size_t)wl * 128 + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0;
+      uint32_t hw[8], lw[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        uint16_t h0, l0, h1, l1;
+        split16(v[2 * j] * scale, bf, h0, l0);
+        split16(v[2 * j + 1] * scale, bf, h1, l1);
+        hw[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lw[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+      }
+      uint4* dh = reinterpret_cast<uint4*>(p.v_hi + off);
+      dh[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      dh[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+      if (p.want_lo) {
+        uint4* dl = reinterpret_cast<uint4*>(p.v_lo + off);
+        dl[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        dl[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+      }
+    }
+  }
+};
+
+// ======================================================================================
+// exp_h1 products: D[p][(w, 2k + c)] = ((E - I) X)[p][k].c for the walker (X = W) or the
+// Taylor sum (X = acc). First product: W1 = W + D into the Taylor B operand (hi/lo);
+// last product: W_new = acc + D back into the FP32 walker slab. propagation.py:73, 91.
+// ======================================================================================
+
+struct EpiExp {
+  struct Params {
+    float* w;                 // walker slab [nw][n][o] complex64
+    const uint16_t* acc_hi;   // last product: Taylor sum operand [nw*R][nk]
+    const uint16_t* acc_lo;
+    uint16_t* t0_hi;          // first product: Taylor B operand [nw][NT][2nq]
+    uint16_t* t0_lo;
+    int n, o, R, nk, nq, NT, nw, bf16, last;
+  };
+  static constexpr int kSmemBytes = 0;
+  __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
+                             unsigned char*, bool) {
+    const int pr = m0 + q * 32 + lane;
+    const bool bf = p.bf16 != 0;
+#pragma unroll 1
+    for (int c0 = 0; c0 < bn; c0 += 16) {
+      float v[16];
+      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
+      ptx::tmem_ld_wait();
+      if (pr >= p.n) continue;
+#pragma unroll 4
+      for (int j = 0; j < 16; ++j) {
+        const int col = n0 + c0 + j, w = col / p.R, rr = col % p.R;
+        if (w >= p.nw || rr >= 2 * p.o) continue;
+        const int k = rr >> 1, c = rr & 1;
+        float* wp = p.w + (((size_t)w * p.n + pr) * p.o + k) * 2 + c;
+        if (p.last) {
+          const size_t ai = ((size_t)w * p.R + rr) * p.nk + pr;
+          const float a = h2f(p.acc_hi[ai], bf) + h2f(p.acc_lo[ai], bf);
+          *wp = a + v[j];
+        } else {
+          const float w1 = *wp + v[j];
+          uint16_t h, l, hn, ln;
+          split16(w1, bf, h, l);
+          split16(-w1, bf, hn, ln);
+          const size_t base = (size_t)w * p.NT * 2 * p.nq;
+          const size_t r0 = base + (size_t)(2 * k) * 2 * p.nq, r1 = r0 + 2 * p.nq;
+          if (c == 0) {  // row 2k: [Tr | -Ti], row 2k+1: [Ti | Tr]
+            p.t0_hi[r0 + pr] = h;
+            p.t0_lo[r0 + pr] = l;
+            p.t0_hi[r1 + p.nq + pr] = h;
+            p.t0_lo[r1 + p.nq + pr] = l;
+          } else {
+            p.t0_hi[r0 + p.nq + pr] = hn;
+            p.t0_lo[r0 + p.nq + pr] = ln;
+            p.t0_hi[r1 + pr] = h;
+            p.t0_lo[r1 + pr] = l;
+          }
+        }
+      }
+    }
+  }
+};
+
+// ======================================================================================
+// Energy GEMM epilogue (wavefunctions.py:535-540, 725-741): the tile holds
+// f_g[i][k] = (rot_chol_g G^T)[i][k] for gpt values of g (rows g_local*o + i) and wpt walkers
+// (columns w_local*R + 2k + re/im). Per (g, w): c_g = tr f_g and exc_g = sum_ik f_ik f_ki.
+// Writes c[w][g] and the tile's partial sum of exc per walker.
+// ======================================================================================
+
+struct EpiEnergy {
+  struct Params {
+    const float* ren_inv;
+    const float* g_inv;
+    int o, R, gpt, nchol, nw, mt;
+    double2* c_out;     // [nw][nchol]
+    double2* exc_part;  // [nw][mt]
+  };
+  static constexpr int kCols = 241;
+  static constexpr int kMaxPairs = 256;  // gpt * wpt
+  static constexpr int kMaxWpt = 32;
+  static constexpr int kSmemBytes = 128 * kCols * 4 + kMaxPairs * 8 + kMaxWpt * 16;
+  __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
+                             unsigned char* smem, bool) {
+    float* F = reinterpret_cast<float*>(smem);
+    float2* cs = reinterpret_cast<float2*>(F + 128 * kCols);  // [kMaxPairs]
+    double* exx = reinterpret_cast<double*>(cs + kMaxPairs);  // [kMaxWpt] re, then im
+    double* exy = exx + kMaxWpt;
+    const int t = q * 32 + lane;  // 0..127 (lane quadrant order)
+    const int r = t;
+    const int wpt = bn / p.R;
+    const int tile_m = m0 / 128;
+    const int g0 = tile_m * p.gpt;
+    const int gcount = min(p.gpt, p.nchol - g0);
+    const int w0 = n0 / p.R;
+#pragma unroll 1
+    for (int c0 = 0; c0 < bn; c0 += 16) {
+      float v[16];
+      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
+      ptx::tmem_ld_wait();
+#pragma unroll
+      for (int j = 0; j < 16; ++j) F[r * kCols + c0 + j] = v[j];
+    }
+    for (int i = t; i < kMaxPairs; i += 128) cs[i] = make_float2(0.f, 0.f);
+    for (int i = t; i < kMaxWpt; i += 128) {
+      exx[i] = 0.0;
+      exy[i] = 0.0;
+    }
+    ptx::named_bar_sync(1, 128);
+    // items (g_local, w_local, i)
+    const int npair = gcount * wpt;
+    for (int it = t; it < npair * p.o; it += 128) {
+      const int pi = it / p.o, i = it % p.o;
+      const int gl = pi / wpt, wl = pi % wpt;
+      const float* Fi = F + (gl * p.o + i) * kCols + wl * p.R;
+      float ex = 0.f, ey = 0.f;
+      for (int k = 0; k < p.o; ++k) {
+        const float* Fk = F + (gl * p.o + k) * kCols + wl * p.R;
+        const float ar = Fi[2 * k], ai = Fi[2 * k + 1];
+        const float br = Fk[2 * i], bi = Fk[2 * i + 1];
+        ex = fmaf(ar, br, fmaf(-ai, bi, ex));
+        ey = fmaf(ar, bi, fmaf(ai, br, ey));
+      }
+      atomicAdd(&cs[pi].x, Fi[2 * i]);
+      atomicAdd(&cs[pi].y, Fi[2 * i + 1]);
+      const int wglob = w0 + wl;
+      const float s = (wglob < p.nw) ? p.ren_inv[g0 + gl] * p.g_inv[wglob] : 0.f;
+      atomicAdd(&exx[wl], (double)(ex * s * s));
+      atomicAdd(&exy[wl], (double)(ey * s * s));
+    }
+    ptx::named_bar_sync(1, 128);
+    for (int pi = t; pi < npair; pi += 128) {
+      const int gl = pi / wpt, wl = pi % wpt, wg = w0 + wl, g = g0 + gl;
+      if (wg < p.nw) {
+        const float s = p.ren_inv[g] * p.g_inv[wg];
+        p.c_out[(size_t)wg * p.nchol + g] = c2(cs[pi].x * s, cs[pi].y * s);
+      }
+    }
+    for (int wl = t; wl < wpt; wl += 128) {
+      const int wg = w0 + wl;
+      if (wg < p.nw) p.exc_part[(size_t)wg * p.mt + tile_m] = c2(exx[wl], exy[wl]);
+    }
+  }
+};
+
+}  // namespace afq

@@ -30,6 +30,7 @@ __global__ void k_green_overlap(const afq_ctx_dev c, const WT* __restrict__ w_up
   __shared__ double red[32];
   __shared__ int piv_sh;
   __shared__ double2 det_sh;
+  __shared__ double2 colj[64];
   // smem: W [norb][kmax] double2, Aug [o][2o] double2, C [norb][kmax] double
   double2* Ws = reinterpret_cast<double2*>(smem_raw);
   double2* Aug = Ws + (size_t)norb * c.kmax;
@@ -97,12 +98,13 @@ __global__ void k_green_overlap(const afq_ctx_dev c, const WT* __restrict__ w_up
       const double2 inv = cdiv(c2(1.0, 0.0), pv);
       __syncthreads();
       for (int e = tid; e < 2 * o; e += nt) Aug[j * 2 * o + e] = cmul(Aug[j * 2 * o + e], inv);
+      // snapshot the multipliers (column j) before any thread overwrites them
+      for (int r = tid; r < o; r += nt) colj[r] = Aug[r * 2 * o + j];
       __syncthreads();
       for (int e = tid; e < o * 2 * o; e += nt) {
         int r = e / (2 * o), col = e % (2 * o);
         if (r == j) continue;
-        double2 f = Aug[r * 2 * o + j];
-        Aug[e] = csub(Aug[e], cmul(f, Aug[j * 2 * o + col]));
+        Aug[e] = csub(Aug[e], cmul(colj[r], Aug[j * 2 * o + col]));
       }
       __syncthreads();
     }
@@ -320,16 +322,20 @@ __global__ void __launch_bounds__(256) k_taylor_f64(const afq_ctx_dev c, int w0,
 // ======================================================================================
 
 __global__ void k_weights(int nw, double dt, double2 h0_prop, const double2* __restrict__ shift,
-                          const double2* __restrict__ fbt, const double2* __restrict__ ovl_new,
-                          double2* __restrict__ ovl, double* __restrict__ weights,
-                          double* __restrict__ scalars) {
+                          const double2* __restrict__ fbt, int ntiles,
+                          const double2* __restrict__ ovl_new, double2* __restrict__ ovl,
+                          double* __restrict__ weights, double* __restrict__ scalars) {
   __shared__ double red[32];
   const double sqdt = sqrt(dt);
   const double pcs = scalars[AFQ_S_POP_CONTROL_SHIFT];
   double sum = 0.0;
   for (int w = threadIdx.x; w < nw; w += blockDim.x) {
     double2 ratio = cdiv(ovl_new[w], ovl[w]);
-    double2 sh = shift[w], fb = fbt[w];
+    double2 sh = c2(0, 0), fb = c2(0, 0);
+    for (int t = 0; t < ntiles; ++t) {
+      sh = cadd(sh, shift[(size_t)w * ntiles + t]);
+      fb = cadd(fb, fbt[(size_t)w * ntiles + t]);
+    }
     double2 arg = c2(-sqdt * sh.x + fb.x + dt * (pcs + h0_prop.x),
                      -sqdt * sh.y + fb.y + dt * h0_prop.y);
     double2 imp = cmul(cexp_(arg), ratio);
@@ -460,71 +466,91 @@ __global__ void k_energy_final(const afq_ctx_dev c, int nchunks, const double2* 
 }
 
 // ======================================================================================
-// Householder QR, FP64, LAPACK zgeqr2 + zung2r conventions (R has a real diagonal,
+// Householder QR, LAPACK zgeqr2 + zung2r conventions (R has a real diagonal,
 // beta = -sign(Re alpha) * |(alpha, x)|). One CTA per (walker, slab). Q overwrites W.
+// Arithmetic in the walker's precision (FP64 for complex128 walkers, FP32 for complex64).
 // linalg_utils.py:51-65 (jnp.linalg.qr, reduced mode).
 // ======================================================================================
+
+template <typename CT> struct QrT;
+template <> struct QrT<double2> {
+  using R = double;
+  AFQ_D static double2 mk(double a, double b) { return make_double2(a, b); }
+};
+template <> struct QrT<float2> {
+  using R = float;
+  AFQ_D static float2 mk(float a, float b) { return make_float2(a, b); }
+};
+
+AFQ_D float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+AFQ_D double warp_sum_t(double v) { return warp_sum(v); }
+AFQ_D float warp_sum_t(float v) { return warp_sumf(v); }
 
 template <typename WT>
 __global__ void __launch_bounds__(256) k_qr_householder(const afq_ctx_dev c, WT* __restrict__ w_up,
                                                         WT* __restrict__ w_dn) {
-  using CT = typename CplxOf<WT>::type;
+  using CT = typename CplxOf<WT>::type;  // compute in the storage precision
+  using R = typename QrT<CT>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int wlk = blockIdx.x, s = blockIdx.y;
   const int m = c.norb, k = c.kslab[s];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5,
             nwarp = nt >> 5;
-  double2* A = reinterpret_cast<double2*>(smem_raw);  // [m][k]
-  double2* y = A + (size_t)m * k;                      // [k]
-  double2* tau = y + k;                                // [k]
+  CT* A = reinterpret_cast<CT*>(smem_raw);  // [m][k]
+  CT* y = A + (size_t)m * k;                // [k]
+  CT* tau = y + k;                          // [k]
   __shared__ double red[32];
-  __shared__ double2 sc_sh, beta_sh;
+  __shared__ CT sc_sh, beta_sh;
   CT* W = reinterpret_cast<CT*>(s == 0 ? w_up : w_dn) + (size_t)wlk * m * k;
-  for (int i = tid; i < m * k; i += nt) A[i] = ld_c(W + i);
+  for (int i = tid; i < m * k; i += nt) A[i] = W[i];
   __syncthreads();
   // ---- factorisation
   for (int j = 0; j < k; ++j) {
-    double xn = 0.0;
-    for (int r = j + 1 + tid; r < m; r += nt) xn += cabs2(A[r * k + j]);
-    xn = block_sum(xn, red);
+    double xnd = 0.0;
+    for (int r = j + 1 + tid; r < m; r += nt) xnd += (double)cabs2(A[r * k + j]);
+    xnd = block_sum(xnd, red);
     if (tid == 0) {
-      double2 alpha = A[j * k + j];
-      double xnorm = sqrt(xn);
-      if (xnorm == 0.0 && alpha.y == 0.0) {
-        tau[j] = c2(0, 0);
+      const CT alpha = A[j * k + j];
+      const R xn = (R)xnd;
+      if (xn == (R)0 && alpha.y == (R)0) {
+        tau[j] = QrT<CT>::mk(0, 0);
         beta_sh = alpha;
-        sc_sh = c2(1.0, 0.0);
+        sc_sh = QrT<CT>::mk(1, 0);
       } else {
-        double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn);
-        double beta = (alpha.x >= 0.0) ? -nrm : nrm;
-        tau[j] = c2((beta - alpha.x) / beta, -alpha.y / beta);
-        sc_sh = cdiv(c2(1.0, 0.0), csub(alpha, c2(beta, 0.0)));
-        beta_sh = c2(beta, 0.0);
+        const R nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn);
+        const R beta = (alpha.x >= (R)0) ? -nrm : nrm;
+        tau[j] = QrT<CT>::mk((beta - alpha.x) / beta, -alpha.y / beta);
+        sc_sh = cdiv(QrT<CT>::mk(1, 0), csub(alpha, QrT<CT>::mk(beta, 0)));
+        beta_sh = QrT<CT>::mk(beta, 0);
       }
     }
     __syncthreads();
-    const double2 scl = sc_sh;
+    const CT scl = sc_sh;
     for (int r = j + 1 + tid; r < m; r += nt) A[r * k + j] = cmul(A[r * k + j], scl);
-    if (tid == 0) A[j * k + j] = c2(1.0, 0.0);
+    if (tid == 0) A[j * k + j] = QrT<CT>::mk(1, 0);
     __syncthreads();
     // y[col] = sum_r conj(v[r]) A[r][col], col > j ; then A -= conj(tau) v y
     for (int col = j + 1 + wid; col < k; col += nwarp) {
-      double yx = 0, yy = 0;
+      R yx = 0, yy = 0;
       for (int r = j + lane; r < m; r += 32) {
-        double2 p = cmulc(A[r * k + col], A[r * k + j]);  // A[r][col] * conj(v[r])
-        yx += p.x;
-        yy += p.y;
+        const CT pr = cmulc(A[r * k + col], A[r * k + j]);
+        yx += pr.x;
+        yy += pr.y;
       }
-      yx = warp_sum(yx);
-      yy = warp_sum(yy);
-      if (lane == 0) y[col] = c2(yx, yy);
+      yx = warp_sum_t(yx);
+      yy = warp_sum_t(yy);
+      if (lane == 0) y[col] = QrT<CT>::mk(yx, yy);
     }
     __syncthreads();
-    const double2 ct = cconj(tau[j]);
+    const CT ct = cconj(tau[j]);
     const int ncol = k - j - 1;
     if (ncol > 0) {
       for (int e = tid; e < (m - j) * ncol; e += nt) {
-        int r = j + e / ncol, col = j + 1 + e % ncol;
+        const int r = j + e / ncol, col = j + 1 + e % ncol;
         A[r * k + col] = csub(A[r * k + col], cmul(ct, cmul(A[r * k + j], y[col])));
       }
     }
@@ -535,36 +561,36 @@ __global__ void __launch_bounds__(256) k_qr_householder(const afq_ctx_dev c, WT*
   // ---- form Q (zung2r): columns from last to first
   for (int j = k - 1; j >= 0; --j) {
     if (j < k - 1) {
-      if (tid == 0) A[j * k + j] = c2(1.0, 0.0);
+      if (tid == 0) A[j * k + j] = QrT<CT>::mk(1, 0);
       __syncthreads();
       for (int col = j + 1 + wid; col < k; col += nwarp) {
-        double yx = 0, yy = 0;
+        R yx = 0, yy = 0;
         for (int r = j + lane; r < m; r += 32) {
-          double2 p = cmulc(A[r * k + col], A[r * k + j]);
-          yx += p.x;
-          yy += p.y;
+          const CT pr = cmulc(A[r * k + col], A[r * k + j]);
+          yx += pr.x;
+          yy += pr.y;
         }
-        yx = warp_sum(yx);
-        yy = warp_sum(yy);
-        if (lane == 0) y[col] = c2(yx, yy);
+        yx = warp_sum_t(yx);
+        yy = warp_sum_t(yy);
+        if (lane == 0) y[col] = QrT<CT>::mk(yx, yy);
       }
       __syncthreads();
-      const double2 t = tau[j];
+      const CT t = tau[j];
       const int ncol = k - j - 1;
       for (int e = tid; e < (m - j) * ncol; e += nt) {
-        int r = j + e / ncol, col = j + 1 + e % ncol;
+        const int r = j + e / ncol, col = j + 1 + e % ncol;
         A[r * k + col] = csub(A[r * k + col], cmul(t, cmul(A[r * k + j], y[col])));
       }
       __syncthreads();
     }
-    const double2 t = tau[j];
-    const double2 mt = c2(-t.x, -t.y);
+    const CT t = tau[j];
+    const CT mt = QrT<CT>::mk(-t.x, -t.y);
     for (int r = j + 1 + tid; r < m; r += nt) A[r * k + j] = cmul(mt, A[r * k + j]);
-    if (tid == 0) A[j * k + j] = c2(1.0 - t.x, -t.y);
-    for (int r = tid; r < j; r += nt) A[r * k + j] = c2(0, 0);
+    if (tid == 0) A[j * k + j] = QrT<CT>::mk(1 - t.x, -t.y);
+    for (int r = tid; r < j; r += nt) A[r * k + j] = QrT<CT>::mk(0, 0);
     __syncthreads();
   }
-  for (int i = tid; i < m * k; i += nt) st_c(W + i, A[i]);
+  for (int i = tid; i < m * k; i += nt) W[i] = A[i];
 }
 
 // ======================================================================================
@@ -775,11 +801,11 @@ int launch_taylor_f64(const afq_ctx_dev& c, int w0, int nwc, const double2* vhs,
   return launch_err("taylor_f64");
 }
 
-int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt,
+int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt, int ntiles,
                    const double2* ovl_new, double2* ovl, double* weights, double* scalars,
                    cudaStream_t st) {
-  k_weights<<<1, 1024, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt, ovl_new,
-                                ovl, weights, scalars);
+  k_weights<<<1, 1024, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt, ntiles,
+                                ovl_new, ovl, weights, scalars);
   return launch_err("weights");
 }
 
@@ -796,7 +822,7 @@ int launch_energy_f64(const afq_ctx_dev& c, int nchunks, int gchunk, const doubl
 
 template <typename WT>
 int launch_qr(const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
-  size_t smem = ((size_t)c.norb * c.kmax + 2 * c.kmax) * sizeof(double2);
+  size_t smem = ((size_t)c.norb * c.kmax + 2 * c.kmax) * sizeof(typename CplxOf<WT>::type);
   auto kfn = k_qr_householder<WT>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kfn<<<dim3(c.nw, c.nslab), 256, smem, st>>>(c, (WT*)wu, (WT*)wd);

@@ -1,9 +1,9 @@
-// Mixed-precision (16-bit tcgen05) path: tensor maps, GEMM launchers, test hooks.
+// Mixed-precision (16-bit tcgen05) path: tensor maps, workspace layout, one-time operand
+// preparation, the per-walker Taylor kernel, GEMM launches and the test hook.
 #include <stdio.h>
 #include <string.h>
 
-#include "afq_gemm.cuh"
-#include "afq_tc.cuh"
+#include "afq_mixed_kernels.cuh"
 
 namespace afq {
 
@@ -63,35 +63,796 @@ static int launch_check(const char* what) {
   return 0;
 }
 
-template <int BN, int STAGES, class Epi>
+#define TC_CHECK(x)    \
+  do {                 \
+    int _e = (x);      \
+    if (_e) return _e; \
+  } while (0)
+
+template <int BNMAX, int STAGES, class Epi>
 static int launch_gemm(const GemmMaps& maps, int nterms, int k_tiles, int m_tiles, int n_tiles,
-                       bool bf16, const typename Epi::Params& ep, int* status, cudaStream_t st) {
-  constexpr int smem = gemm_smem_bytes<BN, STAGES, Epi>();
-  auto kfn = k_gemm_tc<BN, STAGES, Epi>;
+                       int bn, bool bf16, const typename Epi::Params& ep, int* status,
+                       cudaStream_t st, int a_row0 = 0) {
+  if (bn % 16 || bn < 16 || bn > BNMAX) {
+    afq_set_error("gemm: bn %d invalid", bn);
+    return -1;
+  }
+  constexpr int smem = gemm_smem_bytes<BNMAX, STAGES, Epi>();
+  static_assert(smem <= 232448, "shared memory");
+  auto kfn = k_gemm_tc<BNMAX, STAGES, Epi>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  kfn<<<dim3(n_tiles, m_tiles), kGemmThreads, smem, st>>>(maps, nterms, k_tiles,
-                                                          ptx::idesc_f16(128, BN, bf16 ? 1 : 0), ep,
-                                                          status);
+  kfn<<<dim3(n_tiles, m_tiles), kGemmThreads, smem, st>>>(
+      maps, nterms, k_tiles, bn, a_row0, ptx::idesc_f16(128, bn, bf16 ? 1 : 0), ep, status);
   return launch_check("gemm_tc");
 }
 
-// ---- mixed-precision path (filled in below) -------------------------------------------
+// ======================================================================================
+// Taylor kernel (propagation.py:76-90): per walker slab, T_0 = W1 (B operand from the
+// first exp_h1 product), T_m = V T_{m-1} / m on the tensor cores with V = [Vr | Vi] held in
+// shared memory, acc = sum_m T_m in FP32 registers. The first `split` products use
+// V_hi T_hi + V_hi T_lo + V_lo T_hi. Writes acc as the B operand of the last exp_h1 product.
+// One CTA (4 warps, thread p <-> orbital row p <-> TMEM lane p) per walker.
+// ======================================================================================
 
-static int not_ready() {
-  afq_set_error("mixed precision path is not built yet");
-  return -2;
+struct TaylorDev {
+  int n, o, nq, NT, R, nk, nterms, split, bf16, w0;
+  uint16_t* acc_hi;
+  uint16_t* acc_lo;
+};
+
+static inline size_t taylor_smem(int nq, int NT, bool lo) {
+  const int KT = 2 * nq / 64;
+  return 1024 + (size_t)KT * 128 * 128 * (lo ? 2 : 1) + (size_t)KT * NT * 128 * 2 + 64;
 }
 
-size_t tc_workspace_bytes(const afq_ctx_dev&, int) { return 256; }
-int tc_init(TcState*, const afq_ctx_dev&, const afq_hamiltonian&, const double*, int, char*, cudaStream_t) {
-  return not_ready();
+__global__ void __launch_bounds__(128, 1)
+    k_taylor_tc(const __grid_constant__ CUtensorMap mv_hi, const __grid_constant__ CUtensorMap mv_lo,
+                const __grid_constant__ CUtensorMap mt_hi, const __grid_constant__ CUtensorMap mt_lo,
+                const TaylorDev td, int* status) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int KT = 2 * td.nq / 64;
+  const bool has_lo = td.split > 0;
+  const uint32_t VT = 128 * 128;    // bytes per V k-tile
+  const uint32_t BT = td.NT * 128;  // bytes per B k-tile
+  unsigned char* Vh = smem;
+  unsigned char* Vl = Vh + KT * VT;
+  unsigned char* Bh = Vl + (has_lo ? KT * VT : 0);
+  unsigned char* Bl = Bh + KT * BT;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Bl + KT * BT);
+  uint64_t* ld_bar = bars;
+  uint64_t* mma_bar = bars + 1;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int wl = blockIdx.x, wg = td.w0 + wl;
+  const uint32_t tcols = gemm_tmem_cols(td.NT);
+  const bool bf = td.bf16 != 0;
+  bool ok = true;
+
+  if (tid == 0) {
+    ptx::mbar_init(ld_bar, 1);
+    ptx::mbar_init(mma_bar, 1);
+    ptx::fence_mbar_init();
+  }
+  if (warp == 0) {
+    ptx::tmem_alloc(tmem_holder, tcols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (tid == 0) {
+    const uint32_t bytes = KT * VT * (has_lo ? 2 : 1) + KT * BT * 2;
+    ptx::mbar_expect_tx(ld_bar, bytes);
+    for (int kt = 0; kt < KT; ++kt) {
+      ptx::tma_load_2d(Vh + kt * VT, &mv_hi, ld_bar, kt * 64, wl * 128);
+      if (has_lo) ptx::tma_load_2d(Vl + kt * VT, &mv_lo, ld_bar, kt * 64, wl * 128);
+      ptx::tma_load_2d(Bh + kt * BT, &mt_hi, ld_bar, kt * 64, wg * td.NT);
+      ptx::tma_load_2d(Bl + kt * BT, &mt_lo, ld_bar, kt * 64, wg * td.NT);
+    }
+  }
+  if (!ptx::mbar_wait(ld_bar, 0)) ok = false;
+
+  const int p = tid;
+  const bool prow = p < td.n;
+  const int o2 = 2 * td.o;
+  float acc[64];
+  {
+    const int kt = p / 64, kc = p % 64;
+#pragma unroll
+    for (int r = 0; r < 64; ++r) {
+      if (r < o2 && prow) {
+        const uint32_t off = kt * BT + sw128(r, kc);
+        acc[r] = h2f(*reinterpret_cast<const uint16_t*>(Bh + off), bf) +
+                 h2f(*reinterpret_cast<const uint16_t*>(Bl + off), bf);
+      } else {
+        acc[r] = 0.f;
+      }
+    }
+  }
+  const uint32_t idesc = ptx::idesc_f16(128, td.NT, bf ? 1 : 0);
+  const uint32_t sVh = ptx::smem_u32(Vh), sVl = ptx::smem_u32(Vl), sBh = ptx::smem_u32(Bh),
+                 sBl = ptx::smem_u32(Bl);
+  for (int m = 1; m < td.nterms; ++m) {
+    if (tid == 0 && ok) {
+      ptx::tc_fence_after();
+      uint32_t nmma = 0;
+      const int ngroups = (m <= td.split) ? 3 : 1;
+      for (int gi = 0; gi < ngroups; ++gi) {
+        const uint32_t va = gi == 2 ? sVl : sVh;
+        const uint32_t ba = gi == 1 ? sBl : sBh;
+        for (int kt = 0; kt < KT; ++kt)
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            ptx::mma_f16(tmem, ptx::desc_kmajor_sw128(va + kt * VT + kk * 32),
+                         ptx::desc_kmajor_sw128(ba + kt * BT + kk * 32), idesc, nmma > 0 ? 1u : 0u);
+            ++nmma;
+          }
+      }
+      ptx::mma_commit(mma_bar);
+    }
+    if (ok && !ptx::mbar_wait(mma_bar, (m - 1) & 1)) ok = false;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    ptx::tc_fence_after();
+    float d[64];
+#pragma unroll
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      if (c0 < td.NT) {
+        float v[16];
+        ptx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+        ptx::tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) d[c0 + j] = v[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) d[c0 + j] = 0.f;
+      }
+    }
+    const float invm = 1.0f / (float)m;
+#pragma unroll
+    for (int r = 0; r < 64; ++r) {
+      d[r] = (r < o2) ? d[r] * invm : 0.f;
+      acc[r] += d[r];
+    }
+    if (m + 1 < td.nterms) {
+      const bool lo_next = (m + 1) <= td.split;
+      if (prow) {
+        const int kt0 = p / 64, kc0 = p % 64;                      // K = p
+        const int kt1 = (td.nq + p) / 64, kc1 = (td.nq + p) % 64;  // K = nq + p
+#pragma unroll 4
+        for (int k = 0; k < 32; ++k) {
+          if (k < td.o) {
+            const float tr = d[2 * k], ti = d[2 * k + 1];
+            uint16_t hr, lr, hi_, li, hni, lni;
+            split16(tr, bf, hr, lr);
+            split16(ti, bf, hi_, li);
+            split16(-ti, bf, hni, lni);
+            const uint32_t a0 = kt0 * BT + sw128(2 * k, kc0), a1 = kt1 * BT + sw128(2 * k, kc1);
+            const uint32_t b0 = kt0 * BT + sw128(2 * k + 1, kc0), b1 = kt1 * BT + sw128(2 * k + 1, kc1);
+            *reinterpret_cast<uint16_t*>(Bh + a0) = hr;
+            *reinterpret_cast<uint16_t*>(Bh + a1) = hni;
+            *reinterpret_cast<uint16_t*>(Bh + b0) = hi_;
+            *reinterpret_cast<uint16_t*>(Bh + b1) = hr;
+            if (lo_next) {
+              *reinterpret_cast<uint16_t*>(Bl + a0) = lr;
+              *reinterpret_cast<uint16_t*>(Bl + a1) = lni;
+              *reinterpret_cast<uint16_t*>(Bl + b0) = li;
+              *reinterpret_cast<uint16_t*>(Bl + b1) = lr;
+            }
+          }
+        }
+      }
+      ptx::fence_proxy_async();
+      ptx::tc_fence_before();
+      __syncthreads();
+    }
+  }
+  if (prow) {
+    uint16_t* oh = td.acc_hi + (size_t)wg * td.R * td.nk + p;
+    uint16_t* ol = td.acc_lo + (size_t)wg * td.R * td.nk + p;
+#pragma unroll
+    for (int r = 0; r < 64; ++r) {
+      if (r < o2) {
+        uint16_t h, l;
+        split16(acc[r], bf, h, l);
+        oh[(size_t)r * td.nk] = h;
+        ol[(size_t)r * td.nk] = l;
+      }
+    }
+  }
+  if (!ok) atomicOr(status, 2);
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, tcols);
+  }
 }
-int tc_force_bias(TcState&, const afq_ctx_dev&, const double2*, double2*, double, cudaStream_t) { return not_ready(); }
-int tc_energy(TcState&, const afq_ctx_dev&, const double2*, double2*, double2*, cudaStream_t) { return not_ready(); }
-int tc_propagate_chunk(TcState&, const afq_ctx_dev&, int, int, const double2*, void*, void*, cudaStream_t) {
-  return not_ready();
+
+// ======================================================================================
+// One-time operand preparation
+// ======================================================================================
+
+__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
 }
-int tc_orthonormalize(TcState&, const afq_ctx_dev&, void*, void*, cudaStream_t) { return not_ready(); }
+
+// 2^-e_g with 2^e_g max|src[g][:]| in (0.5, 1]
+__global__ void k_row_scale(const double* __restrict__ src, int len, float* __restrict__ inv) {
+  __shared__ float mx_sh[32];
+  const int g = blockIdx.x;
+  float mx = 0.f;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) mx = fmaxf(mx, fabsf((float)src[(size_t)g * len + i]));
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) mx_sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float v = 0.f;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) v = fmaxf(v, mx_sh[i]);
+    inv[g] = 1.0f / pow2_scale(v);
+  }
+}
+
+// rows g of src [nchol][len] -> dst[g][ld] (hi/lo) scaled by 1/inv[g]
+__global__ void k_prep_rows_scaled(const double* __restrict__ src, int len, int ld, int bf16,
+                                   const float* __restrict__ inv, uint16_t* __restrict__ hi,
+                                   uint16_t* __restrict__ lo) {
+  const int g = blockIdx.x;
+  const double scl = 1.0 / (double)inv[g];
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    uint16_t h, l;
+    split16((float)(src[(size_t)g * len + i] * scl), bf16 != 0, h, l);
+    hi[(size_t)g * ld + i] = h;
+    lo[(size_t)g * ld + i] = l;
+  }
+}
+
+// energy A operand: rot_chol_b [nchol][o][n] -> rows (g / gpt) * 128 + (g % gpt) * o + i
+__global__ void k_prep_ren(const double* __restrict__ rc, int o, int n, int nk, int gpt, int bf16,
+                           const float* __restrict__ inv, uint16_t* __restrict__ hi,
+                           uint16_t* __restrict__ lo) {
+  const int g = blockIdx.x;
+  const double scl = 1.0 / (double)inv[g];
+  const size_t row0 = (size_t)(g / gpt) * 128 + (size_t)(g % gpt) * o;
+  for (int e = threadIdx.x; e < o * n; e += blockDim.x) {
+    const int i = e / n, p = e % n;
+    uint16_t h, l;
+    split16((float)(rc[(size_t)g * o * n + e] * scl), bf16 != 0, h, l);
+    hi[(row0 + i) * nk + p] = h;
+    lo[(row0 + i) * nk + p] = l;
+  }
+}
+
+// vhs B operand: chol [nchol][n*n] -> lop[(p*nq + q)][g], 32x32 tiles through shared memory
+__global__ void k_prep_lop(const double* __restrict__ chol, int nchol, int n, int nq, int ldg, int bf16,
+                           uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
+  __shared__ float tile[32][33];
+  const int pq0 = blockIdx.x * 32, g0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int g = g0 + r, pq = pq0 + tx;
+    tile[r][tx] = (g < nchol && pq < n * n) ? (float)chol[(size_t)g * n * n + pq] : 0.f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int pq = pq0 + r, g = g0 + tx;
+    if (pq < n * n && g < nchol) {
+      const int pp = pq / n, qq = pq % n;
+      uint16_t h, l;
+      split16(tile[tx][r], bf16 != 0, h, l);
+      hi[((size_t)pp * nq + qq) * ldg + g] = h;
+      lo[((size_t)pp * nq + qq) * ldg + g] = l;
+    }
+  }
+}
+
+// exp_h1 A operand: E - I -> [128][nk]
+__global__ void k_prep_eop(const double* __restrict__ e, int n, int nk, int bf16, uint16_t* __restrict__ hi,
+                           uint16_t* __restrict__ lo) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * n; i += gridDim.x * blockDim.x) {
+    const int p = i / n, q = i % n;
+    const double v = e[i] - (p == q ? 1.0 : 0.0);
+    uint16_t h, l;
+    split16((float)v, bf16 != 0, h, l);
+    hi[(size_t)p * nk + q] = h;
+    lo[(size_t)p * nk + q] = l;
+  }
+}
+
+// local energy from c_g and exchange partials (wavefunctions.py:540, 735-741)
+__global__ void k_energy_final_mixed(int nw, int nchol, int nblk, int mt0, int mt1, int mode, double h0,
+                                     const double2* __restrict__ c_out, const double2* __restrict__ exc,
+                                     const double2* __restrict__ ene1, double2* __restrict__ out) {
+  __shared__ double red[32];
+  const int w = blockIdx.x;
+  double a[5][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  const double2* c0 = c_out + (size_t)w * nchol;
+  const double2* c1 = c_out + ((size_t)nw + w) * nchol;
+  for (int g = threadIdx.x; g < nchol; g += blockDim.x) {
+    const double2 u = c0[g];
+    const double2 uu = cmul(u, u);
+    a[0][0] += uu.x;
+    a[0][1] += uu.y;
+    if (nblk == 2) {
+      const double2 d = c1[g];
+      const double2 dd = cmul(d, d), ud = cmul(u, d);
+      a[1][0] += dd.x;
+      a[1][1] += dd.y;
+      a[2][0] += ud.x;
+      a[2][1] += ud.y;
+    }
+  }
+  for (int t = threadIdx.x; t < mt0; t += blockDim.x) {
+    const double2 e = exc[(size_t)w * mt0 + t];
+    a[3][0] += e.x;
+    a[3][1] += e.y;
+  }
+  if (nblk == 2)
+    for (int t = threadIdx.x; t < mt1; t += blockDim.x) {
+      const double2 e = exc[(size_t)nw * mt0 + (size_t)w * mt1 + t];
+      a[4][0] += e.x;
+      a[4][1] += e.y;
+    }
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 2; ++j) a[i][j] = block_sum(a[i][j], red);
+  if (threadIdx.x == 0) {
+    double2 e1 = ene1[w], e2;
+    const double2 s0 = c2(a[0][0], a[0][1]), s1 = c2(a[1][0], a[1][1]), s2 = c2(a[2][0], a[2][1]);
+    const double2 x0 = c2(a[3][0], a[3][1]), x1 = c2(a[4][0], a[4][1]);
+    if (mode == 0) {
+      e2 = csub(cscale(s0, 2.0), x0);
+      e1 = cscale(e1, 2.0);
+    } else if (mode == 1) {
+      e2 = csub(s0, x0);
+    } else {
+      e2 = cscale(csub(cadd(cadd(s0, s1), cscale(s2, 2.0)), cadd(x0, x1)), 0.5);
+    }
+    out[w] = cadd(cadd(e2, e1), c2(h0, 0.0));
+  }
+}
+
+// ======================================================================================
+// host side
+// ======================================================================================
+
+namespace {
+
+struct TcLayout {
+  size_t off = 0;
+  size_t take(size_t b) {
+    size_t o = off;
+    off += (b + 1023) & ~(size_t)1023;
+    return o;
+  }
+};
+
+inline int rup(int x, int m) { return (x + m - 1) / m * m; }
+
+// rows per walker R = 2o rounded to 8, walkers per N tile wpt with R * wpt % 16 == 0,
+// R * wpt <= 256 (and gpt * wpt <= kMaxPairs, wpt <= kMaxWpt for the energy tile)
+void walker_rows(int o, int* R, int* wpt, int gpt = 0) {
+  const int r = rup(2 * o, 8);
+  int w = 256 / r;
+  if (gpt > 0) {
+    if (w > EpiEnergy::kMaxPairs / gpt) w = EpiEnergy::kMaxPairs / gpt;
+    if (w > EpiEnergy::kMaxWpt) w = EpiEnergy::kMaxWpt;
+    if (r * w > 240) w = 240 / r;
+  }
+  if (r % 16) w -= (w & 1);
+  if (w < 1) w = (r % 16) ? 2 : 1;
+  *R = r;
+  *wpt = w;
+}
+
+struct Plan {
+  TcState t;
+  size_t total;
+  size_t o_rc_fb[2], o_rc_inv, o_lop[2], o_eop[2][2], o_ren[2][2], o_ren_inv[2];
+  size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gen[2][2];
+  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_trial32[2], o_rh1[2];
+};
+
+int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
+  TcState& t = P->t;
+  memset(P, 0, sizeof(*P));
+  if (cfg == 0) cfg = kMixedDefault;
+  t.cfg = cfg;
+  t.bf16 = (cfg & kUseBf16) != 0;
+  t.n = c.norb;
+  if (t.n > 128) {
+    afq_set_error("mixed precision path: norb <= 128 (the Taylor operand lives in shared memory)");
+    return -2;
+  }
+  t.nq = t.n <= 64 ? 64 : 128;
+  t.nk = rup(t.n, 8);
+  t.nw = c.nw;
+  t.nwc = nwc;
+  t.nslab = c.nslab;
+  t.nblk = c.nspin_g;
+  t.kfb = c.ktot;
+  t.ldfb = rup(t.kfb, 8);
+  t.ldg = rup(c.nchol, 8);
+  for (int s = 0; s < t.nslab; ++s) {
+    t.o_slab[s] = c.kslab[s];
+    walker_rows(t.o_slab[s], &t.R[s], &t.wpt[s]);
+    t.bn_w[s] = t.R[s] * t.wpt[s];
+    t.NT[s] = rup(2 * t.o_slab[s], 16);
+    if (t.NT[s] > 64) {
+      afq_set_error("mixed precision path: at most 32 electrons per spin");
+      return -2;
+    }
+  }
+  for (int b = 0; b < t.nblk; ++b) {
+    t.o_blk[b] = c.gocc[b];
+    t.gpt[b] = 128 / t.o_blk[b];
+    walker_rows(t.o_blk[b], &t.Rb[b], &t.wptb[b], t.gpt[b]);
+    t.bnb[b] = t.Rb[b] * t.wptb[b];
+    t.mt_en[b] = (c.nchol + t.gpt[b] - 1) / t.gpt[b];
+  }
+  t.fb_bn = c.nchol >= 256 ? 256 : rup(c.nchol, 16);
+  t.fb_ntiles = (c.nchol + t.fb_bn - 1) / t.fb_bn;
+  t.n_fb_terms = 1 + ((cfg & kFbDyn) ? 1 : 0) + ((cfg & kFbStat) ? 1 : 0);
+  t.n_vhs_terms = 1 + ((cfg & kVhsDyn) ? 1 : 0) + ((cfg & kVhsStat) ? 1 : 0);
+  t.n_e_terms = 1 + ((cfg & kExpDyn) ? 1 : 0) + ((cfg & kExpStat) ? 1 : 0);
+  t.n_en_terms = 1 + ((cfg & kEneDyn) ? 1 : 0) + ((cfg & kEneStat) ? 1 : 0);
+  t.taylor_split = (cfg >> kTaylorShift) & 7;
+  TcLayout L;
+  const size_t H = 2;  // bytes per 16-bit element
+  for (int i = 0; i < 2; ++i) P->o_rc_fb[i] = L.take((size_t)c.nchol * t.ldfb * H);
+  P->o_rc_inv = L.take((size_t)c.nchol * 4);
+  for (int i = 0; i < 2; ++i) P->o_lop[i] = L.take((size_t)t.n * t.nq * t.ldg * H);
+  for (int s = 0; s < t.nslab; ++s)
+    for (int i = 0; i < 2; ++i) P->o_eop[s][i] = L.take((size_t)128 * t.nk * H);
+  for (int b = 0; b < t.nblk; ++b) {
+    for (int i = 0; i < 2; ++i) P->o_ren[b][i] = L.take((size_t)t.mt_en[b] * 128 * t.nk * H);
+    P->o_ren_inv[b] = L.take((size_t)c.nchol * 4);
+  }
+  for (int i = 0; i < 2; ++i) P->o_gfb[i] = L.take((size_t)2 * t.nw * t.ldfb * H);
+  for (int i = 0; i < 2; ++i) P->o_xt[i] = L.take((size_t)2 * t.nw * t.ldg * H);
+  for (int i = 0; i < 2; ++i) P->o_vbuf[i] = L.take((size_t)nwc * 128 * 2 * t.nq * H);
+  for (int s = 0; s < t.nslab; ++s)
+    for (int i = 0; i < 2; ++i) {
+      P->o_wt[s][i] = L.take((size_t)t.nw * t.R[s] * t.nk * H);
+      P->o_acc[s][i] = L.take((size_t)t.nw * t.R[s] * t.nk * H);
+      P->o_t0[s][i] = L.take((size_t)t.nw * t.NT[s] * 2 * t.nq * H);
+    }
+  for (int b = 0; b < t.nblk; ++b)
+    for (int i = 0; i < 2; ++i) P->o_gen[b][i] = L.take((size_t)t.nw * t.Rb[b] * t.nk * H);
+  P->o_ginv = L.take((size_t)t.nw * 4);
+  P->o_ene1 = L.take((size_t)t.nw * 16);
+  P->o_pshift = L.take((size_t)t.nw * t.fb_ntiles * 16);
+  P->o_pfbt = L.take((size_t)t.nw * t.fb_ntiles * 16);
+  P->o_cout = L.take((size_t)t.nblk * t.nw * c.nchol * 16);
+  P->o_exc = L.take((size_t)t.nw * (t.mt_en[0] + t.mt_en[1]) * 16);
+  P->o_status = L.take(256);
+  for (int s = 0; s < 2; ++s) P->o_trial32[s] = L.take((size_t)t.n * 64 * 4);
+  for (int b = 0; b < 2; ++b) P->o_rh1[b] = L.take((size_t)t.n * 64 * 4);
+  P->total = L.off + 1024;
+  return 0;
+}
+
+MixedDev mixed_dev(const TcState& t, const afq_ctx_dev& c) {
+  MixedDev m;
+  memset(&m, 0, sizeof(m));
+  m.n = t.n;
+  m.nq = t.nq;
+  m.nk = t.nk;
+  m.ldfb = t.ldfb;
+  m.ldg = t.ldg;
+  m.nw = t.nw;
+  m.nchol = c.nchol;
+  m.nslab = t.nslab;
+  m.nblk = t.nblk;
+  m.kfb = t.kfb;
+  m.restricted_square = c.restricted_square;
+  m.energy_mode = c.energy_mode;
+  m.bf16 = t.bf16 ? 1 : 0;
+  m.h0 = c.h0;
+  for (int s = 0; s < 2; ++s) {
+    m.o_slab[s] = s < t.nslab ? t.o_slab[s] : 0;
+    m.R[s] = t.R[s];
+    m.o_blk[s] = s < t.nblk ? t.o_blk[s] : 0;
+    m.Rb[s] = t.Rb[s];
+    m.trial32[s] = t.trial32[s];
+    m.rh1_32[s] = t.rh1_32[s];
+    m.g_fb[s] = t.g_fb[s];
+    for (int i = 0; i < 2; ++i) {
+      m.gen[s][i] = t.gen[s][i];
+      m.wt[s][i] = t.wt[s][i];
+    }
+  }
+  m.g_inv = t.g_inv;
+  m.ene1 = t.ene1;
+  return m;
+}
+
+}  // namespace
+
+size_t tc_workspace_bytes(const afq_ctx_dev& c, int nwc, int32_t cfg) {
+  Plan P;
+  if (make_plan(c, nwc, cfg, &P)) return 0;
+  return P.total;
+}
+
+int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const double* rccat, int nwc,
+            int32_t cfg, char* ws, cudaStream_t st) {
+  Plan P;
+  TC_CHECK(make_plan(c, nwc, cfg, &P));
+  TcState& t = P.t;
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(ws) + 1023) & ~uintptr_t(1023));
+  auto U = [&](size_t o) { return reinterpret_cast<uint16_t*>(base + o); };
+  for (int i = 0; i < 2; ++i) {
+    t.rc_fb[i] = U(P.o_rc_fb[i]);
+    t.lop[i] = U(P.o_lop[i]);
+    t.g_fb[i] = U(P.o_gfb[i]);
+    t.xt[i] = U(P.o_xt[i]);
+    t.vbuf[i] = U(P.o_vbuf[i]);
+    for (int s = 0; s < t.nslab; ++s) {
+      t.eop[s][i] = U(P.o_eop[s][i]);
+      t.wt[s][i] = U(P.o_wt[s][i]);
+      t.acc[s][i] = U(P.o_acc[s][i]);
+      t.t0[s][i] = U(P.o_t0[s][i]);
+    }
+    for (int b = 0; b < t.nblk; ++b) {
+      t.ren[b][i] = U(P.o_ren[b][i]);
+      t.gen[b][i] = U(P.o_gen[b][i]);
+    }
+  }
+  t.rc_inv = reinterpret_cast<float*>(base + P.o_rc_inv);
+  for (int b = 0; b < t.nblk; ++b) t.ren_inv[b] = reinterpret_cast<float*>(base + P.o_ren_inv[b]);
+  t.g_inv = reinterpret_cast<float*>(base + P.o_ginv);
+  t.ene1 = reinterpret_cast<double2*>(base + P.o_ene1);
+  t.part_shift = reinterpret_cast<double2*>(base + P.o_pshift);
+  t.part_fbt = reinterpret_cast<double2*>(base + P.o_pfbt);
+  t.c_out = reinterpret_cast<double2*>(base + P.o_cout);
+  t.exc_part = reinterpret_cast<double2*>(base + P.o_exc);
+  t.status = reinterpret_cast<int*>(base + P.o_status);
+  for (int s = 0; s < 2; ++s) {
+    t.trial32[s] = reinterpret_cast<float*>(base + P.o_trial32[s]);
+    t.rh1_32[s] = reinterpret_cast<float*>(base + P.o_rh1[s]);
+  }
+  // zero everything once: padding rows and columns of every operand stay zero afterwards
+  cudaError_t e = cudaMemsetAsync(base, 0, P.total - 1024, st);
+  if (e != cudaSuccess) {
+    afq_set_error("memset: %s", cudaGetErrorString(e));
+    return (int)e;
+  }
+  const int bf = t.bf16 ? 1 : 0;
+  for (int s = 0; s < t.nslab; ++s) {
+    k_to_f32<<<64, 256, 0, st>>>(c.trial[s], const_cast<float*>(t.trial32[s]), (long)t.n * t.o_slab[s]);
+    k_prep_eop<<<64, 256, 0, st>>>(c.exp_h1[s], t.n, t.nk, bf, t.eop[s][0], t.eop[s][1]);
+  }
+  for (int b = 0; b < t.nblk; ++b) {
+    k_to_f32<<<64, 256, 0, st>>>(c.rot_h1[b], const_cast<float*>(t.rh1_32[b]), (long)t.n * t.o_blk[b]);
+    k_row_scale<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.o_blk[b] * t.n, t.ren_inv[b]);
+    k_prep_ren<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.o_blk[b], t.n, t.nk, t.gpt[b], bf, t.ren_inv[b],
+                                        t.ren[b][0], t.ren[b][1]);
+  }
+  const double* rcsrc = c.nspin_g == 2 ? rccat : c.rot_chol[0];
+  k_row_scale<<<c.nchol, 256, 0, st>>>(rcsrc, t.kfb, t.rc_inv);
+  k_prep_rows_scaled<<<c.nchol, 256, 0, st>>>(rcsrc, t.kfb, t.ldfb, bf, t.rc_inv, t.rc_fb[0], t.rc_fb[1]);
+  k_prep_lop<<<dim3((t.n * t.n + 31) / 32, (c.nchol + 31) / 32), 256, 0, st>>>(h.chol, c.nchol, t.n, t.nq,
+                                                                             t.ldg, bf, t.lop[0], t.lop[1]);
+  TC_CHECK(launch_check("mixed operand preparation"));
+  // ---- tensor maps
+  const bool b16 = t.bf16;
+  auto mk = [&](CUtensorMap* m, const void* p, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box) {
+    return make_tmap_16(m, p, rows, cols, ld, box, b16);
+  };
+  {  // force bias: A = g_fb (walker-dependent), B = rc_fb (static)
+    int i = 0;
+    TC_CHECK(mk(&t.m_fb.a[i], t.g_fb[0], 2 * t.nw, t.kfb, t.ldfb, 128));
+    TC_CHECK(mk(&t.m_fb.b[i++], t.rc_fb[0], c.nchol, t.kfb, t.ldfb, t.fb_bn));
+    if (t.cfg & kFbDyn) {
+      TC_CHECK(mk(&t.m_fb.a[i], t.g_fb[1], 2 * t.nw, t.kfb, t.ldfb, 128));
+      TC_CHECK(mk(&t.m_fb.b[i++], t.rc_fb[0], c.nchol, t.kfb, t.ldfb, t.fb_bn));
+    }
+    if (t.cfg & kFbStat) {
+      TC_CHECK(mk(&t.m_fb.a[i], t.g_fb[0], 2 * t.nw, t.kfb, t.ldfb, 128));
+      TC_CHECK(mk(&t.m_fb.b[i++], t.rc_fb[1], c.nchol, t.kfb, t.ldfb, t.fb_bn));
+    }
+  }
+  {  // vhs: A = xt (walker-dependent), B = lop (static)
+    int i = 0;
+    const uint64_t nrows = (uint64_t)t.n * t.nq;
+    TC_CHECK(mk(&t.m_vhs.a[i], t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
+    TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[0], nrows, c.nchol, t.ldg, 256));
+    if (t.cfg & kVhsDyn) {
+      TC_CHECK(mk(&t.m_vhs.a[i], t.xt[1], 2 * t.nw, c.nchol, t.ldg, 128));
+      TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[0], nrows, c.nchol, t.ldg, 256));
+    }
+    if (t.cfg & kVhsStat) {
+      TC_CHECK(mk(&t.m_vhs.a[i], t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
+      TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[1], nrows, c.nchol, t.ldg, 256));
+    }
+  }
+  for (int s = 0; s < t.nslab; ++s) {  // exp_h1 products: A = eop (static), B = wt / acc
+    const uint64_t rows = (uint64_t)t.nw * t.R[s];
+    for (int which = 0; which < 2; ++which) {
+      GemmMaps& m = which == 0 ? t.m_e1[s] : t.m_e2[s];
+      uint16_t** bop = which == 0 ? t.wt[s] : t.acc[s];
+      int i = 0;
+      TC_CHECK(mk(&m.a[i], t.eop[s][0], 128, t.n, t.nk, 128));
+      TC_CHECK(mk(&m.b[i++], bop[0], rows, t.n, t.nk, t.bn_w[s]));
+      if (t.cfg & kExpDyn) {
+        TC_CHECK(mk(&m.a[i], t.eop[s][0], 128, t.n, t.nk, 128));
+        TC_CHECK(mk(&m.b[i++], bop[1], rows, t.n, t.nk, t.bn_w[s]));
+      }
+      if (t.cfg & kExpStat) {
+        TC_CHECK(mk(&m.a[i], t.eop[s][1], 128, t.n, t.nk, 128));
+        TC_CHECK(mk(&m.b[i++], bop[0], rows, t.n, t.nk, t.bn_w[s]));
+      }
+    }
+    TC_CHECK(mk(&t.m_vt[s][0], t.vbuf[0], (uint64_t)nwc * 128, 2 * t.nq, 2 * t.nq, 128));
+    TC_CHECK(mk(&t.m_vt[s][1], t.vbuf[1], (uint64_t)nwc * 128, 2 * t.nq, 2 * t.nq, 128));
+    TC_CHECK(mk(&t.m_t0[s][0], t.t0[s][0], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
+    TC_CHECK(mk(&t.m_t0[s][1], t.t0[s][1], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
+  }
+  for (int b = 0; b < t.nblk; ++b) {  // energy: A = ren (static), B = gen (walker-dependent)
+    const uint64_t arows = (uint64_t)t.mt_en[b] * 128, brows = (uint64_t)t.nw * t.Rb[b];
+    int i = 0;
+    TC_CHECK(mk(&t.m_en[b].a[i], t.ren[b][0], arows, t.n, t.nk, 128));
+    TC_CHECK(mk(&t.m_en[b].b[i++], t.gen[b][0], brows, t.n, t.nk, t.bnb[b]));
+    if (t.cfg & kEneDyn) {
+      TC_CHECK(mk(&t.m_en[b].a[i], t.ren[b][0], arows, t.n, t.nk, 128));
+      TC_CHECK(mk(&t.m_en[b].b[i++], t.gen[b][1], brows, t.n, t.nk, t.bnb[b]));
+    }
+    if (t.cfg & kEneStat) {
+      TC_CHECK(mk(&t.m_en[b].a[i], t.ren[b][1], arows, t.n, t.nk, 128));
+      TC_CHECK(mk(&t.m_en[b].b[i++], t.gen[b][0], brows, t.n, t.nk, t.bnb[b]));
+    }
+  }
+  t.ready = 1;
+  *out = t;
+  return 0;
+}
+
+int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl, bool write_ops,
+             cudaStream_t st) {
+  MixedDev md = mixed_dev(t, c);
+  const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
+  const size_t smem = (size_t)t.n * omax * 8 + (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 +
+                      (size_t)omax * 2 * omax * 8 + (size_t)t.n * omax * 4;
+  cudaFuncSetAttribute(k_green_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_green_mixed<<<t.nw, 256, smem, st>>>(md, static_cast<const float2*>(wu), static_cast<const float2*>(wd),
+                                         ovl, write_ops ? 1 : 0);
+  return launch_check("green_mixed");
+}
+
+static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, double2* fb_out, cudaStream_t st) {
+  EpiFB::Params ep;
+  memset(&ep, 0, sizeof(ep));
+  ep.fields = fields;
+  ep.mf = c.mf;
+  ep.rc_inv = t.rc_inv;
+  ep.g_inv = t.g_inv;
+  ep.alpha = c.energy_mode == 0 ? 2.0f : 1.0f;
+  ep.sqdt = (float)sqrt(c.dt);
+  ep.nw = t.nw;
+  ep.nchol = c.nchol;
+  ep.ldg = t.ldg;
+  ep.ntiles = t.fb_ntiles;
+  ep.bf16 = t.bf16 ? 1 : 0;
+  ep.xt_hi = t.xt[0];
+  ep.xt_lo = t.xt[1];
+  ep.part_shift = t.part_shift;
+  ep.part_fbt = t.part_fbt;
+  ep.fb_out = fb_out;
+  const int kt = (t.kfb + 63) / 64, mt = (2 * t.nw + 127) / 128;
+  return launch_gemm<256, 4, EpiFB>(t.m_fb, t.n_fb_terms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st);
+}
+
+int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
+  return fb_gemm(t, c, nullptr, out, st);
+}
+
+int tc_field_shifts(TcState& t, const afq_ctx_dev& c, const double* fields, cudaStream_t st) {
+  return fb_gemm(t, c, fields, nullptr, st);
+}
+
+static int exp_gemm(TcState& t, const afq_ctx_dev& c, int s, bool last, float2* w, cudaStream_t st) {
+  EpiExp::Params ep;
+  memset(&ep, 0, sizeof(ep));
+  ep.w = reinterpret_cast<float*>(w);
+  ep.acc_hi = t.acc[s][0];
+  ep.acc_lo = t.acc[s][1];
+  ep.t0_hi = t.t0[s][0];
+  ep.t0_lo = t.t0[s][1];
+  ep.n = t.n;
+  ep.o = t.o_slab[s];
+  ep.R = t.R[s];
+  ep.nk = t.nk;
+  ep.nq = t.nq;
+  ep.NT = t.NT[s];
+  ep.nw = t.nw;
+  ep.bf16 = t.bf16 ? 1 : 0;
+  ep.last = last ? 1 : 0;
+  const int kt = (t.n + 63) / 64, nt = (t.nw * t.R[s] + t.bn_w[s] - 1) / t.bn_w[s];
+  return launch_gemm<256, 2, EpiExp>(last ? t.m_e2[s] : t.m_e1[s], t.n_e_terms, kt, 1, nt, t.bn_w[s], t.bf16,
+                                     ep, t.status, st);
+}
+
+int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
+  float2* W[2] = {static_cast<float2*>(wu), static_cast<float2*>(wd)};
+  for (int s = 0; s < t.nslab; ++s) TC_CHECK(exp_gemm(t, c, s, false, W[s], st));
+  const int nchunks = t.nw / t.nwc;
+  const bool want_lo = t.taylor_split > 0;
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int w0 = ch * t.nwc;
+    EpiVHS::Params ev;
+    ev.v_hi = t.vbuf[0];
+    ev.v_lo = t.vbuf[1];
+    ev.n = t.n;
+    ev.nq = t.nq;
+    ev.rows = 2 * t.nwc;
+    ev.bf16 = t.bf16 ? 1 : 0;
+    ev.want_lo = want_lo ? 1 : 0;
+    ev.sqdt = (float)sqrt(c.dt);
+    const int kt = (c.nchol + 63) / 64, mt = (2 * t.nwc + 127) / 128, nt = (t.n * t.nq + 255) / 256;
+    TC_CHECK((launch_gemm<256, 4, EpiVHS>(t.m_vhs, t.n_vhs_terms, kt, mt, nt, 256, t.bf16, ev, t.status, st,
+                                         2 * w0)));
+    for (int s = 0; s < t.nslab; ++s) {
+      TaylorDev td;
+      td.n = t.n;
+      td.o = t.o_slab[s];
+      td.nq = t.nq;
+      td.NT = t.NT[s];
+      td.R = t.R[s];
+      td.nk = t.nk;
+      td.nterms = c.n_exp_terms;
+      td.split = t.taylor_split;
+      td.bf16 = t.bf16 ? 1 : 0;
+      td.w0 = w0;
+      td.acc_hi = t.acc[s][0];
+      td.acc_lo = t.acc[s][1];
+      const size_t smem = taylor_smem(t.nq, t.NT[s], want_lo);
+      cudaFuncSetAttribute(k_taylor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_taylor_tc<<<t.nwc, 128, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0], t.m_t0[s][1], td,
+                                            t.status);
+      TC_CHECK(launch_check("taylor_tc"));
+    }
+  }
+  for (int s = 0; s < t.nslab; ++s) TC_CHECK(exp_gemm(t, c, s, true, W[s], st));
+  return 0;
+}
+
+int tc_weights(TcState& t, const afq_ctx_dev& c, const double2* ovl_new, double2* ovl, double* weights,
+               double* scalars, cudaStream_t st) {
+  return launch_weights(c, t.part_shift, t.part_fbt, t.fb_ntiles, ovl_new, ovl, weights, scalars, st);
+}
+
+int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
+  for (int b = 0; b < t.nblk; ++b) {
+    EpiEnergy::Params ep;
+    ep.ren_inv = t.ren_inv[b];
+    ep.g_inv = t.g_inv;
+    ep.o = t.o_blk[b];
+    ep.R = t.Rb[b];
+    ep.gpt = t.gpt[b];
+    ep.nchol = c.nchol;
+    ep.nw = t.nw;
+    ep.mt = t.mt_en[b];
+    ep.c_out = t.c_out + (size_t)b * t.nw * c.nchol;
+    ep.exc_part = t.exc_part + (b == 0 ? 0 : (size_t)t.nw * t.mt_en[0]);
+    const int kt = (t.n + 63) / 64, nt = (t.nw * t.Rb[b] + t.bnb[b] - 1) / t.bnb[b];
+    TC_CHECK((launch_gemm<240, 2, EpiEnergy>(t.m_en[b], t.n_en_terms, kt, t.mt_en[b], nt, t.bnb[b], t.bf16, ep,
+                                            t.status, st)));
+  }
+  k_energy_final_mixed<<<t.nw, 256, 0, st>>>(t.nw, c.nchol, t.nblk, t.mt_en[0], t.nblk == 2 ? t.mt_en[1] : 0,
+                                             c.energy_mode, c.h0, t.c_out, t.exc_part, t.ene1, out);
+  return launch_check("energy_final_mixed");
+}
+
+int tc_orthonormalize(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
+  return launch_qr<float>(c, wu, wd, st);
+}
 
 }  // namespace afq
 
@@ -105,8 +866,8 @@ extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long 
     afq_set_error("afq_test_gemm_f16: bad arguments");
     return -1;
   }
-  if (bn != 64 && bn != 128 && bn != 240 && bn != 256) {
-    afq_set_error("afq_test_gemm_f16: bn must be 64, 128, 240 or 256");
+  if (bn % 16 || bn < 16 || bn > 256) {
+    afq_set_error("afq_test_gemm_f16: bn must be a multiple of 16 in [16, 256]");
     return -1;
   }
   GemmMaps maps;
@@ -121,10 +882,5 @@ extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long 
   EpiStoreF32::Params ep{d, M, N, (long)N};
   const int kt = (K + 63) / 64, mt = (M + 127) / 128, nt = (N + bn - 1) / bn;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  switch (bn) {
-    case 64: return launch_gemm<64, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
-    case 128: return launch_gemm<128, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
-    case 240: return launch_gemm<240, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
-    default: return launch_gemm<256, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bf16, ep, status, st);
-  }
+  return launch_gemm<256, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bn, bf16, ep, status, st);
 }

@@ -1,22 +1,82 @@
-// Mixed-precision (BF16 tensor-core) path: operands, plans and launchers.
+// Mixed-precision path: FP32 walkers, FP16 (or BF16) tcgen05 contractions with hi/lo
+// split correction, FP32 small dense algebra with FP64 log-determinants, FP64 weights and
+// energy sums. Operand layouts (16-bit, row-major, K contiguous; "hi/lo" = x ~ hi + lo):
+//   g_fb   [2 nw][ldfb]       rows (w, re/im), cols (spin block, i, p) = G_s[i][p] * 2^e_w
+//   rc_fb  [nchol][ldfb]      rows g, cols (spin block, i, p) = rot_chol_s[g][i][p] * 2^e_g
+//   xt     [2 nw][ldg]        rows (w, re/im), cols g = shifted fields
+//   lop    [norb * nq][ldg]   rows (p, q) (q padded to nq), cols g = chol_g[p][q]
+//   vbuf   [nwc][128][2 nq]   per walker [Vr | Vi] (rows >= norb and q >= norb zero)
+//   eop[s] [128][nk]          exp_h1_s - I (rows >= norb zero)
+//   wt[s], acc[s] [nw * R_s][nk]  rows (w, 2k + re/im), cols p: walker / Taylor sum
+//   t0[s]  [nw][NT_s][2 nq]   Taylor B operand: row 2k = [Tr | -Ti], row 2k+1 = [Ti | Tr]
+//   ren[b] [mt_b * 128][nk]   rows (g-group tile, g_local * o + i) = rot_chol_b[g][i][:] * 2^e_g
+//   gen[b] [nw * R_b][nk]     rows (w, 2k + re/im), cols p = G_b[k][p] * 2^e_w
 #pragma once
+#include "afq_gemm.cuh"
 #include "afq_kernels.cuh"
 
 namespace afq {
 
+// accuracy options of the mixed path (afq_dims.mixed_config; 0 selects kMixedDefault)
+enum MixedBits : int32_t {
+  kFbDyn = 1 << 0,      // force bias: lo part of G
+  kFbStat = 1 << 1,     // force bias: lo part of rot_chol
+  kVhsDyn = 1 << 2,     // vhs: lo part of the shifted fields
+  kVhsStat = 1 << 3,    // vhs: lo part of chol
+  kExpDyn = 1 << 4,     // exp_h1 products: lo part of the walker / Taylor sum
+  kExpStat = 1 << 5,    // exp_h1 products: lo part of exp_h1 - I
+  kEneDyn = 1 << 6,     // energy: lo part of G
+  kEneStat = 1 << 7,    // energy: lo part of rot_chol
+  kTaylorShift = 8,     // bits 8..10: Taylor products computed with split operands
+  kUseBf16 = 1 << 11,   // bf16 operands instead of fp16
+  kExplicit = 1 << 30,  // set by callers that pass an explicit configuration
+};
+constexpr int32_t kMixedDefault = kFbDyn | kFbStat | kVhsDyn | kVhsStat | kExpDyn | kExpStat |
+                                  kEneDyn | kEneStat | (2 << kTaylorShift);
+
 struct TcState {
   int ready;
+  int cfg;
+  bool bf16;
+  int n, nq, nk, ldfb, ldg, kfb;
+  int nw, nwc;
+  int nslab, nblk;          // walker slabs, Green blocks
+  int o_slab[2], R[2], wpt[2], bn_w[2], NT[2];
+  int o_blk[2], Rb[2], wptb[2], bnb[2], gpt[2], mt_en[2];
+  int fb_bn, fb_ntiles;
+  // static operands [hi, lo]
+  uint16_t *rc_fb[2], *lop[2], *eop[2][2], *ren[2][2];
+  float* rc_inv;            // [nchol] 2^-e_g for rc_fb
+  float* ren_inv[2];        // [nchol] 2^-e_g for ren
+  // dynamic operands
+  uint16_t *g_fb[2], *xt[2], *vbuf[2], *wt[2][2], *acc[2][2], *t0[2][2], *gen[2][2];
+  float* g_inv;             // [nw] 2^-e_w
+  double2* ene1;            // [nw]
+  double2* part_shift;      // [nw][fb_ntiles]
+  double2* part_fbt;        // [nw][fb_ntiles]
+  double2* c_out;           // [nblk][nw][nchol]
+  double2* exc_part;        // [nblk][nw][mt_en]
+  const float* trial32[2];  // [norb][o_s] trial in FP32
+  const float* rh1_32[2];   // [o_b][norb] rot_h1 in FP32
+  int* status;              // device word: nonzero after a pipeline timeout
+  // tensor maps
+  GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_en[2];
+  CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
+  CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
+  int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;
 };
 
-size_t tc_workspace_bytes(const afq_ctx_dev& c, int nw_chunk);
+size_t tc_workspace_bytes(const afq_ctx_dev& c, int nw_chunk, int32_t mixed_config);
 int tc_init(TcState* t, const afq_ctx_dev& c, const afq_hamiltonian& h, const double* rccat,
-            int nw_chunk, char* ws, cudaStream_t st);
-int tc_force_bias(TcState& t, const afq_ctx_dev& c, const double2* green, double2* out,
-                  double alpha, cudaStream_t st);
-int tc_energy(TcState& t, const afq_ctx_dev& c, const double2* green, double2* epart,
-              double2* out, cudaStream_t st);
-int tc_propagate_chunk(TcState& t, const afq_ctx_dev& c, int w0, int nwc, const double2* xt,
-                       void* wu, void* wd, cudaStream_t st);
+            int nw_chunk, int32_t mixed_config, char* ws, cudaStream_t st);
+int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl,
+             bool write_ops, cudaStream_t st);
+int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st);
+int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st);
+int tc_field_shifts(TcState& t, const afq_ctx_dev& c, const double* fields, cudaStream_t st);
+int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st);
+int tc_weights(TcState& t, const afq_ctx_dev& c, const double2* ovl_new, double2* ovl,
+               double* weights, double* scalars, cudaStream_t st);
 int tc_orthonormalize(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st);
 
 }  // namespace afq

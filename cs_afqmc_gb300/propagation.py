@@ -98,6 +98,7 @@ class propagator_restricted:
     n_exp_terms: int = 6
     n_batch: int = 1
     precision: str = "fp64"
+    mixed_config: int = 0  # accuracy options of the mixed path (0 = library default)
 
     restricted = True
 
@@ -108,7 +109,7 @@ class propagator_restricted:
     def _engine(self, trial, ham_data, wave_data, walkers) -> _engine.Engine:
         return _engine.engine_for(trial, ham_data, wave_data, walkers, dt=self.dt,
                                   n_exp_terms=self.n_exp_terms, n_batch=self.n_batch,
-                                  need_propagation=True)
+                                  need_propagation=True, mixed_config=self.mixed_config)
 
     def _cast_walkers(self, walkers):
         if isinstance(walkers, (list, tuple)):
@@ -210,7 +211,7 @@ class propagator_restricted:
 
     def __hash__(self) -> int:
         return hash((type(self).__name__, self.dt, self.n_walkers, self.n_exp_terms,
-                     self.n_batch, self.precision))
+                     self.n_batch, self.precision, self.mixed_config))
 
 
 @dataclass

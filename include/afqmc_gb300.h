@@ -57,6 +57,7 @@ typedef struct afq_dims {
   int32_t precision;    /* afq_precision */
   int32_t n_exp_terms;  /* Taylor terms of exp(vhs), reference default 6 */
   int32_t n_batch;      /* walker chunks for the vhs workspace (>= 1, divides n_walkers) */
+  int32_t mixed_config; /* AFQ_PREC_MIXED accuracy options; 0 = library default */
   double dt;
 } afq_dims;
 

@@ -22,8 +22,10 @@ CASES = [
     dict(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=5),
     dict(kind="rhf", restricted=True, norb=7, nelec=(3, 3), nchol=5, nw=3),   # odd tiny
     dict(kind="rhf", restricted=True, norb=40, nelec=(9, 9), nchol=70, nw=4),
+    dict(kind="rhf", restricted=True, norb=120, nelec=(20, 20), nchol=200, nw=4),
+    dict(kind="uhf", restricted=False, norb=60, nelec=(10, 8), nchol=90, nw=4),
 ]
-IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40"]
+IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40", "rhf-120", "uhf-60"]
 
 
 @pytest.fixture(params=list(range(len(CASES))), ids=IDS)

@@ -1,0 +1,94 @@
+"""Mixed-precision CUDA path (complex64 walkers, FP16 split tensor-core contractions,
+FP32 small dense algebra, FP64 log-determinants/weights/sums) against the FP64 oracle on
+identical inputs, through the C ABI.
+
+Tolerances (relative to the largest magnitude of each compared array):
+  overlaps 2e-5, force bias 5e-5 (G comes from an FP32 inverse of S = C^T W; the noisy test
+  walkers make S ill-conditioned, which amplifies FP32 rounding), local energies 2e-5,
+  one-step walkers / weights 2e-5, QR 1e-5, two driver blocks: energies 5e-5.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import afqmc_oracle as O
+from tests.helpers import Case, rel_err, to_np
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    dict(kind="rhf", restricted=True, norb=12, nelec=(3, 3), nchol=30, nw=8),
+    dict(kind="rhf", restricted=False, norb=10, nelec=(4, 4), nchol=17, nw=6),
+    dict(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=5),
+    dict(kind="rhf", restricted=True, norb=7, nelec=(3, 3), nchol=5, nw=3),
+    dict(kind="rhf", restricted=True, norb=40, nelec=(9, 9), nchol=70, nw=14),
+    dict(kind="rhf", restricted=True, norb=120, nelec=(20, 20), nchol=600, nw=16),
+    dict(kind="uhf", restricted=False, norb=60, nelec=(10, 8), nchol=300, nw=12),
+]
+IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40", "rhf-120", "uhf-60"]
+
+
+@pytest.fixture(params=list(range(len(CASES))), ids=IDS)
+def case(request):
+    return Case(precision="mixed", **CASES[request.param])
+
+
+def _flat(w):
+    return np.concatenate([x.ravel() for x in w]) if isinstance(w, list) else w.ravel()
+
+
+def test_measurements(case):
+    w = case.gpu_walkers()
+    w64 = [x.astype(np.complex64).astype(np.complex128) for x in case.walkers0] if isinstance(
+        case.walkers0, list) else case.walkers0.astype(np.complex64).astype(np.complex128)
+    ov = to_np(case.trial.calc_overlap(w, case.wave_data))
+    fb = to_np(case.trial.calc_force_bias(w, case.ham_data, case.wave_data))
+    en = to_np(case.trial.calc_energy(w, case.ham_data, case.wave_data))
+    mo = case.sys.mo_coeff
+    assert rel_err(ov, case.o_trial.overlap(w64, mo)) < 2e-5
+    assert rel_err(fb, case.o_trial.force_bias(w64, case.o_ham, mo)) < 5e-5
+    assert rel_err(en, case.o_trial.energy(w64, case.o_ham, mo)) < 2e-5
+
+
+def test_one_step(case):
+    rng = np.random.default_rng(3)
+    fields = rng.standard_normal((case.nw, case.nchol))
+    w0 = [x.astype(np.complex64).astype(np.complex128) for x in case.walkers0] if isinstance(
+        case.walkers0, list) else case.walkers0.astype(np.complex64).astype(np.complex128)
+    po = case.oracle_prop_data(w0)
+    po = case.o_prop.propagate(case.o_trial, case.o_ham, po, fields, case.sys.mo_coeff)
+    pg = case.gpu_prop_data()
+    pg = case.prop.propagate(case.trial, case.ham_data, pg, fields, case.wave_data)
+    assert rel_err(_flat(to_np(pg["walkers"])), _flat(po["walkers"])) < 2e-5
+    assert rel_err(to_np(pg["weights"]), po["weights"]) < 2e-5
+    assert rel_err(to_np(pg["overlaps"]), po["overlaps"]) < 5e-5
+
+
+def test_qr(case):
+    w0 = [x.astype(np.complex64).astype(np.complex128) for x in case.walkers0] if isinstance(
+        case.walkers0, list) else case.walkers0.astype(np.complex64).astype(np.complex128)
+    po = case.oracle_prop_data(w0)
+    po = case.o_prop.orthonormalize_walkers(po)
+    pg = case.gpu_prop_data()
+    pg = case.prop.orthonormalize_walkers(pg)
+    assert rel_err(_flat(to_np(pg["walkers"])), _flat(po["walkers"])) < 1e-5
+
+
+def test_phaseless_blocks(case):
+    from cs_afqmc_gb300 import driver, sampling
+    nb, n_sr, n_ene, n_prop = 2, 1, 2, 3
+    rng = np.random.default_rng(21)
+    fields = rng.standard_normal((nb, n_sr, n_ene, n_prop, case.nw, case.nchol))
+    zetas = rng.uniform(size=(nb, n_sr + 1))
+    samp_o = O.Sampler(n_prop_steps=n_prop, n_ene_blocks=n_ene, n_sr_blocks=n_sr)
+    w0 = [x.astype(np.complex64).astype(np.complex128) for x in case.walkers0] if isinstance(
+        case.walkers0, list) else case.walkers0.astype(np.complex64).astype(np.complex128)
+    po = case.oracle_prop_data(w0)
+    e_o, w_o, po = O.run_blocks(samp_o, case.o_prop, case.o_trial, case.o_ham, po,
+                                case.sys.mo_coeff, lambda n: fields[n], lambda n: zetas[n], nb)
+    samp = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=n_ene, n_sr_blocks=n_sr)
+    pg = case.gpu_prop_data()
+    e_g, w_g, pg = driver.run_blocks(samp, case.ham, case.ham_data, case.prop, pg, case.trial,
+                                     case.wave_data, nb, fields=fields, zetas=zetas)
+    assert rel_err(to_np(e_g), e_o) < 5e-5
+    assert rel_err(to_np(w_g), w_o) < 5e-5

@@ -14,7 +14,7 @@ from cs_afqmc_gb300._engine import stream_ptr
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(128, 64, 64, 64), (300, 250, 200, 128), (256, 480, 600, 240), (1000, 700, 136, 256),
+SHAPES = [(128, 64, 64, 64), (300, 250, 200, 128), (256, 480, 600, 240), (1000, 700, 136, 256), (200, 300, 72, 48), (130, 600, 2400, 208),
           (64, 16, 8, 64)]
 
 
