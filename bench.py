@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Walker-steps/s of the phaseless-AFQMC hot path (propagation + local energy) on GB300.
+
+One bench step = one driver block of the precision-pattern workload
+(RHF, norb 120, 20+20 electrons, 600 Cholesky vectors, 1024 walkers, dt 0.005):
+sampler.propagate_phaseless with 5 propagation steps x 4 energy blocks (QR, overlaps and
+local energies after every 5 steps, block energy, population control), local SR, then the
+driver's block end (weight record, QR, global SR, e_estimate update) = 20 x 1024
+walker-steps. Auxiliary fields are drawn on the device (Philox) inside the step for `value`,
+and copied from pinned host memory every step for `e2e`.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+       [--precision mixed|fp64] [--workload NAME] [--no-cpu-baseline]
+Under torchrun (N > 1) every rank runs an independent replica with its own seed (walkers
+only couple through block-end reductions, which a replica does not need); value = total
+walker-steps of all ranks / max time over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker-steps/s at equal energy error vs FP64 GPU path"
+UNIT = "walker-steps/s"
+DEFAULT_WORKLOAD = "rhf_norb120_nocc20_nchol600_nw1024"
+N_PROP, N_ENE, N_SR = 5, 4, 1
+L2_BYTES = 129e6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    ap.add_argument("--n-batch", type=int, default=4)
+    ap.add_argument("--mixed-config", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-procs", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.idx)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------------------
+# algorithmic work per kernel launch (real flops; complex x real MAC = 4, complex x complex = 8)
+# ---------------------------------------------------------------------------------------
+
+def flops_per_launch(cls: str, w: dict, n_batch: int) -> float:
+    n, o, G, nw = w["norb"], w["nelec"][0], w["nchol"], w["n_walkers"]
+    nwc = nw // n_batch
+    table = {
+        "vhs_gemm": 4.0 * G * n * n * nwc,                 # i sqrt(dt) x~ . chol
+        "taylor": 5 * 8.0 * n * n * o * nwc,               # 5 products V T
+        "exp_h1_gemm": 4.0 * n * n * o * nw,               # (E - I) W, one product
+        "force_bias_gemm": 4.0 * G * o * n * nw,           # G . rot_chol
+        "energy_gemm": 4.0 * G * n * o * o * nw,           # rot_chol_g G^T for all g
+    }
+    return table.get(cls, 0.0)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return d, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the profiled kernels from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------------
+
+def build_workload(name: str, precision: str, n_batch: int, mixed_config: int, seed: int):
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import hamiltonian, propagation, sampling, synthetic, wavefunctions
+    from cs_afqmc_gb300.propagation import RngKey
+
+    w = dict(synthetic.WORKLOADS[name])
+    s = synthetic.molecular(w["norb"], w["nelec"], w["nchol"], seed=1, kind=w["kind"])
+    ham = hamiltonian.hamiltonian(w["norb"])
+    trial = (wavefunctions.rhf if w["kind"] == "rhf" else wavefunctions.uhf)(w["norb"], w["nelec"])
+    wave = {"mo_coeff": s.mo_coeff, "rdm1": s.rdm1}
+    hd = {"h0": s.h0, "h1": s.h1, "chol": s.chol, "ene0": 0.0}
+    hd = ham.build_measurement_intermediates(hd, trial, wave)
+    P = propagation.propagator_restricted if w["kind"] == "rhf" else propagation.propagator_unrestricted
+    prop = P(dt=w["dt"], n_walkers=w["n_walkers"], n_exp_terms=6, n_batch=n_batch,
+             precision=precision, mixed_config=mixed_config)
+    hd = ham.build_propagation_intermediates(hd, prop, trial, wave)
+    restricted = w["kind"] == "rhf"
+    pd = prop.init_prop_data(trial, wave, hd, init_walkers=s.init_walkers(w["n_walkers"], restricted))
+    pd["key"] = RngKey(seed)
+    samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=N_SR)
+    return w, s, ham, trial, wave, hd, prop, pd, samp
+
+
+def run_ours(args, rank, world, local):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import _lib
+    from cs_afqmc_gb300._engine import stream_ptr
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    cpu_pool = None
+    want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
+    w = dict(__import__("cs_afqmc_gb300.synthetic", fromlist=["x"]).WORKLOADS[args.workload])
+    cpu_procs = args.cpu_procs or max(1, (os.cpu_count() or 2) - 2)
+    if want_cpu:
+        from oracle.cpu_bench import CpuPool
+        cpu_pool = CpuPool(cpu_procs, w["norb"], w["nelec"][0], w["nchol"], 16, w["dt"])
+
+    w, s, ham, trial, wave, hd, prop, pd, samp = build_workload(
+        args.workload, args.precision, args.n_batch, args.mixed_config, seed=1000 + rank)
+    nw, G = w["n_walkers"], w["nchol"]
+    ws_per_step = N_PROP * N_ENE * N_SR * nw
+    lib = _lib.load()
+
+    def step(fields=None, zetas=None):
+        nonlocal pd
+        e, pd = samp.propagate_phaseless(ham, hd, prop, pd, trial, wave, fields=fields, zetas=zetas)
+        zg = samp.draw_zetas(pd, 1) if zetas is None else zetas_g
+        eng = pd["_engine"]
+        st = pd.state(eng)
+        _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), e.data_ptr(), zg.data_ptr(),
+                  wsum.data_ptr(), stream_ptr())
+        return e
+
+    e_buf = torch.zeros(1, dtype=torch.float64, device="cuda")
+    wsum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    zetas_g = torch.full((1,), 0.5, dtype=torch.float64, device="cuda")
+
+    def step_dev():
+        e = step()
+        e_buf.copy_(e.reshape(1))
+
+    for _ in range(args.warmup):
+        step_dev()
+    torch.cuda.synchronize()
+
+    # ---- timed region: device-resident inputs (fields drawn on the device) ----
+    clk = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    lib.afq_profile_enable(1)
+    clk.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.steps):
+        step_dev()
+    t1.record()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = t0.elapsed_time(t1)
+    prof = _lib.profile_read_all()
+    lib.afq_profile_enable(0)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.item()
+    ms_per_step = ms / args.steps
+    value = world * ws_per_step * args.steps / (ms / 1e3)
+    launches = sum(v[1] for v in prof.values())
+    block_energy = e_buf.item()
+
+    # ---- e2e: host fields (pinned) copied in every step, block energy copied out ----
+    fshape = (N_SR, N_ENE, N_PROP, nw, G)
+    rng = np.random.default_rng(77 + rank)
+    host_fields = [torch.from_numpy(rng.standard_normal(fshape)).pin_memory() for _ in range(2)]
+    host_z = torch.from_numpy(rng.uniform(size=(N_SR,))).pin_memory()
+    out_host = torch.empty((args.steps, 2), dtype=torch.float64).pin_memory()
+    dev_fields = torch.empty(fshape, dtype=torch.float64, device="cuda")
+    dev_z = torch.empty(N_SR, dtype=torch.float64, device="cuda")
+    res = torch.empty(2, dtype=torch.float64, device="cuda")
+    for i in range(2):
+        dev_fields.copy_(host_fields[i], non_blocking=True)
+        dev_z.copy_(host_z, non_blocking=True)
+        e = step(dev_fields, dev_z)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0.record()
+    for i in range(args.steps):
+        dev_fields.copy_(host_fields[i % 2], non_blocking=True)
+        dev_z.copy_(host_z, non_blocking=True)
+        e = step(dev_fields, dev_z)
+        res[0].copy_(e)
+        res[1].copy_(wsum[0])
+        out_host[i].copy_(res, non_blocking=True)
+    t1.record()
+    torch.cuda.synchronize()
+    ms_e2e = t0.elapsed_time(t1)
+    if dist:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = t.item()
+    e2e = {"value": world * ws_per_step * args.steps / (ms_e2e / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": int(host_fields[0].numel() * 8 + host_z.numel() * 8),
+           "d2h_bytes_per_step": int(out_host[0].numel() * 8)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel ----
+    peaks, peak_kind = load_peaks()
+    kernels = {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items() if v[1] > 0}
+    total_k_ms = sum(v[0] for v in prof.values()) or 1.0
+    for k in kernels:
+        kernels[k]["share"] = round(prof[k][0] / total_k_ms, 4)
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    fl = flops_per_launch(dom, w, args.n_batch)
+    traffic = load_traffic().get(f"{args.workload}:{args.precision}:{dom}")
+    if fl > 0 and dom_n > 0:
+        achieved = fl / (dom_ms / dom_n / 1e3) / 1e12
+        peak = peaks["bf16_tflops"] if args.precision == "mixed" else 1.04
+        roof = {"kernel": dom, "bound": "tensor", "achieved": round(achieved, 2), "peak": peak,
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic,
+                "flops_per_launch": fl,
+                "peak_source": (f"{peak_kind} bf16 dense (MEASURED_PEAKS.json); fp16 runs at the "
+                                "bf16 rate" if args.precision == "mixed" else
+                                "fp64 DGEMM measured on this pool's GB300 (1.04 TFLOP/s)")}
+    else:
+        roof = {"kernel": dom, "bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": None, "traffic": traffic}
+
+    # ---- CPU baseline (FP64 oracle, one process per core) ----
+    cpu = None
+    if cpu_pool is not None:
+        try:
+            cpu_pool.run(2, 1)  # warm-up (imports, system build)
+            ws, sec = cpu_pool.run(10, 2)
+            cpu = {"value": round(ws / sec, 2), "unit": UNIT, "cores": cpu_procs, "kind": "port",
+                   "sample": (f"{args.workload}: {cpu_procs} processes x 16 walkers x 10 steps "
+                              f"(QR + local energy every 5), FP64 NumPy oracle, 1 BLAS thread each, "
+                              f"{sec:.1f} s wall")}
+        except Exception as ex:  # noqa: BLE001
+            cpu = {"value": None, "unit": UNIT, "cores": cpu_procs, "kind": "port",
+                   "sample": f"failed: {ex!r}"[:200]}
+        finally:
+            cpu_pool.close()
+
+    ws_bytes = nw * G * 8 * N_PROP * N_ENE + nw * w["norb"] * w["nelec"][0] * (8 if args.precision == "mixed" else 16)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": ("fp16 tensor-core contractions with hi/lo split, fp32 walkers and small "
+                  "linear algebra, fp64 log-determinants/weights/sums") if args.precision == "mixed" else "fp64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "norb": w["norb"], "nelec": list(w["nelec"]),
+                   "nchol": G, "n_walkers": nw, "dt": w["dt"], "precision": args.precision,
+                   "step": f"1 driver block = {N_PROP}x{N_ENE}x{N_SR} propagation steps, QR + energy every {N_PROP}, local SR, block end",
+                   "walker_steps_per_step": ws_per_step, "n_batch": args.n_batch,
+                   "l2": f"inputs larger than L2: fields alone are {ws_bytes/1e6:.0f} MB per step (> 129 MB L2)",
+                   "replicas": "independent replicas per GPU" if world > 1 else "single GPU",
+                   "last_block_energy": block_energy},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clocks, "kernels": kernels,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------------
+# reference arm: the reference's CPU path, restated (JAX is not installed), on host cores
+# ---------------------------------------------------------------------------------------
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return
+    sys.path.insert(0, ROOT)
+    from cs_afqmc_gb300 import synthetic
+    from oracle.cpu_bench import CpuPool
+
+    w = dict(synthetic.WORKLOADS[args.workload])
+    procs = args.cpu_procs or (os.cpu_count() or 1)
+    nw_per = max(1, min(16, w["n_walkers"] // procs))
+    pool = CpuPool(procs, w["norb"], w["nelec"][0], w["nchol"], nw_per, w["dt"])
+    n_steps, n_meas = 5, 1
+    try:
+        for _ in range(args.warmup):
+            pool.run(n_steps, n_meas)
+        tot_ws, tot_s = 0, 0.0
+        for _ in range(args.steps):
+            ws, sec = pool.run(n_steps, n_meas)
+            tot_ws += ws
+            tot_s += sec
+    finally:
+        pool.close()
+    value = tot_ws / tot_s
+    sample = (f"{args.workload}: per step {procs} processes x {nw_per} walkers x {n_steps} "
+              f"propagation steps + {n_meas} QR/energy, FP64 NumPy restatement of the reference "
+              f"(JAX not installed), 1 BLAS thread per process")
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * tot_s / args.steps, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "norb": w["norb"], "nelec": list(w["nelec"]),
+                       "nchol": w["nchol"], "n_walkers": w["n_walkers"], "dt": w["dt"]},
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -65,6 +65,12 @@ _SIGS = {
                                                ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                _vp, _vp, _vp, _vp]),
     "afq_block_end": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp]),
+    "afq_profile_enable": (ctypes.c_int, [ctypes.c_int]),
+    "afq_profile_reset": (ctypes.c_int, []),
+    "afq_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_int64)]),
+    "afq_profile_class_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "afq_profile_num_classes": (ctypes.c_int, []),
     "afq_fill_normal": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, _vp]),
     "afq_fill_uniform": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, _vp]),
 }
@@ -113,3 +119,14 @@ def check(rc: int, what: str) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(load(), name)(*args), name)
+
+
+def profile_read_all() -> dict:
+    """{class name: (total ms, launches)} since the last afq_profile_enable/reset."""
+    lib = load()
+    out = {}
+    for c in range(lib.afq_profile_num_classes()):
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(lib.afq_profile_read(c, ctypes.byref(ms), ctypes.byref(n)), "afq_profile_read")
+        out[lib.afq_profile_class_name(c).decode()] = (ms.value, n.value)
+    return out

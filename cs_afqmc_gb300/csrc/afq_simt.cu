@@ -8,6 +8,7 @@
 #include <math.h>
 #include "afq_common.cuh"
 #include "afq_kernels.cuh"
+#include "afq_prof.cuh"
 
 namespace afq {
 
@@ -771,13 +772,17 @@ int launch_green(const afq_ctx_dev& c, const void* wu, const void* wd, double2* 
                 (size_t)c.norb * c.kmax * sizeof(double);
   auto kfn = k_green_overlap<WT>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<c.nw, 256, smem, st>>>(c, (const WT*)wu, (const WT*)wd, green, ovl, write_green ? 1 : 0);
+  {
+    ProfScope _ps(K_GREEN, st);
+    kfn<<<c.nw, 256, smem, st>>>(c, (const WT*)wu, (const WT*)wd, green, ovl, write_green ? 1 : 0);
+  }
   return launch_err("green_overlap");
 }
 
 int launch_gemm_cr(bool b_kn, int M, int N, int K, const double2* A, long lda, const double* B,
                    long ldb, double2* C, long ldc, double2 alpha, cudaStream_t st) {
   dim3 grid((N + 63) / 64, (M + 63) / 64);
+  ProfScope _ps(b_kn ? K_VHS : K_FB, st);
   if (b_kn)
     k_gemm_cr<true><<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha);
   else
@@ -787,7 +792,10 @@ int launch_gemm_cr(bool b_kn, int M, int N, int K, const double2* A, long lda, c
 
 int launch_field_shifts(const afq_ctx_dev& c, const double* fields, const double2* fb,
                         double2* xt, double2* shift, double2* fbt, cudaStream_t st) {
-  k_field_shifts<<<c.nw, 256, 0, st>>>(c.nchol, sqrt(c.dt), fields, fb, c.mf, xt, shift, fbt);
+  {
+    ProfScope _ps(K_FIELD, st);
+    k_field_shifts<<<c.nw, 256, 0, st>>>(c.nchol, sqrt(c.dt), fields, fb, c.mf, xt, shift, fbt);
+  }
   return launch_err("field_shifts");
 }
 
@@ -797,15 +805,21 @@ int launch_taylor_f64(const afq_ctx_dev& c, int w0, int nwc, const double2* vhs,
   size_t smem = 2 * (size_t)c.norb * c.kmax * sizeof(double2);
   auto kfn = k_taylor_f64<WT>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<dim3(nwc, c.nslab), 256, smem, st>>>(c, w0, vhs, (WT*)wu, (WT*)wd);
+  {
+    ProfScope _ps(K_TAYLOR, st);
+    kfn<<<dim3(nwc, c.nslab), 256, smem, st>>>(c, w0, vhs, (WT*)wu, (WT*)wd);
+  }
   return launch_err("taylor_f64");
 }
 
 int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt, int ntiles,
                    const double2* ovl_new, double2* ovl, double* weights, double* scalars,
                    cudaStream_t st) {
-  k_weights<<<1, 1024, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt, ntiles,
-                                ovl_new, ovl, weights, scalars);
+  {
+    ProfScope _ps(K_WEIGHTS, st);
+    k_weights<<<1, 1024, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt, ntiles,
+                                  ovl_new, ovl, weights, scalars);
+  }
   return launch_err("weights");
 }
 
@@ -813,10 +827,16 @@ int launch_energy_f64(const afq_ctx_dev& c, int nchunks, int gchunk, const doubl
                       double2* epart, double2* energy, cudaStream_t st) {
   size_t smem = (size_t)c.ktot * sizeof(double2) + 2 * (size_t)c.kmax * c.kmax * sizeof(double2);
   cudaFuncSetAttribute(k_energy_f64_part, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_energy_f64_part<<<dim3(c.nw, nchunks), 256, smem, st>>>(c, gchunk, green, epart);
+  {
+    ProfScope _ps(K_ENERGY, st);
+    k_energy_f64_part<<<dim3(c.nw, nchunks), 256, smem, st>>>(c, gchunk, green, epart);
+  }
   int e = launch_err("energy_part");
   if (e) return e;
-  k_energy_final<<<c.nw, 256, 0, st>>>(c, nchunks, green, epart, energy);
+  {
+    ProfScope _ps(K_ENERGY_FIN, st);
+    k_energy_final<<<c.nw, 256, 0, st>>>(c, nchunks, green, epart, energy);
+  }
   return launch_err("energy_final");
 }
 
@@ -825,14 +845,20 @@ int launch_qr(const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
   size_t smem = ((size_t)c.norb * c.kmax + 2 * c.kmax) * sizeof(typename CplxOf<WT>::type);
   auto kfn = k_qr_householder<WT>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<dim3(c.nw, c.nslab), 256, smem, st>>>(c, (WT*)wu, (WT*)wd);
+  {
+    ProfScope _ps(K_QR, st);
+    kfn<<<dim3(c.nw, c.nslab), 256, smem, st>>>(c, (WT*)wu, (WT*)wd);
+  }
   return launch_err("qr_householder");
 }
 
 template <typename WT>
 int launch_sr(const afq_ctx_dev& c, const double* zeta, double* weights, double* cum, int32_t* idx,
               void* wu, void* wd, void* wcopy, cudaStream_t st) {
-  k_sr_indices<<<1, 1024, 0, st>>>(c.nw, zeta, weights, cum, idx);
+  {
+    ProfScope _ps(K_SR, st);
+    k_sr_indices<<<1, 1024, 0, st>>>(c.nw, zeta, weights, cum, idx);
+  }
   int e = launch_err("sr_indices");
   if (e) return e;
   using CT = typename CplxOf<WT>::type;
@@ -843,7 +869,10 @@ int launch_sr(const afq_ctx_dev& c, const double* zeta, double* weights, double*
     size_t bytes = elems * c.nw * sizeof(CT);
     char* cp = (char*)wcopy + off;
     cudaMemcpyAsync(cp, w, bytes, cudaMemcpyDeviceToDevice, st);
-    k_gather_slab<WT><<<c.nw, 256, 0, st>>>((int)elems, idx, (const WT*)cp, (WT*)w);
+    {
+      ProfScope _ps(K_SR, st);
+      k_gather_slab<WT><<<c.nw, 256, 0, st>>>((int)elems, idx, (const WT*)cp, (WT*)w);
+    }
     off += bytes;
   }
   return launch_err("sr_gather");
@@ -851,24 +880,36 @@ int launch_sr(const afq_ctx_dev& c, const double* zeta, double* weights, double*
 
 int launch_block_stats(const afq_ctx_dev& c, const double2* energy, const double* weights,
                        double* scalars, double* be, double* bw, cudaStream_t st) {
-  k_block_stats<<<1, 1024, 0, st>>>(c.nw, c.dt, energy, weights, scalars, be, bw);
+  {
+    ProfScope _ps(K_STATS, st);
+    k_block_stats<<<1, 1024, 0, st>>>(c.nw, c.dt, energy, weights, scalars, be, bw);
+  }
   return launch_err("block_stats");
 }
 
 int launch_phaseless_begin(double* scalars, cudaStream_t st) {
-  k_phaseless_begin<<<1, 1, 0, st>>>(scalars);
+  {
+    ProfScope _ps(K_STATS, st);
+    k_phaseless_begin<<<1, 1, 0, st>>>(scalars);
+  }
   return launch_err("phaseless_begin");
 }
 
 int launch_phaseless_end(int nblk, double denom, const double* be, const double* bw,
                          double* scalars, double* energy, cudaStream_t st) {
-  k_phaseless_end<<<1, 32, 0, st>>>(nblk, denom, be, bw, scalars, energy);
+  {
+    ProfScope _ps(K_STATS, st);
+    k_phaseless_end<<<1, 32, 0, st>>>(nblk, denom, be, bw, scalars, energy);
+  }
   return launch_err("phaseless_end");
 }
 
 int launch_driver_update(const afq_ctx_dev& c, const double* weights, const double* energy,
                          double* scalars, double* wsum, cudaStream_t st) {
-  k_driver_update<<<1, 1024, 0, st>>>(c.nw, weights, energy, scalars, wsum);
+  {
+    ProfScope _ps(K_STATS, st);
+    k_driver_update<<<1, 1024, 0, st>>>(c.nw, weights, energy, scalars, wsum);
+  }
   return launch_err("driver_update");
 }
 
@@ -879,13 +920,19 @@ int launch_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, c
   }
   int64_t pairs = (n + 1) / 2;
   if (pairs == 0) return 0;
-  k_fill_normal<<<(unsigned)((pairs + 255) / 256), 256, 0, st>>>(out, n, seed, offset);
+  {
+    ProfScope _ps(K_RNG, st);
+    k_fill_normal<<<(unsigned)((pairs + 255) / 256), 256, 0, st>>>(out, n, seed, offset);
+  }
   return launch_err("fill_normal");
 }
 
 int launch_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t st) {
   if (n == 0) return 0;
-  k_fill_uniform<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, seed, offset);
+  {
+    ProfScope _ps(K_RNG, st);
+    k_fill_uniform<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, seed, offset);
+  }
   return launch_err("fill_uniform");
 }
 

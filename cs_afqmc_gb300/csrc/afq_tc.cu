@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include "afq_mixed_kernels.cuh"
+#include "afq_prof.cuh"
 
 namespace afq {
 
@@ -70,7 +71,7 @@ static int launch_check(const char* what) {
   } while (0)
 
 template <int BNMAX, int STAGES, class Epi>
-static int launch_gemm(const GemmMaps& maps, int nterms, int k_tiles, int m_tiles, int n_tiles,
+static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, int m_tiles, int n_tiles,
                        int bn, bool bf16, const typename Epi::Params& ep, int* status,
                        cudaStream_t st, int a_row0 = 0) {
   if (bn % 16 || bn < 16 || bn > BNMAX) {
@@ -81,8 +82,11 @@ static int launch_gemm(const GemmMaps& maps, int nterms, int k_tiles, int m_tile
   static_assert(smem <= 232448, "shared memory");
   auto kfn = k_gemm_tc<BNMAX, STAGES, Epi>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  kfn<<<dim3(n_tiles, m_tiles), kGemmThreads, smem, st>>>(
-      maps, nterms, k_tiles, bn, a_row0, ptx::idesc_f16(128, bn, bf16 ? 1 : 0), ep, status);
+  {
+    ProfScope _ps(cls, st);
+    kfn<<<dim3(n_tiles, m_tiles), kGemmThreads, smem, st>>>(
+        maps, nterms, k_tiles, bn, a_row0, ptx::idesc_f16(128, bn, bf16 ? 1 : 0), ep, status);
+  }
   return launch_check("gemm_tc");
 }
 
@@ -625,6 +629,7 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
     return (int)e;
   }
   const int bf = t.bf16 ? 1 : 0;
+  ProfScope _ps(K_PREP, st);
   for (int s = 0; s < t.nslab; ++s) {
     k_to_f32<<<64, 256, 0, st>>>(c.trial[s], const_cast<float*>(t.trial32[s]), (long)t.n * t.o_slab[s]);
     k_prep_eop<<<64, 256, 0, st>>>(c.exp_h1[s], t.n, t.nk, bf, t.eop[s][0], t.eop[s][1]);
@@ -721,8 +726,11 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   const size_t smem = (size_t)t.n * omax * 8 + (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 +
                       (size_t)omax * 2 * omax * 8 + (size_t)t.n * omax * 4;
   cudaFuncSetAttribute(k_green_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_green_mixed<<<t.nw, 256, smem, st>>>(md, static_cast<const float2*>(wu), static_cast<const float2*>(wd),
-                                         ovl, write_ops ? 1 : 0);
+  {
+    ProfScope _ps(K_GREEN, st);
+    k_green_mixed<<<t.nw, 256, smem, st>>>(md, static_cast<const float2*>(wu), static_cast<const float2*>(wd),
+                                           ovl, write_ops ? 1 : 0);
+  }
   return launch_check("green_mixed");
 }
 
@@ -746,7 +754,7 @@ static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, doubl
   ep.part_fbt = t.part_fbt;
   ep.fb_out = fb_out;
   const int kt = (t.kfb + 63) / 64, mt = (2 * t.nw + 127) / 128;
-  return launch_gemm<256, 4, EpiFB>(t.m_fb, t.n_fb_terms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st);
+  return launch_gemm<256, 4, EpiFB>(K_FB, t.m_fb, t.n_fb_terms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st);
 }
 
 int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
@@ -775,7 +783,7 @@ static int exp_gemm(TcState& t, const afq_ctx_dev& c, int s, bool last, float2* 
   ep.bf16 = t.bf16 ? 1 : 0;
   ep.last = last ? 1 : 0;
   const int kt = (t.n + 63) / 64, nt = (t.nw * t.R[s] + t.bn_w[s] - 1) / t.bn_w[s];
-  return launch_gemm<256, 2, EpiExp>(last ? t.m_e2[s] : t.m_e1[s], t.n_e_terms, kt, 1, nt, t.bn_w[s], t.bf16,
+  return launch_gemm<256, 2, EpiExp>(K_EXP, last ? t.m_e2[s] : t.m_e1[s], t.n_e_terms, kt, 1, nt, t.bn_w[s], t.bf16,
                                      ep, t.status, st);
 }
 
@@ -796,7 +804,7 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.want_lo = want_lo ? 1 : 0;
     ev.sqdt = (float)sqrt(c.dt);
     const int kt = (c.nchol + 63) / 64, mt = (2 * t.nwc + 127) / 128, nt = (t.n * t.nq + 255) / 256;
-    TC_CHECK((launch_gemm<256, 4, EpiVHS>(t.m_vhs, t.n_vhs_terms, kt, mt, nt, 256, t.bf16, ev, t.status, st,
+    TC_CHECK((launch_gemm<256, 4, EpiVHS>(K_VHS, t.m_vhs, t.n_vhs_terms, kt, mt, nt, 256, t.bf16, ev, t.status, st,
                                          2 * w0)));
     for (int s = 0; s < t.nslab; ++s) {
       TaylorDev td;
@@ -814,8 +822,11 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
       td.acc_lo = t.acc[s][1];
       const size_t smem = taylor_smem(t.nq, t.NT[s], want_lo);
       cudaFuncSetAttribute(k_taylor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_taylor_tc<<<t.nwc, 128, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0], t.m_t0[s][1], td,
-                                            t.status);
+      {
+        ProfScope _ps(K_TAYLOR, st);
+        k_taylor_tc<<<t.nwc, 128, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0], t.m_t0[s][1], td,
+                                              t.status);
+      }
       TC_CHECK(launch_check("taylor_tc"));
     }
   }
@@ -842,11 +853,14 @@ int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
     ep.c_out = t.c_out + (size_t)b * t.nw * c.nchol;
     ep.exc_part = t.exc_part + (b == 0 ? 0 : (size_t)t.nw * t.mt_en[0]);
     const int kt = (t.n + 63) / 64, nt = (t.nw * t.Rb[b] + t.bnb[b] - 1) / t.bnb[b];
-    TC_CHECK((launch_gemm<240, 2, EpiEnergy>(t.m_en[b], t.n_en_terms, kt, t.mt_en[b], nt, t.bnb[b], t.bf16, ep,
+    TC_CHECK((launch_gemm<240, 2, EpiEnergy>(K_ENERGY, t.m_en[b], t.n_en_terms, kt, t.mt_en[b], nt, t.bnb[b], t.bf16, ep,
                                             t.status, st)));
   }
-  k_energy_final_mixed<<<t.nw, 256, 0, st>>>(t.nw, c.nchol, t.nblk, t.mt_en[0], t.nblk == 2 ? t.mt_en[1] : 0,
-                                             c.energy_mode, c.h0, t.c_out, t.exc_part, t.ene1, out);
+  {
+    ProfScope _ps(K_ENERGY_FIN, st);
+    k_energy_final_mixed<<<t.nw, 256, 0, st>>>(t.nw, c.nchol, t.nblk, t.mt_en[0], t.nblk == 2 ? t.mt_en[1] : 0,
+                                               c.energy_mode, c.h0, t.c_out, t.exc_part, t.ene1, out);
+  }
   return launch_check("energy_final_mixed");
 }
 
@@ -882,5 +896,5 @@ extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long 
   EpiStoreF32::Params ep{d, M, N, (long)N};
   const int kt = (K + 63) / 64, mt = (M + 127) / 128, nt = (N + bn - 1) / bn;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  return launch_gemm<256, 4, EpiStoreF32>(maps, nterms, kt, mt, nt, bn, bf16, ep, status, st);
+  return launch_gemm<256, 4, EpiStoreF32>(K_PREP, maps, nterms, kt, mt, nt, bn, bf16, ep, status, st);
 }

@@ -187,6 +187,20 @@ int afq_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, void
  * propagation.py:236-237. */
 int afq_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream);
 
+/* ---- launch accounting ----------------------------------------------------------------
+ * Diagnostics with no counterpart in the reference (which has no profiler hooks). Every
+ * kernel launch is counted per kernel class; with timing enabled, each launch is also
+ * bracketed by a CUDA-event pair recorded on its own stream. */
+
+/* Reset counters; on != 0 also records event pairs around every launch. */
+int afq_profile_enable(int on);
+int afq_profile_reset(void);
+/* Launches of class `cls` since the last reset and, when timing is on, their summed
+ * device time in milliseconds (synchronises on the recorded events). */
+int afq_profile_read(int cls, double* total_ms, int64_t* launches);
+const char* afq_profile_class_name(int cls);
+int afq_profile_num_classes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,21 +78,21 @@ def rhf_green(walkers: np.ndarray, mo: np.ndarray) -> np.ndarray:
 def rhf_force_bias_restricted(walkers, rot_chol, mo) -> np.ndarray:
     """2 sum_ij rot_chol[g,i,j] G[i,j] (wavefunctions.py:503-511)."""
     g = rhf_green(walkers, mo)
-    return 2.0 * np.einsum("gij,wij->wg", rot_chol, g)
+    return 2.0 * np.einsum("gij,wij->wg", rot_chol, g, optimize=True)
 
 
 def rhf_force_bias(walkers_up, walkers_dn, rot_chol, mo) -> np.ndarray:
     """Two-slab walkers, G_up + G_dn contracted once (wavefunctions.py:513-527)."""
     g = rhf_green(walkers_up, mo) + rhf_green(walkers_dn, mo)
-    return np.einsum("gij,wij->wg", rot_chol, g)
+    return np.einsum("gij,wij->wg", rot_chol, g, optimize=True)
 
 
 def _exchange_coulomb(rot_chol: np.ndarray, green: np.ndarray):
     """f_g = rot_chol_g G^T per walker; returns (c [nw,G], exc [nw]) with c_g = tr f_g and
     exc = sum_g sum_ik f_g[i,k] f_g[k,i] (wavefunctions.py:537-539)."""
-    f = np.einsum("gij,wkj->wgik", rot_chol, green)
-    c = np.einsum("wgii->wg", f)
-    exc = np.einsum("wgik,wgki->w", f, f)
+    f = np.einsum("gij,wkj->wgik", rot_chol, green, optimize=True)
+    c = np.einsum("wgii->wg", f, optimize=True)
+    exc = np.einsum("wgik,wgki->w", f, f, optimize=True)
     return c, exc
 
 
@@ -100,7 +100,7 @@ def rhf_energy_restricted(walkers, h0, rot_h1, rot_chol, mo) -> np.ndarray:
     """Mixed local energy, RHF restricted walkers (wavefunctions.py:529-541):
     h0 + 2 sum G*rot_h1 + 2 sum_g c_g^2 - exc."""
     g = rhf_green(walkers, mo)
-    ene1 = 2.0 * np.einsum("wij,ij->w", g, rot_h1)
+    ene1 = 2.0 * np.einsum("wij,ij->w", g, rot_h1, optimize=True)
     c, exc = _exchange_coulomb(rot_chol, g)
     ene2 = 2.0 * np.sum(c * c, axis=1) - exc
     return ene2 + ene1 + h0
@@ -109,7 +109,7 @@ def rhf_energy_restricted(walkers, h0, rot_h1, rot_chol, mo) -> np.ndarray:
 def rhf_energy(walkers_up, walkers_dn, h0, rot_h1, rot_chol, mo) -> np.ndarray:
     """Two-slab walkers with the RHF trial (wavefunctions.py:543-561)."""
     g = rhf_green(walkers_up, mo) + rhf_green(walkers_dn, mo)
-    ene1 = np.einsum("wij,ij->w", g, rot_h1)
+    ene1 = np.einsum("wij,ij->w", g, rot_h1, optimize=True)
     c, exc = _exchange_coulomb(rot_chol, g)
     return np.sum(c * c, axis=1) - exc + ene1 + h0
 
@@ -154,7 +154,8 @@ def uhf_energy(walkers_up, walkers_dn, h0, rot_h1, rot_chol, mo) -> np.ndarray:
     """(sum c_up^2 + sum c_dn^2 + 2 sum c_up c_dn - exc_up - exc_dn)/2 + ene1 + h0
     (wavefunctions.py:711-743)."""
     g = uhf_green(walkers_up, walkers_dn, mo)
-    ene1 = np.einsum("wij,ij->w", g[0], rot_h1[0]) + np.einsum("wij,ij->w", g[1], rot_h1[1])
+    ene1 = (np.einsum("wij,ij->w", g[0], rot_h1[0], optimize=True)
+            + np.einsum("wij,ij->w", g[1], rot_h1[1], optimize=True))
     c_up, exc_up = _exchange_coulomb(rot_chol[0], g[0])
     c_dn, exc_dn = _exchange_coulomb(rot_chol[1], g[1])
     ene2 = (
@@ -245,11 +246,11 @@ def build_propagation_intermediates(
     """
     chol = np.asarray(ham_data["chol"]).reshape(-1, norb, norb)
     rho = rdm1[0] + rdm1[1]
-    mf = 1.0j * np.einsum("gij,ij->g", chol, rho)
+    mf = 1.0j * np.einsum("gij,ij->g", chol, rho, optimize=True)
     ham_data["mf_shifts"] = mf
     ham_data["h0_prop"] = -ham_data["h0"] - np.sum(mf**2) / 2.0
-    v0 = 0.5 * np.einsum("gik,gjk->ij", chol, chol)
-    v1 = np.real(1.0j * np.einsum("g,gik->ik", mf, chol))
+    v0 = 0.5 * np.einsum("gik,gjk->ij", chol, chol, optimize=True)
+    v1 = np.real(1.0j * np.einsum("g,gik->ik", mf, chol, optimize=True))
     h1 = np.asarray(ham_data["h1"])
     if restricted:
         h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
