@@ -79,7 +79,8 @@ _SIGS = {
 _TEST_SIGS = {
     "afq_test_gemm_f16": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_long, ctypes.c_long, _vp,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         _vp, _vp]),
 }
 _SIGS.update(_TEST_SIGS)
 

@@ -11,6 +11,13 @@
 // warp 1 owns the TMEM allocation and lane 0 issues the MMAs; warps 2..5 run the epilogue
 // (warp w reads TMEM lanes 32*(w%4) .. 32*(w%4)+31). Every wait is bounded: on a timeout the
 // CTA records a nonzero word in *status and still frees its TMEM.
+//
+// Accumulation. The tensor core adds each MMA's products into the FP32 accumulator with
+// truncation, which biases long sums toward zero by about 6e-9 * K relative (measured on
+// GB300: -1.5e-5 at K = 2400). With drain = d > 0 the MMAs of every d consecutive K tiles go
+// into a fresh accumulator (two, used alternately), and the epilogue warps add each finished
+// accumulator into a third TMEM region with round-to-nearest FP32 adds while the tensor
+// core fills the other one. Every truncated run then spans 4 d MMAs only.
 #pragma once
 #include "afq_ptx.cuh"
 
@@ -42,19 +49,22 @@ __host__ __device__ constexpr int gemm_smem_bytes() {
 template <int BNMAX, int STAGES, class Epi>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     k_gemm_tc(const __grid_constant__ GemmMaps maps, int nterms, int k_tiles, int bn, int a_row0,
-              uint32_t idesc, const __grid_constant__ typename Epi::Params ep, int* status) {
+              int drain, uint32_t idesc, const __grid_constant__ typename Epi::Params ep,
+              int* status) {
   static_assert(BNMAX % 16 == 0 && BNMAX >= 16 && BNMAX <= 256, "BNMAX");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr int A_BYTES = 128 * 128;  // 128 rows x 64 x 16-bit
   constexpr int STAGE = A_BYTES + BNMAX * 128;
-  const uint32_t TMEM_COLS = gemm_tmem_cols(bn);
+  const uint32_t TMEM_COLS = gemm_tmem_cols(drain ? 3 * bn : bn);
   const uint32_t tx_bytes = A_BYTES + bn * 128;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
   uint64_t* empty = full + STAGES;
   uint64_t* accb = empty + STAGES;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(accb + 1);
+  uint64_t* accfull = accb + 1;    // [2]
+  uint64_t* accempty = accb + 3;   // [2]
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(accb + 5);
   unsigned char* epi_smem = smem + STAGES * STAGE + 256;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -67,6 +77,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       ptx::mbar_init(&empty[s], 1);
     }
     ptx::mbar_init(accb, 1);
+    for (int a = 0; a < 2; ++a) {
+      ptx::mbar_init(&accfull[a], 1);
+      ptx::mbar_init(&accempty[a], 4);  // one arrival per epilogue warp
+    }
     ptx::fence_mbar_init();
   }
   if (warp == 1) {
@@ -105,27 +119,94 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      for (int it = 0; it < total; ++it) {
-        const int s = it % STAGES, r = it / STAGES;
-        if (!ptx::mbar_wait(&full[s], r & 1)) {
-          ok = false;
-          break;
-        }
-        ptx::tc_fence_after();
-        const uint32_t sa = ptx::smem_u32(smem + s * STAGE), sb = sa + A_BYTES;
+      if (!drain) {
+        for (int it = 0; it < total; ++it) {
+          const int s = it % STAGES, r = it / STAGES;
+          if (!ptx::mbar_wait(&full[s], r & 1)) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t sa = ptx::smem_u32(smem + s * STAGE), sb = sa + A_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          ptx::mma_f16(tmem, ptx::desc_kmajor_sw128(sa + kk * 32), ptx::desc_kmajor_sw128(sb + kk * 32),
-                       idesc, (it > 0 || kk > 0) ? 1u : 0u);
+          for (int kk = 0; kk < 4; ++kk) {
+            ptx::mma_f16(tmem, ptx::desc_kmajor_sw128(sa + kk * 32), ptx::desc_kmajor_sw128(sb + kk * 32),
+                         idesc, (it > 0 || kk > 0) ? 1u : 0u);
+          }
+          ptx::mma_commit(&empty[s]);
         }
-        ptx::mma_commit(&empty[s]);
+        ptx::mma_commit(accb);
+      } else {
+        const int nruns = (total + drain - 1) / drain;
+        for (int run = 0; run < nruns && ok; ++run) {
+          const int a = run & 1;
+          if (run >= 2 && !ptx::mbar_wait(&accempty[a], ((run - 2) >> 1) & 1)) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t dacc = tmem + (uint32_t)((1 + a) * bn);
+          const int it0 = run * drain, it1 = min(total, it0 + drain);
+          for (int it = it0; it < it1; ++it) {
+            const int s = it % STAGES, r = it / STAGES;
+            if (!ptx::mbar_wait(&full[s], r & 1)) {
+              ok = false;
+              break;
+            }
+            ptx::tc_fence_after();
+            const uint32_t sa = ptx::smem_u32(smem + s * STAGE), sb = sa + A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              ptx::mma_f16(dacc, ptx::desc_kmajor_sw128(sa + kk * 32), ptx::desc_kmajor_sw128(sb + kk * 32),
+                           idesc, (it > it0 || kk > 0) ? 1u : 0u);
+            }
+            ptx::mma_commit(&empty[s]);
+          }
+          ptx::mma_commit(&accfull[a]);
+        }
+        // every MMA this thread issued has completed before TMEM is released
+        ptx::mma_commit(accb);
+        if (!ptx::mbar_wait(accb, 0)) ok = false;
       }
-      ptx::mma_commit(accb);
     }
   } else {
     const int q = warp & 3;
-    const bool got = ptx::mbar_wait(accb, 0);
-    ptx::tc_fence_after();
+    bool got = true;
+    if (!drain) {
+      got = ptx::mbar_wait(accb, 0);
+      ptx::tc_fence_after();
+    } else {
+      const int nruns = (total + drain - 1) / drain;
+      const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+      for (int run = 0; run < nruns; ++run) {
+        const int a = run & 1;
+        if (!ptx::mbar_wait(&accfull[a], (run >> 1) & 1)) {
+          got = false;
+          break;
+        }
+        ptx::tc_fence_after();
+#pragma unroll 1
+        for (int c0 = 0; c0 < bn; c0 += 16) {
+          float v[16];
+          ptx::tmem_ld16(tmem + lane_off + (uint32_t)((1 + a) * bn + c0), v);
+          if (run > 0) {
+            float sum[16];
+            ptx::tmem_ld16(tmem + lane_off + (uint32_t)c0, sum);
+            ptx::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] += sum[j];
+          } else {
+            ptx::tmem_ld_wait();
+          }
+          ptx::tmem_st16(tmem + lane_off + (uint32_t)c0, v);
+        }
+        ptx::tmem_st_wait();
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&accempty[a]);
+      }
+      ptx::tc_fence_after();
+    }
     if (!got) ok = false;
     Epi::run(ep, m0, n0, bn, tmem, q, lane, epi_smem, got);
   }

@@ -37,13 +37,13 @@ __device__ __forceinline__ float pow2_scale(float amax) {
 // Plain-data view of the mixed state passed to kernels.
 struct MixedDev {
   int n, nq, nk, ldfb, ldg, nw, nchol, nslab, nblk, kfb, restricted_square, energy_mode;
-  int o_slab[2], R[2], o_blk[2], Rb[2];
+  int o_slab[2], R[2], o_blk[2], ldkb[2];
   int bf16;
   double h0;
   const float* trial32[2];
   const float* rh1_32[2];
   uint16_t* g_fb[2];
-  uint16_t* gen[2][2];
+  uint16_t* g_blk[2][2];  // per-block Green operand (two Green blocks only)
   uint16_t* wt[2][2];
   float* g_inv;
   double2* ene1;
@@ -52,11 +52,12 @@ struct MixedDev {
 // ======================================================================================
 // Green's function, overlap and operand packing. One CTA per walker.
 // S_s = C_s^T W_s (FP32), Gauss-Jordan on [S | I] in FP32 with partial pivoting, the
-// determinant kept as FP64 log-modulus and phase. G_s = (W_s S_s^-1)^T (FP32).
+// determinant accumulated in FP64 as the signed product of the pivots (for both spins and
+// squared for restricted walkers). G_s = (W_s S_s^-1)^T (FP32).
 // wavefunctions.py:478-501 (rhf), 658-692 (uhf).
 // ======================================================================================
 
-__global__ void __launch_bounds__(256) k_green_mixed(const MixedDev md, const float2* __restrict__ wu,
+__global__ void __launch_bounds__(128) k_green_mixed(const MixedDev md, const float2* __restrict__ wu,
                                                      const float2* __restrict__ wd,
                                                      double2* __restrict__ ovl, int write_ops) {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -71,8 +72,7 @@ __global__ void __launch_bounds__(256) k_green_mixed(const MixedDev md, const fl
   __shared__ int piv_sh;
   __shared__ float gmax_sh[32];
   __shared__ float2 colj[64];
-  double logabs = 0.0;          // thread 0 only
-  double2 phase = c2(1.0, 0.0);  // thread 0 only
+  double2 det = c2(1.0, 0.0);  // thread 0 only: product of the FP32 pivots, in FP64
   const bool bf = md.bf16 != 0;
 
   for (int s = 0; s < md.nslab; ++s) {
@@ -138,11 +138,8 @@ __global__ void __launch_bounds__(256) k_green_mixed(const MixedDev md, const fl
       __syncthreads();
       const float2 pv = Aug[j * 2 * o + j];
       if (tid == 0) {
-        const double m = hypot((double)pv.x, (double)pv.y);
-        logabs += log(m);
-        double2 u = c2(pv.x / m, pv.y / m);
-        if (pr != j) u = c2(-u.x, -u.y);
-        phase = cmul(phase, u);
+        det = cmul(det, c2((double)pv.x, (double)pv.y));
+        if (pr != j) det = c2(-det.x, -det.y);
       }
       const float2 inv = cdiv(make_float2(1.f, 0.f), pv);
       __syncthreads();
@@ -170,16 +167,7 @@ __global__ void __launch_bounds__(256) k_green_mixed(const MixedDev md, const fl
     }
     __syncthreads();
   }
-  if (tid == 0 && ovl) {
-    double la = logabs;
-    double2 ph = phase;
-    if (md.restricted_square) {
-      la *= 2.0;
-      ph = cmul(ph, ph);
-    }
-    const double m = exp(la);
-    ovl[w] = c2(m * ph.x, m * ph.y);
-  }
+  if (tid == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
   if (!write_ops) return;
   // ---- scale, pack, ene1
   float mx = 0.f;
@@ -206,17 +194,17 @@ __global__ void __launch_bounds__(256) k_green_mixed(const MixedDev md, const fl
     split16(g.y * scl, bf, h, l);
     md.g_fb[0][(size_t)(2 * w + 1) * md.ldfb + e] = h;
     md.g_fb[1][(size_t)(2 * w + 1) * md.ldfb + e] = l;
-    // energy operand of block b: row (w, 2k + c), column p
+    // per-block operand (exchange / Coulomb contractions of each spin separately)
     const int b = (md.nblk == 2 && e >= md.o_blk[0] * n) ? 1 : 0;
     const int eb = e - b * md.o_blk[0] * n;
-    const int k = eb / n, p = eb % n;
-    const size_t row = (size_t)w * md.Rb[b] + 2 * k;
-    split16(g.x * scl, bf, h, l);
-    md.gen[b][0][row * md.nk + p] = h;
-    md.gen[b][1][row * md.nk + p] = l;
-    split16(g.y * scl, bf, h, l);
-    md.gen[b][0][(row + 1) * md.nk + p] = h;
-    md.gen[b][1][(row + 1) * md.nk + p] = l;
+    if (md.nblk == 2) {
+      split16(g.x * scl, bf, h, l);
+      md.g_blk[b][0][(size_t)(2 * w) * md.ldkb[b] + eb] = h;
+      md.g_blk[b][1][(size_t)(2 * w) * md.ldkb[b] + eb] = l;
+      split16(g.y * scl, bf, h, l);
+      md.g_blk[b][0][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = h;
+      md.g_blk[b][1][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = l;
+    }
     const float r1 = md.rh1_32[b][eb];
     e1x += (double)(g.x * r1);
     e1y += (double)(g.y * r1);
@@ -404,83 +392,67 @@ struct EpiExp {
 };
 
 // ======================================================================================
-// Energy GEMM epilogue (wavefunctions.py:535-540, 725-741): the tile holds
-// f_g[i][k] = (rot_chol_g G^T)[i][k] for gpt values of g (rows g_local*o + i) and wpt walkers
-// (columns w_local*R + 2k + re/im). Per (g, w): c_g = tr f_g and exc_g = sum_ik f_ik f_ki.
-// Writes c[w][g] and the tile's partial sum of exc per walker.
+// Exchange epilogue. D[(i,q)][(w, re/im)] = Z_w[(i,q)] = sum_(k,p) U[(i,q),(k,p)] G_w[k,p] with
+// U[(i,q),(k,p)] = sum_g rot_chol_g[i,p] rot_chol_g[k,q], so that the exchange sum of
+// wavefunctions.py:539 (and 737-738), exc = sum_g sum_ik f_g[i,k] f_g[k,i] with
+// f_g = rot_chol_g G^T, equals sum_(i,q) Z_w[(i,q)] G_w[i,q]. Writes the tile's partial sum
+// of exc per walker (rows of the tile summed), unscaled.
 // ======================================================================================
 
-struct EpiEnergy {
+struct EpiExc {
   struct Params {
-    const float* ren_inv;
-    const float* g_inv;
-    int o, R, gpt, nchol, nw, mt;
-    double2* c_out;     // [nw][nchol]
-    double2* exc_part;  // [nw][mt]
+    const uint16_t* g_hi;  // [2 nw][ldk] Green operand (rows 2w, 2w+1 = re, im)
+    const uint16_t* g_lo;
+    const float* g_inv;    // [nw]
+    float u_inv;
+    int kb, ldk, nw, mt, bf16;
+    double2* exc_part;     // [nw][mt]
   };
-  static constexpr int kCols = 241;
-  static constexpr int kMaxPairs = 256;  // gpt * wpt
-  static constexpr int kMaxWpt = 32;
-  static constexpr int kSmemBytes = 128 * kCols * 4 + kMaxPairs * 8 + kMaxWpt * 16;
+  static constexpr int kSmemBytes = 4 * 128 * 8;
   __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
                              unsigned char* smem, bool) {
-    float* F = reinterpret_cast<float*>(smem);
-    float2* cs = reinterpret_cast<float2*>(F + 128 * kCols);  // [kMaxPairs]
-    double* exx = reinterpret_cast<double*>(cs + kMaxPairs);  // [kMaxWpt] re, then im
-    double* exy = exx + kMaxWpt;
-    const int t = q * 32 + lane;  // 0..127 (lane quadrant order)
-    const int r = t;
-    const int wpt = bn / p.R;
-    const int tile_m = m0 / 128;
-    const int g0 = tile_m * p.gpt;
-    const int gcount = min(p.gpt, p.nchol - g0);
-    const int w0 = n0 / p.R;
+    float2* part = reinterpret_cast<float2*>(smem);  // [4][128]
+    const int r = m0 + q * 32 + lane;
+    const bool rv = r < p.kb;
+    const bool bf = p.bf16 != 0;
 #pragma unroll 1
     for (int c0 = 0; c0 < bn; c0 += 16) {
       float v[16];
       ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
       ptx::tmem_ld_wait();
 #pragma unroll
-      for (int j = 0; j < 16; ++j) F[r * kCols + c0 + j] = v[j];
-    }
-    for (int i = t; i < kMaxPairs; i += 128) cs[i] = make_float2(0.f, 0.f);
-    for (int i = t; i < kMaxWpt; i += 128) {
-      exx[i] = 0.0;
-      exy[i] = 0.0;
-    }
-    ptx::named_bar_sync(1, 128);
-    // items (g_local, w_local, i)
-    const int npair = gcount * wpt;
-    for (int it = t; it < npair * p.o; it += 128) {
-      const int pi = it / p.o, i = it % p.o;
-      const int gl = pi / wpt, wl = pi % wpt;
-      const float* Fi = F + (gl * p.o + i) * kCols + wl * p.R;
-      float ex = 0.f, ey = 0.f;
-      for (int k = 0; k < p.o; ++k) {
-        const float* Fk = F + (gl * p.o + k) * kCols + wl * p.R;
-        const float ar = Fi[2 * k], ai = Fi[2 * k + 1];
-        const float br = Fk[2 * i], bi = Fk[2 * i + 1];
-        ex = fmaf(ar, br, fmaf(-ai, bi, ex));
-        ey = fmaf(ar, bi, fmaf(ai, br, ey));
-      }
-      atomicAdd(&cs[pi].x, Fi[2 * i]);
-      atomicAdd(&cs[pi].y, Fi[2 * i + 1]);
-      const int wglob = w0 + wl;
-      const float s = (wglob < p.nw) ? p.ren_inv[g0 + gl] * p.g_inv[wglob] : 0.f;
-      atomicAdd(&exx[wl], (double)(ex * s * s));
-      atomicAdd(&exy[wl], (double)(ey * s * s));
-    }
-    ptx::named_bar_sync(1, 128);
-    for (int pi = t; pi < npair; pi += 128) {
-      const int gl = pi / wpt, wl = pi % wpt, wg = w0 + wl, g = g0 + gl;
-      if (wg < p.nw) {
-        const float s = p.ren_inv[g] * p.g_inv[wg];
-        p.c_out[(size_t)wg * p.nchol + g] = c2(cs[pi].x * s, cs[pi].y * s);
+      for (int jj = 0; jj < 8; ++jj) {
+        const int w = (n0 + c0) / 2 + jj;
+        float px = 0.f, py = 0.f;
+        if (rv && w < p.nw) {
+          const size_t ir = (size_t)(2 * w) * p.ldk + r, ii = ir + p.ldk;
+          const float gr = h2f(p.g_hi[ir], bf) + h2f(p.g_lo[ir], bf);
+          const float gi = h2f(p.g_hi[ii], bf) + h2f(p.g_lo[ii], bf);
+          const float zr = v[2 * jj], zi = v[2 * jj + 1];
+          px = zr * gr - zi * gi;
+          py = zr * gi + zi * gr;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          px += __shfl_xor_sync(0xffffffffu, px, off);
+          py += __shfl_xor_sync(0xffffffffu, py, off);
+        }
+        if (lane == 0) part[q * 128 + c0 / 2 + jj] = make_float2(px, py);
       }
     }
-    for (int wl = t; wl < wpt; wl += 128) {
-      const int wg = w0 + wl;
-      if (wg < p.nw) p.exc_part[(size_t)wg * p.mt + tile_m] = c2(exx[wl], exy[wl]);
+    ptx::named_bar_sync(1, 128);
+    const int t = q * 32 + lane;
+    if (t < bn / 2) {
+      const int w = n0 / 2 + t;
+      if (w < p.nw) {
+        double sx = 0.0, sy = 0.0;
+        for (int qq = 0; qq < 4; ++qq) {
+          sx += part[qq * 128 + t].x;
+          sy += part[qq * 128 + t].y;
+        }
+        const double s = (double)p.g_inv[w] * (double)p.g_inv[w] * (double)p.u_inv;
+        p.exc_part[(size_t)w * p.mt + m0 / 128] = c2(sx * s, sy * s);
+      }
     }
   }
 };

@@ -325,37 +325,40 @@ __global__ void __launch_bounds__(256) k_taylor_f64(const afq_ctx_dev c, int w0,
 __global__ void k_weights(int nw, double dt, double2 h0_prop, const double2* __restrict__ shift,
                           const double2* __restrict__ fbt, int ntiles,
                           const double2* __restrict__ ovl_new, double2* __restrict__ ovl,
-                          double* __restrict__ weights, double* __restrict__ scalars) {
-  __shared__ double red[32];
+                          double* __restrict__ weights, const double* __restrict__ scalars) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
   const double sqdt = sqrt(dt);
   const double pcs = scalars[AFQ_S_POP_CONTROL_SHIFT];
-  double sum = 0.0;
-  for (int w = threadIdx.x; w < nw; w += blockDim.x) {
-    double2 ratio = cdiv(ovl_new[w], ovl[w]);
-    double2 sh = c2(0, 0), fb = c2(0, 0);
-    for (int t = 0; t < ntiles; ++t) {
-      sh = cadd(sh, shift[(size_t)w * ntiles + t]);
-      fb = cadd(fb, fbt[(size_t)w * ntiles + t]);
-    }
-    double2 arg = c2(-sqdt * sh.x + fb.x + dt * (pcs + h0_prop.x),
-                     -sqdt * sh.y + fb.y + dt * h0_prop.y);
-    double2 imp = cmul(cexp_(arg), ratio);
-    double2 ph = cmul(cexp_(c2(-sqdt * sh.x, -sqdt * sh.y)), ratio);
-    double theta = atan2(ph.y, ph.x);
-    double v = hypot(imp.x, imp.y) * cos(theta);
-    if (isnan(v)) v = 0.0;
-    if (v < 1.0e-3) v = 0.0;
-    if (v > 100.0) v = 0.0;
-    double nwgt = v * weights[w];
-    if (nwgt > 100.0) nwgt = 0.0;
-    weights[w] = nwgt;
-    ovl[w] = ovl_new[w];
-    sum += nwgt;
+  double2 ratio = cdiv(ovl_new[w], ovl[w]);
+  double2 sh = c2(0, 0), fb = c2(0, 0);
+  for (int t = 0; t < ntiles; ++t) {
+    sh = cadd(sh, shift[(size_t)w * ntiles + t]);
+    fb = cadd(fb, fbt[(size_t)w * ntiles + t]);
   }
+  double2 arg = c2(-sqdt * sh.x + fb.x + dt * (pcs + h0_prop.x), -sqdt * sh.y + fb.y + dt * h0_prop.y);
+  double2 imp = cmul(cexp_(arg), ratio);
+  double2 ph = cmul(cexp_(c2(-sqdt * sh.x, -sqdt * sh.y)), ratio);
+  double theta = atan2(ph.y, ph.x);
+  double v = hypot(imp.x, imp.y) * cos(theta);
+  if (isnan(v)) v = 0.0;
+  if (v < 1.0e-3) v = 0.0;
+  if (v > 100.0) v = 0.0;
+  double nwgt = v * weights[w];
+  if (nwgt > 100.0) nwgt = 0.0;
+  weights[w] = nwgt;
+  ovl[w] = ovl_new[w];
+}
+
+// pop_control_ene_shift = e_estimate - 0.1 log(sum w / nw) / dt (propagation.py:161-163)
+__global__ void k_pop_control(int nw, double dt, const double* __restrict__ weights,
+                              double* __restrict__ scalars) {
+  __shared__ double red[32];
+  double sum = 0.0;
+  for (int w = threadIdx.x; w < nw; w += blockDim.x) sum += weights[w];
   sum = block_sum(sum, red);
   if (threadIdx.x == 0)
-    scalars[AFQ_S_POP_CONTROL_SHIFT] =
-        scalars[AFQ_S_E_ESTIMATE] - 0.1 * log(sum / (double)nw) / dt;
+    scalars[AFQ_S_POP_CONTROL_SHIFT] = scalars[AFQ_S_E_ESTIMATE] - 0.1 * log(sum / (double)nw) / dt;
 }
 
 // ======================================================================================
@@ -737,12 +740,15 @@ __global__ void k_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t of
   if (i0 >= n) return;
   uint64_t ctr = (offset >> 1) + (uint64_t)pair;
   uint4 r = philox4x32(ctr, seed);
-  double u1 = u53(r.x, r.y), u2 = u53(r.z, r.w);
-  double rad = sqrt(-2.0 * log(u1));
-  double s, co;
-  sincospi(2.0 * u2, &s, &co);
-  out[i0] = rad * co;
-  if (i0 + 1 < n) out[i0 + 1] = rad * s;
+  // Box-Muller in FP32 arithmetic (FP64 transcendentals are slow on this part); u1 uses
+  // 32 random bits in (0, 1], so the radius reaches 6.7 sigma
+  const float u1 = ((float)r.x + 1.0f) * 2.3283064365386963e-10f;
+  const float u2 = (float)(r.z >> 8) * 5.9604644775390625e-08f;
+  const float rad = sqrtf(-2.0f * logf(u1));
+  float s, co;
+  sincospif(2.0f * u2, &s, &co);
+  out[i0] = (double)(rad * co);
+  if (i0 + 1 < n) out[i0 + 1] = (double)(rad * s);
 }
 
 __global__ void k_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset) {
@@ -817,8 +823,12 @@ int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fb
                    cudaStream_t st) {
   {
     ProfScope _ps(K_WEIGHTS, st);
-    k_weights<<<1, 1024, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt, ntiles,
-                                  ovl_new, ovl, weights, scalars);
+    k_weights<<<(c.nw + 31) / 32, 32, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt,
+                                               ntiles, ovl_new, ovl, weights, scalars);
+  }
+  {
+    ProfScope _ps(K_WEIGHTS, st);
+    k_pop_control<<<1, 1024, 0, st>>>(c.nw, c.dt, weights, scalars);
   }
   return launch_err("weights");
 }

@@ -70,11 +70,12 @@ static int launch_check(const char* what) {
     if (_e) return _e; \
   } while (0)
 
+// drain > 0: K tiles per truncated accumulation run (see afq_gemm.cuh); needs 3 bn <= 512
 template <int BNMAX, int STAGES, class Epi>
 static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, int m_tiles, int n_tiles,
                        int bn, bool bf16, const typename Epi::Params& ep, int* status,
-                       cudaStream_t st, int a_row0 = 0) {
-  if (bn % 16 || bn < 16 || bn > BNMAX) {
+                       cudaStream_t st, int a_row0 = 0, int drain = 0) {
+  if (bn % 16 || bn < 16 || bn > BNMAX || (drain && 3 * bn > 512)) {
     afq_set_error("gemm: bn %d invalid", bn);
     return -1;
   }
@@ -85,7 +86,7 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
   {
     ProfScope _ps(cls, st);
     kfn<<<dim3(n_tiles, m_tiles), kGemmThreads, smem, st>>>(
-        maps, nterms, k_tiles, bn, a_row0, ptx::idesc_f16(128, bn, bf16 ? 1 : 0), ep, status);
+        maps, nterms, k_tiles, bn, a_row0, drain, ptx::idesc_f16(128, bn, bf16 ? 1 : 0), ep, status);
   }
   return launch_check("gemm_tc");
 }
@@ -95,7 +96,9 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
 // first exp_h1 product), T_m = V T_{m-1} / m on the tensor cores with V = [Vr | Vi] held in
 // shared memory, acc = sum_m T_m in FP32 registers. The first `split` products use
 // V_hi T_hi + V_hi T_lo + V_lo T_hi. Writes acc as the B operand of the last exp_h1 product.
-// One CTA (4 warps, thread p <-> orbital row p <-> TMEM lane p) per walker.
+// One CTA (4 warps, thread p <-> orbital row p <-> TMEM lane p) per walker. Each K tile of
+// V_hi T_hi, and each correction product, accumulates in its own 64-column TMEM region (the
+// tensor core truncates when it accumulates), summed with round-to-nearest in registers.
 // ======================================================================================
 
 struct TaylorDev {
@@ -130,7 +133,7 @@ __global__ void __launch_bounds__(128, 1)
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int wl = blockIdx.x, wg = td.w0 + wl;
-  const uint32_t tcols = gemm_tmem_cols(td.NT);
+  const uint32_t tcols = gemm_tmem_cols((KT + 2) * 64);
   const bool bf = td.bf16 != 0;
   bool ok = true;
 
@@ -183,18 +186,19 @@ __global__ void __launch_bounds__(128, 1)
   for (int m = 1; m < td.nterms; ++m) {
     if (tid == 0 && ok) {
       ptx::tc_fence_after();
-      uint32_t nmma = 0;
       const int ngroups = (m <= td.split) ? 3 : 1;
       for (int gi = 0; gi < ngroups; ++gi) {
         const uint32_t va = gi == 2 ? sVl : sVh;
         const uint32_t ba = gi == 1 ? sBl : sBh;
-        for (int kt = 0; kt < KT; ++kt)
+        for (int kt = 0; kt < KT; ++kt) {
+          // region: one per K tile for the main product, one per correction product
+          const uint32_t dreg = tmem + (uint32_t)(64 * (gi == 0 ? kt : KT + gi - 1));
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            ptx::mma_f16(tmem, ptx::desc_kmajor_sw128(va + kt * VT + kk * 32),
-                         ptx::desc_kmajor_sw128(ba + kt * BT + kk * 32), idesc, nmma > 0 ? 1u : 0u);
-            ++nmma;
-          }
+          for (int kk = 0; kk < 4; ++kk)
+            ptx::mma_f16(dreg, ptx::desc_kmajor_sw128(va + kt * VT + kk * 32),
+                         ptx::desc_kmajor_sw128(ba + kt * BT + kk * 32), idesc,
+                         (kk > 0 || (gi > 0 && kt > 0)) ? 1u : 0u);
+        }
       }
       ptx::mma_commit(mma_bar);
     }
@@ -205,17 +209,19 @@ __global__ void __launch_bounds__(128, 1)
     }
     ptx::tc_fence_after();
     float d[64];
+    const int nreg = KT + ((m <= td.split) ? 2 : 0);
 #pragma unroll
     for (int c0 = 0; c0 < 64; c0 += 16) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) d[c0 + j] = 0.f;
       if (c0 < td.NT) {
-        float v[16];
-        ptx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
-        ptx::tmem_ld_wait();
+        for (int rg = 0; rg < nreg; ++rg) {
+          float v[16];
+          ptx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(64 * rg + c0), v);
+          ptx::tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) d[c0 + j] = v[j];
-      } else {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) d[c0 + j] = 0.f;
+          for (int j = 0; j < 16; ++j) d[c0 + j] += v[j];
+        }
       }
     }
     const float invm = 1.0f / (float)m;
@@ -318,19 +324,52 @@ __global__ void k_prep_rows_scaled(const double* __restrict__ src, int len, int 
   }
 }
 
-// energy A operand: rot_chol_b [nchol][o][n] -> rows (g / gpt) * 128 + (g % gpt) * o + i
-__global__ void k_prep_ren(const double* __restrict__ rc, int o, int n, int nk, int gpt, int bf16,
-                           const float* __restrict__ inv, uint16_t* __restrict__ hi,
-                           uint16_t* __restrict__ lo) {
-  const int g = blockIdx.x;
-  const double scl = 1.0 / (double)inv[g];
-  const size_t row0 = (size_t)(g / gpt) * 128 + (size_t)(g % gpt) * o;
-  for (int e = threadIdx.x; e < o * n; e += blockDim.x) {
-    const int i = e / n, p = e % n;
+// exchange matrix: V[(i,p),(k,q)] = sum_g rc[g][i*n+p] rc[g][k*n+q] in FP64, written as
+// U[(i,q),(k,p)] (FP32 scratch, row stride ldk); *amax <- max |U| (float bits, non-negative)
+__global__ void k_prep_u(const double* __restrict__ rc, int nchol, int kb, int n, int ldk,
+                         float* __restrict__ u, unsigned* __restrict__ amax) {
+  __shared__ double xa[16][33], xb[16][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  double acc[4] = {0, 0, 0, 0};
+  for (int g0 = 0; g0 < nchol; g0 += 16) {
+    for (int e = threadIdx.x; e < 16 * 32; e += 256) {
+      const int gg = e / 32, cc = e % 32, g = g0 + gg;
+      xa[gg][cc] = (g < nchol && r0 + cc < kb) ? rc[(size_t)g * kb + r0 + cc] : 0.0;
+      xb[gg][cc] = (g < nchol && c0 + cc < kb) ? rc[(size_t)g * kb + c0 + cc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int gg = 0; gg < 16; ++gg) {
+      const double bv = xb[gg][tx];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[j] = fma(xa[gg][ty + 8 * j], bv, acc[j]);
+    }
+    __syncthreads();
+  }
+  float mx = 0.f;
+  for (int j = 0; j < 4; ++j) {
+    const int vr = r0 + ty + 8 * j, vc = c0 + tx;  // V row (i,p), V column (k,q)
+    if (vr < kb && vc < kb) {
+      const int i = vr / n, pp = vr % n, k = vc / n, qq = vc % n;
+      const float val = (float)acc[j];
+      u[(size_t)(i * n + qq) * ldk + (k * n + pp)] = val;
+      mx = fmaxf(mx, fabsf(val));
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if (tx == 0) atomicMax(amax, __float_as_uint(mx));
+}
+
+// U (FP32 scratch) * 2^e -> hi/lo, 2^e from the max
+__global__ void k_split_u(const float* __restrict__ u, long n, const unsigned* __restrict__ amax, int bf16,
+                          uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
+  const float scl = pow2_scale(__uint_as_float(*amax));
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     uint16_t h, l;
-    split16((float)(rc[(size_t)g * o * n + e] * scl), bf16 != 0, h, l);
-    hi[(row0 + i) * nk + p] = h;
-    lo[(row0 + i) * nk + p] = l;
+    split16(u[i] * scl, bf16 != 0, h, l);
+    hi[i] = h;
+    lo[i] = l;
   }
 }
 
@@ -440,15 +479,10 @@ struct TcLayout {
 inline int rup(int x, int m) { return (x + m - 1) / m * m; }
 
 // rows per walker R = 2o rounded to 8, walkers per N tile wpt with R * wpt % 16 == 0,
-// R * wpt <= 256 (and gpt * wpt <= kMaxPairs, wpt <= kMaxWpt for the energy tile)
-void walker_rows(int o, int* R, int* wpt, int gpt = 0) {
+// R * wpt <= 256
+void walker_rows(int o, int* R, int* wpt) {
   const int r = rup(2 * o, 8);
   int w = 256 / r;
-  if (gpt > 0) {
-    if (w > EpiEnergy::kMaxPairs / gpt) w = EpiEnergy::kMaxPairs / gpt;
-    if (w > EpiEnergy::kMaxWpt) w = EpiEnergy::kMaxWpt;
-    if (r * w > 240) w = 240 / r;
-  }
   if (r % 16) w -= (w & 1);
   if (w < 1) w = (r % 16) ? 2 : 1;
   *R = r;
@@ -458,9 +492,9 @@ void walker_rows(int o, int* R, int* wpt, int gpt = 0) {
 struct Plan {
   TcState t;
   size_t total;
-  size_t o_rc_fb[2], o_rc_inv, o_lop[2], o_eop[2][2], o_ren[2][2], o_ren_inv[2];
-  size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gen[2][2];
-  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_trial32[2], o_rh1[2];
+  size_t o_rc_fb[2], o_rc_inv, o_lop[2], o_eop[2][2], o_u[2][2], o_rcb[2][2], o_rcb_inv[2], o_utmp;
+  size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gblk[2][2];
+  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_trial32[2], o_rh1[2];
 };
 
 int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
@@ -493,15 +527,26 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
       return -2;
     }
   }
+  size_t umax = 0;
   for (int b = 0; b < t.nblk; ++b) {
     t.o_blk[b] = c.gocc[b];
-    t.gpt[b] = 128 / t.o_blk[b];
-    walker_rows(t.o_blk[b], &t.Rb[b], &t.wptb[b], t.gpt[b]);
-    t.bnb[b] = t.Rb[b] * t.wptb[b];
-    t.mt_en[b] = (c.nchol + t.gpt[b] - 1) / t.gpt[b];
+    t.kb[b] = t.o_blk[b] * t.n;
+    t.ldkb[b] = rup(t.kb[b], 8);
+    t.mt_z[b] = (t.kb[b] + 127) / 128;
+    const size_t ub = (size_t)t.kb[b] * t.ldkb[b];
+    if (ub > umax) umax = ub;
   }
-  t.fb_bn = c.nchol >= 256 ? 256 : rup(c.nchol, 16);
-  t.fb_ntiles = (c.nchol + t.fb_bn - 1) / t.fb_bn;
+  // force-bias tile width: the widest of 256/128/64 that still gives >= 148 CTAs
+  {
+    const int mtl = (2 * c.nw + 127) / 128;
+    t.fb_bn = c.nchol >= 128 ? 128 : rup(c.nchol, 16);
+    while (mtl * ((c.nchol + t.fb_bn - 1) / t.fb_bn) < 148) {
+      const int next = rup(t.fb_bn / 2, 16);
+      if (next < 64) break;
+      t.fb_bn = next;
+    }
+    t.fb_ntiles = (c.nchol + t.fb_bn - 1) / t.fb_bn;
+  }
   t.n_fb_terms = 1 + ((cfg & kFbDyn) ? 1 : 0) + ((cfg & kFbStat) ? 1 : 0);
   t.n_vhs_terms = 1 + ((cfg & kVhsDyn) ? 1 : 0) + ((cfg & kVhsStat) ? 1 : 0);
   t.n_e_terms = 1 + ((cfg & kExpDyn) ? 1 : 0) + ((cfg & kExpStat) ? 1 : 0);
@@ -515,9 +560,13 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   for (int s = 0; s < t.nslab; ++s)
     for (int i = 0; i < 2; ++i) P->o_eop[s][i] = L.take((size_t)128 * t.nk * H);
   for (int b = 0; b < t.nblk; ++b) {
-    for (int i = 0; i < 2; ++i) P->o_ren[b][i] = L.take((size_t)t.mt_en[b] * 128 * t.nk * H);
-    P->o_ren_inv[b] = L.take((size_t)c.nchol * 4);
+    for (int i = 0; i < 2; ++i) P->o_u[b][i] = L.take((size_t)t.kb[b] * t.ldkb[b] * H);
+    if (t.nblk == 2) {
+      for (int i = 0; i < 2; ++i) P->o_rcb[b][i] = L.take((size_t)c.nchol * t.ldkb[b] * H);
+      P->o_rcb_inv[b] = L.take((size_t)c.nchol * 4);
+    }
   }
+  P->o_utmp = L.take(umax * 4);
   for (int i = 0; i < 2; ++i) P->o_gfb[i] = L.take((size_t)2 * t.nw * t.ldfb * H);
   for (int i = 0; i < 2; ++i) P->o_xt[i] = L.take((size_t)2 * t.nw * t.ldg * H);
   for (int i = 0; i < 2; ++i) P->o_vbuf[i] = L.take((size_t)nwc * 128 * 2 * t.nq * H);
@@ -527,15 +576,17 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
       P->o_acc[s][i] = L.take((size_t)t.nw * t.R[s] * t.nk * H);
       P->o_t0[s][i] = L.take((size_t)t.nw * t.NT[s] * 2 * t.nq * H);
     }
-  for (int b = 0; b < t.nblk; ++b)
-    for (int i = 0; i < 2; ++i) P->o_gen[b][i] = L.take((size_t)t.nw * t.Rb[b] * t.nk * H);
+  if (t.nblk == 2)
+    for (int b = 0; b < t.nblk; ++b)
+      for (int i = 0; i < 2; ++i) P->o_gblk[b][i] = L.take((size_t)2 * t.nw * t.ldkb[b] * H);
   P->o_ginv = L.take((size_t)t.nw * 4);
   P->o_ene1 = L.take((size_t)t.nw * 16);
   P->o_pshift = L.take((size_t)t.nw * t.fb_ntiles * 16);
   P->o_pfbt = L.take((size_t)t.nw * t.fb_ntiles * 16);
   P->o_cout = L.take((size_t)t.nblk * t.nw * c.nchol * 16);
-  P->o_exc = L.take((size_t)t.nw * (t.mt_en[0] + t.mt_en[1]) * 16);
+  P->o_exc = L.take((size_t)t.nw * (t.mt_z[0] + t.mt_z[1]) * 16);
   P->o_status = L.take(256);
+  P->o_amax = L.take(256);
   for (int s = 0; s < 2; ++s) P->o_trial32[s] = L.take((size_t)t.n * 64 * 4);
   for (int b = 0; b < 2; ++b) P->o_rh1[b] = L.take((size_t)t.n * 64 * 4);
   P->total = L.off + 1024;
@@ -563,12 +614,12 @@ MixedDev mixed_dev(const TcState& t, const afq_ctx_dev& c) {
     m.o_slab[s] = s < t.nslab ? t.o_slab[s] : 0;
     m.R[s] = t.R[s];
     m.o_blk[s] = s < t.nblk ? t.o_blk[s] : 0;
-    m.Rb[s] = t.Rb[s];
+    m.ldkb[s] = t.ldkb[s];
     m.trial32[s] = t.trial32[s];
     m.rh1_32[s] = t.rh1_32[s];
     m.g_fb[s] = t.g_fb[s];
     for (int i = 0; i < 2; ++i) {
-      m.gen[s][i] = t.gen[s][i];
+      m.g_blk[s][i] = t.g_blk[s][i];
       m.wt[s][i] = t.wt[s][i];
     }
   }
@@ -605,12 +656,17 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
       t.t0[s][i] = U(P.o_t0[s][i]);
     }
     for (int b = 0; b < t.nblk; ++b) {
-      t.ren[b][i] = U(P.o_ren[b][i]);
-      t.gen[b][i] = U(P.o_gen[b][i]);
+      t.u[b][i] = U(P.o_u[b][i]);
+      // one Green block (RHF): the block operands are the force-bias operands themselves
+      t.g_blk[b][i] = t.nblk == 2 ? U(P.o_gblk[b][i]) : t.g_fb[i];
+      t.rc_blk[b][i] = t.nblk == 2 ? U(P.o_rcb[b][i]) : t.rc_fb[i];
     }
   }
   t.rc_inv = reinterpret_cast<float*>(base + P.o_rc_inv);
-  for (int b = 0; b < t.nblk; ++b) t.ren_inv[b] = reinterpret_cast<float*>(base + P.o_ren_inv[b]);
+  for (int b = 0; b < t.nblk; ++b)
+    t.rc_blk_inv[b] = t.nblk == 2 ? reinterpret_cast<float*>(base + P.o_rcb_inv[b]) : t.rc_inv;
+  t.u_tmp = reinterpret_cast<float*>(base + P.o_utmp);
+  unsigned* amax = reinterpret_cast<unsigned*>(base + P.o_amax);
   t.g_inv = reinterpret_cast<float*>(base + P.o_ginv);
   t.ene1 = reinterpret_cast<double2*>(base + P.o_ene1);
   t.part_shift = reinterpret_cast<double2*>(base + P.o_pshift);
@@ -636,9 +692,25 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   }
   for (int b = 0; b < t.nblk; ++b) {
     k_to_f32<<<64, 256, 0, st>>>(c.rot_h1[b], const_cast<float*>(t.rh1_32[b]), (long)t.n * t.o_blk[b]);
-    k_row_scale<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.o_blk[b] * t.n, t.ren_inv[b]);
-    k_prep_ren<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.o_blk[b], t.n, t.nk, t.gpt[b], bf, t.ren_inv[b],
-                                        t.ren[b][0], t.ren[b][1]);
+    if (t.nblk == 2) {
+      k_row_scale<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.kb[b], t.rc_blk_inv[b]);
+      k_prep_rows_scaled<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.kb[b], t.ldkb[b], bf, t.rc_blk_inv[b],
+                                                  t.rc_blk[b][0], t.rc_blk[b][1]);
+    }
+    // exchange matrix of this block: FP64 accumulation, power-of-two scaling, hi/lo split
+    cudaMemsetAsync(amax, 0, 4, st);
+    k_prep_u<<<dim3((t.kb[b] + 31) / 32, (t.kb[b] + 31) / 32), 256, 0, st>>>(c.rot_chol[b], c.nchol, t.kb[b],
+                                                                           t.n, t.ldkb[b], t.u_tmp, amax);
+    const long ucount = (long)t.kb[b] * t.ldkb[b];
+    k_split_u<<<1024, 256, 0, st>>>(t.u_tmp, ucount, amax, bf, t.u[b][0], t.u[b][1]);
+    unsigned amax_h = 0;
+    cudaMemcpyAsync(&amax_h, amax, 4, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);  // set-up only: the unscale factor is a host constant
+    float am;
+    memcpy(&am, &amax_h, 4);
+    int ex = 0;
+    if (am > 0.f) frexpf(am, &ex);
+    t.u_inv[b] = ldexpf(1.0f, ex);
   }
   const double* rcsrc = c.nspin_g == 2 ? rccat : c.rot_chol[0];
   k_row_scale<<<c.nchol, 256, 0, st>>>(rcsrc, t.kfb, t.rc_inv);
@@ -668,14 +740,14 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
     int i = 0;
     const uint64_t nrows = (uint64_t)t.n * t.nq;
     TC_CHECK(mk(&t.m_vhs.a[i], t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
-    TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[0], nrows, c.nchol, t.ldg, 256));
+    TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[0], nrows, c.nchol, t.ldg, 128));
     if (t.cfg & kVhsDyn) {
       TC_CHECK(mk(&t.m_vhs.a[i], t.xt[1], 2 * t.nw, c.nchol, t.ldg, 128));
-      TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[0], nrows, c.nchol, t.ldg, 256));
+      TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[0], nrows, c.nchol, t.ldg, 128));
     }
     if (t.cfg & kVhsStat) {
       TC_CHECK(mk(&t.m_vhs.a[i], t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
-      TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[1], nrows, c.nchol, t.ldg, 256));
+      TC_CHECK(mk(&t.m_vhs.b[i++], t.lop[1], nrows, c.nchol, t.ldg, 128));
     }
   }
   for (int s = 0; s < t.nslab; ++s) {  // exp_h1 products: A = eop (static), B = wt / acc
@@ -700,18 +772,34 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
     TC_CHECK(mk(&t.m_t0[s][0], t.t0[s][0], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
     TC_CHECK(mk(&t.m_t0[s][1], t.t0[s][1], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
   }
-  for (int b = 0; b < t.nblk; ++b) {  // energy: A = ren (static), B = gen (walker-dependent)
-    const uint64_t arows = (uint64_t)t.mt_en[b] * 128, brows = (uint64_t)t.nw * t.Rb[b];
-    int i = 0;
-    TC_CHECK(mk(&t.m_en[b].a[i], t.ren[b][0], arows, t.n, t.nk, 128));
-    TC_CHECK(mk(&t.m_en[b].b[i++], t.gen[b][0], brows, t.n, t.nk, t.bnb[b]));
-    if (t.cfg & kEneDyn) {
-      TC_CHECK(mk(&t.m_en[b].a[i], t.ren[b][0], arows, t.n, t.nk, 128));
-      TC_CHECK(mk(&t.m_en[b].b[i++], t.gen[b][1], brows, t.n, t.nk, t.bnb[b]));
+  for (int b = 0; b < t.nblk; ++b) {
+    // Coulomb: c_g = G_b . rot_chol_b (A = Green operand, B = rot_chol operand)
+    {
+      int i = 0;
+      TC_CHECK(mk(&t.m_c[b].a[i], t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+      TC_CHECK(mk(&t.m_c[b].b[i++], t.rc_blk[b][0], c.nchol, t.kb[b], t.ldkb[b], t.fb_bn));
+      if (t.cfg & kEneDyn) {
+        TC_CHECK(mk(&t.m_c[b].a[i], t.g_blk[b][1], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+        TC_CHECK(mk(&t.m_c[b].b[i++], t.rc_blk[b][0], c.nchol, t.kb[b], t.ldkb[b], t.fb_bn));
+      }
+      if (t.cfg & kEneStat) {
+        TC_CHECK(mk(&t.m_c[b].a[i], t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+        TC_CHECK(mk(&t.m_c[b].b[i++], t.rc_blk[b][1], c.nchol, t.kb[b], t.ldkb[b], t.fb_bn));
+      }
     }
-    if (t.cfg & kEneStat) {
-      TC_CHECK(mk(&t.m_en[b].a[i], t.ren[b][1], arows, t.n, t.nk, 128));
-      TC_CHECK(mk(&t.m_en[b].b[i++], t.gen[b][0], brows, t.n, t.nk, t.bnb[b]));
+    // exchange: Z = U_b . G_b (A = U, B = Green operand)
+    {
+      int i = 0;
+      TC_CHECK(mk(&t.m_z[b].a[i], t.u[b][0], t.kb[b], t.kb[b], t.ldkb[b], 128));
+      TC_CHECK(mk(&t.m_z[b].b[i++], t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+      if (t.cfg & kEneDyn) {
+        TC_CHECK(mk(&t.m_z[b].a[i], t.u[b][0], t.kb[b], t.kb[b], t.ldkb[b], 128));
+        TC_CHECK(mk(&t.m_z[b].b[i++], t.g_blk[b][1], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+      }
+      if (t.cfg & kEneStat) {
+        TC_CHECK(mk(&t.m_z[b].a[i], t.u[b][1], t.kb[b], t.kb[b], t.ldkb[b], 128));
+        TC_CHECK(mk(&t.m_z[b].b[i++], t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+      }
     }
   }
   t.ready = 1;
@@ -728,20 +816,22 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   cudaFuncSetAttribute(k_green_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   {
     ProfScope _ps(K_GREEN, st);
-    k_green_mixed<<<t.nw, 256, smem, st>>>(md, static_cast<const float2*>(wu), static_cast<const float2*>(wd),
+    k_green_mixed<<<t.nw, 128, smem, st>>>(md, static_cast<const float2*>(wu), static_cast<const float2*>(wd),
                                            ovl, write_ops ? 1 : 0);
   }
   return launch_check("green_mixed");
 }
 
-static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, double2* fb_out, cudaStream_t st) {
+static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, double2* fb_out, cudaStream_t st,
+                   const GemmMaps* maps = nullptr, const float* rc_inv = nullptr, float alpha = 0.f,
+                   int kdim = 0) {
   EpiFB::Params ep;
   memset(&ep, 0, sizeof(ep));
   ep.fields = fields;
   ep.mf = c.mf;
-  ep.rc_inv = t.rc_inv;
+  ep.rc_inv = rc_inv ? rc_inv : t.rc_inv;
   ep.g_inv = t.g_inv;
-  ep.alpha = c.energy_mode == 0 ? 2.0f : 1.0f;
+  ep.alpha = alpha != 0.f ? alpha : (c.energy_mode == 0 ? 2.0f : 1.0f);
   ep.sqdt = (float)sqrt(c.dt);
   ep.nw = t.nw;
   ep.nchol = c.nchol;
@@ -753,8 +843,13 @@ static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, doubl
   ep.part_shift = t.part_shift;
   ep.part_fbt = t.part_fbt;
   ep.fb_out = fb_out;
-  const int kt = (t.kfb + 63) / 64, mt = (2 * t.nw + 127) / 128;
-  return launch_gemm<256, 4, EpiFB>(K_FB, t.m_fb, t.n_fb_terms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st);
+  const int kt = ((kdim ? kdim : t.kfb) + 63) / 64, mt = (2 * t.nw + 127) / 128;
+  const int cls = maps ? K_ENERGY : K_FB;
+  const GemmMaps& m = maps ? *maps : t.m_fb;
+  const int nterms = maps ? t.n_en_terms : t.n_fb_terms;
+  if (t.fb_bn <= 64)  // narrow tiles: a smaller ring lets two CTAs share an SM
+    return launch_gemm<64, 4, EpiFB>(cls, m, nterms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st, 0, 1);
+  return launch_gemm<128, 4, EpiFB>(cls, m, nterms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st, 0, 1);
 }
 
 int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
@@ -803,9 +898,9 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.bf16 = t.bf16 ? 1 : 0;
     ev.want_lo = want_lo ? 1 : 0;
     ev.sqdt = (float)sqrt(c.dt);
-    const int kt = (c.nchol + 63) / 64, mt = (2 * t.nwc + 127) / 128, nt = (t.n * t.nq + 255) / 256;
-    TC_CHECK((launch_gemm<256, 4, EpiVHS>(K_VHS, t.m_vhs, t.n_vhs_terms, kt, mt, nt, 256, t.bf16, ev, t.status, st,
-                                         2 * w0)));
+    const int kt = (c.nchol + 63) / 64, mt = (2 * t.nwc + 127) / 128, nt = (t.n * t.nq + 127) / 128;
+    TC_CHECK((launch_gemm<128, 4, EpiVHS>(K_VHS, t.m_vhs, t.n_vhs_terms, kt, mt, nt, 128, t.bf16, ev, t.status, st,
+                                         2 * w0, 1)));
     for (int s = 0; s < t.nslab; ++s) {
       TaylorDev td;
       td.n = t.n;
@@ -839,26 +934,30 @@ int tc_weights(TcState& t, const afq_ctx_dev& c, const double2* ovl_new, double2
   return launch_weights(c, t.part_shift, t.part_fbt, t.fb_ntiles, ovl_new, ovl, weights, scalars, st);
 }
 
+// local energy (wavefunctions.py:529-561, 711-743): Coulomb c_g from a force-bias-like GEMM,
+// exchange from the U GEMM, both per spin block; ene1 comes from the Green kernel.
 int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
   for (int b = 0; b < t.nblk; ++b) {
-    EpiEnergy::Params ep;
-    ep.ren_inv = t.ren_inv[b];
+    TC_CHECK(fb_gemm(t, c, nullptr, t.c_out + (size_t)b * t.nw * c.nchol, st, &t.m_c[b], t.rc_blk_inv[b], 1.0f,
+                     t.kb[b]));
+    EpiExc::Params ep;
+    ep.g_hi = t.g_blk[b][0];
+    ep.g_lo = t.g_blk[b][1];
     ep.g_inv = t.g_inv;
-    ep.o = t.o_blk[b];
-    ep.R = t.Rb[b];
-    ep.gpt = t.gpt[b];
-    ep.nchol = c.nchol;
+    ep.u_inv = t.u_inv[b];
+    ep.kb = t.kb[b];
+    ep.ldk = t.ldkb[b];
     ep.nw = t.nw;
-    ep.mt = t.mt_en[b];
-    ep.c_out = t.c_out + (size_t)b * t.nw * c.nchol;
-    ep.exc_part = t.exc_part + (b == 0 ? 0 : (size_t)t.nw * t.mt_en[0]);
-    const int kt = (t.n + 63) / 64, nt = (t.nw * t.Rb[b] + t.bnb[b] - 1) / t.bnb[b];
-    TC_CHECK((launch_gemm<240, 2, EpiEnergy>(K_ENERGY, t.m_en[b], t.n_en_terms, kt, t.mt_en[b], nt, t.bnb[b], t.bf16, ep,
-                                            t.status, st)));
+    ep.mt = t.mt_z[b];
+    ep.bf16 = t.bf16 ? 1 : 0;
+    ep.exc_part = t.exc_part + (b == 0 ? 0 : (size_t)t.nw * t.mt_z[0]);
+    const int kt = (t.kb[b] + 63) / 64, nt = (2 * t.nw + 127) / 128;
+    TC_CHECK((launch_gemm<128, 4, EpiExc>(K_ENERGY, t.m_z[b], t.n_en_terms, kt, t.mt_z[b], nt, 128, t.bf16, ep,
+                                         t.status, st, 0, 1)));
   }
   {
     ProfScope _ps(K_ENERGY_FIN, st);
-    k_energy_final_mixed<<<t.nw, 256, 0, st>>>(t.nw, c.nchol, t.nblk, t.mt_en[0], t.nblk == 2 ? t.mt_en[1] : 0,
+    k_energy_final_mixed<<<t.nw, 256, 0, st>>>(t.nw, c.nchol, t.nblk, t.mt_z[0], t.nblk == 2 ? t.mt_z[1] : 0,
                                                c.energy_mode, c.h0, t.c_out, t.exc_part, t.ene1, out);
   }
   return launch_check("energy_final_mixed");
@@ -874,7 +973,7 @@ int tc_orthonormalize(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cuda
 
 extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stride,
                                  long b_term_stride, float* d, int M, int N, int K, int lda,
-                                 int ldb, int bf16, int bn, int* status, void* stream) {
+                                 int ldb, int bf16, int bn, int drain, int* status, void* stream) {
   using namespace afq;
   if (!a || !b || !d || !status || M < 1 || N < 1 || K < 1 || nterms < 1 || nterms > 3) {
     afq_set_error("afq_test_gemm_f16: bad arguments");
@@ -896,5 +995,6 @@ extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long 
   EpiStoreF32::Params ep{d, M, N, (long)N};
   const int kt = (K + 63) / 64, mt = (M + 127) / 128, nt = (N + bn - 1) / bn;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  return launch_gemm<256, 4, EpiStoreF32>(K_PREP, maps, nterms, kt, mt, nt, bn, bf16, ep, status, st);
+  return launch_gemm<256, 4, EpiStoreF32>(K_PREP, maps, nterms, kt, mt, nt, bn, bf16, ep, status, st, 0,
+                                          drain);
 }

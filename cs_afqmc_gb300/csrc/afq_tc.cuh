@@ -9,8 +9,10 @@
 //   eop[s] [128][nk]          exp_h1_s - I (rows >= norb zero)
 //   wt[s], acc[s] [nw * R_s][nk]  rows (w, 2k + re/im), cols p: walker / Taylor sum
 //   t0[s]  [nw][NT_s][2 nq]   Taylor B operand: row 2k = [Tr | -Ti], row 2k+1 = [Ti | Tr]
-//   ren[b] [mt_b * 128][nk]   rows (g-group tile, g_local * o + i) = rot_chol_b[g][i][:] * 2^e_g
-//   gen[b] [nw * R_b][nk]     rows (w, 2k + re/im), cols p = G_b[k][p] * 2^e_w
+//   u[b]   [kb][ldkb]         rows (i, q), cols (k, p): sum_g rot_chol_b[g,i,p] rot_chol_b[g,k,q]
+//                             (exchange matrix, scaled by a power of two)
+//   g_blk[b] [2 nw][ldkb]     Green operand of spin block b alone (UHF; RHF uses g_fb)
+//   rc_blk[b] [nchol][ldkb]   rot_chol of spin block b alone (UHF; RHF uses rc_fb)
 #pragma once
 #include "afq_gemm.cuh"
 #include "afq_kernels.cuh"
@@ -42,25 +44,27 @@ struct TcState {
   int nw, nwc;
   int nslab, nblk;          // walker slabs, Green blocks
   int o_slab[2], R[2], wpt[2], bn_w[2], NT[2];
-  int o_blk[2], Rb[2], wptb[2], bnb[2], gpt[2], mt_en[2];
+  int o_blk[2], kb[2], ldkb[2], mt_z[2];
   int fb_bn, fb_ntiles;
   // static operands [hi, lo]
-  uint16_t *rc_fb[2], *lop[2], *eop[2][2], *ren[2][2];
+  uint16_t *rc_fb[2], *lop[2], *eop[2][2], *u[2][2], *rc_blk[2][2];
   float* rc_inv;            // [nchol] 2^-e_g for rc_fb
-  float* ren_inv[2];        // [nchol] 2^-e_g for ren
+  float* rc_blk_inv[2];     // [nchol] 2^-e_g for rc_blk
+  float u_inv[2];           // 2^-e of u[b]
+  float* u_tmp;             // FP32 scratch for building u (set-up only)
   // dynamic operands
-  uint16_t *g_fb[2], *xt[2], *vbuf[2], *wt[2][2], *acc[2][2], *t0[2][2], *gen[2][2];
+  uint16_t *g_fb[2], *xt[2], *vbuf[2], *wt[2][2], *acc[2][2], *t0[2][2], *g_blk[2][2];
   float* g_inv;             // [nw] 2^-e_w
   double2* ene1;            // [nw]
   double2* part_shift;      // [nw][fb_ntiles]
   double2* part_fbt;        // [nw][fb_ntiles]
   double2* c_out;           // [nblk][nw][nchol]
-  double2* exc_part;        // [nblk][nw][mt_en]
+  double2* exc_part;        // [nblk][nw][mt_z]
   const float* trial32[2];  // [norb][o_s] trial in FP32
   const float* rh1_32[2];   // [o_b][norb] rot_h1 in FP32
   int* status;              // device word: nonzero after a pipeline timeout
   // tensor maps
-  GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_en[2];
+  GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2], m_z[2];
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
   int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;

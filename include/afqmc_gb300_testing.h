@@ -18,11 +18,12 @@ extern "C" {
 /* D[M,N] (fp32, row-major) = sum_{t < nterms} A_t[M,K] * B_t[N,K]^T on the tcgen05 tensor
  * cores. A_t = a + t*a_term_stride, B_t = b + t*b_term_stride (elements); rows of A and B
  * are K-major with leading dimensions lda/ldb (multiples of 8). bf16 != 0: bfloat16 inputs,
- * else float16. bn: output tile width (multiple of 16, <= 256). *status (device int) becomes
- * nonzero if a pipeline wait timed out. */
+ * else float16. bn: output tile width (multiple of 16, <= 256; <= 160 with drain).
+ * drain: 0 = one accumulator; d > 0 = a fresh accumulator every d K tiles, summed with
+ * round-to-nearest. *status (device int) becomes nonzero if a pipeline wait timed out. */
 int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stride,
                       long b_term_stride, float* d, int M, int N, int K, int lda, int ldb,
-                      int bf16, int bn, int* status, void* stream);
+                      int bf16, int bn, int drain, int* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -11,7 +11,8 @@ from oracle import afqmc_oracle as O
 
 class Case:
     def __init__(self, kind="rhf", norb=12, nelec=(3, 3), nchol=30, nw=8, dt=0.005,
-                 restricted=True, precision="fp64", seed=5, perturb=0.2, n_batch=1):
+                 restricted=True, precision="fp64", seed=5, perturb=0.2, n_batch=1,
+                 orthonormal=False):
         import torch
         from cs_afqmc_gb300 import hamiltonian, propagation, wavefunctions
 
@@ -36,6 +37,11 @@ class Case:
                 w = np.repeat(m[None].astype(np.complex128), nw, 0)
                 ws.append(w + perturb * (rng.standard_normal(w.shape) + 1j * rng.standard_normal(w.shape)))
             self.walkers0 = ws
+        if orthonormal:  # walkers as they are at a measurement: right after the QR
+            if isinstance(self.walkers0, list):
+                self.walkers0 = [np.linalg.qr(x)[0] for x in self.walkers0]
+            else:
+                self.walkers0 = np.linalg.qr(self.walkers0)[0]
         # ---- oracle
         self.o_trial = O.Trial(kind, norb, nelec)
         ho = {"h0": s.h0, "h1": s.h1.copy(), "chol": s.chol.copy()}

@@ -21,7 +21,10 @@ SHAPES = [(128, 64, 64, 64), (300, 250, 200, 128), (256, 480, 600, 240), (1000, 
 @pytest.mark.parametrize("M,N,K,bn", SHAPES)
 @pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
 @pytest.mark.parametrize("nterms", [1, 3])
-def test_gemm_matches_fp32(M, N, K, bn, dtype, nterms):
+@pytest.mark.parametrize("drain", [0, 1])
+def test_gemm_matches_fp32(M, N, K, bn, dtype, nterms, drain):
+    if drain and bn > 160:
+        pytest.skip("drained accumulation needs 3 bn <= 512 TMEM columns")
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)
     lda = (K + 7) // 8 * 8
     a = torch.randn(nterms, M, lda, device="cuda", generator=g).to(dtype)
@@ -29,10 +32,32 @@ def test_gemm_matches_fp32(M, N, K, bn, dtype, nterms):
     d = torch.full((M, N), float("nan"), device="cuda", dtype=torch.float32)
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     _lib.call("afq_test_gemm_f16", a.data_ptr(), b.data_ptr(), nterms, M * lda, N * lda,
-              d.data_ptr(), M, N, K, lda, lda, int(dtype == torch.bfloat16), bn,
+              d.data_ptr(), M, N, K, lda, lda, int(dtype == torch.bfloat16), bn, drain,
               status.data_ptr(), stream_ptr())
     ref = sum(a[t, :, :K].float() @ b[t, :, :K].float().T for t in range(nterms))
     torch.cuda.synchronize()
     assert status.item() == 0
     err = (d - ref).abs().max().item()
     assert err <= 1e-5 * K * nterms * 16, err
+
+
+@pytest.mark.parametrize("drain", [0, 1, 2])
+def test_accumulation_bias(drain):
+    """The tensor core truncates when it accumulates: positive sums over K = 2400 come out
+    ~1.5e-5 low with one accumulator. Drained accumulation (a fresh accumulator every
+    `drain` K tiles, summed with round-to-nearest) must bring the mean bias below 1e-6."""
+    M, N, K = 256, 256, 2400
+    g = torch.Generator(device="cuda").manual_seed(5)
+    a = (torch.rand(1, M, K, device="cuda", generator=g) * 0.5 + 0.5).half()
+    b = (torch.rand(1, N, K, device="cuda", generator=g) * 0.5 + 0.5).half()
+    d = torch.empty(M, N, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("afq_test_gemm_f16", a.data_ptr(), b.data_ptr(), 1, 0, 0, d.data_ptr(), M, N, K, K, K,
+              0, 128, drain, status.data_ptr(), stream_ptr())
+    ref = a[0].double() @ b[0].double().T
+    bias = ((d.double() - ref) / ref).mean().item()
+    assert status.item() == 0
+    if drain == 0:
+        assert bias < -5e-6  # the hardware behaviour this scheme corrects
+    else:
+        assert abs(bias) < 1e-6, bias
