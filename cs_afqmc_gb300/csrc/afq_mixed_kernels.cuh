@@ -50,164 +50,253 @@ struct MixedDev {
 };
 
 // ======================================================================================
-// Green's function, overlap and operand packing. One CTA per walker.
-// S_s = C_s^T W_s (FP32), Gauss-Jordan on [S | I] in FP32 with partial pivoting, the
-// determinant accumulated in FP64 as the signed product of the pivots (for both spins and
-// squared for restricted walkers). G_s = (W_s S_s^-1)^T (FP32).
-// wavefunctions.py:478-501 (rhf), 658-692 (uhf).
+// Green's function, overlap and operand packing, in three kernels
+// (wavefunctions.py:478-501 rhf, 658-692 uhf):
+//   k_green_s   one CTA per walker, thread p <-> orbital p: S_s = C_s^T W_s (FP32) into a
+//               scratch buffer, plus the walker operand of the exp_h1 products;
+//   k_green_inv one warp per walker: in-place Gauss-Jordan with partial pivoting on S_s in
+//               registers (lane r <-> row r), the determinant as the FP64 signed product of
+//               the pivots (over both spins; squared for restricted walkers), S_s^-1 back to
+//               the scratch buffer (or the determinant alone);
+//   k_green_g   one CTA per walker, thread p: G_s[:, p] = (W_s S_s^-1)^T[:, p] (FP32), the
+//               per-walker power-of-two scale, the 16-bit operands and ene1 = sum G * rot_h1.
 // ======================================================================================
 
-__global__ void __launch_bounds__(128) k_green_mixed(const MixedDev md, const float2* __restrict__ wu,
-                                                     const float2* __restrict__ wd,
-                                                     double2* __restrict__ ovl, int write_ops) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  const int w = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, n = md.n;
-  const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
-  const int gtot = md.o_blk[0] + md.o_blk[1];
-  float2* Ws = reinterpret_cast<float2*>(sm);       // [n][omax]
-  float2* Gs = Ws + (size_t)n * omax;                // [gtot][n]
-  float2* Aug = Gs + (size_t)gtot * n;               // [omax][2 omax]
-  float* Cs = reinterpret_cast<float*>(Aug + (size_t)omax * 2 * omax);  // [n][omax]
-  __shared__ double red[32];
-  __shared__ int piv_sh;
-  __shared__ float gmax_sh[32];
-  __shared__ float2 colj[64];
-  double2 det = c2(1.0, 0.0);  // thread 0 only: product of the FP32 pivots, in FP64
-  const bool bf = md.bf16 != 0;
+constexpr int kGreenMaxO = 32;
 
+__global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2* __restrict__ wu,
+                                                 const float2* __restrict__ wd,
+                                                 float2* __restrict__ sbuf, int write_ops) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int w = blockIdx.x, tid = threadIdx.x, n = md.n;
+  const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
+  const int o4max = (omax + 3) & ~3;
+  float2* Ws = reinterpret_cast<float2*>(sm);                   // [n][o4] (columns >= o zero)
+  float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * o4max);  // [n][o]
+  const bool bf = md.bf16 != 0;
   for (int s = 0; s < md.nslab; ++s) {
-    const int o = md.o_slab[s];
+    const int o = md.o_slab[s], o4 = (o + 3) & ~3;
     const float2* W = (s == 0 ? wu : wd) + (size_t)w * n * o;
     const float* C = md.trial32[s];
-    for (int i = tid; i < n * o; i += nt) {
-      Ws[i] = W[i];
-      Cs[i] = C[i];
+    // coalesced copies; W rows padded to a multiple of 4 columns for 16-byte loads
+    for (int e = tid; e < n * o4; e += 128) {
+      const int pp = e / o4, k = e - pp * o4;
+      Ws[e] = (k < o) ? W[pp * o + k] : make_float2(0.f, 0.f);
     }
+    for (int e = tid; e < n * o; e += 128) Cs[e] = C[e];
     __syncthreads();
-    if (write_ops) {
-      // walker operand for the exp_h1 products: row (w, 2k + c), column p
-      const int R = md.R[s];
-      uint16_t* hi = md.wt[s][0] + (size_t)w * R * md.nk;
-      uint16_t* lo = md.wt[s][1] + (size_t)w * R * md.nk;
-      for (int e = tid; e < 2 * o * n; e += nt) {
-        const int rr = e / n, p = e % n;
-        const float2 v = Ws[p * o + (rr >> 1)];
+    if (write_ops && tid < n) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
+      uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + tid;
+      uint16_t* lo = md.wt[s][1] + (size_t)w * md.R[s] * md.nk + tid;
+      for (int k = 0; k < o; ++k) {
+        const float2 v = Ws[tid * o4 + k];
         uint16_t h, l;
-        split16((rr & 1) ? v.y : v.x, bf, h, l);
-        hi[(size_t)rr * md.nk + p] = h;
-        lo[(size_t)rr * md.nk + p] = l;
+        split16(v.x, bf, h, l);
+        hi[(size_t)(2 * k) * md.nk] = h;
+        lo[(size_t)(2 * k) * md.nk] = l;
+        split16(v.y, bf, h, l);
+        hi[(size_t)(2 * k + 1) * md.nk] = h;
+        lo[(size_t)(2 * k + 1) * md.nk] = l;
       }
     }
-    for (int e = tid; e < o * o; e += nt) {
-      const int i = e / o, k = e % o;
-      float2 a = make_float2(0.f, 0.f);
-      for (int p = 0; p < n; ++p) {
-        const float cv = Cs[p * o + i];
-        const float2 wv = Ws[p * o + k];
-        a.x = fmaf(cv, wv.x, a.x);
-        a.y = fmaf(cv, wv.y, a.y);
+    // S[i][k..k+3] = sum_p C[p][i] W[p][k..k+3]
+    float2* S = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
+    const int nk4 = o4 / 4;
+    for (int e = tid; e < o * nk4; e += 128) {
+      const int i = e / nk4, k0 = (e - i * nk4) * 4;
+      float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+      for (int pp = 0; pp < n; ++pp) {
+        const float cv = Cs[pp * o + i];
+        const float4 x = *reinterpret_cast<const float4*>(&Ws[pp * o4 + k0]);
+        const float4 y = *reinterpret_cast<const float4*>(&Ws[pp * o4 + k0 + 2]);
+        a0.x = fmaf(cv, x.x, a0.x); a0.y = fmaf(cv, x.y, a0.y);
+        a1.x = fmaf(cv, x.z, a1.x); a1.y = fmaf(cv, x.w, a1.y);
+        a2.x = fmaf(cv, y.x, a2.x); a2.y = fmaf(cv, y.y, a2.y);
+        a3.x = fmaf(cv, y.z, a3.x); a3.y = fmaf(cv, y.w, a3.y);
       }
-      Aug[i * 2 * o + k] = a;
-      Aug[i * 2 * o + o + k] = make_float2(i == k ? 1.f : 0.f, 0.f);
+      float2* Si = S + i * kGreenMaxO + k0;
+      Si[0] = a0;
+      if (k0 + 1 < o) Si[1] = a1;
+      if (k0 + 2 < o) Si[2] = a2;
+      if (k0 + 3 < o) Si[3] = a3;
     }
     __syncthreads();
+  }
+}
+
+template <int OM>
+__global__ void __launch_bounds__(256) k_green_inv(const MixedDev md, float2* __restrict__ sbuf,
+                                                   double2* __restrict__ ovl, int write_inv) {
+  const int lane = threadIdx.x & 31;
+  const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (w >= md.nw) return;
+  double2 det = c2(1.0, 0.0);
+  for (int s = 0; s < md.nslab; ++s) {
+    const int o = md.o_slab[s];
+    float2* S = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
+    float2 a[OM];
+#pragma unroll
+    for (int c = 0; c < OM; ++c)
+      a[c] = (lane < o && c < o) ? S[lane * kGreenMaxO + c] : make_float2(0.f, 0.f);
+    int partner = lane;  // lane j: the row exchanged with row j at step j
+#pragma unroll 1
     for (int j = 0; j < o; ++j) {
-      if (tid < 32) {
-        float best = -1.f;
-        int bi = j;
-        for (int r = j + tid; r < o; r += 32) {
-          const float2 v = Aug[r * 2 * o + j];
-          const float m = fabsf(v.x) + fabsf(v.y);
-          if (m > best) { best = m; bi = r; }
-        }
-        for (int off = 16; off > 0; off >>= 1) {
-          const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (tid == 0) piv_sh = bi;
+      float2 aj = make_float2(0.f, 0.f);  // a[j], selected without dynamic register indexing
+#pragma unroll
+      for (int c = 0; c < OM; ++c)
+        if (c == j) aj = a[c];
+      float best = (lane >= j && lane < o) ? fabsf(aj.x) + fabsf(aj.y) : -1.f;
+      int bi = lane;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
       }
-      __syncthreads();
-      const int pr = piv_sh;
-      if (pr != j)
-        for (int e = tid; e < 2 * o; e += nt) {
-          const float2 t = Aug[j * 2 * o + e];
-          Aug[j * 2 * o + e] = Aug[pr * 2 * o + e];
-          Aug[pr * 2 * o + e] = t;
+      const int pr = bi;
+      if (lane == j) partner = pr;
+      if (pr != j) {
+        const int src = lane == j ? pr : (lane == pr ? j : lane);
+#pragma unroll
+        for (int c = 0; c < OM; ++c) {
+          a[c].x = __shfl_sync(0xffffffffu, a[c].x, src);
+          a[c].y = __shfl_sync(0xffffffffu, a[c].y, src);
         }
-      __syncthreads();
-      const float2 pv = Aug[j * 2 * o + j];
-      if (tid == 0) {
+        aj.x = __shfl_sync(0xffffffffu, aj.x, src);
+        aj.y = __shfl_sync(0xffffffffu, aj.y, src);
+      }
+      float2 rowj[OM];
+#pragma unroll
+      for (int c = 0; c < OM; ++c) {
+        rowj[c].x = __shfl_sync(0xffffffffu, a[c].x, j);
+        rowj[c].y = __shfl_sync(0xffffffffu, a[c].y, j);
+      }
+      const float2 pv = make_float2(__shfl_sync(0xffffffffu, aj.x, j), __shfl_sync(0xffffffffu, aj.y, j));
+      if (lane == 0) {
         det = cmul(det, c2((double)pv.x, (double)pv.y));
         if (pr != j) det = c2(-det.x, -det.y);
       }
       const float2 inv = cdiv(make_float2(1.f, 0.f), pv);
-      __syncthreads();
-      for (int e = tid; e < 2 * o; e += nt) Aug[j * 2 * o + e] = cmul(Aug[j * 2 * o + e], inv);
-      // snapshot the multipliers (column j) before any thread overwrites them
-      for (int r = tid; r < o; r += nt) colj[r] = Aug[r * 2 * o + j];
-      __syncthreads();
-      for (int e = tid; e < o * 2 * o; e += nt) {
-        const int r = e / (2 * o), col = e % (2 * o);
-        if (r == j) continue;
-        Aug[e] = csub(Aug[e], cmul(colj[r], Aug[j * 2 * o + col]));
+      if (write_inv) {
+#pragma unroll
+        for (int c = 0; c < OM; ++c) rowj[c] = (c == j) ? inv : cmul(rowj[c], inv);
+        if (lane == j) {
+#pragma unroll
+          for (int c = 0; c < OM; ++c) a[c] = rowj[c];
+        } else {
+#pragma unroll
+          for (int c = 0; c < OM; ++c) a[c] = csub((c == j) ? make_float2(0.f, 0.f) : a[c], cmul(aj, rowj[c]));
+        }
+      } else if (lane > j) {  // determinant only: forward elimination
+        const float2 f = cmul(aj, inv);
+#pragma unroll
+        for (int c = 0; c < OM; ++c)
+          if (c > j) a[c] = csub(a[c], cmul(f, rowj[c]));
       }
-      __syncthreads();
     }
-    if (write_ops) {
+    if (write_inv) {
+      // undo the row exchanges as column exchanges, last first
+#pragma unroll 1
+      for (int j = o - 1; j >= 0; --j) {
+        const int pj = __shfl_sync(0xffffffffu, partner, j);
+        if (pj != j) {
+          float2 x = make_float2(0.f, 0.f), y = x;
+#pragma unroll
+          for (int c = 0; c < OM; ++c) {
+            if (c == j) x = a[c];
+            if (c == pj) y = a[c];
+          }
+#pragma unroll
+          for (int c = 0; c < OM; ++c) {
+            if (c == j) a[c] = y;
+            if (c == pj) a[c] = x;
+          }
+        }
+      }
+      if (lane < o) {
+#pragma unroll
+        for (int c = 0; c < OM; ++c)
+          if (c < o) S[lane * kGreenMaxO + c] = a[c];
+      }
+    }
+  }
+  if (lane == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
+}
+
+__global__ void __launch_bounds__(128) k_green_g(const MixedDev md, const float2* __restrict__ wu,
+                                                 const float2* __restrict__ wd,
+                                                 const float2* __restrict__ sbuf) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = md.n;
+  const int gtot = md.o_blk[0] + md.o_blk[1];
+  float2* Gs = reinterpret_cast<float2*>(sm);                 // [gtot][n]
+  float2* Si = Gs + (size_t)gtot * n;                          // [kGreenMaxO][kGreenMaxO]
+  float2* Wsm = Si + kGreenMaxO * kGreenMaxO;                  // [n][o] walker slab
+  __shared__ double red[32];
+  __shared__ float fred[4];
+  const bool bf = md.bf16 != 0;
+  const bool prow = tid < n;
+  for (int s = 0; s < md.nslab; ++s) {
+    const int o = md.o_slab[s];
+    const float2* Ssrc = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
+    for (int e = tid; e < kGreenMaxO * kGreenMaxO; e += 128) Si[e] = Ssrc[e];
+    const float2* Wg = (s == 0 ? wu : wd) + (size_t)w * n * o;
+    for (int e = tid; e < n * o; e += 128) Wsm[e] = Wg[e];
+    __syncthreads();
+    if (prow) {
+      float2 wr[kGreenMaxO];
+#pragma unroll
+      for (int k = 0; k < kGreenMaxO; ++k) wr[k] = (k < o) ? Wsm[tid * o + k] : make_float2(0.f, 0.f);
       const int b = md.nblk == 2 ? s : 0;
       float2* Gb = Gs + (size_t)(b == 0 ? 0 : md.o_blk[0]) * n;
-      for (int e = tid; e < o * n; e += nt) {
-        const int i = e / n, p = e % n;
-        float2 a = make_float2(0.f, 0.f);
-        for (int k = 0; k < o; ++k) a = cadd(a, cmul(Ws[p * o + k], Aug[k * 2 * o + o + i]));
-        if (md.nblk == 1 && s == 1) a = cadd(a, Gb[e]);  // RHF two slabs: G_up + G_dn
-        Gb[e] = a;
+      for (int i = 0; i < o; ++i) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kGreenMaxO; ++k)
+          if (k < o) acc = cadd(acc, cmul(wr[k], Si[k * kGreenMaxO + i]));
+        if (md.nblk == 1 && s == 1) acc = cadd(acc, Gb[(size_t)i * n + tid]);  // RHF two slabs
+        Gb[(size_t)i * n + tid] = acc;
       }
     }
     __syncthreads();
   }
-  if (tid == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
-  if (!write_ops) return;
-  // ---- scale, pack, ene1
   float mx = 0.f;
-  for (int e = tid; e < gtot * n; e += nt) mx = fmaxf(mx, fmaxf(fabsf(Gs[e].x), fabsf(Gs[e].y)));
+  if (prow)
+    for (int i = 0; i < gtot; ++i) {
+      const float2 g = Gs[(size_t)i * n + tid];
+      mx = fmaxf(mx, fmaxf(fabsf(g.x), fabsf(g.y)));
+    }
   for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-  if ((tid & 31) == 0) gmax_sh[tid >> 5] = mx;
+  if (lane == 0) fred[warp] = mx;
   __syncthreads();
-  if (tid < 32) {
-    float v = tid < (nt >> 5) ? gmax_sh[tid] : 0.f;
-    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
-    if (tid == 0) gmax_sh[0] = v;
-  }
-  __syncthreads();
-  const float scl = pow2_scale(gmax_sh[0]);
+  const float scl = pow2_scale(fmaxf(fmaxf(fred[0], fred[1]), fmaxf(fred[2], fred[3])));
   if (tid == 0) md.g_inv[w] = 1.0f / scl;
   double e1x = 0.0, e1y = 0.0;
-  for (int e = tid; e < gtot * n; e += nt) {
-    const float2 g = Gs[e];
-    // force-bias operand: rows (2w, 2w+1), column e
-    uint16_t h, l;
-    split16(g.x * scl, bf, h, l);
-    md.g_fb[0][(size_t)(2 * w) * md.ldfb + e] = h;
-    md.g_fb[1][(size_t)(2 * w) * md.ldfb + e] = l;
-    split16(g.y * scl, bf, h, l);
-    md.g_fb[0][(size_t)(2 * w + 1) * md.ldfb + e] = h;
-    md.g_fb[1][(size_t)(2 * w + 1) * md.ldfb + e] = l;
-    // per-block operand (exchange / Coulomb contractions of each spin separately)
-    const int b = (md.nblk == 2 && e >= md.o_blk[0] * n) ? 1 : 0;
-    const int eb = e - b * md.o_blk[0] * n;
-    if (md.nblk == 2) {
+  if (prow) {
+    for (int i = 0; i < gtot; ++i) {
+      const float2 g = Gs[(size_t)i * n + tid];
+      const int e = i * n + tid;
+      uint16_t h, l;
       split16(g.x * scl, bf, h, l);
-      md.g_blk[b][0][(size_t)(2 * w) * md.ldkb[b] + eb] = h;
-      md.g_blk[b][1][(size_t)(2 * w) * md.ldkb[b] + eb] = l;
+      md.g_fb[0][(size_t)(2 * w) * md.ldfb + e] = h;
+      md.g_fb[1][(size_t)(2 * w) * md.ldfb + e] = l;
       split16(g.y * scl, bf, h, l);
-      md.g_blk[b][0][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = h;
-      md.g_blk[b][1][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = l;
+      md.g_fb[0][(size_t)(2 * w + 1) * md.ldfb + e] = h;
+      md.g_fb[1][(size_t)(2 * w + 1) * md.ldfb + e] = l;
+      const int b = (md.nblk == 2 && i >= md.o_blk[0]) ? 1 : 0;
+      const int eb = e - b * md.o_blk[0] * n;
+      if (md.nblk == 2) {  // per-block operand (exchange / Coulomb of each spin separately)
+        split16(g.x * scl, bf, h, l);
+        md.g_blk[b][0][(size_t)(2 * w) * md.ldkb[b] + eb] = h;
+        md.g_blk[b][1][(size_t)(2 * w) * md.ldkb[b] + eb] = l;
+        split16(g.y * scl, bf, h, l);
+        md.g_blk[b][0][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = h;
+        md.g_blk[b][1][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = l;
+      }
+      const float r1 = md.rh1_32[b][eb];
+      e1x += (double)(g.x * r1);
+      e1y += (double)(g.y * r1);
     }
-    const float r1 = md.rh1_32[b][eb];
-    e1x += (double)(g.x * r1);
-    e1y += (double)(g.y * r1);
   }
   e1x = block_sum(e1x, red);
   e1y = block_sum(e1y, red);
@@ -347,43 +436,62 @@ struct EpiExp {
     int n, o, R, nk, nq, NT, nw, bf16, last;
   };
   static constexpr int kSmemBytes = 0;
+  // Walker-major: R (a multiple of 16) columns per walker, so each walker is R/16 whole
+  // TMEM chunks; thread p handles orbital row p of every walker of the tile.
   __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
                              unsigned char*, bool) {
     const int pr = m0 + q * 32 + lane;
     const bool bf = p.bf16 != 0;
+    const int wpt = bn / p.R, w0 = n0 / p.R;
+    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
 #pragma unroll 1
-    for (int c0 = 0; c0 < bn; c0 += 16) {
-      float v[16];
-      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
+    for (int wl = 0; wl < wpt; ++wl) {
+      float v[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        if (c0 < p.R) {
+          float t[16];
+          ptx::tmem_ld16(tmem + lane_off + (uint32_t)(wl * p.R + c0), t);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[c0 + j] = t[j];
+        }
+      }
       ptx::tmem_ld_wait();
-      if (pr >= p.n) continue;
-#pragma unroll 4
-      for (int j = 0; j < 16; ++j) {
-        const int col = n0 + c0 + j, w = col / p.R, rr = col % p.R;
-        if (w >= p.nw || rr >= 2 * p.o) continue;
-        const int k = rr >> 1, c = rr & 1;
-        float* wp = p.w + (((size_t)w * p.n + pr) * p.o + k) * 2 + c;
-        if (p.last) {
-          const size_t ai = ((size_t)w * p.R + rr) * p.nk + pr;
-          const float a = h2f(p.acc_hi[ai], bf) + h2f(p.acc_lo[ai], bf);
-          *wp = a + v[j];
-        } else {
-          const float w1 = *wp + v[j];
-          uint16_t h, l, hn, ln;
-          split16(w1, bf, h, l);
-          split16(-w1, bf, hn, ln);
-          const size_t base = (size_t)w * p.NT * 2 * p.nq;
-          const size_t r0 = base + (size_t)(2 * k) * 2 * p.nq, r1 = r0 + 2 * p.nq;
-          if (c == 0) {  // row 2k: [Tr | -Ti], row 2k+1: [Ti | Tr]
-            p.t0_hi[r0 + pr] = h;
-            p.t0_lo[r0 + pr] = l;
-            p.t0_hi[r1 + p.nq + pr] = h;
-            p.t0_lo[r1 + p.nq + pr] = l;
-          } else {
+      const int w = w0 + wl;
+      if (pr >= p.n || w >= p.nw) continue;
+      float2* wrow = reinterpret_cast<float2*>(p.w) + ((size_t)w * p.n + pr) * p.o;
+      if (p.last) {
+        const size_t ab = (size_t)w * p.R * p.nk + pr;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          if (k < p.o) {
+            const size_t i0 = ab + (size_t)(2 * k) * p.nk, i1 = i0 + p.nk;
+            const float ar = h2f(p.acc_hi[i0], bf) + h2f(p.acc_lo[i0], bf);
+            const float ai = h2f(p.acc_hi[i1], bf) + h2f(p.acc_lo[i1], bf);
+            wrow[k] = make_float2(ar + v[2 * k], ai + v[2 * k + 1]);
+          }
+        }
+      } else {
+        const size_t base = (size_t)w * p.NT * 2 * p.nq;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          if (k < p.o) {
+            const float2 x = wrow[k];
+            const float wr = x.x + v[2 * k], wi = x.y + v[2 * k + 1];
+            uint16_t hr, lr, hi_, li, hn, ln;
+            split16(wr, bf, hr, lr);
+            split16(wi, bf, hi_, li);
+            split16(-wi, bf, hn, ln);
+            const size_t r0 = base + (size_t)(2 * k) * 2 * p.nq, r1 = r0 + 2 * p.nq;
+            // row 2k: [Tr | -Ti], row 2k+1: [Ti | Tr]
+            p.t0_hi[r0 + pr] = hr;
+            p.t0_lo[r0 + pr] = lr;
             p.t0_hi[r0 + p.nq + pr] = hn;
             p.t0_lo[r0 + p.nq + pr] = ln;
-            p.t0_hi[r1 + pr] = h;
-            p.t0_lo[r1 + pr] = l;
+            p.t0_hi[r1 + pr] = hi_;
+            p.t0_lo[r1 + pr] = li;
+            p.t0_hi[r1 + p.nq + pr] = hr;
+            p.t0_lo[r1 + p.nq + pr] = lr;
           }
         }
       }

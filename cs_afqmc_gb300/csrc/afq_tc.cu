@@ -478,13 +478,12 @@ struct TcLayout {
 
 inline int rup(int x, int m) { return (x + m - 1) / m * m; }
 
-// rows per walker R = 2o rounded to 8, walkers per N tile wpt with R * wpt % 16 == 0,
-// R * wpt <= 256
+// rows per walker R = 2o rounded up to a multiple of 16 (each walker is a whole number of
+// 16-column TMEM chunks in the exp_h1 products), walkers per N tile wpt with R * wpt <= 256
 void walker_rows(int o, int* R, int* wpt) {
-  const int r = rup(2 * o, 8);
+  const int r = rup(2 * o, 16);
   int w = 256 / r;
-  if (r % 16) w -= (w & 1);
-  if (w < 1) w = (r % 16) ? 2 : 1;
+  if (w < 1) w = 1;
   *R = r;
   *wpt = w;
 }
@@ -494,7 +493,7 @@ struct Plan {
   size_t total;
   size_t o_rc_fb[2], o_rc_inv, o_lop[2], o_eop[2][2], o_u[2][2], o_rcb[2][2], o_rcb_inv[2], o_utmp;
   size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gblk[2][2];
-  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_trial32[2], o_rh1[2];
+  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_sbuf, o_trial32[2], o_rh1[2];
 };
 
 int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
@@ -587,6 +586,7 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   P->o_exc = L.take((size_t)t.nw * (t.mt_z[0] + t.mt_z[1]) * 16);
   P->o_status = L.take(256);
   P->o_amax = L.take(256);
+  P->o_sbuf = L.take((size_t)t.nslab * t.nw * 32 * 32 * 8);
   for (int s = 0; s < 2; ++s) P->o_trial32[s] = L.take((size_t)t.n * 64 * 4);
   for (int b = 0; b < 2; ++b) P->o_rh1[b] = L.take((size_t)t.n * 64 * 4);
   P->total = L.off + 1024;
@@ -674,6 +674,7 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   t.c_out = reinterpret_cast<double2*>(base + P.o_cout);
   t.exc_part = reinterpret_cast<double2*>(base + P.o_exc);
   t.status = reinterpret_cast<int*>(base + P.o_status);
+  t.sbuf = reinterpret_cast<float2*>(base + P.o_sbuf);
   for (int s = 0; s < 2; ++s) {
     t.trial32[s] = reinterpret_cast<float*>(base + P.o_trial32[s]);
     t.rh1_32[s] = reinterpret_cast<float*>(base + P.o_rh1[s]);
@@ -807,19 +808,45 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   return 0;
 }
 
+template <int OM>
+static void launch_green_inv(const MixedDev& md, float2* sbuf, double2* ovl, bool inv, cudaStream_t st) {
+  k_green_inv<OM><<<(md.nw + 7) / 8, 256, 0, st>>>(md, sbuf, ovl, inv ? 1 : 0);
+}
+
 int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl, bool write_ops,
              cudaStream_t st) {
   MixedDev md = mixed_dev(t, c);
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
-  const size_t smem = (size_t)t.n * omax * 8 + (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 +
-                      (size_t)omax * 2 * omax * 8 + (size_t)t.n * omax * 4;
-  cudaFuncSetAttribute(k_green_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (omax > kGreenMaxO) {
+    afq_set_error("mixed precision path: at most %d electrons per spin", kGreenMaxO);
+    return -2;
+  }
+  const float2* w0 = static_cast<const float2*>(wu);
+  const float2* w1 = static_cast<const float2*>(wd);
+  const size_t smem_s = (size_t)t.n * ((omax + 3) & ~3) * 8 + (size_t)t.n * omax * 4;
+  cudaFuncSetAttribute(k_green_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s);
   {
     ProfScope _ps(K_GREEN, st);
-    k_green_mixed<<<t.nw, 128, smem, st>>>(md, static_cast<const float2*>(wu), static_cast<const float2*>(wd),
-                                           ovl, write_ops ? 1 : 0);
+    k_green_s<<<t.nw, 128, smem_s, st>>>(md, w0, w1, t.sbuf, write_ops ? 1 : 0);
   }
-  return launch_check("green_mixed");
+  TC_CHECK(launch_check("green_s"));
+  {
+    ProfScope _ps(K_GREEN, st);
+    if (omax <= 8) launch_green_inv<8>(md, t.sbuf, ovl, write_ops, st);
+    else if (omax <= 16) launch_green_inv<16>(md, t.sbuf, ovl, write_ops, st);
+    else if (omax <= 24) launch_green_inv<24>(md, t.sbuf, ovl, write_ops, st);
+    else launch_green_inv<32>(md, t.sbuf, ovl, write_ops, st);
+  }
+  TC_CHECK(launch_check("green_inv"));
+  if (!write_ops) return 0;
+  const size_t smem_g = (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 + (size_t)kGreenMaxO * kGreenMaxO * 8 +
+                        (size_t)t.n * omax * 8;
+  cudaFuncSetAttribute(k_green_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g);
+  {
+    ProfScope _ps(K_GREEN, st);
+    k_green_g<<<t.nw, 128, smem_g, st>>>(md, w0, w1, t.sbuf);
+  }
+  return launch_check("green_g");
 }
 
 static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, double2* fb_out, cudaStream_t st,

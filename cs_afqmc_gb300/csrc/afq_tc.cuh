@@ -63,6 +63,7 @@ struct TcState {
   const float* trial32[2];  // [norb][o_s] trial in FP32
   const float* rh1_32[2];   // [o_b][norb] rot_h1 in FP32
   int* status;              // device word: nonzero after a pipeline timeout
+  float2* sbuf;             // [nslab][nw][32][32] overlap matrices / their inverses
   // tensor maps
   GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2], m_z[2];
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
