@@ -65,6 +65,8 @@ _SIGS = {
                                                ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                _vp, _vp, _vp, _vp]),
     "afq_block_end": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp]),
+    "afq_calc_force_bias_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                   ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "afq_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "afq_profile_reset": (ctypes.c_int, []),
     "afq_profile_read": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),

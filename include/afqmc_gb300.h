@@ -187,6 +187,24 @@ int afq_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, void
  * propagation.py:236-237. */
 int afq_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream);
 
+/* ---- allocation-free variant --------------------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device memory (code
+ * running inside another runtime's memory arena, such as a JAX/XLA custom call that only
+ * receives pre-allocated buffers, or a process whose device memory is reserved up front):
+ * the force bias of afq_calc_force_bias for an RHF trial and restricted complex128 walkers,
+ * in FP64, with no context, no workspace and no allocation. The Green's function it needs
+ * as scratch lives in a 40 MiB static device array inside the library (held by every GPU
+ * that loads the library until the process exits), so n_walkers * nocc * norb must not
+ * exceed 2,621,440; larger sizes return a negative code with a message.
+ * trial: [norb, nocc] float64; rot_chol: [nchol, nocc, norb] float64; walkers:
+ * [n_walkers, norb, nocc] complex128; force_bias: [n_walkers, nchol] complex128 (out).
+ * The first call on each device looks up the array's device address (make that first call
+ * before any stream capture). All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race; serialise them. */
+int afq_calc_force_bias_noalloc(int32_t norb, int32_t nocc, int32_t nchol, int32_t n_walkers,
+                                const double* trial, const double* rot_chol, const void* walkers,
+                                double* force_bias, void* stream);
+
 /* ---- launch accounting ----------------------------------------------------------------
  * Diagnostics with no counterpart in the reference (which has no profiler hooks). Every
  * kernel launch is counted per kernel class; with timing enabled, each launch is also
