@@ -11,6 +11,10 @@ and copied from pinned host memory every step for `e2e`.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
        [--precision mixed|fp64] [--workload NAME] [--no-cpu-baseline]
+       [--energy-blocks B] [--energy-only [--energy-control | --energy-sync]]
+`energy_check` in the line: B driver blocks of the mixed path and of the FP64 GPU path
+from the same walkers and the same Philox draws, blocked energies compared (the accuracy
+half of the metric) and both paths' walker-steps/s on that work.
 Under torchrun (N > 1) every rank runs an independent replica with its own seed (walkers
 only couple through block-end reductions, which a replica does not need); value = total
 walker-steps of all ranks / max time over ranks.
@@ -44,10 +48,18 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
-    ap.add_argument("--n-batch", type=int, default=4)
+    ap.add_argument("--n-batch", type=int, default=1)
     ap.add_argument("--mixed-config", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-procs", type=int, default=0)
+    ap.add_argument("--energy-blocks", type=int, default=4,
+                    help="driver blocks of the mixed-vs-FP64 energy comparison (0: skip)")
+    ap.add_argument("--energy-only", action="store_true",
+                    help="run only the mixed-vs-FP64 energy comparison and print its line")
+    ap.add_argument("--energy-control", action="store_true",
+                    help="add an FP64 run from perturbed walkers to the energy comparison")
+    ap.add_argument("--energy-sync", action="store_true",
+                    help="with --energy-only: per-block comparison from the FP64 run's states")
     return ap.parse_args()
 
 
@@ -147,7 +159,8 @@ def load_traffic():
 # our arm
 # ---------------------------------------------------------------------------------------
 
-def build_workload(name: str, precision: str, n_batch: int, mixed_config: int, seed: int):
+def build_workload(name: str, precision: str, n_batch: int, mixed_config: int, seed: int,
+                   perturb: float = 0.0):
     import numpy as np
     import torch
 
@@ -166,10 +179,157 @@ def build_workload(name: str, precision: str, n_batch: int, mixed_config: int, s
              precision=precision, mixed_config=mixed_config)
     hd = ham.build_propagation_intermediates(hd, prop, trial, wave)
     restricted = w["kind"] == "rhf"
-    pd = prop.init_prop_data(trial, wave, hd, init_walkers=s.init_walkers(w["n_walkers"], restricted))
+    iw = s.init_walkers(w["n_walkers"], restricted)
+    if perturb:  # relative perturbation of the initial walkers (decorrelation control)
+        g = np.random.default_rng(99)
+        iw = [x * (1 + perturb * g.standard_normal(x.shape)) for x in iw] if isinstance(iw, list) \
+            else iw * (1 + perturb * g.standard_normal(iw.shape))
+    pd = prop.init_prop_data(trial, wave, hd, init_walkers=iw)
     pd["key"] = RngKey(seed)
     samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=N_SR)
     return w, s, ham, trial, wave, hd, prop, pd, samp
+
+
+def energy_check(args, n_blocks: int, seed: int = 4242, control: bool = False) -> dict:
+    """Blocked energy of the mixed path against the FP64 GPU path fed identical draws.
+
+    Both runs start from the same walkers and take their fields and SR uniforms from the
+    same Philox key, so block n of both consumes the same numbers; the FP64 path matches
+    the FP64 oracle to 1e-9 (tests/test_gpu_fp64_parity.py), so it stands in for the
+    oracle at this size. Block 0 is a warm-up (context set-up); blocks 1..n-1 are timed
+    with CUDA events, giving both paths' walker-steps/s on the same work.
+
+    Identical draws keep two runs on the same trajectory only while every stochastic
+    reconfiguration and clamp decision agrees; one flipped decision decorrelates them.
+    `first_decorrelated_block` is the first block whose energies differ by more than
+    0.1 mHa. With control=True a third run, the FP64 path from initial walkers perturbed
+    by 1e-12 (relative), shows how far FP64 rounding alone moves a trajectory."""
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import driver
+
+    runs = {}
+    variants = [("mixed", "mixed", 0.0), ("fp64", "fp64", 0.0)]
+    if control:
+        variants.append(("fp64_perturbed", "fp64", 1e-12))
+    for name, prec, perturb in variants:
+        w, s, ham, trial, wave, hd, prop, pd, samp = build_workload(
+            args.workload, prec, args.n_batch, args.mixed_config, seed, perturb=perturb)
+        be0, bw0, pd = driver.run_blocks(samp, ham, hd, prop, pd, trial, wave, 1)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        be1, bw1, pd = driver.run_blocks(samp, ham, hd, prop, pd, trial, wave, n_blocks - 1)
+        t1.record()
+        torch.cuda.synchronize()
+        sec = t0.elapsed_time(t1) / 1e3
+        be = torch.cat([be0, be1]).cpu().numpy()
+        bw = torch.cat([bw0, bw1]).cpu().numpy()
+        ws = (n_blocks - 1) * N_PROP * N_ENE * N_SR * w["n_walkers"]
+        runs[name] = (be, bw, ws / sec if sec > 0 else None)
+        del pd, prop, hd, ham, trial
+        torch.cuda.empty_cache()
+
+    def compare(a, b):
+        (ea, wa, _), (eb, wb, _) = runs[a], runs[b]
+        d = ea - eb
+        nb = len(d)
+        far = np.nonzero(np.abs(d) > 1e-4)[0]
+        first = int(far[0]) if len(far) else None
+        locked = nb if first is None else first
+        ba = float(np.sum(ea * wa) / np.sum(wa))
+        bb = float(np.sum(eb * wb) / np.sum(wb))
+        out = {"blocked_diff_mha": 1e3 * (ba - bb),
+               "block_diff_mean_mha": 1e3 * float(np.mean(d)),
+               "block_diff_stderr_mha": 1e3 * float(np.std(d, ddof=1) / np.sqrt(nb)) if nb > 1 else None,
+               "block_diff_max_abs_mha": 1e3 * float(np.max(np.abs(d))),
+               "first_decorrelated_block": first,
+               "locked_blocks": locked,
+               "locked_max_abs_diff_mha": 1e3 * float(np.max(np.abs(d[:locked]))) if locked else None,
+               "within_0p1_mha": bool(abs(ba - bb) < 1e-4)}
+        if nb <= 400:
+            out["block_diff_mha"] = [round(1e3 * float(x), 5) for x in d]
+        return out
+
+    (em, wm, vm), (ef, wf, vf) = runs["mixed"], runs["fp64"]
+    nb = len(ef)
+    res = {
+        "blocks": nb, "walker_steps_per_block": N_PROP * N_ENE * N_SR * w["n_walkers"],
+        "blocked_energy_mixed": float(np.sum(em * wm) / np.sum(wm)),
+        "blocked_energy_fp64": float(np.sum(ef * wf) / np.sum(wf)),
+        "fp64_block_energy_stderr_mha": 1e3 * float(np.std(ef, ddof=1) / np.sqrt(nb)) if nb > 1 else None,
+        "mixed_vs_fp64": compare("mixed", "fp64"),
+        "mixed_walker_steps_per_s": vm, "fp64_walker_steps_per_s": vf,
+        "mixed_over_fp64": (vm / vf) if vm and vf else None,
+        "draws": "identical fields and SR uniforms (same Philox key), same initial walkers",
+    }
+    if control:
+        res["fp64_perturbed_vs_fp64"] = compare("fp64_perturbed", "fp64")
+    return res
+
+
+def energy_check_sync(args, n_blocks: int, seed: int = 4242) -> dict:
+    """Per-block energy error of the mixed path from the FP64 trajectory's own states.
+
+    Before every block the FP64 run's state (walkers cast to complex64, weights, scalars,
+    Philox offset) is copied into the mixed run, both propagate the block on the same draws,
+    and only the FP64 run continues (block end: weight record, QR, global SR). The block
+    energy difference then measures the mixed arithmetic over one block (20 steps, 4 energy
+    measurements) free of the trajectory decorrelation that a single flipped SR or clamp
+    decision causes in free-running comparisons; the blocked difference uses the FP64
+    block weights."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import _lib
+    from cs_afqmc_gb300._engine import stream_ptr
+
+    wm = build_workload(args.workload, "mixed", args.n_batch, args.mixed_config, seed)
+    wf = build_workload(args.workload, "fp64", args.n_batch, args.mixed_config, seed)
+    ham_m, trial_m, wave_m, hd_m, prop_m, pd_m, samp = wm[2], wm[3], wm[4], wm[5], wm[6], wm[7], wm[8]
+    ham_f, trial_f, wave_f, hd_f, prop_f, pd_f = wf[2], wf[3], wf[4], wf[5], wf[6], wf[7]
+    em, ef, bw = [], [], []
+    wsum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for _ in range(n_blocks):
+        if isinstance(pd_f["walkers"], list):
+            for a, b in zip(pd_m["walkers"], pd_f["walkers"]):
+                a.copy_(b.to(a.dtype))
+        else:
+            pd_m["walkers"].copy_(pd_f["walkers"].to(pd_m["walkers"].dtype))
+        pd_m["weights"].copy_(pd_f["weights"])
+        dict.__getitem__(pd_m, "_scalars").copy_(dict.__getitem__(pd_f, "_scalars"))
+        pd_m["key"].offset = pd_f["key"].offset
+        e_m, pd_m = samp.propagate_phaseless(ham_m, hd_m, prop_m, pd_m, trial_m, wave_m)
+        e_f, pd_f = samp.propagate_phaseless(ham_f, hd_f, prop_f, pd_f, trial_f, wave_f)
+        zg = samp.draw_zetas(pd_f, 1)
+        eng = pd_f["_engine"]
+        st = pd_f.state(eng)
+        e_hold = e_f.reshape(1).clone()
+        _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), e_hold.data_ptr(), zg.data_ptr(),
+                  wsum.data_ptr(), stream_ptr())
+        em.append(e_m.item())
+        ef.append(e_hold.item())
+        bw.append(wsum.item())
+    em, ef, bw = np.array(em), np.array(ef), np.array(bw)
+    d = em - ef
+    nb = len(d)
+    blocked = float(np.sum(bw * d) / np.sum(bw))
+    return {
+        "blocks": nb,
+        "blocked_energy_fp64": float(np.sum(bw * ef) / np.sum(bw)),
+        "blocked_diff_mha": 1e3 * blocked,
+        "block_diff_mean_mha": 1e3 * float(np.mean(d)),
+        "block_diff_stderr_mha": 1e3 * float(np.std(d, ddof=1) / np.sqrt(nb)) if nb > 1 else None,
+        "block_diff_rms_mha": 1e3 * float(np.sqrt(np.mean(d * d))),
+        "block_diff_max_abs_mha": 1e3 * float(np.max(np.abs(d))),
+        "fp64_block_energy_stderr_mha": 1e3 * float(np.std(ef, ddof=1) / np.sqrt(nb)) if nb > 1 else None,
+        "within_0p1_mha": bool(abs(blocked) < 1e-4),
+        "draws": "every block from the FP64 run's state, identical fields and SR uniforms",
+    }
 
 
 def run_ours(args, rank, world, local):
@@ -182,6 +342,16 @@ def run_ours(args, rank, world, local):
     from cs_afqmc_gb300._engine import stream_ptr
 
     torch.cuda.set_device(local)
+    if args.energy_only:
+        if rank == 0:
+            if args.energy_sync:
+                ec = energy_check_sync(args, max(2, args.energy_blocks))
+            else:
+                ec = energy_check(args, max(2, args.energy_blocks), control=args.energy_control)
+            print(json.dumps({"metric": "blocked energy, mixed vs FP64 GPU path, identical draws",
+                              "workload": args.workload, "n_batch": args.n_batch,
+                              "mixed_config": args.mixed_config, "energy_check": ec}), flush=True)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -331,6 +501,9 @@ def run_ours(args, rank, world, local):
         finally:
             cpu_pool.close()
 
+    # ---- accuracy at this workload: mixed vs FP64 GPU path on identical draws ----
+    ec = energy_check(args, args.energy_blocks) if args.energy_blocks > 1 and world == 1 else None
+
     ws_bytes = nw * G * 8 * N_PROP * N_ENE + nw * w["norb"] * w["nelec"][0] * (8 if args.precision == "mixed" else 16)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -347,7 +520,7 @@ def run_ours(args, rank, world, local):
                    "replicas": "independent replicas per GPU" if world > 1 else "single GPU",
                    "last_block_energy": block_energy},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-        "clocks": clocks, "kernels": kernels,
+        "clocks": clocks, "kernels": kernels, "energy_check": ec,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -175,6 +175,50 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     if (!drain) {
       got = ptx::mbar_wait(accb, 0);
       ptx::tc_fence_after();
+    } else if constexpr (BNMAX <= 128) {
+      // Running sum in registers (thread = TMEM lane = output row, BNMAX columns): a drain
+      // is one TMEM read of the finished accumulator; the sum goes to TMEM columns [0, bn)
+      // once, after the last run, for the epilogue.
+      const int nruns = (total + drain - 1) / drain;
+      const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+      float sum[BNMAX];
+#pragma unroll
+      for (int j = 0; j < BNMAX; ++j) sum[j] = 0.f;
+      for (int run = 0; run < nruns; ++run) {
+        const int a = run & 1;
+        if (!ptx::mbar_wait(&accfull[a], (run >> 1) & 1)) {
+          got = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        const uint32_t src = tmem + lane_off + (uint32_t)((1 + a) * bn);
+#pragma unroll
+        for (int h = 0; h < BNMAX; h += 64) {
+          if (h < bn) {
+            float v[64];
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
+              if (h + c < bn) ptx::tmem_ld16p(src + h + c, v + c);
+            ptx::tmem_ld_wait();
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
+              if (h + c < bn) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) sum[h + c + j] += v[c + j];
+              }
+          }
+        }
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&accempty[a]);
+      }
+      if (got) {
+#pragma unroll
+        for (int c = 0; c < BNMAX; c += 16)
+          if (c < bn) ptx::tmem_st16p(tmem + lane_off + (uint32_t)c, sum + c);
+        ptx::tmem_st_wait();
+      }
+      ptx::tc_fence_after();
     } else {
       const int nruns = (total + drain - 1) / drain;
       const uint32_t lane_off = (uint32_t)(q * 32) << 16;

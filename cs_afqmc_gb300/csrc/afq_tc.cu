@@ -551,6 +551,10 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   t.n_e_terms = 1 + ((cfg & kExpDyn) ? 1 : 0) + ((cfg & kExpStat) ? 1 : 0);
   t.n_en_terms = 1 + ((cfg & kEneDyn) ? 1 : 0) + ((cfg & kEneStat) ? 1 : 0);
   t.taylor_split = (cfg >> kTaylorShift) & 7;
+  {
+    const int d = (cfg >> kDrainShift) & 7;
+    t.drain = d == 0 ? kDrainDefault : d == 7 ? 0 : d;
+  }
   TcLayout L;
   const size_t H = 2;  // bytes per 16-bit element
   for (int i = 0; i < 2; ++i) P->o_rc_fb[i] = L.take((size_t)c.nchol * t.ldfb * H);
@@ -875,8 +879,10 @@ static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, doubl
   const GemmMaps& m = maps ? *maps : t.m_fb;
   const int nterms = maps ? t.n_en_terms : t.n_fb_terms;
   if (t.fb_bn <= 64)  // narrow tiles: a smaller ring lets two CTAs share an SM
-    return launch_gemm<64, 4, EpiFB>(cls, m, nterms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st, 0, 1);
-  return launch_gemm<128, 4, EpiFB>(cls, m, nterms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st, 0, 1);
+    return launch_gemm<64, 4, EpiFB>(cls, m, nterms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st, 0,
+                                     t.drain);
+  return launch_gemm<128, 4, EpiFB>(cls, m, nterms, kt, mt, t.fb_ntiles, t.fb_bn, t.bf16, ep, t.status, st, 0,
+                                    t.drain);
 }
 
 int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
@@ -927,7 +933,7 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.sqdt = (float)sqrt(c.dt);
     const int kt = (c.nchol + 63) / 64, mt = (2 * t.nwc + 127) / 128, nt = (t.n * t.nq + 127) / 128;
     TC_CHECK((launch_gemm<128, 4, EpiVHS>(K_VHS, t.m_vhs, t.n_vhs_terms, kt, mt, nt, 128, t.bf16, ev, t.status, st,
-                                         2 * w0, 1)));
+                                         2 * w0, t.drain)));
     for (int s = 0; s < t.nslab; ++s) {
       TaylorDev td;
       td.n = t.n;
@@ -980,7 +986,7 @@ int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
     ep.exc_part = t.exc_part + (b == 0 ? 0 : (size_t)t.nw * t.mt_z[0]);
     const int kt = (t.kb[b] + 63) / 64, nt = (2 * t.nw + 127) / 128;
     TC_CHECK((launch_gemm<128, 4, EpiExc>(K_ENERGY, t.m_z[b], t.n_en_terms, kt, t.mt_z[b], nt, 128, t.bf16, ep,
-                                         t.status, st, 0, 1)));
+                                         t.status, st, 0, t.drain)));
   }
   {
     ProfScope _ps(K_ENERGY_FIN, st);
@@ -1022,6 +1028,10 @@ extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long 
   EpiStoreF32::Params ep{d, M, N, (long)N};
   const int kt = (K + 63) / 64, mt = (M + 127) / 128, nt = (N + bn - 1) / bn;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // bn <= 128 runs the instantiation the product GEMMs use (register-resident drain)
+  if (bn <= 128)
+    return launch_gemm<128, 4, EpiStoreF32>(K_PREP, maps, nterms, kt, mt, nt, bn, bf16, ep, status, st, 0,
+                                            drain);
   return launch_gemm<256, 4, EpiStoreF32>(K_PREP, maps, nterms, kt, mt, nt, bn, bf16, ep, status, st, 0,
                                           drain);
 }

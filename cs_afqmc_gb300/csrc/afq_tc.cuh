@@ -31,8 +31,11 @@ enum MixedBits : int32_t {
   kEneStat = 1 << 7,    // energy: lo part of rot_chol
   kTaylorShift = 8,     // bits 8..10: Taylor products computed with split operands
   kUseBf16 = 1 << 11,   // bf16 operands instead of fp16
+  kDrainShift = 12,     // bits 12..14: K tiles per truncated accumulation run in the force
+                        // bias, vhs and exchange GEMMs (0: default, 7: no draining)
   kExplicit = 1 << 30,  // set by callers that pass an explicit configuration
 };
+constexpr int kDrainDefault = 2;  // K tiles per drained run unless the configuration says
 constexpr int32_t kMixedDefault = kFbDyn | kFbStat | kVhsDyn | kVhsStat | kExpDyn | kExpStat |
                                   kEneDyn | kEneStat | (2 << kTaylorShift);
 
@@ -69,6 +72,7 @@ struct TcState {
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
   int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;
+  int drain;                // K tiles per drained accumulation run (0: not drained)
 };
 
 size_t tc_workspace_bytes(const afq_ctx_dev& c, int nw_chunk, int32_t mixed_config);

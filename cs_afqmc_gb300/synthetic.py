@@ -149,6 +149,10 @@ WORKLOADS = {
     # single large system, precision pattern
     "rhf_norb120_nocc20_nchol600_nw1024": dict(norb=120, nelec=(20, 20), nchol=600,
                                                n_walkers=1024, dt=0.005, kind="rhf"),
+    # one 256-walker chunk of the system above: the same per-launch kernel shapes with
+    # n_batch=1, a quarter of the device memory (profiling case)
+    "rhf_norb120_nocc20_nchol600_nw256": dict(norb=120, nelec=(20, 20), nchol=600,
+                                              n_walkers=256, dt=0.005, kind="rhf"),
     # differentiation pattern (UHF)
     "uhf_norb60_nocc10x8_nchol300_nw512": dict(norb=60, nelec=(10, 8), nchol=300,
                                                n_walkers=512, dt=0.005, kind="uhf"),

@@ -57,7 +57,13 @@ typedef struct afq_dims {
   int32_t precision;    /* afq_precision */
   int32_t n_exp_terms;  /* Taylor terms of exp(vhs), reference default 6 */
   int32_t n_batch;      /* walker chunks for the vhs workspace (>= 1, divides n_walkers) */
-  int32_t mixed_config; /* AFQ_PREC_MIXED accuracy options; 0 = library default */
+  int32_t mixed_config; /* AFQ_PREC_MIXED accuracy options; 0 = library default (767).
+                           bits 0..7: lo (correction) terms of G / rot_chol (force bias),
+                           fields / chol (vhs), walker / exp_h1 (exp_h1 products), G /
+                           rot_chol (energy); bits 8..10: Taylor products with split
+                           operands; bit 11: bf16 instead of fp16; bits 12..14: K tiles per
+                           drained accumulation run of the force-bias, vhs and exchange
+                           GEMMs (0 = default, 7 = undrained) */
   double dt;
 } afq_dims;
 
