@@ -45,6 +45,9 @@ struct afq_ctx {
   int32_t* sr_idx;
   double* cum;
   afq::TcState tc;  // tensor-core (mixed precision) operands and plans
+  // Inside afq_propagate_phaseless only (mixed path): what the scratch buffers hold for the
+  // current walkers. 0 nothing, 1 S^-1 and the walker operand, 2 also G and its operands.
+  int gstate;
 };
 
 namespace {
@@ -166,9 +169,14 @@ bool is_fp64(const afq_ctx* c) { return c->d.precision == AFQ_PREC_FP64; }
 
 // Green's function + overlap. FP64: G into c->green. Mixed: the 16-bit operands of the
 // force-bias, energy and exp_h1 contractions (wg) and/or the overlap.
-int green(afq_ctx* c, const void* wu, const void* wd, double2* g, double2* ovl, bool wg, cudaStream_t st) {
+// chain (mixed path, inside afq_propagate_phaseless): keep S^-1 and record in c->gstate what
+// the next propagation step can reuse.
+int green(afq_ctx* c, const void* wu, const void* wd, double2* g, double2* ovl, bool wg, cudaStream_t st,
+          bool chain = false) {
   if (is_fp64(c)) return afq::launch_green<double>(c->dev, wu, wd, g, ovl, wg, st);
-  return afq::tc_green(c->tc, c->dev, wu, wd, ovl, wg, st);
+  CHECK(afq::tc_green(c->tc, c->dev, wu, wd, ovl, wg, st, chain));
+  c->gstate = chain ? (wg ? 2 : 1) : 0;
+  return 0;
 }
 
 int force_bias_from_green(afq_ctx* c, double2* out, cudaStream_t st) {
@@ -198,14 +206,19 @@ int check_state(const afq_ctx* c, const afq_walker_state* s) {
   return 0;
 }
 
-int propagate_impl(afq_ctx* c, afq_walker_state* s, const double* fields, cudaStream_t st) {
+// chain: a step inside afq_propagate_phaseless, where the Green's-function work of the
+// previous overlap evaluation on the same walkers (c->gstate) is reused.
+int propagate_impl(afq_ctx* c, afq_walker_state* s, const double* fields, cudaStream_t st,
+                   bool chain = false) {
   const afq_ctx_dev& d = c->dev;
   if (!is_fp64(c)) {
     // mixed: operands -> fused force bias / field shifts -> exp_h1, vhs + Taylor, exp_h1
-    CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, nullptr, true, st));
+    const int have = chain ? c->gstate : 0;
+    if (have == 0) CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, nullptr, true, st));
+    else if (have == 1) CHECK(afq::tc_green_from_inverse(c->tc, d, s->walkers_up, s->walkers_dn, st));
     CHECK(afq::tc_field_shifts(c->tc, d, fields, st));
     CHECK(afq::tc_propagate_walkers(c->tc, d, s->walkers_up, s->walkers_dn, st));
-    CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, c->ovl_new, false, st));
+    CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, c->ovl_new, false, st, chain));
     return afq::tc_weights(c->tc, d, c->ovl_new, reinterpret_cast<double2*>(s->overlaps), s->weights,
                            s->scalars, st);
   }
@@ -411,7 +424,8 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
   cudaStream_t st = S(stream);
   const afq_ctx_dev& d = ctx->dev;
   double2* ovl = reinterpret_cast<double2*>(state->overlaps);
-  CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+  ctx->gstate = 0;
+  CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st, true));
   CHECK(afq::launch_phaseless_begin(state->scalars, st));
   const size_t step_elems = (size_t)d.nw * d.nchol;
   int blk = 0;
@@ -419,17 +433,20 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
     for (int eb = 0; eb < n_ene_blocks; ++eb, ++blk) {
       for (int p = 0; p < n_prop_steps; ++p) {
         const double* f = fields + ((size_t)blk * n_prop_steps + p) * step_elems;
-        CHECK(propagate_impl(ctx, state, f, st));
+        CHECK(propagate_impl(ctx, state, f, st, true));
       }
+      ctx->gstate = 0;
       CHECK(qr_impl(ctx, state, st));
-      CHECK(green(ctx, state->walkers_up, state->walkers_dn, ctx->green, ovl, true, st));
+      CHECK(green(ctx, state->walkers_up, state->walkers_dn, ctx->green, ovl, true, st, true));
       CHECK(energy_from_green(ctx, ctx->ene, st));
       CHECK(afq::launch_block_stats(d, ctx->ene, state->weights, state->scalars, block_energy + blk,
                                     block_weight + blk, st));
     }
+    ctx->gstate = 0;
     CHECK(sr_impl(ctx, state, zetas + sr, nullptr, st));
-    CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+    CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st, true));
   }
+  ctx->gstate = 0;
   return afq::launch_phaseless_end(blk, (double)n_sr_blocks * n_ene_blocks * d.nw, block_energy,
                                    block_weight, state->scalars, energy, st);
 }

@@ -64,6 +64,25 @@ struct MixedDev {
 
 constexpr int kGreenMaxO = 32;
 
+// dst[map(e)] = src[e] for e < n by a block of NT threads, 8 independent loads in flight per
+// thread before the shared-memory stores (the copies are latency-bound otherwise)
+template <int NT, class T, class Map>
+__device__ __forceinline__ void copy_batched(T* dst, const T* __restrict__ src, int n, Map map) {
+  for (int base = threadIdx.x; base < n; base += 8 * NT) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * NT;
+      if (e < n) v[u] = src[e];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * NT;
+      if (e < n) dst[map(e)] = v[u];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2* __restrict__ wu,
                                                  const float2* __restrict__ wd,
                                                  float2* __restrict__ sbuf, int write_ops) {
@@ -79,11 +98,13 @@ __global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2
     const float2* W = (s == 0 ? wu : wd) + (size_t)w * n * o;
     const float* C = md.trial32[s];
     // coalesced copies; W rows padded to a multiple of 4 columns for 16-byte loads
-    for (int e = tid; e < n * o4; e += 128) {
-      const int pp = e / o4, k = e - pp * o4;
-      Ws[e] = (k < o) ? W[pp * o + k] : make_float2(0.f, 0.f);
-    }
-    for (int e = tid; e < n * o; e += 128) Cs[e] = C[e];
+    if (o4 != o)
+      for (int e = tid; e < n * (o4 - o); e += 128) {
+        const int pp = e / (o4 - o), k = o + e - pp * (o4 - o);
+        Ws[pp * o4 + k] = make_float2(0.f, 0.f);
+      }
+    copy_batched<128>(Ws, W, n * o, [o, o4](int e) { return (e / o) * o4 + e % o; });
+    copy_batched<128>(Cs, C, n * o, [](int e) { return e; });
     __syncthreads();
     if (write_ops && tid < n) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
       uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + tid;
@@ -239,9 +260,10 @@ __global__ void __launch_bounds__(128) k_green_g(const MixedDev md, const float2
   for (int s = 0; s < md.nslab; ++s) {
     const int o = md.o_slab[s];
     const float2* Ssrc = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
-    for (int e = tid; e < kGreenMaxO * kGreenMaxO; e += 128) Si[e] = Ssrc[e];
+    // the o rows of S^-1 (row stride kGreenMaxO) and the walker slab
+    copy_batched<128>(Si, Ssrc, o * kGreenMaxO, [](int e) { return e; });
     const float2* Wg = (s == 0 ? wu : wd) + (size_t)w * n * o;
-    for (int e = tid; e < n * o; e += 128) Wsm[e] = Wg[e];
+    copy_batched<128>(Wsm, Wg, n * o, [](int e) { return e; });
     __syncthreads();
     if (prow) {
       float2 wr[kGreenMaxO];
@@ -460,38 +482,61 @@ struct EpiExp {
       const int w = w0 + wl;
       if (pr >= p.n || w >= p.nw) continue;
       float2* wrow = reinterpret_cast<float2*>(p.w) + ((size_t)w * p.n + pr) * p.o;
+      // loads are issued 8 orbitals at a time before the stores of those orbitals (the stores
+      // may alias the loads for the compiler, which would otherwise wait one load latency per k)
       if (p.last) {
         const size_t ab = (size_t)w * p.R * p.nk + pr;
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
-          if (k < p.o) {
-            const size_t i0 = ab + (size_t)(2 * k) * p.nk, i1 = i0 + p.nk;
-            const float ar = h2f(p.acc_hi[i0], bf) + h2f(p.acc_lo[i0], bf);
-            const float ai = h2f(p.acc_hi[i1], bf) + h2f(p.acc_lo[i1], bf);
-            wrow[k] = make_float2(ar + v[2 * k], ai + v[2 * k + 1]);
+        for (int k0 = 0; k0 < 32; k0 += 8) {
+          if (k0 < p.o) {
+            uint16_t ah[16], al[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r)
+              if (2 * k0 + r < 2 * p.o) {
+                ah[r] = p.acc_hi[ab + (size_t)(2 * k0 + r) * p.nk];
+                al[r] = p.acc_lo[ab + (size_t)(2 * k0 + r) * p.nk];
+              }
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const int k = k0 + kk;
+              if (k < p.o) {
+                const float ar = h2f(ah[2 * kk], bf) + h2f(al[2 * kk], bf);
+                const float ai = h2f(ah[2 * kk + 1], bf) + h2f(al[2 * kk + 1], bf);
+                wrow[k] = make_float2(ar + v[2 * k], ai + v[2 * k + 1]);
+              }
+            }
           }
         }
       } else {
         const size_t base = (size_t)w * p.NT * 2 * p.nq;
 #pragma unroll
-        for (int k = 0; k < 32; ++k) {
-          if (k < p.o) {
-            const float2 x = wrow[k];
-            const float wr = x.x + v[2 * k], wi = x.y + v[2 * k + 1];
-            uint16_t hr, lr, hi_, li, hn, ln;
-            split16(wr, bf, hr, lr);
-            split16(wi, bf, hi_, li);
-            split16(-wi, bf, hn, ln);
-            const size_t r0 = base + (size_t)(2 * k) * 2 * p.nq, r1 = r0 + 2 * p.nq;
-            // row 2k: [Tr | -Ti], row 2k+1: [Ti | Tr]
-            p.t0_hi[r0 + pr] = hr;
-            p.t0_lo[r0 + pr] = lr;
-            p.t0_hi[r0 + p.nq + pr] = hn;
-            p.t0_lo[r0 + p.nq + pr] = ln;
-            p.t0_hi[r1 + pr] = hi_;
-            p.t0_lo[r1 + pr] = li;
-            p.t0_hi[r1 + p.nq + pr] = hr;
-            p.t0_lo[r1 + p.nq + pr] = lr;
+        for (int k0 = 0; k0 < 32; k0 += 8) {
+          if (k0 < p.o) {
+            float2 xw[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+              if (k0 + kk < p.o) xw[kk] = wrow[k0 + kk];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const int k = k0 + kk;
+              if (k < p.o) {
+                const float wr = xw[kk].x + v[2 * k], wi = xw[kk].y + v[2 * k + 1];
+                uint16_t hr, lr, hi_, li, hn, ln;
+                split16(wr, bf, hr, lr);
+                split16(wi, bf, hi_, li);
+                split16(-wi, bf, hn, ln);
+                const size_t r0 = base + (size_t)(2 * k) * 2 * p.nq, r1 = r0 + 2 * p.nq;
+                // row 2k: [Tr | -Ti], row 2k+1: [Ti | Tr]
+                p.t0_hi[r0 + pr] = hr;
+                p.t0_lo[r0 + pr] = lr;
+                p.t0_hi[r0 + p.nq + pr] = hn;
+                p.t0_lo[r0 + p.nq + pr] = ln;
+                p.t0_hi[r1 + pr] = hi_;
+                p.t0_lo[r1 + pr] = li;
+                p.t0_hi[r1 + p.nq + pr] = hr;
+                p.t0_lo[r1 + p.nq + pr] = lr;
+              }
+            }
           }
         }
       }

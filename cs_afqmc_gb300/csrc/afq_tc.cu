@@ -211,18 +211,21 @@ __global__ void __launch_bounds__(128, 1)
     float d[64];
     const int nreg = KT + ((m <= td.split) ? 2 : 0);
 #pragma unroll
-    for (int c0 = 0; c0 < 64; c0 += 16) {
+    for (int j = 0; j < 64; ++j) d[j] = 0.f;
+    // one TMEM load wait per region: all column chunks of the region are in flight together
+    for (int rg = 0; rg < nreg; ++rg) {
+      float v[64];
+      const uint32_t src = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(64 * rg);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) d[c0 + j] = 0.f;
-      if (c0 < td.NT) {
-        for (int rg = 0; rg < nreg; ++rg) {
-          float v[16];
-          ptx::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(64 * rg + c0), v);
-          ptx::tmem_ld_wait();
+      for (int c0 = 0; c0 < 64; c0 += 16)
+        if (c0 < td.NT) ptx::tmem_ld16p(src + c0, v + c0);
+      ptx::tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 16; ++j) d[c0 + j] += v[j];
+      for (int c0 = 0; c0 < 64; c0 += 16)
+        if (c0 < td.NT) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) d[c0 + j] += v[c0 + j];
         }
-      }
     }
     const float invm = 1.0f / (float)m;
 #pragma unroll
@@ -818,7 +821,7 @@ static void launch_green_inv(const MixedDev& md, float2* sbuf, double2* ovl, boo
 }
 
 int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl, bool write_ops,
-             cudaStream_t st) {
+             cudaStream_t st, bool keep_inverse) {
   MixedDev md = mixed_dev(t, c);
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
   if (omax > kGreenMaxO) {
@@ -831,18 +834,28 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   cudaFuncSetAttribute(k_green_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s);
   {
     ProfScope _ps(K_GREEN, st);
-    k_green_s<<<t.nw, 128, smem_s, st>>>(md, w0, w1, t.sbuf, write_ops ? 1 : 0);
+    k_green_s<<<t.nw, 128, smem_s, st>>>(md, w0, w1, t.sbuf, (write_ops || keep_inverse) ? 1 : 0);
   }
   TC_CHECK(launch_check("green_s"));
+  const bool inv = write_ops || keep_inverse;
   {
     ProfScope _ps(K_GREEN, st);
-    if (omax <= 8) launch_green_inv<8>(md, t.sbuf, ovl, write_ops, st);
-    else if (omax <= 16) launch_green_inv<16>(md, t.sbuf, ovl, write_ops, st);
-    else if (omax <= 24) launch_green_inv<24>(md, t.sbuf, ovl, write_ops, st);
-    else launch_green_inv<32>(md, t.sbuf, ovl, write_ops, st);
+    if (omax <= 8) launch_green_inv<8>(md, t.sbuf, ovl, inv, st);
+    else if (omax <= 16) launch_green_inv<16>(md, t.sbuf, ovl, inv, st);
+    else if (omax <= 24) launch_green_inv<24>(md, t.sbuf, ovl, inv, st);
+    else launch_green_inv<32>(md, t.sbuf, ovl, inv, st);
   }
   TC_CHECK(launch_check("green_inv"));
   if (!write_ops) return 0;
+  return tc_green_from_inverse(t, c, wu, wd, st);
+}
+
+int tc_green_from_inverse(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd,
+                          cudaStream_t st) {
+  MixedDev md = mixed_dev(t, c);
+  const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
+  const float2* w0 = static_cast<const float2*>(wu);
+  const float2* w1 = static_cast<const float2*>(wd);
   const size_t smem_g = (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 + (size_t)kGreenMaxO * kGreenMaxO * 8 +
                         (size_t)t.n * omax * 8;
   cudaFuncSetAttribute(k_green_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g);

@@ -78,8 +78,13 @@ struct TcState {
 size_t tc_workspace_bytes(const afq_ctx_dev& c, int nw_chunk, int32_t mixed_config);
 int tc_init(TcState* t, const afq_ctx_dev& c, const afq_hamiltonian& h, const double* rccat,
             int nw_chunk, int32_t mixed_config, char* ws, cudaStream_t st);
+// write_ops: S, S^-1 and the walker operand, then G and its 16-bit operands. keep_inverse
+// (without write_ops): S, the walker operand, S^-1 kept in the scratch buffer and the
+// overlap, so that a later tc_green_from_inverse on the same walkers only forms G.
 int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl,
-             bool write_ops, cudaStream_t st);
+             bool write_ops, cudaStream_t st, bool keep_inverse = false);
+int tc_green_from_inverse(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd,
+                          cudaStream_t st);
 int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st);
 int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st);
 int tc_field_shifts(TcState& t, const afq_ctx_dev& c, const double* fields, cudaStream_t st);
