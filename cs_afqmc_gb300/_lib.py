@@ -83,6 +83,9 @@ _TEST_SIGS = {
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          _vp, _vp]),
+    "afq_test_gemm_split": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, _vp, _vp]),
 }
 _SIGS.update(_TEST_SIGS)
 

@@ -442,6 +442,40 @@ struct EpiVHS {
   }
 };
 
+// The same scatter for the persistent split GEMM: row R of the chunk, 128 columns from col0.
+struct EpiVHSSplit {
+  using Params = EpiVHS::Params;
+  __device__ __forceinline__ static void store(const Params& p, int R, int col0, const float* v) {
+    if (R >= p.rows) return;
+    const int wl = R >> 1, c = R & 1;
+    const bool bf = p.bf16 != 0;
+    const float scale = c == 0 ? p.sqdt : -p.sqdt;
+#pragma unroll
+    for (int c0 = 0; c0 < 128; c0 += 16) {
+      const int col = col0 + c0, pr = col / p.nq, q0 = col % p.nq;
+      if (pr >= p.n) continue;
+      const size_t off = ((size_t)wl * 128 + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0;
+      uint32_t hw[8], lw[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        uint16_t h0, l0, h1, l1;
+        split16(v[c0 + 2 * j] * scale, bf, h0, l0);
+        split16(v[c0 + 2 * j + 1] * scale, bf, h1, l1);
+        hw[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lw[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+      }
+      uint4* dh = reinterpret_cast<uint4*>(p.v_hi + off);
+      dh[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      dh[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
+      if (p.want_lo) {
+        uint4* dl = reinterpret_cast<uint4*>(p.v_lo + off);
+        dl[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        dl[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+      }
+    }
+  }
+};
+
 // ======================================================================================
 // exp_h1 products: D[p][(w, 2k + c)] = ((E - I) X)[p][k].c for the walker (X = W) or the
 // Taylor sum (X = acc). First product: W1 = W + D into the Taylor B operand (hi/lo);

@@ -91,6 +91,25 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
   return launch_check("gemm_tc");
 }
 
+// persistent split-precision GEMM (afq_gemm_split.cuh): one CTA per SM, at most one per tile
+template <class Epi>
+static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms,
+                        const typename Epi::Params& ep, int* status, cudaStream_t st) {
+  const int ntiles = g.m_tiles * g.n_tiles;
+  if (ntiles < 1 || g.k_tiles < 1 || g.drain < 1) {
+    afq_set_error("split gemm: bad sizes");
+    return -1;
+  }
+  auto kfn = k_gemm_split<Epi>;
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
+  const int grid = ntiles < num_sms ? ntiles : num_sms;
+  {
+    ProfScope _ps(cls, st);
+    kfn<<<grid, kSplitThreads, kSplitSmem, st>>>(maps, g, ep, status);
+  }
+  return launch_check("gemm_split");
+}
+
 // ======================================================================================
 // Taylor kernel (propagation.py:76-90): per walker slab, T_0 = W1 (B operand from the
 // first exp_h1 product), T_m = V T_{m-1} / m on the tensor cores with V = [Vr | Vi] held in
@@ -744,6 +763,17 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
       TC_CHECK(mk(&t.m_fb.b[i++], t.rc_fb[1], c.nchol, t.kfb, t.ldfb, t.fb_bn));
     }
   }
+  {  // vhs planes for the persistent split GEMM (B boxes of 256 rows)
+    const uint64_t nrows = (uint64_t)t.n * t.nq;
+    TC_CHECK(mk(&t.m_vhs_split.a_hi, t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
+    TC_CHECK(mk(&t.m_vhs_split.a_lo, t.xt[1], 2 * t.nw, c.nchol, t.ldg, 128));
+    TC_CHECK(mk(&t.m_vhs_split.b_hi, t.lop[0], nrows, c.nchol, t.ldg, kSplitBN));
+    TC_CHECK(mk(&t.m_vhs_split.b_lo, t.lop[1], nrows, c.nchol, t.ldg, kSplitBN));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&t.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || t.num_sms < 1)
+      t.num_sms = 148;
+  }
   {  // vhs: A = xt (walker-dependent), B = lop (static)
     int i = 0;
     const uint64_t nrows = (uint64_t)t.n * t.nq;
@@ -944,9 +974,16 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.bf16 = t.bf16 ? 1 : 0;
     ev.want_lo = want_lo ? 1 : 0;
     ev.sqdt = (float)sqrt(c.dt);
-    const int kt = (c.nchol + 63) / 64, mt = (2 * t.nwc + 127) / 128, nt = (t.n * t.nq + 127) / 128;
-    TC_CHECK((launch_gemm<128, 4, EpiVHS>(K_VHS, t.m_vhs, t.n_vhs_terms, kt, mt, nt, 128, t.bf16, ev, t.status, st,
-                                         2 * w0, t.drain)));
+    SplitArgs sa;
+    sa.k_tiles = (c.nchol + 63) / 64;
+    sa.m_tiles = (2 * t.nwc + 127) / 128;
+    sa.n_tiles = (t.n * t.nq + kSplitBN - 1) / kSplitBN;
+    sa.a_row0 = 2 * w0;
+    sa.has_alo = (t.cfg & kVhsDyn) ? 1 : 0;
+    sa.has_blo = (t.cfg & kVhsStat) ? 1 : 0;
+    sa.drain = t.drain > 0 ? t.drain : sa.k_tiles;
+    sa.idesc = ptx::idesc_f16(128, kSplitBN, t.bf16 ? 1 : 0);
+    TC_CHECK(launch_split<EpiVHSSplit>(K_VHS, t.m_vhs_split, sa, t.num_sms, ev, t.status, st));
     for (int s = 0; s < t.nslab; ++s) {
       TaylorDev td;
       td.n = t.n;
@@ -1016,6 +1053,37 @@ int tc_orthonormalize(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cuda
 }  // namespace afq
 
 // ---- test hooks (include/afqmc_gb300_testing.h) ---------------------------------------
+
+extern "C" int afq_test_gemm_split(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo,
+                                   float* d, int M, int N, int K, int lda, int ldb, int bf16, int drain,
+                                   int* status, void* stream) {
+  using namespace afq;
+  if (!a_hi || !b_hi || !d || !status || M < 1 || N < 1 || K < 1 || drain < 0) {
+    afq_set_error("afq_test_gemm_split: bad arguments");
+    return -1;
+  }
+  SplitMaps maps;
+  memset(&maps, 0, sizeof(maps));
+  int e = make_tmap_16(&maps.a_hi, a_hi, M, K, lda, 128, bf16 != 0);
+  if (!e && a_lo) e = make_tmap_16(&maps.a_lo, a_lo, M, K, lda, 128, bf16 != 0);
+  if (!e) e = make_tmap_16(&maps.b_hi, b_hi, N, K, ldb, kSplitBN, bf16 != 0);
+  if (!e && b_lo) e = make_tmap_16(&maps.b_lo, b_lo, N, K, ldb, kSplitBN, bf16 != 0);
+  if (e) return e;
+  SplitArgs g;
+  g.k_tiles = (K + 63) / 64;
+  g.m_tiles = (M + 127) / 128;
+  g.n_tiles = (N + kSplitBN - 1) / kSplitBN;
+  g.a_row0 = 0;
+  g.has_alo = a_lo ? 1 : 0;
+  g.has_blo = b_lo ? 1 : 0;
+  g.drain = drain > 0 ? drain : g.k_tiles;
+  g.idesc = ptx::idesc_f16(128, kSplitBN, bf16 ? 1 : 0);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 148;
+  SplitStoreF32::Params ep{d, M, N, (long)N};
+  return launch_split<SplitStoreF32>(K_PREP, maps, g, sms, ep, status, reinterpret_cast<cudaStream_t>(stream));
+}
 
 extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stride,
                                  long b_term_stride, float* d, int M, int N, int K, int lda,

@@ -15,6 +15,7 @@
 //   rc_blk[b] [nchol][ldkb]   rot_chol of spin block b alone (UHF; RHF uses rc_fb)
 #pragma once
 #include "afq_gemm.cuh"
+#include "afq_gemm_split.cuh"
 #include "afq_kernels.cuh"
 
 namespace afq {
@@ -73,6 +74,8 @@ struct TcState {
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
   int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;
   int drain;                // K tiles per drained accumulation run (0: not drained)
+  int num_sms;              // persistent grid size
+  SplitMaps m_vhs_split;    // vhs operand planes for the persistent split GEMM
 };
 
 size_t tc_workspace_bytes(const afq_ctx_dev& c, int nw_chunk, int32_t mixed_config);

@@ -41,6 +41,60 @@ def test_gemm_matches_fp32(M, N, K, bn, dtype, nterms, drain):
     assert err <= 1e-5 * K * nterms * 16, err
 
 
+SPLIT_SHAPES = [(128, 256, 64), (300, 700, 600), (2048, 15360, 600), (130, 250, 136), (64, 16, 8),
+                (512, 1024, 2400)]
+
+
+@pytest.mark.parametrize("M,N,K", SPLIT_SHAPES)
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("terms", ["hi", "hi+alo", "all"])
+@pytest.mark.parametrize("drain", [0, 1, 2])
+def test_split_gemm_matches_fp32(M, N, K, dtype, terms, drain):
+    """Persistent split GEMM: A_hi B_hi^T (+ A_lo B_hi^T) (+ A_hi B_lo^T) against torch FP32."""
+    g = torch.Generator(device="cuda").manual_seed(M + 3 * N + K)
+    lda = (K + 7) // 8 * 8
+    ah = torch.randn(M, lda, device="cuda", generator=g).to(dtype)
+    al = (torch.randn(M, lda, device="cuda", generator=g) * 1e-3).to(dtype)
+    bh = torch.randn(N, lda, device="cuda", generator=g).to(dtype)
+    bl = (torch.randn(N, lda, device="cuda", generator=g) * 1e-3).to(dtype)
+    use_al, use_bl = terms in ("hi+alo", "all"), terms == "all"
+    d = torch.full((M, N), float("nan"), device="cuda", dtype=torch.float32)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("afq_test_gemm_split", ah.data_ptr(), al.data_ptr() if use_al else None, bh.data_ptr(),
+              bl.data_ptr() if use_bl else None, d.data_ptr(), M, N, K, lda, lda,
+              int(dtype == torch.bfloat16), drain, status.data_ptr(), stream_ptr())
+    A, B = ah[:, :K].float(), bh[:, :K].float()
+    ref = A @ B.T
+    if use_al:
+        ref = ref + al[:, :K].float() @ B.T
+    if use_bl:
+        ref = ref + A @ bl[:, :K].float().T
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    err = (d - ref).abs().max().item()
+    assert err <= 1e-5 * K * 16, err
+
+
+@pytest.mark.parametrize("drain", [0, 1, 2])
+def test_split_accumulation_bias(drain):
+    """Drained runs of the split GEMM remove the tensor core's truncation bias (K = 2400)."""
+    M, N, K = 256, 512, 2400
+    g = torch.Generator(device="cuda").manual_seed(6)
+    a = (torch.rand(M, K, device="cuda", generator=g) * 0.5 + 0.5).half()
+    b = (torch.rand(N, K, device="cuda", generator=g) * 0.5 + 0.5).half()
+    d = torch.empty(M, N, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.call("afq_test_gemm_split", a.data_ptr(), None, b.data_ptr(), None, d.data_ptr(), M, N, K, K, K,
+              0, drain, status.data_ptr(), stream_ptr())
+    ref = a.double() @ b.double().T
+    bias = ((d.double() - ref) / ref).mean().item()
+    assert status.item() == 0
+    if drain == 0:
+        assert bias < -5e-6
+    else:
+        assert abs(bias) < 1e-6, bias
+
+
 @pytest.mark.parametrize("drain", [0, 1, 2])
 def test_accumulation_bias(drain):
     """The tensor core truncates when it accumulates: positive sums over K = 2400 come out
