@@ -227,59 +227,72 @@ __global__ void __launch_bounds__(128, 1)
       break;
     }
     ptx::tc_fence_after();
-    float d[64];
+    // Per 16-column chunk of T_m (rows 2k, 2k+1 of 8 orbitals k): the accumulator regions
+    // are loaded together (one wait), summed in region order, scaled by 1/m, added to the
+    // Taylor sum and, unless this is the last term, written as the next B operand. Indices
+    // stay compile-time so nothing goes to local memory.
     const int nreg = KT + ((m <= td.split) ? 2 : 0);
-#pragma unroll
-    for (int j = 0; j < 64; ++j) d[j] = 0.f;
-    // one TMEM load wait per region: all column chunks of the region are in flight together
-    for (int rg = 0; rg < nreg; ++rg) {
-      float v[64];
-      const uint32_t src = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(64 * rg);
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16)
-        if (c0 < td.NT) ptx::tmem_ld16p(src + c0, v + c0);
-      ptx::tmem_ld_wait();
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16)
-        if (c0 < td.NT) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) d[c0 + j] += v[c0 + j];
-        }
-    }
     const float invm = 1.0f / (float)m;
+    const bool store_next = m + 1 < td.nterms;
+    const bool lo_next = (m + 1) <= td.split;
+    const int kt0 = p / 64, kc0 = p % 64;                      // K = p
+    const int kt1 = (td.nq + p) / 64, kc1 = (td.nq + p) % 64;  // K = nq + p
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
-    for (int r = 0; r < 64; ++r) {
-      d[r] = (r < o2) ? d[r] * invm : 0.f;
-      acc[r] += d[r];
-    }
-    if (m + 1 < td.nterms) {
-      const bool lo_next = (m + 1) <= td.split;
-      if (prow) {
-        const int kt0 = p / 64, kc0 = p % 64;                      // K = p
-        const int kt1 = (td.nq + p) / 64, kc1 = (td.nq + p) % 64;  // K = nq + p
-#pragma unroll 4
-        for (int k = 0; k < 32; ++k) {
-          if (k < td.o) {
-            const float tr = d[2 * k], ti = d[2 * k + 1];
-            uint16_t hr, lr, hi_, li, hni, lni;
-            split16(tr, bf, hr, lr);
-            split16(ti, bf, hi_, li);
-            split16(-ti, bf, hni, lni);
-            const uint32_t a0 = kt0 * BT + sw128(2 * k, kc0), a1 = kt1 * BT + sw128(2 * k, kc1);
-            const uint32_t b0 = kt0 * BT + sw128(2 * k + 1, kc0), b1 = kt1 * BT + sw128(2 * k + 1, kc1);
-            *reinterpret_cast<uint16_t*>(Bh + a0) = hr;
-            *reinterpret_cast<uint16_t*>(Bh + a1) = hni;
-            *reinterpret_cast<uint16_t*>(Bh + b0) = hi_;
-            *reinterpret_cast<uint16_t*>(Bh + b1) = hr;
-            if (lo_next) {
-              *reinterpret_cast<uint16_t*>(Bl + a0) = lr;
-              *reinterpret_cast<uint16_t*>(Bl + a1) = lni;
-              *reinterpret_cast<uint16_t*>(Bl + b0) = li;
-              *reinterpret_cast<uint16_t*>(Bl + b1) = lr;
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      if (c0 < td.NT) {
+        float dd[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) dd[j] = 0.f;
+#pragma unroll
+        for (int g0 = 0; g0 < 6; g0 += 3) {  // regions in two groups of three
+          if (g0 < nreg) {
+            float v[3][16];
+#pragma unroll
+            for (int rg = 0; rg < 3; ++rg)
+              if (g0 + rg < nreg) ptx::tmem_ld16p(lane_base + (uint32_t)(64 * (g0 + rg) + c0), v[rg]);
+            ptx::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+#pragma unroll
+              for (int rg = 0; rg < 3; ++rg)
+                if (g0 + rg < nreg) dd[j] += v[rg][j];
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          dd[j] = (c0 + j < o2) ? dd[j] * invm : 0.f;
+          acc[c0 + j] += dd[j];
+        }
+        if (store_next && prow) {
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk) {
+            const int k = c0 / 2 + kk;
+            if (k < td.o) {
+              const float tr = dd[2 * kk], ti = dd[2 * kk + 1];
+              uint16_t hr, lr, hi_, li, hni, lni;
+              split16(tr, bf, hr, lr);
+              split16(ti, bf, hi_, li);
+              split16(-ti, bf, hni, lni);
+              const uint32_t a0 = kt0 * BT + sw128(2 * k, kc0), a1 = kt1 * BT + sw128(2 * k, kc1);
+              const uint32_t b0 = kt0 * BT + sw128(2 * k + 1, kc0), b1 = kt1 * BT + sw128(2 * k + 1, kc1);
+              *reinterpret_cast<uint16_t*>(Bh + a0) = hr;
+              *reinterpret_cast<uint16_t*>(Bh + a1) = hni;
+              *reinterpret_cast<uint16_t*>(Bh + b0) = hi_;
+              *reinterpret_cast<uint16_t*>(Bh + b1) = hr;
+              if (lo_next) {
+                *reinterpret_cast<uint16_t*>(Bl + a0) = lr;
+                *reinterpret_cast<uint16_t*>(Bl + a1) = lni;
+                *reinterpret_cast<uint16_t*>(Bl + b0) = li;
+                *reinterpret_cast<uint16_t*>(Bl + b1) = lr;
+              }
             }
           }
         }
       }
+    }
+    if (store_next) {
       ptx::fence_proxy_async();
       ptx::tc_fence_before();
       __syncthreads();
