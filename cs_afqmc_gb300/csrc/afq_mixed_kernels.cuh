@@ -477,6 +477,117 @@ struct EpiVHSSplit {
 };
 
 // ======================================================================================
+// QR of the FP32 walker slabs (propagation.py:251-253 -> linalg_utils.py:51-65): the
+// LAPACK Householder factorisation (zgeqr2) and explicit Q (zung2r), one warp per slab with
+// the slab in shared memory (row stride k | 1: conflict-free column walks) and only
+// warp-level synchronisation. Column sums (the reflector applied to the trailing columns)
+// are owned by lane = column; the rank-1 updates by lane = row. The squared norm below
+// the diagonal is accumulated in FP64, as in the block-per-walker kernel.
+// ======================================================================================
+
+constexpr int kQrWarps = 4;
+
+__host__ __device__ constexpr int qr_ld(int k) { return k | 1; }
+
+__global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k, float2* __restrict__ wbase) {
+  extern __shared__ __align__(16) unsigned char qsm_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wlk = blockIdx.x * kQrWarps + warp;
+  if (wlk >= nw) return;  // warp-level work only: no block barrier below
+  const int ld = qr_ld(k);
+  float2* A = reinterpret_cast<float2*>(qsm_raw) + (size_t)warp * ((size_t)m * ld + 64);
+  float2* y = A + (size_t)m * ld;
+  float2* tau = y + 32;
+  float2* W = wbase + (size_t)wlk * m * k;
+  for (int i = lane; i < m * k; i += 32) {
+    const int r = i / k;
+    A[r * ld + (i - r * k)] = W[i];
+  }
+  __syncwarp();
+  // ---- factorisation
+  for (int j = 0; j < k; ++j) {
+    double xnd = 0.0;
+    for (int r = j + 1 + lane; r < m; r += 32) xnd += (double)cabs2(A[r * ld + j]);
+    xnd = warp_sum(xnd);
+    const float2 alpha = A[j * ld + j];
+    const float xn = (float)xnd;
+    float2 t, scl, beta;
+    if (xn == 0.f && alpha.y == 0.f) {
+      t = make_float2(0.f, 0.f);
+      beta = alpha;
+      scl = make_float2(1.f, 0.f);
+    } else {
+      const float nrm = sqrtf(alpha.x * alpha.x + alpha.y * alpha.y + xn);
+      const float b = (alpha.x >= 0.f) ? -nrm : nrm;
+      t = make_float2((b - alpha.x) / b, -alpha.y / b);
+      scl = cdiv(make_float2(1.f, 0.f), csub(alpha, make_float2(b, 0.f)));
+      beta = make_float2(b, 0.f);
+    }
+    __syncwarp();
+    for (int r = j + 1 + lane; r < m; r += 32) A[r * ld + j] = cmul(A[r * ld + j], scl);
+    if (lane == 0) {
+      A[j * ld + j] = make_float2(1.f, 0.f);
+      tau[j] = t;
+    }
+    __syncwarp();
+    const int col = j + 1 + lane;
+    if (col < k) {
+      float yx = 0.f, yy = 0.f;
+      for (int r = j; r < m; ++r) {
+        const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
+        yx += pr.x;
+        yy += pr.y;
+      }
+      y[col] = make_float2(yx, yy);
+    }
+    __syncwarp();
+    const float2 ct = make_float2(t.x, -t.y);
+    for (int r = j + lane; r < m; r += 32) {
+      const float2 v = A[r * ld + j];
+      for (int cc = j + 1; cc < k; ++cc)
+        A[r * ld + cc] = csub(A[r * ld + cc], cmul(ct, cmul(v, y[cc])));
+    }
+    __syncwarp();
+    if (lane == 0) A[j * ld + j] = beta;
+    __syncwarp();
+  }
+  // ---- form Q (zung2r): columns from last to first
+  for (int j = k - 1; j >= 0; --j) {
+    const float2 t = tau[j];
+    if (j < k - 1) {
+      if (lane == 0) A[j * ld + j] = make_float2(1.f, 0.f);
+      __syncwarp();
+      const int col = j + 1 + lane;
+      if (col < k) {
+        float yx = 0.f, yy = 0.f;
+        for (int r = j; r < m; ++r) {
+          const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
+          yx += pr.x;
+          yy += pr.y;
+        }
+        y[col] = make_float2(yx, yy);
+      }
+      __syncwarp();
+      for (int r = j + lane; r < m; r += 32) {
+        const float2 v = A[r * ld + j];
+        for (int cc = j + 1; cc < k; ++cc)
+          A[r * ld + cc] = csub(A[r * ld + cc], cmul(t, cmul(v, y[cc])));
+      }
+      __syncwarp();
+    }
+    const float2 mt = make_float2(-t.x, -t.y);
+    for (int r = j + 1 + lane; r < m; r += 32) A[r * ld + j] = cmul(mt, A[r * ld + j]);
+    if (lane == 0) A[j * ld + j] = make_float2(1.f - t.x, -t.y);
+    for (int r = lane; r < j; r += 32) A[r * ld + j] = make_float2(0.f, 0.f);
+    __syncwarp();
+  }
+  for (int i = lane; i < m * k; i += 32) {
+    const int r = i / k;
+    W[i] = A[r * ld + (i - r * k)];
+  }
+}
+
+// ======================================================================================
 // exp_h1 products: D[p][(w, 2k + c)] = ((E - I) X)[p][k].c for the walker (X = W) or the
 // Taylor sum (X = acc). First product: W1 = W + D into the Taylor B operand (hi/lo);
 // last product: W_new = acc + D back into the FP32 walker slab. propagation.py:73, 91.

@@ -1060,7 +1060,19 @@ int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
 }
 
 int tc_orthonormalize(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
-  return launch_qr<float>(c, wu, wd, st);
+  for (int s = 0; s < c.nslab; ++s) {
+    const int k = c.kslab[s];
+    if (k > 32) return launch_qr<float>(c, wu, wd, st);
+    const size_t smem = (size_t)kQrWarps * ((size_t)c.norb * qr_ld(k) + 64) * sizeof(float2);
+    cudaFuncSetAttribute(k_qr_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+      ProfScope _ps(K_QR, st);
+      k_qr_warp<<<(c.nw + kQrWarps - 1) / kQrWarps, 32 * kQrWarps, smem, st>>>(
+          c.nw, c.norb, k, static_cast<float2*>(s == 0 ? wu : wd));
+    }
+    TC_CHECK(launch_check("qr_warp"));
+  }
+  return 0;
 }
 
 }  // namespace afq
