@@ -65,6 +65,10 @@ _SIGS = {
                                                ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                _vp, _vp, _vp, _vp]),
     "afq_block_end": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp]),
+    "afq_field_block": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_int32, _vp, _vp,
+                                       _vp, _vp]),
+    "afq_cs_outlier_removal": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_double, _vp,
+                                              _vp]),
     "afq_calc_force_bias_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                    ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "afq_profile_enable": (ctypes.c_int, [ctypes.c_int]),

@@ -451,6 +451,41 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
                                    block_weight, state->scalars, energy, st);
 }
 
+int afq_field_block(afq_ctx* ctx, afq_walker_state* state, const double* fields, int32_t n_prop_steps,
+                    double* local_energies, double* block_energy, double* block_weight, void* stream) {
+  if (!ctx || !fields || !block_energy || !block_weight) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (n_prop_steps < 1) {
+    afq_set_error("n_prop_steps must be >= 1");
+    return -1;
+  }
+  CHECK(check_state(ctx, state));
+  cudaStream_t st = S(stream);
+  const afq_ctx_dev& d = ctx->dev;
+  const size_t step_elems = (size_t)d.nw * d.nchol;
+  for (int p = 0; p < n_prop_steps; ++p) CHECK(propagate_impl(ctx, state, fields + p * step_elems, st));
+  CHECK(qr_impl(ctx, state, st));
+  CHECK(green(ctx, state->walkers_up, state->walkers_dn, ctx->green, reinterpret_cast<double2*>(state->overlaps),
+              true, st));
+  CHECK(energy_from_green(ctx, ctx->ene, st));
+  CHECK(afq::launch_block_stats(d, ctx->ene, state->weights, state->scalars, block_energy, block_weight, st));
+  if (local_energies) CHECK(afq::launch_clamped_energies(d, ctx->ene, state->scalars, local_energies, st));
+  return 0;
+}
+
+int afq_cs_outlier_removal(double* weights1, double* weights2, const double* local_energies1,
+                           const double* local_energies2, int32_t n_walkers, double z_thresh, double* sums,
+                           void* stream) {
+  if (!weights1 || !weights2 || !local_energies1 || !local_energies2 || !sums || n_walkers < 1) {
+    afq_set_error("afq_cs_outlier_removal: bad arguments");
+    return -1;
+  }
+  return afq::launch_cs_outlier(weights1, weights2, local_energies1, local_energies2, n_walkers, z_thresh, sums,
+                                S(stream));
+}
+
 int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, const double* zeta,
                   double* block_weight, void* stream) {
   if (!ctx || !energy || !zeta || !block_weight) { afq_set_error("NULL argument"); return -1; }

@@ -47,6 +47,10 @@ int launch_sr(const afq_ctx_dev& c, const double* zeta, double* weights, double*
 int launch_block_stats(const afq_ctx_dev& c, const double2* energy, const double* weights,
                        double* scalars, double* be, double* bw, cudaStream_t st);
 int launch_phaseless_begin(double* scalars, cudaStream_t st);
+int launch_clamped_energies(const afq_ctx_dev& c, const double2* energy, const double* scalars,
+                            double* out, cudaStream_t st);
+int launch_cs_outlier(double* w1, double* w2, const double* e1, const double* e2, int nw,
+                      double z_thresh, double* sums, cudaStream_t st);
 int launch_phaseless_end(int nblk, double denom, const double* be, const double* bw,
                          double* scalars, double* energy, cudaStream_t st);
 int launch_driver_update(const afq_ctx_dev& c, const double* weights, const double* energy,

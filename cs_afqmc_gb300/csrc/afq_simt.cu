@@ -670,6 +670,64 @@ __global__ void k_block_stats(int nw, double dt, const double2* __restrict__ ene
   }
 }
 
+// en_samples (corr_sample.py:482-491): Re(E) clamped to e_estimate beyond sqrt(2/dt)
+__global__ void k_clamped_energies(int nw, double dt, const double2* __restrict__ energy,
+                                   const double* __restrict__ scalars, double* __restrict__ out) {
+  const double e_est = scalars[AFQ_S_E_ESTIMATE];
+  const double lim = sqrt(2.0 / dt);
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) {
+    const double e = energy[w].x;
+    out[w] = (fabs(e - e_est) > lim) ? e_est : e;
+  }
+}
+
+// corr_otler_rm (corr_sample.py:557-594) + the weighted sums of cs_step (673-694), one CTA.
+// mean and population std in two passes, as jnp.mean / jnp.std; the larger z-score selected
+// with jnp.where(z1 > z2, z1, z2) semantics (a NaN z1 selects z2).
+__global__ void k_cs_outlier(int nw, double z_thresh, double* __restrict__ w1, double* __restrict__ w2,
+                             const double* __restrict__ e1, const double* __restrict__ e2,
+                             double* __restrict__ sums) {
+  __shared__ double red[32];
+  double s1 = 0, s2 = 0;
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) {
+    s1 += w1[i];
+    s2 += w2[i];
+  }
+  const double m1 = block_sum(s1, red) / nw, m2 = block_sum(s2, red) / nw;
+  double v1 = 0, v2 = 0;
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) {
+    v1 += (w1[i] - m1) * (w1[i] - m1);
+    v2 += (w2[i] - m2) * (w2[i] - m2);
+  }
+  const double sd1 = sqrt(block_sum(v1, red) / nw), sd2 = sqrt(block_sum(v2, red) / nw);
+  double a1 = 0, b1 = 0, a2 = 0, b2 = 0;
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) {
+    const double z1 = fabs(w1[i] - m1) / sd1, z2 = fabs(w2[i] - m2) / sd2;
+    const double z = (z1 > z2) ? z1 : z2;
+    double x1 = w1[i], x2 = w2[i];
+    if (z > z_thresh) {
+      x1 = 0.0;
+      x2 = 0.0;
+    }
+    w1[i] = x1;
+    w2[i] = x2;
+    a1 += e1[i] * x1;
+    b1 += x1;
+    a2 += e2[i] * x2;
+    b2 += x2;
+  }
+  a1 = block_sum(a1, red);
+  b1 = block_sum(b1, red);
+  a2 = block_sum(a2, red);
+  b2 = block_sum(b2, red);
+  if (threadIdx.x == 0) {
+    sums[0] = a1;
+    sums[1] = b1;
+    sums[2] = a2;
+    sums[3] = b2;
+  }
+}
+
 __global__ void k_phaseless_begin(double* scalars) {
   scalars[AFQ_S_N_KILLED] = 0.0;
   scalars[AFQ_S_POP_CONTROL_SHIFT] = scalars[AFQ_S_E_ESTIMATE];
@@ -895,6 +953,24 @@ int launch_block_stats(const afq_ctx_dev& c, const double2* energy, const double
     k_block_stats<<<1, 1024, 0, st>>>(c.nw, c.dt, energy, weights, scalars, be, bw);
   }
   return launch_err("block_stats");
+}
+
+int launch_clamped_energies(const afq_ctx_dev& c, const double2* energy, const double* scalars,
+                            double* out, cudaStream_t st) {
+  {
+    ProfScope _ps(K_STATS, st);
+    k_clamped_energies<<<(c.nw + 255) / 256, 256, 0, st>>>(c.nw, c.dt, energy, scalars, out);
+  }
+  return launch_err("clamped_energies");
+}
+
+int launch_cs_outlier(double* w1, double* w2, const double* e1, const double* e2, int nw,
+                      double z_thresh, double* sums, cudaStream_t st) {
+  {
+    ProfScope _ps(K_STATS, st);
+    k_cs_outlier<<<1, 1024, 0, st>>>(nw, z_thresh, w1, w2, e1, e2, sums);
+  }
+  return launch_err("cs_outlier");
 }
 
 int launch_phaseless_begin(double* scalars, cudaStream_t st) {

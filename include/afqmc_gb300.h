@@ -184,6 +184,29 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
 int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, const double* zeta,
                   double* block_weight, void* stream);
 
+/* ---- correlated sampling (ad_afqmc/corr_sample/corr_sample.py) ---------------------- */
+
+/* One correlated-sampling block of one system with the given fields (float64
+ * [n_prop_steps, nw, nchol]): n_prop_steps phaseless steps, killed-walker count, QR,
+ * overlaps, local energies clamped to e_estimate beyond sqrt(2/dt), block energy and weight,
+ * pop_control_ene_shift <- 0.9 shift + 0.1 block energy. No stochastic reconfiguration.
+ * local_energies (float64 [nw], may be NULL), block_energy and block_weight (one double each)
+ * are device pointers. Replaces corr_sample.field_block_scan (corr_sample.py:514-555) with
+ * the en_samples clamp (482-491). */
+int afq_field_block(afq_ctx* ctx, afq_walker_state* state, const double* fields,
+                    int32_t n_prop_steps, double* local_energies, double* block_energy,
+                    double* block_weight, void* stream);
+
+/* Weight-outlier removal of a correlated pair, then the step sums of cs_steps_scan:
+ * z_i = |w_i - mean(w)| / std(w) (population std) for each system, and every walker whose
+ * larger z exceeds z_thresh gets weight 0 in both systems; sums[0..3] = (sum e1 w1,
+ * sum w1, sum e2 w2, sum w2) over the updated weights. Device pointers; weights updated in
+ * place. Replaces corr_sample.corr_otler_rm (corr_sample.py:557-594) and the sums of
+ * cs_steps_scan.cs_step (corr_sample.py:673-694). */
+int afq_cs_outlier_removal(double* weights1, double* weights2, const double* local_energies1,
+                           const double* local_energies2, int32_t n_walkers, double z_thresh,
+                           double* sums, void* stream);
+
 /* Standard normal draws (Philox4x32-10 + Box-Muller), float64 [n], counter-based:
  * element i depends only on (seed, offset + i). Stands in for jax.random.normal in
  * sampling.py:61-69. */

@@ -466,6 +466,48 @@ def run_blocks(
     return np.array(energies), np.array(weights), prop_data
 
 
+# ---------------------------------------------------------------------------------------
+# correlated sampling (ad_afqmc/corr_sample/corr_sample.py)
+# ---------------------------------------------------------------------------------------
+
+def en_samples(prop, trial, ham_data, prop_data, mo) -> np.ndarray:
+    """Real local energies clamped to e_estimate beyond sqrt(2/dt) (corr_sample.py:482-491)."""
+    e = np.real(trial.energy(prop_data["walkers"], ham_data, mo))
+    return np.where(np.abs(e - prop_data["e_estimate"]) > np.sqrt(2.0 / prop.dt), prop_data["e_estimate"], e)
+
+
+def corr_otler_rm(w1: np.ndarray, w2: np.ndarray, z_thresh: float = 5.0):
+    """Weight-outlier removal of a correlated pair (corr_sample.py:557-594): population-std
+    z-scores of each system, the larger of the two per walker (jnp.where semantics), weights
+    of walkers above z_thresh set to 0 in both systems."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        z1 = np.abs(w1 - np.mean(w1)) / np.std(w1)
+        z2 = np.abs(w2 - np.mean(w2)) / np.std(w2)
+    z = np.where(z1 > z2, z1, z2)
+    return np.where(z > z_thresh, 0.0, w1), np.where(z > z_thresh, 0.0, w2)
+
+
+def cs_steps_scan(sampler: "Sampler", sys1: tuple, sys2: tuple, fields: np.ndarray):
+    """Correlated blocks of two systems on shared fields (corr_sample.py:596-694).
+    sys = (prop, trial, ham_data, prop_data, mo); fields [steps, n_prop_steps, nw, G].
+    Each step: field_block_scan of both systems (Sampler.block_scan: n_prop_steps steps, QR,
+    overlaps, block energy, pop-control update, no SR), outlier removal, then the sums
+    (sum E w, sum w) of both. Returns (prop_data1, prop_data2, loc_en1, loc_w1, loc_en2, loc_w2)."""
+    p1, t1, h1, pd1, mo1 = sys1
+    p2, t2, h2, pd2, mo2 = sys2
+    out = []
+    for f in fields:
+        pd1, _, _ = sampler.block_scan(p1, t1, h1, pd1, mo1, f)
+        pd2, _, _ = sampler.block_scan(p2, t2, h2, pd2, mo2, f)
+        pd1["weights"], pd2["weights"] = corr_otler_rm(pd1["weights"], pd2["weights"])
+        e1 = en_samples(p1, t1, h1, pd1, mo1)
+        e2 = en_samples(p2, t2, h2, pd2, mo2)
+        out.append((np.sum(e1 * pd1["weights"]), np.sum(pd1["weights"]),
+                    np.sum(e2 * pd2["weights"]), np.sum(pd2["weights"])))
+    out = np.array(out)
+    return pd1, pd2, out[:, 0], out[:, 1], out[:, 2], out[:, 3]
+
+
 def blocking_analysis(weights: np.ndarray, energies: np.ndarray, neql: int = 0):
     """Weighted mean and plateau error of blocked samples (stat_utils.py:8-52), computed in
     float64 throughout (the reference's blocked arrays are float32)."""
