@@ -495,6 +495,8 @@ def cs_steps_scan(sampler: "Sampler", sys1: tuple, sys2: tuple, fields: np.ndarr
     (sum E w, sum w) of both. Returns (prop_data1, prop_data2, loc_en1, loc_w1, loc_en2, loc_w2)."""
     p1, t1, h1, pd1, mo1 = sys1
     p2, t2, h2, pd2, mo2 = sys2
+    for pd in (pd1, pd2):  # corr_sample.init_prop sets it (corr_sample.py:472)
+        pd.setdefault("n_killed_walkers", 0)
     out = []
     for f in fields:
         pd1, _, _ = sampler.block_scan(p1, t1, h1, pd1, mo1, f)
