@@ -43,7 +43,7 @@ L2_BYTES = 129e6
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
@@ -58,6 +58,9 @@ def parse():
                     help="run only the mixed-vs-FP64 energy comparison and print its line")
     ap.add_argument("--energy-control", action="store_true",
                     help="add an FP64 run from perturbed walkers to the energy comparison")
+    ap.add_argument("--cs-derivative", action="store_true",
+                    help="correlated-sampling derivative dE/dlambda on the UHF workload")
+    ap.add_argument("--cs-blocks", type=int, default=10)
     ap.add_argument("--energy-sync", action="store_true",
                     help="with --energy-only: per-block comparison from the FP64 run's states")
     return ap.parse_args()
@@ -87,7 +90,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200", "-i", str(self.idx)],
+                 "-lms", "50", "-i", str(self.idx)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -571,9 +574,82 @@ def run_reference(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def cs_derivative(args) -> dict:
+    """Differentiation pattern by correlated sampling: dE/dlambda of h1 + lambda D from two
+    systems at lambda = +-1e-4 on identical fields (cs_steps_scan), for the UHF workload
+    (norb 60, 10+8 electrons, 300 Cholesky vectors, 512 walkers, 50 steps per block).
+    D is a seeded symmetric N(0, 0.05) matrix. Run in the mixed and the FP64 precision on
+    the same draws; reports the per-block derivative statistics and walker-steps/s."""
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import corr_sample, hamiltonian, propagation, sampling, synthetic, wavefunctions
+    from cs_afqmc_gb300.propagation import RngKey
+
+    name = "uhf_norb60_nocc10x8_nchol300_nw512"
+    w = dict(synthetic.WORKLOADS[name])
+    norb, lam = w["norb"], 1e-4
+    rng = np.random.default_rng(2024)
+    d = rng.normal(0.0, 0.05, (norb, norb))
+    d = np.triu(d) + np.triu(d, 1).T
+    steps, n_prop = args.cs_blocks, 50
+    res = {"workload": name, "lambda": lam, "blocks": steps, "steps_per_block": n_prop,
+           "fields": "identical draws for both systems and both precisions (Philox key of system 1)"}
+    for prec in ("mixed", "fp64"):
+        systems = []
+        for sgn in (1.0, -1.0):
+            s = synthetic.molecular(norb, w["nelec"], w["nchol"], seed=1, kind=w["kind"])
+            s.h1 = s.h1 + sgn * lam * d
+            ham = hamiltonian.hamiltonian(norb)
+            trial = wavefunctions.uhf(norb, w["nelec"])
+            wave = {"mo_coeff": s.mo_coeff, "rdm1": s.rdm1}
+            hd = {"h0": s.h0, "h1": s.h1, "chol": s.chol, "ene0": 0.0}
+            hd = ham.build_measurement_intermediates(hd, trial, wave)
+            prop = propagation.propagator_unrestricted(dt=w["dt"], n_walkers=w["n_walkers"], n_exp_terms=6,
+                                                       n_batch=1, precision=prec)
+            hd = ham.build_propagation_intermediates(hd, prop, trial, wave)
+            pd = prop.init_prop_data(trial, wave, hd, init_walkers=s.init_walkers(w["n_walkers"], False))
+            pd["key"] = RngKey(777)
+            systems.append((pd, hd, prop, trial, wave))
+        samp = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=1, n_sr_blocks=1)
+        (p1, h1, pr1, t1, w1), (p2, h2, pr2, t2, w2) = systems
+        # block 0 warms up both contexts; the timed blocks follow
+        (p1, p2), _ = corr_sample.cs_steps_scan(1, p1, h1, pr1, t1, w1, p2, h2, pr2, t2, w2, samp)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1e = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        (p1, p2), (e1, wt1, e2, wt2) = corr_sample.cs_steps_scan(steps, p1, h1, pr1, t1, w1,
+                                                                 p2, h2, pr2, t2, w2, samp)
+        t1e.record()
+        torch.cuda.synchronize()
+        sec = t0.elapsed_time(t1e) / 1e3
+        e1, wt1, e2, wt2 = (x.cpu().numpy() for x in (e1, wt1, e2, wt2))
+        deriv = (e1 / wt1 - e2 / wt2) / (2 * lam)
+        res[prec] = {
+            "dE_dlambda": float((e1.sum() / wt1.sum() - e2.sum() / wt2.sum()) / (2 * lam)),
+            "per_block_mean": float(deriv.mean()),
+            "per_block_stderr": float(deriv.std(ddof=1) / np.sqrt(len(deriv))) if len(deriv) > 1 else None,
+            "energy_plus": float(e1.sum() / wt1.sum()),
+            "walker_steps_per_s": 2 * steps * n_prop * w["n_walkers"] / sec,
+            "per_block": [round(float(x), 6) for x in deriv],
+        }
+        del systems, p1, p2, h1, h2, pr1, pr2
+        torch.cuda.empty_cache()
+    res["mixed_minus_fp64"] = res["mixed"]["dE_dlambda"] - res["fp64"]["dE_dlambda"]
+    return res
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.cs_derivative:
+        import torch
+        torch.cuda.set_device(local)
+        if rank == 0:
+            print(json.dumps({"metric": "dE/dlambda by correlated sampling, h1 + lambda D",
+                              "cs_derivative": cs_derivative(args)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world, local)
     else:
