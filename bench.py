@@ -58,6 +58,12 @@ def parse():
                     help="run only the mixed-vs-FP64 energy comparison and print its line")
     ap.add_argument("--energy-control", action="store_true",
                     help="add an FP64 run from perturbed walkers to the energy comparison")
+    ap.add_argument("--serving", action="store_true",
+                    help="serving pattern: Poisson stream of jobs through the server")
+    ap.add_argument("--serving-rate", type=float, default=20.0)
+    ap.add_argument("--serving-duration", type=float, default=10.0)
+    ap.add_argument("--serving-norb-max", type=int, default=128)
+    ap.add_argument("--serving-slots", type=int, default=16)
     ap.add_argument("--cs-derivative", action="store_true",
                     help="correlated-sampling derivative dE/dlambda on the UHF workload")
     ap.add_argument("--cs-blocks", type=int, default=10)
@@ -640,9 +646,47 @@ def cs_derivative(args) -> dict:
     return res
 
 
+def serving_bench(args) -> dict:
+    """Serving pattern: a Poisson stream of independent jobs (rate jobs/s for `duration` s,
+    norb uniform in [20, norb_max], nocc = norb // 6, nchol = 5 norb, walkers in
+    {64, 256, 1024}, 100 steps each) through the continuous-batching server. Payloads are
+    generated before the clock; latency = completion - arrival, including upload, set-up,
+    propagation and the result copy."""
+    import numpy as np
+
+    from cs_afqmc_gb300 import serving
+
+    # warm-up: library load, first-call set-up of torch and the contexts
+    warm = serving.JobSpec(job_id=-1, norb=24, nocc=4, nchol=120, n_walkers=64, n_steps=20, seed=1)
+    serving.AfqmcServer().run([(0.0, warm, serving.job_input(warm))])
+    reqs = serving.poisson_requests(args.serving_rate, args.serving_duration, seed=11,
+                                    norb_range=(20, args.serving_norb_max))
+    srv = serving.AfqmcServer(max_active=args.serving_slots)
+    res, wall = srv.run(reqs)
+    lat = np.array([r.latency for r in res])
+    ws = sum(r.spec.n_walkers * r.spec.n_steps for r in res)
+    return {
+        "jobs": len(res), "rate_jobs_per_s": args.serving_rate, "duration_s": args.serving_duration,
+        "norb_range": [20, args.serving_norb_max], "walkers": [64, 256, 1024], "steps": 100,
+        "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+        "latency_mean_s": float(lat.mean()), "latency_max_s": float(lat.max()),
+        "queue_wait_mean_s": float(np.mean([r.t_admitted - r.t_arrival for r in res])),
+        "walker_steps_per_s": ws / wall, "wall_s": wall,
+        "graph_fraction": float(np.mean([r.graph for r in res])),
+        "max_active": args.serving_slots,
+    }
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.serving:
+        import torch
+        torch.cuda.set_device(local)
+        if rank == 0:
+            print(json.dumps({"metric": "serving p50/p99 job latency and aggregate walker-steps/s",
+                              "serving": serving_bench(args)}), flush=True)
+        return
     if args.cs_derivative:
         import torch
         torch.cuda.set_device(local)
