@@ -177,7 +177,11 @@ def build_workload(name: str, precision: str, n_batch: int, mixed_config: int, s
     from cs_afqmc_gb300.propagation import RngKey
 
     w = dict(synthetic.WORKLOADS[name])
-    s = synthetic.molecular(w["norb"], w["nelec"], w["nchol"], seed=1, kind=w["kind"])
+    if w["kind"] == "hubbard":  # real trial: the mixed path takes real trials
+        s = synthetic.hubbard_2d(w["lx"], w["ly"], 1.0, w["u"], w["nelec"], real_trial=True)
+        w["kind"] = "rhf"
+    else:
+        s = synthetic.molecular(w["norb"], w["nelec"], w["nchol"], seed=1, kind=w["kind"])
     ham = hamiltonian.hamiltonian(w["norb"])
     trial = (wavefunctions.rhf if w["kind"] == "rhf" else wavefunctions.uhf)(w["norb"], w["nelec"])
     wave = {"mo_coeff": s.mo_coeff, "rdm1": s.rdm1}
@@ -372,7 +376,7 @@ def run_ours(args, rank, world, local):
     cpu_procs = args.cpu_procs or max(1, (os.cpu_count() or 2) - 2)
     if want_cpu:
         from oracle.cpu_bench import CpuPool
-        cpu_pool = CpuPool(cpu_procs, w["norb"], w["nelec"][0], w["nchol"], 16, w["dt"])
+        cpu_pool = CpuPool(cpu_procs, w["norb"], w["nelec"][0], w["nchol"], 16, w["dt"], kind=w["kind"])
 
     w, s, ham, trial, wave, hd, prop, pd, samp = build_workload(
         args.workload, args.precision, args.n_batch, args.mixed_config, seed=1000 + rank)
@@ -550,7 +554,7 @@ def run_reference(args, rank, world, local):
     w = dict(synthetic.WORKLOADS[args.workload])
     procs = args.cpu_procs or (os.cpu_count() or 1)
     nw_per = max(1, min(16, w["n_walkers"] // procs))
-    pool = CpuPool(procs, w["norb"], w["nelec"][0], w["nchol"], nw_per, w["dt"])
+    pool = CpuPool(procs, w["norb"], w["nelec"][0], w["nchol"], nw_per, w["dt"], kind=w["kind"])
     n_steps, n_meas = 5, 1
     try:
         for _ in range(args.warmup):

@@ -107,9 +107,15 @@ def molecular(norb: int, nelec: Tuple[int, int], nchol: int, seed: int = 0,
 
 def hubbard_2d(lx: int = 8, ly: int = 8, t: float = 1.0, u: float = 4.0,
                nelec: Tuple[int, int] = (28, 28),
-               twist: Tuple[float, float] = (0.01, 0.02)) -> SyntheticSystem:
+               twist: Tuple[float, float] = (0.01, 0.02), real_trial: bool = False) -> SyntheticSystem:
     """Periodic lx x ly Hubbard lattice; L_i = sqrt(U) n_i; complex twisted plane-wave
-    RHF trial (lowest nelec[0] of the twisted dispersion)."""
+    RHF trial (lowest nelec[0] of the twisted dispersion).
+
+    real_trial=True: the trial is instead the lowest nelec[0] eigenvectors of the real
+    hopping matrix plus a tiny site-dependent shift (1e-3 * linspace(-1, 1) on the diagonal)
+    that splits the degenerate shell deterministically. The twist exists to make the
+    free-electron determinant closed-shell; the real version does that with the shift, for
+    paths that take real trials only."""
     n = lx * ly
     h1 = np.zeros((n, n))
     for x in range(lx):
@@ -122,6 +128,12 @@ def hubbard_2d(lx: int = 8, ly: int = 8, t: float = 1.0, u: float = 4.0,
     chol = np.zeros((n, n, n))
     for i in range(n):
         chol[i, i, i] = np.sqrt(u)
+    if real_trial:
+        evals, evecs = np.linalg.eigh(h1 + np.diag(1e-3 * np.linspace(-1.0, 1.0, n)))
+        mo = evecs[:, : nelec[0]].copy()
+        rho = mo @ mo.T
+        return SyntheticSystem(n, tuple(nelec), n, 0.0, np.stack([h1, h1]),
+                               chol.reshape(n, n * n), mo, np.stack([rho, rho]), "rhf")
     ks = []
     for mx in range(lx):
         for my in range(ly):
@@ -153,6 +165,9 @@ WORKLOADS = {
     # n_batch=1, a quarter of the device memory (profiling case)
     "rhf_norb120_nocc20_nchol600_nw256": dict(norb=120, nelec=(20, 20), nchol=600,
                                               n_walkers=256, dt=0.005, kind="rhf"),
+    # 8 x 8 periodic Hubbard lattice, U = 4, 28 + 28 electrons, diagonal Cholesky vectors
+    "hubbard_8x8_u4_n28_nw2048": dict(norb=64, nelec=(28, 28), nchol=64, n_walkers=2048,
+                                      dt=0.01, kind="hubbard", lx=8, ly=8, u=4.0),
     # differentiation pattern (UHF)
     "uhf_norb60_nocc10x8_nchol300_nw512": dict(norb=60, nelec=(10, 8), nchol=300,
                                                n_walkers=512, dt=0.005, kind="uhf"),

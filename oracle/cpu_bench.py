@@ -24,7 +24,12 @@ def _init(norb, nocc, nchol, nw, dt, kind, seed):
     from cs_afqmc_gb300 import synthetic
     from oracle import afqmc_oracle as O
 
-    s = synthetic.molecular(norb, (nocc, nocc), nchol, seed=1, kind=kind)
+    if kind == "hubbard":  # the square periodic lattice with norb sites, real trial
+        side = int(round(norb ** 0.5))
+        s = synthetic.hubbard_2d(side, side, 1.0, 4.0, (nocc, nocc), real_trial=True)
+        kind = "rhf"
+    else:
+        s = synthetic.molecular(norb, (nocc, nocc), nchol, seed=1, kind=kind)
     tr = O.Trial(kind, norb, (nocc, nocc))
     ham = {"h0": 0.0, "h1": s.h1.copy(), "chol": s.chol.copy()}
     ham = tr.build_measurement_intermediates(ham, s.mo_coeff)
