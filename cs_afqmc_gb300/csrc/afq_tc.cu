@@ -115,23 +115,31 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
 // first exp_h1 product), T_m = V T_{m-1} / m on the tensor cores with V = [Vr | Vi] held in
 // shared memory, acc = sum_m T_m in FP32 registers. The first `split` products use
 // V_hi T_hi + V_hi T_lo + V_lo T_hi. Writes acc as the B operand of the last exp_h1 product.
-// One CTA (4 warps, thread p <-> orbital row p <-> TMEM lane p) per walker. Each K tile of
-// V_hi T_hi, and each correction product, accumulates in its own 64-column TMEM region (the
-// tensor core truncates when it accumulates), summed with round-to-nearest in registers.
+//
+// Persistent: one CTA per SM loops over the walkers of the chunk. 8 warps: warp w reads
+// TMEM lanes 32*(w%4).. (thread <-> orbital row p) and owns the output columns of half
+// (w/4) of the walker's orbitals, so the per-product epilogue (TMEM readout, Taylor sum,
+// next B operand) is split over twice the threads. As soon as the last product's MMAs of a
+// walker have completed, the TMA loads of the next walker's V and T_0 are issued, so they
+// overlap that walker's last epilogue and its output.
+// Each K tile of V_hi T_hi, and each correction product, accumulates in its own 64-column
+// TMEM region (the tensor core truncates when it accumulates), summed with round-to-nearest.
 // ======================================================================================
 
 struct TaylorDev {
-  int n, o, nq, NT, R, nk, nterms, split, bf16, w0;
+  int n, o, nq, NT, R, nk, nterms, split, bf16, w0, nwc;
   uint16_t* acc_hi;
   uint16_t* acc_lo;
 };
+
+constexpr int kTaylorThreads = 256;
 
 static inline size_t taylor_smem(int nq, int NT, bool lo) {
   const int KT = 2 * nq / 64;
   return 1024 + (size_t)KT * 128 * 128 * (lo ? 2 : 1) + (size_t)KT * NT * 128 * 2 + 64;
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kTaylorThreads, 1)
     k_taylor_tc(const __grid_constant__ CUtensorMap mv_hi, const __grid_constant__ CUtensorMap mv_lo,
                 const __grid_constant__ CUtensorMap mt_hi, const __grid_constant__ CUtensorMap mt_lo,
                 const TaylorDev td, int* status) {
@@ -150,10 +158,11 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* ld_bar = bars;
   uint64_t* mma_bar = bars + 1;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int wl = blockIdx.x, wg = td.w0 + wl;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int q = warp & 3, half = warp >> 2;
   const uint32_t tcols = gemm_tmem_cols((KT + 2) * 64);
   const bool bf = td.bf16 != 0;
+  const uint32_t ld_bytes = KT * VT * (has_lo ? 2 : 1) + KT * BT * 2;
   bool ok = true;
 
   if (tid == 0) {
@@ -170,147 +179,156 @@ __global__ void __launch_bounds__(128, 1)
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
 
-  if (tid == 0) {
-    const uint32_t bytes = KT * VT * (has_lo ? 2 : 1) + KT * BT * 2;
-    ptx::mbar_expect_tx(ld_bar, bytes);
+  auto issue_loads = [&](int wl) {
+    const int wg = td.w0 + wl;
+    ptx::mbar_expect_tx(ld_bar, ld_bytes);
     for (int kt = 0; kt < KT; ++kt) {
       ptx::tma_load_2d(Vh + kt * VT, &mv_hi, ld_bar, kt * 64, wl * 128);
       if (has_lo) ptx::tma_load_2d(Vl + kt * VT, &mv_lo, ld_bar, kt * 64, wl * 128);
       ptx::tma_load_2d(Bh + kt * BT, &mt_hi, ld_bar, kt * 64, wg * td.NT);
       ptx::tma_load_2d(Bl + kt * BT, &mt_lo, ld_bar, kt * 64, wg * td.NT);
     }
-  }
-  if (!ptx::mbar_wait(ld_bar, 0)) ok = false;
+  };
 
-  const int p = tid;
+  const int p = q * 32 + lane;
   const bool prow = p < td.n;
   const int o2 = 2 * td.o;
-  float acc[64];
-  {
-    const int kt = p / 64, kc = p % 64;
-#pragma unroll
-    for (int r = 0; r < 64; ++r) {
-      if (r < o2 && prow) {
-        const uint32_t off = kt * BT + sw128(r, kc);
-        acc[r] = h2f(*reinterpret_cast<const uint16_t*>(Bh + off), bf) +
-                 h2f(*reinterpret_cast<const uint16_t*>(Bl + off), bf);
-      } else {
-        acc[r] = 0.f;
-      }
-    }
-  }
+  const int c_begin = half * 32;  // this thread's 32 columns (orbitals k = c_begin/2 ..)
+  const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
   const uint32_t idesc = ptx::idesc_f16(128, td.NT, bf ? 1 : 0);
   const uint32_t sVh = ptx::smem_u32(Vh), sVl = ptx::smem_u32(Vl), sBh = ptx::smem_u32(Bh),
                  sBl = ptx::smem_u32(Bl);
-  for (int m = 1; m < td.nterms; ++m) {
-    if (tid == 0 && ok) {
-      ptx::tc_fence_after();
-      const int ngroups = (m <= td.split) ? 3 : 1;
-      for (int gi = 0; gi < ngroups; ++gi) {
-        const uint32_t va = gi == 2 ? sVl : sVh;
-        const uint32_t ba = gi == 1 ? sBl : sBh;
-        for (int kt = 0; kt < KT; ++kt) {
-          // region: one per K tile for the main product, one per correction product
-          const uint32_t dreg = tmem + (uint32_t)(64 * (gi == 0 ? kt : KT + gi - 1));
+  const int kt0 = p / 64, kc0 = p % 64;                      // K = p
+  const int kt1 = (td.nq + p) / 64, kc1 = (td.nq + p) % 64;  // K = nq + p
+
+  if (tid == 0 && blockIdx.x < td.nwc) issue_loads(blockIdx.x);
+  int iter = 0, prod = 0;
+  for (int wl = blockIdx.x; wl < td.nwc && ok; wl += gridDim.x, ++iter) {
+    if (!ptx::mbar_wait(ld_bar, iter & 1)) ok = false;
+    float acc[32];
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            ptx::mma_f16(dreg, ptx::desc_kmajor_sw128(va + kt * VT + kk * 32),
-                         ptx::desc_kmajor_sw128(ba + kt * BT + kk * 32), idesc,
-                         (kk > 0 || (gi > 0 && kt > 0)) ? 1u : 0u);
-        }
+    for (int j = 0; j < 32; ++j) {
+      const int r = c_begin + j;
+      if (r < o2 && prow) {
+        const uint32_t off = kt0 * BT + sw128(r, kc0);
+        acc[j] = h2f(*reinterpret_cast<const uint16_t*>(Bh + off), bf) +
+                 h2f(*reinterpret_cast<const uint16_t*>(Bl + off), bf);
+      } else {
+        acc[j] = 0.f;
       }
-      ptx::mma_commit(mma_bar);
     }
-    if (ok && !ptx::mbar_wait(mma_bar, (m - 1) & 1)) ok = false;
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
+    if (td.nterms <= 1) {  // no products: T_0 alone; the operands are free after the read above
+      __syncthreads();
+      if (tid == 0 && wl + gridDim.x < td.nwc) issue_loads(wl + gridDim.x);
     }
-    ptx::tc_fence_after();
-    // Per 16-column chunk of T_m (rows 2k, 2k+1 of 8 orbitals k): the accumulator regions
-    // are loaded together (one wait), summed in region order, scaled by 1/m, added to the
-    // Taylor sum and, unless this is the last term, written as the next B operand. Indices
-    // stay compile-time so nothing goes to local memory.
-    const int nreg = KT + ((m <= td.split) ? 2 : 0);
-    const float invm = 1.0f / (float)m;
-    const bool store_next = m + 1 < td.nterms;
-    const bool lo_next = (m + 1) <= td.split;
-    const int kt0 = p / 64, kc0 = p % 64;                      // K = p
-    const int kt1 = (td.nq + p) / 64, kc1 = (td.nq + p) % 64;  // K = nq + p
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int m = 1; m < td.nterms; ++m, ++prod) {
+      // every thread has read the B operand (acc init or previous product) before the MMAs
+      ptx::tc_fence_before();
+      __syncthreads();
+      if (tid == 0 && ok) {
+        ptx::tc_fence_after();
+        const int ngroups = (m <= td.split) ? 3 : 1;
+        for (int gi = 0; gi < ngroups; ++gi) {
+          const uint32_t va = gi == 2 ? sVl : sVh;
+          const uint32_t ba = gi == 1 ? sBl : sBh;
+          for (int kt = 0; kt < KT; ++kt) {
+            // region: one per K tile for the main product, one per correction product
+            const uint32_t dreg = tmem + (uint32_t)(64 * (gi == 0 ? kt : KT + gi - 1));
 #pragma unroll
-    for (int c0 = 0; c0 < 64; c0 += 16) {
-      if (c0 < td.NT) {
-        float dd[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) dd[j] = 0.f;
-#pragma unroll
-        for (int g0 = 0; g0 < 6; g0 += 3) {  // regions in two groups of three
-          if (g0 < nreg) {
-            float v[3][16];
-#pragma unroll
-            for (int rg = 0; rg < 3; ++rg)
-              if (g0 + rg < nreg) ptx::tmem_ld16p(lane_base + (uint32_t)(64 * (g0 + rg) + c0), v[rg]);
-            ptx::tmem_ld_wait();
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-#pragma unroll
-              for (int rg = 0; rg < 3; ++rg)
-                if (g0 + rg < nreg) dd[j] += v[rg][j];
-            }
+            for (int kk = 0; kk < 4; ++kk)
+              ptx::mma_f16(dreg, ptx::desc_kmajor_sw128(va + kt * VT + kk * 32),
+                           ptx::desc_kmajor_sw128(ba + kt * BT + kk * 32), idesc,
+                           (kk > 0 || (gi > 0 && kt > 0)) ? 1u : 0u);
           }
         }
+        ptx::mma_commit(mma_bar);
+      }
+      if (ok && !ptx::mbar_wait(mma_bar, prod & 1)) ok = false;
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      ptx::tc_fence_after();
+      const bool last = m + 1 == td.nterms;
+      // the smem operands are free once the last product's MMAs are done: fetch the next walker
+      if (last && tid == 0 && wl + gridDim.x < td.nwc) issue_loads(wl + gridDim.x);
+      const int nreg = KT + ((m <= td.split) ? 2 : 0);
+      const float invm = 1.0f / (float)m;
+      const bool lo_next = (m + 1) <= td.split;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          dd[j] = (c0 + j < o2) ? dd[j] * invm : 0.f;
-          acc[c0 + j] += dd[j];
-        }
-        if (store_next && prow) {
+      for (int cc = 0; cc < 32; cc += 16) {
+        const int c0 = c_begin + cc;
+        if (c0 < td.NT) {
+          float dd[16];
 #pragma unroll
-          for (int kk = 0; kk < 8; ++kk) {
-            const int k = c0 / 2 + kk;
-            if (k < td.o) {
-              const float tr = dd[2 * kk], ti = dd[2 * kk + 1];
-              uint16_t hr, lr, hi_, li, hni, lni;
-              split16(tr, bf, hr, lr);
-              split16(ti, bf, hi_, li);
-              split16(-ti, bf, hni, lni);
-              const uint32_t a0 = kt0 * BT + sw128(2 * k, kc0), a1 = kt1 * BT + sw128(2 * k, kc1);
-              const uint32_t b0 = kt0 * BT + sw128(2 * k + 1, kc0), b1 = kt1 * BT + sw128(2 * k + 1, kc1);
-              *reinterpret_cast<uint16_t*>(Bh + a0) = hr;
-              *reinterpret_cast<uint16_t*>(Bh + a1) = hni;
-              *reinterpret_cast<uint16_t*>(Bh + b0) = hi_;
-              *reinterpret_cast<uint16_t*>(Bh + b1) = hr;
-              if (lo_next) {
-                *reinterpret_cast<uint16_t*>(Bl + a0) = lr;
-                *reinterpret_cast<uint16_t*>(Bl + a1) = lni;
-                *reinterpret_cast<uint16_t*>(Bl + b0) = li;
-                *reinterpret_cast<uint16_t*>(Bl + b1) = lr;
+          for (int j = 0; j < 16; ++j) dd[j] = 0.f;
+#pragma unroll
+          for (int g0 = 0; g0 < 6; g0 += 3) {  // regions in two groups of three
+            if (g0 < nreg) {
+              float v[3][16];
+#pragma unroll
+              for (int rg = 0; rg < 3; ++rg)
+                if (g0 + rg < nreg) ptx::tmem_ld16p(lane_base + (uint32_t)(64 * (g0 + rg) + c0), v[rg]);
+              ptx::tmem_ld_wait();
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+#pragma unroll
+                for (int rg = 0; rg < 3; ++rg)
+                  if (g0 + rg < nreg) dd[j] += v[rg][j];
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            dd[j] = (c0 + j < o2) ? dd[j] * invm : 0.f;
+            acc[cc + j] += dd[j];
+          }
+          if (!last && prow) {
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const int k = c0 / 2 + kk;
+              if (k < td.o) {
+                const float tr = dd[2 * kk], ti = dd[2 * kk + 1];
+                uint16_t hr, lr, hi_, li, hni, lni;
+                split16(tr, bf, hr, lr);
+                split16(ti, bf, hi_, li);
+                split16(-ti, bf, hni, lni);
+                const uint32_t a0 = kt0 * BT + sw128(2 * k, kc0), a1 = kt1 * BT + sw128(2 * k, kc1);
+                const uint32_t b0 = kt0 * BT + sw128(2 * k + 1, kc0), b1 = kt1 * BT + sw128(2 * k + 1, kc1);
+                *reinterpret_cast<uint16_t*>(Bh + a0) = hr;
+                *reinterpret_cast<uint16_t*>(Bh + a1) = hni;
+                *reinterpret_cast<uint16_t*>(Bh + b0) = hi_;
+                *reinterpret_cast<uint16_t*>(Bh + b1) = hr;
+                if (lo_next) {
+                  *reinterpret_cast<uint16_t*>(Bl + a0) = lr;
+                  *reinterpret_cast<uint16_t*>(Bl + a1) = lni;
+                  *reinterpret_cast<uint16_t*>(Bl + b0) = li;
+                  *reinterpret_cast<uint16_t*>(Bl + b1) = lr;
+                }
               }
             }
           }
         }
       }
+      if (!last) ptx::fence_proxy_async();  // generic-proxy smem writes -> async-proxy MMA reads
     }
-    if (store_next) {
-      ptx::fence_proxy_async();
-      ptx::tc_fence_before();
-      __syncthreads();
-    }
-  }
-  if (prow) {
-    uint16_t* oh = td.acc_hi + (size_t)wg * td.R * td.nk + p;
-    uint16_t* ol = td.acc_lo + (size_t)wg * td.R * td.nk + p;
+    if (!ok) break;
+    if (prow) {
+      const int wg = td.w0 + wl;
+      uint16_t* oh = td.acc_hi + (size_t)wg * td.R * td.nk + p;
+      uint16_t* ol = td.acc_lo + (size_t)wg * td.R * td.nk + p;
 #pragma unroll
-    for (int r = 0; r < 64; ++r) {
-      if (r < o2) {
-        uint16_t h, l;
-        split16(acc[r], bf, h, l);
-        oh[(size_t)r * td.nk] = h;
-        ol[(size_t)r * td.nk] = l;
+      for (int j = 0; j < 32; ++j) {
+        const int r = c_begin + j;
+        if (r < o2) {
+          uint16_t h, l;
+          split16(acc[j], bf, h, l);
+          oh[(size_t)r * td.nk] = h;
+          ol[(size_t)r * td.nk] = l;
+        }
       }
     }
   }
+  // never leave a copy in flight (a walker whose loads were issued but that was not reached)
+  if (tid == 0 && !ok) ptx::mbar_wait(ld_bar, iter & 1);
   if (!ok) atomicOr(status, 2);
   ptx::tc_fence_before();
   __syncthreads();
@@ -1009,13 +1027,14 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
       td.split = t.taylor_split;
       td.bf16 = t.bf16 ? 1 : 0;
       td.w0 = w0;
+      td.nwc = t.nwc;
       td.acc_hi = t.acc[s][0];
       td.acc_lo = t.acc[s][1];
       const size_t smem = taylor_smem(t.nq, t.NT[s], want_lo);
       cudaFuncSetAttribute(k_taylor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       {
         ProfScope _ps(K_TAYLOR, st);
-        k_taylor_tc<<<t.nwc, 128, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0], t.m_t0[s][1], td,
+        k_taylor_tc<<<t.nwc < t.num_sms ? t.nwc : t.num_sms, kTaylorThreads, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0], t.m_t0[s][1], td,
                                               t.status);
       }
       TC_CHECK(launch_check("taylor_tc"));
