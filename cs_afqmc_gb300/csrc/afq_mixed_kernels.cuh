@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(128) k_green_g(const MixedDev md, const float2
   const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = md.n;
   const int gtot = md.o_blk[0] + md.o_blk[1];
   float2* Gs = reinterpret_cast<float2*>(sm);                 // [gtot][n]
-  float2* Si = Gs + (size_t)gtot * n;                          // [kGreenMaxO][kGreenMaxO]
+  float2* Si = Gs + (((size_t)gtot * n + 1) & ~(size_t)1);     // [kGreenMaxO][kGreenMaxO], 16-B aligned
   float2* Wsm = Si + kGreenMaxO * kGreenMaxO;                  // [n][o] walker slab
   __shared__ double red[32];
   __shared__ float fred[4];
@@ -271,13 +271,30 @@ __global__ void __launch_bounds__(128) k_green_g(const MixedDev md, const float2
       for (int k = 0; k < kGreenMaxO; ++k) wr[k] = (k < o) ? Wsm[tid * o + k] : make_float2(0.f, 0.f);
       const int b = md.nblk == 2 ? s : 0;
       float2* Gb = Gs + (size_t)(b == 0 ? 0 : md.o_blk[0]) * n;
-      for (int i = 0; i < o; ++i) {
-        float2 acc = make_float2(0.f, 0.f);
+      // four columns i at a time: independent accumulation chains, 16-byte reads of S^-1
+      for (int i0 = 0; i0 < o; i0 += 4) {
+        float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
 #pragma unroll
-        for (int k = 0; k < kGreenMaxO; ++k)
-          if (k < o) acc = cadd(acc, cmul(wr[k], Si[k * kGreenMaxO + i]));
-        if (md.nblk == 1 && s == 1) acc = cadd(acc, Gb[(size_t)i * n + tid]);  // RHF two slabs
-        Gb[(size_t)i * n + tid] = acc;
+        for (int k = 0; k < kGreenMaxO; ++k) {
+          if (k < o) {
+            const float4 s01 = *reinterpret_cast<const float4*>(&Si[k * kGreenMaxO + i0]);
+            const float4 s23 = *reinterpret_cast<const float4*>(&Si[k * kGreenMaxO + i0 + 2]);
+            a0 = cadd(a0, cmul(wr[k], make_float2(s01.x, s01.y)));
+            a1 = cadd(a1, cmul(wr[k], make_float2(s01.z, s01.w)));
+            a2 = cadd(a2, cmul(wr[k], make_float2(s23.x, s23.y)));
+            a3 = cadd(a3, cmul(wr[k], make_float2(s23.z, s23.w)));
+          }
+        }
+        const float2 av[4] = {a0, a1, a2, a3};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u;
+          if (i < o) {
+            float2 acc = av[u];
+            if (md.nblk == 1 && s == 1) acc = cadd(acc, Gb[(size_t)i * n + tid]);  // RHF two slabs
+            Gb[(size_t)i * n + tid] = acc;
+          }
+        }
       }
     }
     __syncthreads();

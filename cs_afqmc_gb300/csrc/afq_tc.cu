@@ -917,7 +917,7 @@ int tc_green_from_inverse(TcState& t, const afq_ctx_dev& c, const void* wu, cons
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
   const float2* w0 = static_cast<const float2*>(wu);
   const float2* w1 = static_cast<const float2*>(wd);
-  const size_t smem_g = (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 + (size_t)kGreenMaxO * kGreenMaxO * 8 +
+  const size_t smem_g = (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 + 8 + (size_t)kGreenMaxO * kGreenMaxO * 8 +
                         (size_t)t.n * omax * 8;
   cudaFuncSetAttribute(k_green_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g);
   {
