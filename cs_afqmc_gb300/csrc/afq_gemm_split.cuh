@@ -41,6 +41,7 @@ constexpr int kSplitSmem = 1024 + kSplitStages * kSplitUnit + 256;
 
 struct SplitArgs {
   int m_tiles, n_tiles, k_tiles;
+  int k_splits;    // K split into this many ranges (tiles = m_tiles * n_tiles * k_splits)
   int a_row0;      // first A row (walker chunk)
   int has_alo;     // A_lo * B_hi term
   int has_blo;     // B_lo * A_hi term
@@ -48,9 +49,9 @@ struct SplitArgs {
   uint32_t idesc;  // M = 128, N = 256
 };
 
-// Epi::store(params, row, col0, v, status): row of D (tile-local origin excluded: global row
-// index without a_row0), 128 consecutive columns col0.. in v[0..127]; columns >= N must be
-// ignored by the epilogue.
+// Epi::store(params, row, col0, v, ks): row of D (global row index without a_row0), 128
+// consecutive columns col0.. in v[0..127], K range ks; columns >= N must be ignored by the
+// epilogue. With k_splits > 1 each K range produces a partial result.
 template <class Epi>
 __global__ void __launch_bounds__(kSplitThreads, 1)
     k_gemm_split(const __grid_constant__ SplitMaps maps, const SplitArgs g,
@@ -66,8 +67,8 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = g.m_tiles * g.n_tiles;
-  const int runs_per_tile = (g.k_tiles + g.drain - 1) / g.drain;
+  const int ntiles = g.m_tiles * g.n_tiles * g.k_splits;
+  const int kps = (g.k_tiles + g.k_splits - 1) / g.k_splits;  // K tiles per split
   const uint32_t tx_bytes = kSplitA * (g.has_alo ? 2 : 1) + kSplitB * (g.has_blo ? 2 : 1);
 
   if (threadIdx.x == 0) {
@@ -100,8 +101,10 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       if (g.has_blo) ptx::prefetch_tmap(&maps.b_lo);
       int it = 0;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int m0 = (tile % g.m_tiles) * 128, n0 = (tile / g.m_tiles) * kSplitBN;
-        for (int kt = 0; kt < g.k_tiles; ++kt, ++it) {
+        const int m0 = (tile % g.m_tiles) * 128, n0 = ((tile / g.m_tiles) % g.n_tiles) * kSplitBN;
+        const int ks = tile / (g.m_tiles * g.n_tiles);
+        const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
+        for (int kt = ka; kt < kb; ++kt, ++it) {
           const int s = it % kSplitStages, r = it / kSplitStages;
           if (r > 0 && !ptx::mbar_wait(&empty[s], (r - 1) & 1)) {
             ok = false;
@@ -123,6 +126,9 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     if (lane == 0) {
       int it = 0, grun = 0;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int ks = tile / (g.m_tiles * g.n_tiles);
+        const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
+        const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
         for (int run = 0; run < runs_per_tile && ok; ++run, ++grun) {
           const int a = grun & 1;
           if (grun >= 2 && !ptx::mbar_wait(&accempty[a], ((grun - 2) >> 1) & 1)) {
@@ -131,7 +137,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
           }
           ptx::tc_fence_after();
           const uint32_t dacc = tmem + (uint32_t)(a * kSplitBN);
-          const int kt0 = run * g.drain, kt1 = min(g.k_tiles, kt0 + g.drain);
+          const int kt0 = ka + run * g.drain, kt1 = min(kb, kt0 + g.drain);
           for (int kt = kt0; kt < kt1; ++kt, ++it) {
             const int s = it % kSplitStages, r = it / kSplitStages;
             if (!ptx::mbar_wait(&full[s], r & 1)) {
@@ -179,7 +185,10 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     int grun = 0;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int m0 = (tile % g.m_tiles) * 128, n0 = (tile / g.m_tiles) * kSplitBN;
+      const int m0 = (tile % g.m_tiles) * 128, n0 = ((tile / g.m_tiles) % g.n_tiles) * kSplitBN;
+      const int ks = tile / (g.m_tiles * g.n_tiles);
+      const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
+      const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
       float sum[128];
 #pragma unroll
       for (int j = 0; j < 128; ++j) sum[j] = 0.f;
@@ -206,7 +215,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
         if (lane == 0) ptx::mbar_arrive(&accempty[a]);
       }
       if (!ok) break;
-      Epi::store(ep, m0 + q * 32 + lane, n0 + half * 128, sum);
+      Epi::store(ep, m0 + q * 32 + lane, n0 + half * 128, sum, ks);
     }
   }
   if (!ok) atomicOr(status, 4);
@@ -225,11 +234,27 @@ struct SplitStoreF32 {
     int M, N;
     long ldd;
   };
-  __device__ __forceinline__ static void store(const Params& p, int row, int col0, const float* v) {
+  __device__ __forceinline__ static void store(const Params& p, int row, int col0, const float* v, int) {
     if (row >= p.M) return;
 #pragma unroll
     for (int j = 0; j < 128; ++j)
       if (col0 + j < p.N) p.d[(long)row * p.ldd + col0 + j] = v[j];
+  }
+};
+
+// Partial results of a K-split GEMM: d[ks][row][col] (fp32, row stride ldd, split stride sst).
+struct SplitPartialF32 {
+  struct Params {
+    float* d;
+    int M, N;
+    long ldd, sst;
+  };
+  __device__ __forceinline__ static void store(const Params& p, int row, int col0, const float* v, int ks) {
+    if (row >= p.M) return;
+    float* dst = p.d + (long)ks * p.sst + (long)row * p.ldd + col0;
+#pragma unroll
+    for (int j = 0; j < 128; j += 4)
+      if (col0 + j < p.N) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
   }
 };
 

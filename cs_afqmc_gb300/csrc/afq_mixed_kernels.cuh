@@ -411,6 +411,71 @@ struct EpiFB {
   }
 };
 
+// Force bias from the K-split partials of fb = G . rot_chol^T (rows (w, re/im)), one CTA
+// per walker: sums the partials in split order, then the same scaling, field shifts and
+// shift_term / fb_term sums as EpiFB (propagation.py:121-127), the sums reduced over all
+// Cholesky vectors (part_shift / part_fbt hold one entry per walker).
+struct FbReduce {
+  const float* part;  // [ksplit][2 nw][ldp]
+  int ksplit, nw, nchol, ldg, bf16;
+  long ldp, sst;
+  const double* fields;
+  const double2* mf;
+  const float* rc_inv;
+  const float* g_inv;
+  float alpha, sqdt;
+  uint16_t* xt_hi;
+  uint16_t* xt_lo;
+  double2* part_shift;  // [nw]
+  double2* part_fbt;    // [nw]
+  double2* fb_out;      // non-null: write the force bias instead
+};
+
+__global__ void __launch_bounds__(256) k_fb_reduce(const FbReduce r) {
+  __shared__ double red[32];
+  const int w = blockIdx.x;
+  const float gi = r.g_inv[w];
+  const bool bf = r.bf16 != 0;
+  float shx = 0.f, shy = 0.f, fbx = 0.f, fby = 0.f;
+  const float* pr = r.part + (long)(2 * w) * r.ldp;
+  const float* pi = pr + r.ldp;
+  for (int g = threadIdx.x; g < r.nchol; g += blockDim.x) {
+    float ar = 0.f, ai = 0.f;
+    for (int ks = 0; ks < r.ksplit; ++ks) {
+      ar += pr[(long)ks * r.sst + g];
+      ai += pi[(long)ks * r.sst + g];
+    }
+    const float fr = ar * r.alpha * gi * r.rc_inv[g], fi = ai * r.alpha * gi * r.rc_inv[g];
+    if (r.fb_out) {
+      r.fb_out[(size_t)w * r.nchol + g] = c2(fr, fi);
+      continue;
+    }
+    const double2 mfd = r.mf[g];
+    const float mfr = (float)mfd.x, mfi = (float)mfd.y;
+    const float sr = -r.sqdt * (-fi - mfr), si = -r.sqdt * (fr - mfi);
+    const float x = (float)r.fields[(size_t)w * r.nchol + g];
+    const float xtr = x - sr, xti = -si;
+    uint16_t h, l;
+    split16(xtr, bf, h, l);
+    r.xt_hi[(size_t)(2 * w) * r.ldg + g] = h;
+    r.xt_lo[(size_t)(2 * w) * r.ldg + g] = l;
+    split16(xti, bf, h, l);
+    r.xt_hi[(size_t)(2 * w + 1) * r.ldg + g] = h;
+    r.xt_lo[(size_t)(2 * w + 1) * r.ldg + g] = l;
+    shx += xtr * mfr - xti * mfi;
+    shy += xtr * mfi + xti * mfr;
+    fbx += x * sr - 0.5f * (sr * sr - si * si);
+    fby += x * si - sr * si;
+  }
+  if (r.fb_out) return;
+  const double a = block_sum((double)shx, red), b = block_sum((double)shy, red);
+  const double c = block_sum((double)fbx, red), d = block_sum((double)fby, red);
+  if (threadIdx.x == 0) {
+    r.part_shift[w] = c2(a, b);
+    r.part_fbt[w] = c2(c, d);
+  }
+}
+
 // ======================================================================================
 // vhs GEMM epilogue (propagation.py:265-271): rows (w, re/im) of xt . chol give
 // V = i sqrt(dt) xt . chol = sqrt(dt) (-(xt_i.L) + i (xt_r.L)); write the Taylor A operand
@@ -462,7 +527,7 @@ struct EpiVHS {
 // The same scatter for the persistent split GEMM: row R of the chunk, 128 columns from col0.
 struct EpiVHSSplit {
   using Params = EpiVHS::Params;
-  __device__ __forceinline__ static void store(const Params& p, int R, int col0, const float* v) {
+  __device__ __forceinline__ static void store(const Params& p, int R, int col0, const float* v, int) {
     if (R >= p.rows) return;
     const int wl = R >> 1, c = R & 1;
     const bool bf = p.bf16 != 0;

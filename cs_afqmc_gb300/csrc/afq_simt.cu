@@ -602,9 +602,23 @@ __global__ void __launch_bounds__(256) k_qr_householder(const afq_ctx_dev c, WT*
 // sequential cumulative sum (same summation order as numpy/jnp.cumsum), then a gather.
 // ======================================================================================
 
+// in_smem: the weights are staged in shared memory (coalesced), scanned there by one
+// thread in index order (the summation order of numpy/jnp.cumsum) and searched there.
 __global__ void k_sr_indices(int nw, const double* __restrict__ zeta, double* __restrict__ weights,
-                             double* __restrict__ cum, int32_t* __restrict__ idx) {
-  if (threadIdx.x == 0) {
+                             double* __restrict__ cum_g, int32_t* __restrict__ idx, int in_smem) {
+  extern __shared__ double cum_s[];
+  double* cum = in_smem ? cum_s : cum_g;
+  if (in_smem) {
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) cum_s[i] = fabs(weights[i]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0;
+      for (int i = 0; i < nw; ++i) {
+        a += cum_s[i];
+        cum_s[i] = a;
+      }
+    }
+  } else if (threadIdx.x == 0) {
     double a = 0.0;
     for (int i = 0; i < nw; ++i) {
       a += fabs(weights[i]);
@@ -925,7 +939,8 @@ int launch_sr(const afq_ctx_dev& c, const double* zeta, double* weights, double*
               void* wu, void* wd, void* wcopy, cudaStream_t st) {
   {
     ProfScope _ps(K_SR, st);
-    k_sr_indices<<<1, 1024, 0, st>>>(c.nw, zeta, weights, cum, idx);
+    const int in_smem = c.nw * 8 <= 48 * 1024 ? 1 : 0;
+    k_sr_indices<<<1, 1024, in_smem ? c.nw * 8 : 0, st>>>(c.nw, zeta, weights, cum, idx, in_smem);
   }
   int e = launch_err("sr_indices");
   if (e) return e;

@@ -95,8 +95,8 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
 template <class Epi>
 static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms,
                         const typename Epi::Params& ep, int* status, cudaStream_t st) {
-  const int ntiles = g.m_tiles * g.n_tiles;
-  if (ntiles < 1 || g.k_tiles < 1 || g.drain < 1) {
+  const int ntiles = g.m_tiles * g.n_tiles * g.k_splits;
+  if (ntiles < 1 || g.k_tiles < 1 || g.drain < 1 || g.k_splits < 1 || g.k_splits > g.k_tiles) {
     afq_set_error("split gemm: bad sizes");
     return -1;
   }
@@ -546,6 +546,7 @@ struct Plan {
   size_t total;
   size_t o_rc_fb[2], o_rc_inv, o_lop[2], o_eop[2][2], o_u[2][2], o_rcb[2][2], o_rcb_inv[2], o_utmp;
   size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gblk[2][2];
+  size_t o_fbpart;
   size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_sbuf, o_trial32[2], o_rh1[2];
 };
 
@@ -599,6 +600,19 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
     }
     t.fb_ntiles = (c.nchol + t.fb_bn - 1) / t.fb_bn;
   }
+  {  // force bias on the persistent split GEMM: enough K splits to cover the SMs
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+      sms = 148;
+    cudaGetLastError();  // a host without a device leaves an error behind
+    const int mt2 = (2 * c.nw + 127) / 128, nt2 = (c.nchol + kSplitBN - 1) / kSplitBN;
+    const int kt = (t.kfb + 63) / 64;
+    int ks = (sms + mt2 * nt2 - 1) / (mt2 * nt2);
+    if (ks > kt / 4) ks = kt / 4;
+    t.fb_ks = ks < 1 ? 1 : ks;
+    t.fb_npad = nt2 * kSplitBN;
+  }
   t.n_fb_terms = 1 + ((cfg & kFbDyn) ? 1 : 0) + ((cfg & kFbStat) ? 1 : 0);
   t.n_vhs_terms = 1 + ((cfg & kVhsDyn) ? 1 : 0) + ((cfg & kVhsStat) ? 1 : 0);
   t.n_e_terms = 1 + ((cfg & kExpDyn) ? 1 : 0) + ((cfg & kExpStat) ? 1 : 0);
@@ -637,6 +651,7 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
       for (int i = 0; i < 2; ++i) P->o_gblk[b][i] = L.take((size_t)2 * t.nw * t.ldkb[b] * H);
   P->o_ginv = L.take((size_t)t.nw * 4);
   P->o_ene1 = L.take((size_t)t.nw * 16);
+  P->o_fbpart = L.take((size_t)t.fb_ks * ((2 * t.nw + 127) / 128 * 128) * t.fb_npad * 4);
   P->o_pshift = L.take((size_t)t.nw * t.fb_ntiles * 16);
   P->o_pfbt = L.take((size_t)t.nw * t.fb_ntiles * 16);
   P->o_cout = L.take((size_t)t.nblk * t.nw * c.nchol * 16);
@@ -727,6 +742,7 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   t.g_inv = reinterpret_cast<float*>(base + P.o_ginv);
   t.ene1 = reinterpret_cast<double2*>(base + P.o_ene1);
   t.part_shift = reinterpret_cast<double2*>(base + P.o_pshift);
+  t.fb_part = reinterpret_cast<float*>(base + P.o_fbpart);
   t.part_fbt = reinterpret_cast<double2*>(base + P.o_pfbt);
   t.c_out = reinterpret_cast<double2*>(base + P.o_cout);
   t.exc_part = reinterpret_cast<double2*>(base + P.o_exc);
@@ -793,6 +809,12 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
       TC_CHECK(mk(&t.m_fb.a[i], t.g_fb[0], 2 * t.nw, t.kfb, t.ldfb, 128));
       TC_CHECK(mk(&t.m_fb.b[i++], t.rc_fb[1], c.nchol, t.kfb, t.ldfb, t.fb_bn));
     }
+  }
+  {  // force-bias planes for the persistent split GEMM
+    TC_CHECK(mk(&t.m_fb_split.a_hi, t.g_fb[0], 2 * t.nw, t.kfb, t.ldfb, 128));
+    TC_CHECK(mk(&t.m_fb_split.a_lo, t.g_fb[1], 2 * t.nw, t.kfb, t.ldfb, 128));
+    TC_CHECK(mk(&t.m_fb_split.b_hi, t.rc_fb[0], c.nchol, t.kfb, t.ldfb, kSplitBN));
+    TC_CHECK(mk(&t.m_fb_split.b_lo, t.rc_fb[1], c.nchol, t.kfb, t.ldfb, kSplitBN));
   }
   {  // vhs planes for the persistent split GEMM (B boxes of 256 rows)
     const uint64_t nrows = (uint64_t)t.n * t.nq;
@@ -949,6 +971,48 @@ static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, doubl
   ep.part_fbt = t.part_fbt;
   ep.fb_out = fb_out;
   const int kt = ((kdim ? kdim : t.kfb) + 63) / 64, mt = (2 * t.nw + 127) / 128;
+  if (!maps) {
+    // force bias: K-split partials on the persistent split GEMM, then one reduction per
+    // walker fused with the field shifts
+    SplitArgs sa;
+    sa.m_tiles = mt;
+    sa.n_tiles = t.fb_npad / kSplitBN;
+    sa.k_tiles = kt;
+    sa.k_splits = t.fb_ks;
+    sa.a_row0 = 0;
+    sa.has_alo = (t.cfg & kFbDyn) ? 1 : 0;
+    sa.has_blo = (t.cfg & kFbStat) ? 1 : 0;
+    sa.drain = t.drain > 0 ? t.drain : kt;
+    sa.idesc = ptx::idesc_f16(128, kSplitBN, t.bf16 ? 1 : 0);
+    const long ldp = t.fb_npad, sst = (long)mt * 128 * t.fb_npad;
+    SplitPartialF32::Params pp{t.fb_part, 2 * t.nw, c.nchol, ldp, sst};
+    TC_CHECK(launch_split<SplitPartialF32>(K_FB, t.m_fb_split, sa, t.num_sms, pp, t.status, st));
+    FbReduce r;
+    r.part = t.fb_part;
+    r.ksplit = t.fb_ks;
+    r.nw = t.nw;
+    r.nchol = c.nchol;
+    r.ldg = t.ldg;
+    r.bf16 = ep.bf16;
+    r.ldp = ldp;
+    r.sst = sst;
+    r.fields = fields;
+    r.mf = c.mf;
+    r.rc_inv = ep.rc_inv;
+    r.g_inv = t.g_inv;
+    r.alpha = ep.alpha;
+    r.sqdt = ep.sqdt;
+    r.xt_hi = t.xt[0];
+    r.xt_lo = t.xt[1];
+    r.part_shift = t.part_shift;
+    r.part_fbt = t.part_fbt;
+    r.fb_out = fb_out;
+    {
+      ProfScope _ps(K_FB, st);
+      k_fb_reduce<<<t.nw, 256, 0, st>>>(r);
+    }
+    return launch_check("fb_reduce");
+  }
   const int cls = maps ? K_ENERGY : K_FB;
   const GemmMaps& m = maps ? *maps : t.m_fb;
   const int nterms = maps ? t.n_en_terms : t.n_fb_terms;
@@ -1007,6 +1071,7 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.sqdt = (float)sqrt(c.dt);
     SplitArgs sa;
     sa.k_tiles = (c.nchol + 63) / 64;
+    sa.k_splits = 1;
     sa.m_tiles = (2 * t.nwc + 127) / 128;
     sa.n_tiles = (t.n * t.nq + kSplitBN - 1) / kSplitBN;
     sa.a_row0 = 2 * w0;
@@ -1046,7 +1111,8 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
 
 int tc_weights(TcState& t, const afq_ctx_dev& c, const double2* ovl_new, double2* ovl, double* weights,
                double* scalars, cudaStream_t st) {
-  return launch_weights(c, t.part_shift, t.part_fbt, t.fb_ntiles, ovl_new, ovl, weights, scalars, st);
+  // the force-bias reduction leaves one shift_term / fb_term sum per walker
+  return launch_weights(c, t.part_shift, t.part_fbt, 1, ovl_new, ovl, weights, scalars, st);
 }
 
 // local energy (wavefunctions.py:529-561, 711-743): Coulomb c_g from a force-bias-like GEMM,
@@ -1115,6 +1181,7 @@ extern "C" int afq_test_gemm_split(const void* a_hi, const void* a_lo, const voi
   if (e) return e;
   SplitArgs g;
   g.k_tiles = (K + 63) / 64;
+  g.k_splits = 1;
   g.m_tiles = (M + 127) / 128;
   g.n_tiles = (N + kSplitBN - 1) / kSplitBN;
   g.a_row0 = 0;

@@ -50,6 +50,9 @@ struct TcState {
   int o_slab[2], R[2], wpt[2], bn_w[2], NT[2];
   int o_blk[2], kb[2], ldkb[2], mt_z[2];
   int fb_bn, fb_ntiles;
+  int fb_ks, fb_npad;       // force bias on the split GEMM: K splits, padded N of the partials
+  float* fb_part;           // [fb_ks][2 nw][fb_npad] K-split partials of the force bias
+  SplitMaps m_fb_split;     // force-bias operand planes (B boxes of 256 rows)
   // static operands [hi, lo]
   uint16_t *rc_fb[2], *lop[2], *eop[2][2], *u[2][2], *rc_blk[2][2];
   float* rc_inv;            // [nchol] 2^-e_g for rc_fb
