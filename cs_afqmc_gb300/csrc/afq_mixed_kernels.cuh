@@ -145,12 +145,20 @@ __global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2
   }
 }
 
+// Gauss-Jordan with partial pivoting, one warp per walker, lane r <-> row r of S in
+// registers. Pivoting is implicit: no rows move; the pivot of step j is the unused row with
+// the largest |re| + |im| in column j (one __reduce_max_sync over a key that orders by that
+// magnitude, ties to the lower row), broadcast to the other lanes. With rows left in place
+// the working matrix ends as P^T S^-1 P^T for the pivot order P, so row r is written to row
+// step(r) and its column c to column piv(c); det(S) = sign(P) * prod(pivots).
 template <int OM>
 __global__ void __launch_bounds__(256) k_green_inv(const MixedDev md, float2* __restrict__ sbuf,
                                                    double2* __restrict__ ovl, int write_inv) {
-  const int lane = threadIdx.x & 31;
-  const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
+  __shared__ int piv_sm[8][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int w = blockIdx.x * 8 + wib;
   if (w >= md.nw) return;
+  int* piv = piv_sm[wib];
   double2 det = c2(1.0, 0.0);
   for (int s = 0; s < md.nslab; ++s) {
     const int o = md.o_slab[s];
@@ -159,87 +167,61 @@ __global__ void __launch_bounds__(256) k_green_inv(const MixedDev md, float2* __
 #pragma unroll
     for (int c = 0; c < OM; ++c)
       a[c] = (lane < o && c < o) ? S[lane * kGreenMaxO + c] : make_float2(0.f, 0.f);
-    int partner = lane;  // lane j: the row exchanged with row j at step j
+    bool used = lane >= o;
+    int my_step = -1;
 #pragma unroll 1
     for (int j = 0; j < o; ++j) {
       float2 aj = make_float2(0.f, 0.f);  // a[j], selected without dynamic register indexing
 #pragma unroll
       for (int c = 0; c < OM; ++c)
         if (c == j) aj = a[c];
-      float best = (lane >= j && lane < o) ? fabsf(aj.x) + fabsf(aj.y) : -1.f;
-      int bi = lane;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      const float mag = fabsf(aj.x) + fabsf(aj.y);
+      const unsigned key = used ? 0u : ((__float_as_uint(mag) & ~31u) | (unsigned)(31 - lane));
+      const int pr = 31 - (int)(__reduce_max_sync(0xffffffffu, key) & 31u);
+      if (lane == pr) {
+        used = true;
+        my_step = j;
       }
-      const int pr = bi;
-      if (lane == j) partner = pr;
-      if (pr != j) {
-        const int src = lane == j ? pr : (lane == pr ? j : lane);
-#pragma unroll
-        for (int c = 0; c < OM; ++c) {
-          a[c].x = __shfl_sync(0xffffffffu, a[c].x, src);
-          a[c].y = __shfl_sync(0xffffffffu, a[c].y, src);
-        }
-        aj.x = __shfl_sync(0xffffffffu, aj.x, src);
-        aj.y = __shfl_sync(0xffffffffu, aj.y, src);
-      }
-      float2 rowj[OM];
+      if (lane == 0) piv[j] = pr;
+      float2 rowp[OM];
 #pragma unroll
       for (int c = 0; c < OM; ++c) {
-        rowj[c].x = __shfl_sync(0xffffffffu, a[c].x, j);
-        rowj[c].y = __shfl_sync(0xffffffffu, a[c].y, j);
+        rowp[c].x = __shfl_sync(0xffffffffu, a[c].x, pr);
+        rowp[c].y = __shfl_sync(0xffffffffu, a[c].y, pr);
       }
-      const float2 pv = make_float2(__shfl_sync(0xffffffffu, aj.x, j), __shfl_sync(0xffffffffu, aj.y, j));
-      if (lane == 0) {
-        det = cmul(det, c2((double)pv.x, (double)pv.y));
-        if (pr != j) det = c2(-det.x, -det.y);
-      }
+      const float2 pv = make_float2(__shfl_sync(0xffffffffu, aj.x, pr), __shfl_sync(0xffffffffu, aj.y, pr));
+      if (lane == 0) det = cmul(det, c2((double)pv.x, (double)pv.y));
       const float2 inv = cdiv(make_float2(1.f, 0.f), pv);
       if (write_inv) {
 #pragma unroll
-        for (int c = 0; c < OM; ++c) rowj[c] = (c == j) ? inv : cmul(rowj[c], inv);
-        if (lane == j) {
+        for (int c = 0; c < OM; ++c) rowp[c] = (c == j) ? inv : cmul(rowp[c], inv);
+        if (lane == pr) {
 #pragma unroll
-          for (int c = 0; c < OM; ++c) a[c] = rowj[c];
+          for (int c = 0; c < OM; ++c) a[c] = rowp[c];
         } else {
 #pragma unroll
-          for (int c = 0; c < OM; ++c) a[c] = csub((c == j) ? make_float2(0.f, 0.f) : a[c], cmul(aj, rowj[c]));
+          for (int c = 0; c < OM; ++c) a[c] = csub((c == j) ? make_float2(0.f, 0.f) : a[c], cmul(aj, rowp[c]));
         }
-      } else if (lane > j) {  // determinant only: forward elimination
+      } else if (!used) {  // determinant only: eliminate below the pivots
         const float2 f = cmul(aj, inv);
 #pragma unroll
         for (int c = 0; c < OM; ++c)
-          if (c > j) a[c] = csub(a[c], cmul(f, rowj[c]));
+          if (c > j) a[c] = csub(a[c], cmul(f, rowp[c]));
       }
     }
-    if (write_inv) {
-      // undo the row exchanges as column exchanges, last first
-#pragma unroll 1
-      for (int j = o - 1; j >= 0; --j) {
-        const int pj = __shfl_sync(0xffffffffu, partner, j);
-        if (pj != j) {
-          float2 x = make_float2(0.f, 0.f), y = x;
-#pragma unroll
-          for (int c = 0; c < OM; ++c) {
-            if (c == j) x = a[c];
-            if (c == pj) y = a[c];
-          }
-#pragma unroll
-          for (int c = 0; c < OM; ++c) {
-            if (c == j) a[c] = y;
-            if (c == pj) a[c] = x;
-          }
-        }
-      }
-      if (lane < o) {
-#pragma unroll
-        for (int c = 0; c < OM; ++c)
-          if (c < o) S[lane * kGreenMaxO + c] = a[c];
-      }
+    __syncwarp();
+    if (lane == 0) {  // sign of the pivot order: parity of its inversions
+      int inv_count = 0;
+      for (int x = 0; x < o; ++x)
+        for (int y = x + 1; y < o; ++y) inv_count += piv[x] > piv[y] ? 1 : 0;
+      if (inv_count & 1) det = c2(-det.x, -det.y);
     }
+    if (write_inv && lane < o) {
+#pragma unroll
+      for (int c = 0; c < OM; ++c)
+        if (c < o) S[my_step * kGreenMaxO + piv[c]] = a[c];
+    }
+    __syncwarp();
   }
   if (lane == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
 }
@@ -468,11 +450,26 @@ __global__ void __launch_bounds__(256) k_fb_reduce(const FbReduce r) {
     fby += x * si - sr * si;
   }
   if (r.fb_out) return;
-  const double a = block_sum((double)shx, red), b = block_sum((double)shy, red);
-  const double c = block_sum((double)fbx, red), d = block_sum((double)fby, red);
+  // the four sums reduced together: warp shuffles, then one shared-memory pass
+  double v[4] = {(double)shx, (double)shy, (double)fbx, (double)fby};
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], off);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) red[4 * wid + j] = v[j];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int i = 0; i < nwarp; ++i) t += red[4 * i + threadIdx.x];
+    red[threadIdx.x] = t;  // each thread wrote only its own slot of warp 0's row
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    r.part_shift[w] = c2(a, b);
-    r.part_fbt[w] = c2(c, d);
+    r.part_shift[w] = c2(red[0], red[1]);
+    r.part_fbt[w] = c2(red[2], red[3]);
   }
 }
 
