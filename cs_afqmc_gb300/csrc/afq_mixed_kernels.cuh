@@ -612,6 +612,7 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
     const int col = j + 1 + lane;
     if (col < k) {
       float yx = 0.f, yy = 0.f;
+#pragma unroll 8
       for (int r = j; r < m; ++r) {
         const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
         yx += pr.x;
@@ -623,6 +624,7 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
     const float2 ct = make_float2(t.x, -t.y);
     for (int r = j + lane; r < m; r += 32) {
       const float2 v = A[r * ld + j];
+#pragma unroll 4
       for (int cc = j + 1; cc < k; ++cc)
         A[r * ld + cc] = csub(A[r * ld + cc], cmul(ct, cmul(v, y[cc])));
     }
@@ -639,6 +641,7 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
       const int col = j + 1 + lane;
       if (col < k) {
         float yx = 0.f, yy = 0.f;
+#pragma unroll 8
         for (int r = j; r < m; ++r) {
           const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
           yx += pr.x;
@@ -649,6 +652,7 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
       __syncwarp();
       for (int r = j + lane; r < m; r += 32) {
         const float2 v = A[r * ld + j];
+#pragma unroll 4
         for (int cc = j + 1; cc < k; ++cc)
           A[r * ld + cc] = csub(A[r * ld + cc], cmul(t, cmul(v, y[cc])));
       }
