@@ -83,34 +83,41 @@ __device__ __forceinline__ void copy_batched(T* dst, const T* __restrict__ src, 
   }
 }
 
+// Row stride (complex elements) of the walker copy in k_green_s: a multiple of 4 columns
+// rounded so that stride / 2 is odd (16-byte aligned rows; the row-per-thread reads of the
+// operand packing then hit each shared-memory bank at most twice per half warp).
+__host__ __device__ constexpr int green_s_ld(int o) {
+  return ((((o + 3) & ~3) >> 1) & 1) ? ((o + 3) & ~3) : ((o + 3) & ~3) + 2;
+}
+
 __global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2* __restrict__ wu,
                                                  const float2* __restrict__ wd,
                                                  float2* __restrict__ sbuf, int write_ops) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int w = blockIdx.x, tid = threadIdx.x, n = md.n;
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
-  const int o4max = (omax + 3) & ~3;
-  float2* Ws = reinterpret_cast<float2*>(sm);                   // [n][o4] (columns >= o zero)
-  float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * o4max);  // [n][o]
+  const int ldmax = green_s_ld(omax);
+  float2* Ws = reinterpret_cast<float2*>(sm);                   // [n][ld] (columns >= o zero)
+  float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * ldmax);  // [n][o]
   const bool bf = md.bf16 != 0;
   for (int s = 0; s < md.nslab; ++s) {
-    const int o = md.o_slab[s], o4 = (o + 3) & ~3;
+    const int o = md.o_slab[s], o4 = (o + 3) & ~3, ld = green_s_ld(o);
     const float2* W = (s == 0 ? wu : wd) + (size_t)w * n * o;
     const float* C = md.trial32[s];
     // coalesced copies; W rows padded to a multiple of 4 columns for 16-byte loads
     if (o4 != o)
       for (int e = tid; e < n * (o4 - o); e += 128) {
         const int pp = e / (o4 - o), k = o + e - pp * (o4 - o);
-        Ws[pp * o4 + k] = make_float2(0.f, 0.f);
+        Ws[pp * ld + k] = make_float2(0.f, 0.f);
       }
-    copy_batched<128>(Ws, W, n * o, [o, o4](int e) { return (e / o) * o4 + e % o; });
+    copy_batched<128>(Ws, W, n * o, [o, ld](int e) { return (e / o) * ld + e % o; });
     copy_batched<128>(Cs, C, n * o, [](int e) { return e; });
     __syncthreads();
     if (write_ops && tid < n) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
       uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + tid;
       uint16_t* lo = md.wt[s][1] + (size_t)w * md.R[s] * md.nk + tid;
       for (int k = 0; k < o; ++k) {
-        const float2 v = Ws[tid * o4 + k];
+        const float2 v = Ws[tid * ld + k];
         uint16_t h, l;
         split16(v.x, bf, h, l);
         hi[(size_t)(2 * k) * md.nk] = h;
@@ -128,8 +135,8 @@ __global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2
       float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
       for (int pp = 0; pp < n; ++pp) {
         const float cv = Cs[pp * o + i];
-        const float4 x = *reinterpret_cast<const float4*>(&Ws[pp * o4 + k0]);
-        const float4 y = *reinterpret_cast<const float4*>(&Ws[pp * o4 + k0 + 2]);
+        const float4 x = *reinterpret_cast<const float4*>(&Ws[pp * ld + k0]);
+        const float4 y = *reinterpret_cast<const float4*>(&Ws[pp * ld + k0 + 2]);
         a0.x = fmaf(cv, x.x, a0.x); a0.y = fmaf(cv, x.y, a0.y);
         a1.x = fmaf(cv, x.z, a1.x); a1.y = fmaf(cv, x.w, a1.y);
         a2.x = fmaf(cv, y.x, a2.x); a2.y = fmaf(cv, y.y, a2.y);
@@ -421,33 +428,53 @@ __global__ void __launch_bounds__(256) k_fb_reduce(const FbReduce r) {
   float shx = 0.f, shy = 0.f, fbx = 0.f, fby = 0.f;
   const float* pr = r.part + (long)(2 * w) * r.ldp;
   const float* pi = pr + r.ldp;
-  for (int g = threadIdx.x; g < r.nchol; g += blockDim.x) {
-    float ar = 0.f, ai = 0.f;
-    for (int ks = 0; ks < r.ksplit; ++ks) {
-      ar += pr[(long)ks * r.sst + g];
-      ai += pi[(long)ks * r.sst + g];
+  // four Cholesky indices per thread at a time, all loads issued before any store (the
+  // 16-bit stores may alias the loads for the compiler)
+  for (int g0 = threadIdx.x; g0 < r.nchol; g0 += 4 * blockDim.x) {
+    float ar[4], ai[4], rc[4], xv[4];
+    double2 mfv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int g = g0 + u * blockDim.x;
+      ar[u] = ai[u] = rc[u] = xv[u] = 0.f;
+      mfv[u] = c2(0.0, 0.0);
+      if (g < r.nchol) {
+        for (int ks = 0; ks < r.ksplit; ++ks) {
+          ar[u] += pr[(long)ks * r.sst + g];
+          ai[u] += pi[(long)ks * r.sst + g];
+        }
+        rc[u] = r.rc_inv[g];
+        if (!r.fb_out) {
+          xv[u] = (float)r.fields[(size_t)w * r.nchol + g];
+          mfv[u] = r.mf[g];
+        }
+      }
     }
-    const float fr = ar * r.alpha * gi * r.rc_inv[g], fi = ai * r.alpha * gi * r.rc_inv[g];
-    if (r.fb_out) {
-      r.fb_out[(size_t)w * r.nchol + g] = c2(fr, fi);
-      continue;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int g = g0 + u * blockDim.x;
+      if (g >= r.nchol) continue;
+      const float fr = ar[u] * r.alpha * gi * rc[u], fi = ai[u] * r.alpha * gi * rc[u];
+      if (r.fb_out) {
+        r.fb_out[(size_t)w * r.nchol + g] = c2(fr, fi);
+        continue;
+      }
+      const float mfr = (float)mfv[u].x, mfi = (float)mfv[u].y;
+      const float sr = -r.sqdt * (-fi - mfr), si = -r.sqdt * (fr - mfi);
+      const float x = xv[u];
+      const float xtr = x - sr, xti = -si;
+      uint16_t h, l;
+      split16(xtr, bf, h, l);
+      r.xt_hi[(size_t)(2 * w) * r.ldg + g] = h;
+      r.xt_lo[(size_t)(2 * w) * r.ldg + g] = l;
+      split16(xti, bf, h, l);
+      r.xt_hi[(size_t)(2 * w + 1) * r.ldg + g] = h;
+      r.xt_lo[(size_t)(2 * w + 1) * r.ldg + g] = l;
+      shx += xtr * mfr - xti * mfi;
+      shy += xtr * mfi + xti * mfr;
+      fbx += x * sr - 0.5f * (sr * sr - si * si);
+      fby += x * si - sr * si;
     }
-    const double2 mfd = r.mf[g];
-    const float mfr = (float)mfd.x, mfi = (float)mfd.y;
-    const float sr = -r.sqdt * (-fi - mfr), si = -r.sqdt * (fr - mfi);
-    const float x = (float)r.fields[(size_t)w * r.nchol + g];
-    const float xtr = x - sr, xti = -si;
-    uint16_t h, l;
-    split16(xtr, bf, h, l);
-    r.xt_hi[(size_t)(2 * w) * r.ldg + g] = h;
-    r.xt_lo[(size_t)(2 * w) * r.ldg + g] = l;
-    split16(xti, bf, h, l);
-    r.xt_hi[(size_t)(2 * w + 1) * r.ldg + g] = h;
-    r.xt_lo[(size_t)(2 * w + 1) * r.ldg + g] = l;
-    shx += xtr * mfr - xti * mfi;
-    shy += xtr * mfi + xti * mfr;
-    fbx += x * sr - 0.5f * (sr * sr - si * si);
-    fby += x * si - sr * si;
   }
   if (r.fb_out) return;
   // the four sums reduced together: warp shuffles, then one shared-memory pass

@@ -913,7 +913,7 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   }
   const float2* w0 = static_cast<const float2*>(wu);
   const float2* w1 = static_cast<const float2*>(wd);
-  const size_t smem_s = (size_t)t.n * ((omax + 3) & ~3) * 8 + (size_t)t.n * omax * 4;
+  const size_t smem_s = (size_t)t.n * green_s_ld(omax) * 8 + (size_t)t.n * omax * 4;
   cudaFuncSetAttribute(k_green_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s);
   {
     ProfScope _ps(K_GREEN, st);
