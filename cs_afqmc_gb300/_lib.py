@@ -20,6 +20,7 @@ AFQ_PREC_FP64, AFQ_PREC_MIXED = 0, 1
 AFQ_S_E_ESTIMATE, AFQ_S_POP_CONTROL_SHIFT, AFQ_S_N_KILLED = 0, 1, 2
 AFQ_S_BLOCK_ENERGY, AFQ_S_BLOCK_WEIGHT, AFQ_S_STATUS = 3, 4, 5
 AFQ_NSCALARS = 8
+AFQ_JVP_NO_SR = 1
 
 _vp = ctypes.c_void_p
 
@@ -65,6 +66,11 @@ _SIGS = {
                                                ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                _vp, _vp, _vp, _vp]),
     "afq_block_end": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp]),
+    "afq_tangent_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(Dims)]),
+    "afq_propagate_phaseless_jvp": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp,
+                                                   _vp, ctypes.c_size_t, _vp, _vp, ctypes.c_int32,
+                                                   ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _vp, _vp,
+                                                   _vp, _vp, _vp, _vp, _vp]),
     "afq_field_block": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_int32, _vp, _vp,
                                        _vp, _vp]),
     "afq_cs_outlier_removal": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_double, _vp,

@@ -10,6 +10,7 @@
 
 #include "afq_common.cuh"
 #include "afq_kernels.cuh"
+#include "afq_tangent.cuh"
 #include "afq_tc.cuh"
 
 static thread_local char g_err[512] = "";
@@ -259,6 +260,72 @@ int sr_impl(afq_ctx* c, afq_walker_state* s, const double* zeta, int32_t* indice
   return 0;
 }
 
+// Tangent workspace of afq_propagate_phaseless_jvp, carved like the main workspace.
+struct TSizes {
+  size_t dw[2], wold[2], dgreen, dfb, dxt, dshift, dfbt, dvhs, dlo, dlo_new, dweights, dscalars, dene, dpart,
+      dsum, total;
+};
+
+TSizes tangent_sizes(const afq_ctx_dev& c, int nw_chunk, int e_chunks, Layout* L) {
+  TSizes s;
+  const size_t nw = c.nw, C16 = sizeof(double2);
+  for (int k = 0; k < 2; ++k) {  // kslab[1] is 0 for restricted walkers
+    s.dw[k] = L->take(nw * c.norb * c.kslab[k] * C16);
+    s.wold[k] = L->take(nw * c.norb * c.kslab[k] * C16);
+  }
+  s.dgreen = L->take(nw * c.ktot * C16);
+  s.dfb = L->take(nw * c.nchol * C16);
+  s.dxt = L->take(nw * c.nchol * C16);
+  s.dshift = L->take(nw * C16);
+  s.dfbt = L->take(nw * C16);
+  s.dvhs = L->take((size_t)nw_chunk * c.norb * c.norb * C16);
+  s.dlo = L->take(nw * C16);
+  s.dlo_new = L->take(nw * C16);
+  s.dweights = L->take(nw * sizeof(double));
+  s.dscalars = L->take(AFQ_NSCALARS * sizeof(double));
+  s.dene = L->take(nw * C16);
+  s.dpart = L->take(nw * e_chunks * 5 * C16);
+  s.dsum = L->take(sizeof(double));
+  s.total = L->off;
+  return s;
+}
+
+// One phaseless step with tangents (propagate_impl's FP64 branch, each stage followed by
+// its tangent).
+int propagate_jvp(afq_ctx* c, afq_walker_state* s, const afq::TangentBufs& t, const double* fields,
+                  cudaStream_t st) {
+  const afq_ctx_dev& d = c->dev;
+  CHECK(afq::t_launch_green(d, t, s->walkers_up, s->walkers_dn, c->green, t.dgreen, c->ovl_new, t.dlo_new, st));
+  CHECK(force_bias_from_green(c, c->fb, st));
+  {
+    const double2 alpha = c2(d.energy_mode == 0 ? 2.0 : 1.0, 0.0);
+    const double* B = d.nspin_g == 2 ? c->rccat : d.rot_chol[0];
+    CHECK(afq::launch_gemm_cr(false, d.nw, d.nchol, d.ktot, t.dgreen, d.ktot, B, d.ktot, t.dfb, d.nchol, alpha,
+                              st));
+  }
+  CHECK(afq::t_launch_field_shifts(d, fields, c->fb, t.dfb, c->xt, t.dxt, c->shift, t.dshift, c->fbt, t.dfbt, st));
+  const int nb = d.nw / c->nw_chunk;
+  const long nn = (long)d.norb * d.norb;
+  const double2 isq = c2(0.0, sqrt(d.dt));
+  for (int b = 0; b < nb; ++b) {
+    const int w0 = b * c->nw_chunk;
+    CHECK(afq::launch_gemm_cr(true, c->nw_chunk, d.norb * d.norb, d.nchol, c->xt + (size_t)w0 * d.nchol, d.nchol,
+                              c->h.chol, nn, c->vhs, nn, isq, st));
+    CHECK(afq::launch_gemm_cr(true, c->nw_chunk, d.norb * d.norb, d.nchol, t.dxt + (size_t)w0 * d.nchol, d.nchol,
+                              c->h.chol, nn, t.dvhs, nn, isq, st));
+    CHECK(afq::t_launch_taylor(d, t, w0, c->nw_chunk, c->vhs, t.dvhs, s->walkers_up, s->walkers_dn, st));
+  }
+  CHECK(afq::t_launch_green(d, t, s->walkers_up, s->walkers_dn, nullptr, nullptr, c->ovl_new, t.dlo_new, st));
+  return afq::t_launch_weights(d, t, c->shift, c->fbt, c->ovl_new, reinterpret_cast<double2*>(s->overlaps),
+                               s->weights, s->scalars, st);
+}
+
+int copy_d2d(void* dst, const void* src, size_t bytes, cudaStream_t st, const char* what) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) { afq_set_error("%s: %s", what, cudaGetErrorString(e)); return (int)e; }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -449,6 +516,116 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
   ctx->gstate = 0;
   return afq::launch_phaseless_end(blk, (double)n_sr_blocks * n_ene_blocks * d.nw, block_energy,
                                    block_weight, state->scalars, energy, st);
+}
+
+size_t afq_tangent_workspace_size(const afq_dims* dims) {
+  afq_ctx_dev c;
+  int nwc, ec, eg;
+  size_t we;
+  if (derive(dims, &c, &nwc, &ec, &eg, &we)) return 0;
+  Layout L;
+  return tangent_sizes(c, nwc, ec, &L).total;
+}
+
+int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const double* dexp_h1_up,
+                                const double* dexp_h1_dn, const double* drot_h1_up, const double* drot_h1_dn,
+                                void* tangent_workspace, size_t tangent_workspace_bytes, const double* fields,
+                                const double* zetas, int32_t n_prop_steps, int32_t n_ene_blocks,
+                                int32_t n_sr_blocks, int32_t flags, double* block_energy, double* block_weight,
+                                double* dblock_energy, double* dblock_weight, double* energy, double* denergy,
+                                void* stream) {
+  const bool do_sr = !(flags & AFQ_JVP_NO_SR);
+  if (!ctx || !fields || (do_sr && !zetas) || !block_energy || !block_weight || !dblock_energy || !dblock_weight || !energy ||
+      !denergy || !dexp_h1_up || !drot_h1_up) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (!is_fp64(ctx)) { afq_set_error("the derivative path needs an FP64 context"); return -1; }
+  if (n_prop_steps < 1 || n_ene_blocks < 1 || n_sr_blocks < 1 || (!do_sr && n_sr_blocks != 1)) {
+    afq_set_error("block counts must be >= 1 (n_sr_blocks == 1 without SR)");
+    return -1;
+  }
+  if (flags & ~AFQ_JVP_NO_SR) { afq_set_error("unknown flags 0x%x", (unsigned)flags); return -1; }
+  CHECK(check_state(ctx, state));
+  const afq_ctx_dev& d = ctx->dev;
+  if (d.nslab == 2 && !dexp_h1_dn) { afq_set_error("unrestricted walkers need dexp_h1_dn"); return -1; }
+  if (d.nspin_g == 2 && !drot_h1_dn) { afq_set_error("the UHF trial needs drot_h1_dn"); return -1; }
+  Layout L;
+  const TSizes ts = tangent_sizes(d, ctx->nw_chunk, ctx->e_chunks, &L);
+  if (!tangent_workspace || tangent_workspace_bytes < ts.total) {
+    afq_set_error("tangent workspace too small: need %zu bytes, got %zu", ts.total, tangent_workspace_bytes);
+    return -1;
+  }
+  if (reinterpret_cast<uintptr_t>(tangent_workspace) & 255) {
+    afq_set_error("tangent workspace must be 256-byte aligned");
+    return -1;
+  }
+  char* tw = static_cast<char*>(tangent_workspace);
+  afq::TangentBufs t;
+  for (int k = 0; k < 2; ++k) {
+    t.dw[k] = reinterpret_cast<double2*>(tw + ts.dw[k]);
+    t.wold[k] = reinterpret_cast<double2*>(tw + ts.wold[k]);
+  }
+  t.dgreen = reinterpret_cast<double2*>(tw + ts.dgreen);
+  t.dfb = reinterpret_cast<double2*>(tw + ts.dfb);
+  t.dxt = reinterpret_cast<double2*>(tw + ts.dxt);
+  t.dshift = reinterpret_cast<double2*>(tw + ts.dshift);
+  t.dfbt = reinterpret_cast<double2*>(tw + ts.dfbt);
+  t.dvhs = reinterpret_cast<double2*>(tw + ts.dvhs);
+  t.dlo = reinterpret_cast<double2*>(tw + ts.dlo);
+  t.dlo_new = reinterpret_cast<double2*>(tw + ts.dlo_new);
+  t.dweights = reinterpret_cast<double*>(tw + ts.dweights);
+  t.dscalars = reinterpret_cast<double*>(tw + ts.dscalars);
+  t.dene = reinterpret_cast<double2*>(tw + ts.dene);
+  t.dpart = reinterpret_cast<double2*>(tw + ts.dpart);
+  t.dsum = reinterpret_cast<double*>(tw + ts.dsum);
+  t.dbe = dblock_energy;
+  t.dbw = dblock_weight;
+  t.dexp[0] = dexp_h1_up;
+  t.dexp[1] = d.nslab == 2 ? dexp_h1_dn : dexp_h1_up;
+  t.drot[0] = drot_h1_up;
+  t.drot[1] = d.nspin_g == 2 ? drot_h1_dn : drot_h1_up;
+  cudaStream_t st = S(stream);
+  // walker, weight, overlap and shift tangents start at zero (driver.py:190-200)
+  {
+    cudaError_t e = cudaMemsetAsync(tangent_workspace, 0, ts.total, st);
+    if (e != cudaSuccess) { afq_set_error("tangent workspace clear: %s", cudaGetErrorString(e)); return (int)e; }
+  }
+  double2* ovl = reinterpret_cast<double2*>(state->overlaps);
+  const size_t welems[2] = {(size_t)d.nw * d.norb * d.kslab[0], (size_t)d.nw * d.norb * d.kslab[1]};
+  void* wslab[2] = {state->walkers_up, state->walkers_dn};
+  ctx->gstate = 0;
+  CHECK(afq::t_launch_green(d, t, state->walkers_up, state->walkers_dn, nullptr, nullptr, ovl, t.dlo, st));
+  CHECK(afq::launch_phaseless_begin(state->scalars, st));
+  const size_t step_elems = (size_t)d.nw * d.nchol;
+  int blk = 0;
+  for (int sr = 0; sr < n_sr_blocks; ++sr) {
+    for (int eb = 0; eb < n_ene_blocks; ++eb, ++blk) {
+      for (int p = 0; p < n_prop_steps; ++p) {
+        const double* f = fields + ((size_t)blk * n_prop_steps + p) * step_elems;
+        CHECK(propagate_jvp(ctx, state, t, f, st));
+      }
+      for (int k = 0; k < d.nslab; ++k)
+        CHECK(copy_d2d(t.wold[k], wslab[k], welems[k] * sizeof(double2), st, "walker copy before QR"));
+      CHECK(qr_impl(ctx, state, st));
+      CHECK(afq::t_launch_qr(d, t, state->walkers_up, state->walkers_dn, st));
+      CHECK(afq::t_launch_green(d, t, state->walkers_up, state->walkers_dn, ctx->green, t.dgreen, ovl, t.dlo, st));
+      CHECK(energy_from_green(ctx, ctx->ene, st));
+      CHECK(afq::t_launch_energy(d, t, ctx->e_chunks, ctx->e_gchunk, ctx->green, st));
+      CHECK(afq::launch_block_stats(d, ctx->ene, state->weights, state->scalars, block_energy + blk,
+                                    block_weight + blk, st));
+      CHECK(afq::t_launch_block_stats(d, t, ctx->ene, state->weights, state->scalars, block_energy + blk,
+                                      dblock_energy + blk, dblock_weight + blk, st));
+    }
+    if (!do_sr) continue;
+    CHECK(afq::t_launch_sr_pre(d, t, st));
+    CHECK(sr_impl(ctx, state, zetas + sr, nullptr, st));
+    CHECK(afq::t_launch_sr_post(d, t, ctx->sr_idx, st));
+    CHECK(afq::t_launch_green(d, t, state->walkers_up, state->walkers_dn, nullptr, nullptr, ovl, t.dlo, st));
+  }
+  CHECK(afq::launch_phaseless_end(blk, (double)n_sr_blocks * n_ene_blocks * d.nw, block_energy, block_weight,
+                                  state->scalars, energy, st));
+  return afq::t_launch_end(blk, block_energy, block_weight, t, nullptr, denergy, st);
 }
 
 int afq_field_block(afq_ctx* ctx, afq_walker_state* state, const double* fields, int32_t n_prop_steps,

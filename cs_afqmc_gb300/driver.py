@@ -38,3 +38,43 @@ def run_blocks(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_da
         _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), be[n:].data_ptr(), zg.data_ptr(),
                   bw[n:].data_ptr(), stream_ptr())
     return be, bw, prop_data
+
+
+def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_data,
+                  n_blocks: int, observable=None, do_sr: bool = True, fields=None, zetas=None):
+    """Forward-mode branch of driver.py (ad_mode "forward" without orbital rotation,
+    driver.py:165-215, 245-308 on one rank): per block the jvp of
+    sampler.propagate_phaseless_ad_norot (do_sr=False: ..._nosr_norot) along the observable,
+    a non-finite derivative replaced by the trial's value sum(rdm1 * op), then the block
+    weight, QR, global SR and e_estimate update of the non-AD branch. observable:
+    (op, constant) or None for (h1, 0) as driver.py:35-40. fields (optional):
+    [n_blocks, n_sr, n_ene, n_prop, nw, G]; zetas (optional): [n_blocks, n_sr + 1].
+    Returns device tensors (block_energy, block_observable, block_weight), each
+    [n_blocks], and prop_data."""
+    if observable is None:
+        op, const = torch.as_tensor(ham_data["h1"]), 0.0
+    else:
+        op, const = observable[0], float(observable[1])
+    op = torch.as_tensor(op, dtype=torch.float64).to(device())
+    rdm1 = trial.get_rdm1(wave_data)
+    trial_observable = torch.sum(rdm1 * op)
+    be = torch.empty(n_blocks, dtype=torch.float64, device=device())
+    bo = torch.empty(n_blocks, dtype=torch.float64, device=device())
+    bw = torch.empty(n_blocks, dtype=torch.float64, device=device())
+    n_sr = sampler.n_sr_blocks if do_sr else 1
+    for n in range(n_blocks):
+        f = None if fields is None else fields[n]
+        z_local = None if (zetas is None or not do_sr) else zetas[n][:n_sr]
+        e, de, prop_data = sampler.propagate_phaseless_ad_norot_jvp(
+            ham, ham_data, op, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f, zetas=z_local)
+        be[n].copy_(e)
+        bo[n].copy_(torch.where(torch.isfinite(de), de, trial_observable) + const)
+        if zetas is None:
+            zg = sampler.draw_zetas(prop_data, 1)
+        else:
+            zg = torch.as_tensor(zetas[n][-1:], dtype=torch.float64).to(device())
+        eng = prop_data["_engine"]
+        st = prop_data.state(eng)
+        _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), be[n:].data_ptr(), zg.data_ptr(),
+                  bw[n:].data_ptr(), stream_ptr())
+    return be, bo, bw, prop_data

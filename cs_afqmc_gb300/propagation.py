@@ -189,25 +189,41 @@ class propagator_restricted:
         return self.stochastic_reconfiguration_local(prop_data, **kw)
 
     # ---- intermediates --------------------------------------------------------------
-    def _build_propagation_intermediates(self, ham_data: dict, trial, wave_data: dict) -> dict:
-        """mf_shifts, h0_prop, exp_h1 = expm(-dt h1_mod/2) (propagation.py:292-325)."""
+    def _mf_v0_v1(self, ham_data: dict, trial, wave_data: dict):
         norb = trial.norb
         rdm1 = trial.get_rdm1(wave_data)
         rho = rdm1[0] + rdm1[1]
         chol = as_dev(ham_data["chol"]).reshape(-1, norb, norb)
         mf = 1.0j * torch.einsum("gij,ij->g", chol, rho).to(torch.complex128)
+        v0 = 0.5 * torch.einsum("gik,gjk->ij", chol, chol)
+        v1 = torch.real(1.0j * torch.einsum("g,gik->ik", mf, chol.to(torch.complex128)))
+        return mf, v0, v1
+
+    def _build_propagation_intermediates(self, ham_data: dict, trial, wave_data: dict) -> dict:
+        """mf_shifts, h0_prop, exp_h1 = expm(-dt h1_mod/2) (propagation.py:292-325)."""
+        mf, v0, v1 = self._mf_v0_v1(ham_data, trial, wave_data)
         ham_data["mf_shifts"] = mf
         h0 = float(np.real(_engine._scalar(ham_data["h0"])))
         ham_data["h0_prop"] = -h0 - torch.sum(mf * mf).item() / 2.0
-        v0 = 0.5 * torch.einsum("gik,gjk->ij", chol, chol)
-        v1 = torch.real(1.0j * torch.einsum("g,gik->ik", mf, chol.to(torch.complex128)))
         h1 = as_dev(ham_data["h1"])
         ham_data["exp_h1"] = self._exp_h1(h1, v0, v1)
         return ham_data
 
+    def exp_h1_tangent(self, ham_data: dict, trial, wave_data: dict, dh1) -> torch.Tensor:
+        """d exp_h1 / d lambda for h1 -> h1 + lambda dh1 (dh1 [2, norb, norb], symmetrised
+        per spin as the measurement intermediates symmetrise h1): the Frechet derivative
+        of expm at -dt h1_mod/2 in the direction -dt dh1_mod/2. mf_shifts and v0, v1 do
+        not depend on h1."""
+        _, v0, v1 = self._mf_v0_v1(ham_data, trial, wave_data)
+        return self._exp_h1_tangent(as_dev(ham_data["h1"]), v0, v1, as_dev(dh1))
+
     def _exp_h1(self, h1, v0, v1):
         h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
         return torch.linalg.matrix_exp(-self.dt * h1_mod / 2.0).contiguous()
+
+    def _exp_h1_tangent(self, h1, v0, v1, dh1):
+        h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
+        return expm_frechet(-self.dt * h1_mod / 2.0, -self.dt * (dh1[0] + dh1[1]) / 4.0)
 
     def __hash__(self) -> int:
         return hash((type(self).__name__, self.dt, self.n_walkers, self.n_exp_terms,
@@ -224,8 +240,23 @@ class propagator_unrestricted(propagator_restricted):
         return torch.stack([torch.linalg.matrix_exp(-self.dt * (h1[0] - v0 - v1) / 2.0),
                             torch.linalg.matrix_exp(-self.dt * (h1[1] - v0 - v1) / 2.0)]).contiguous()
 
+    def _exp_h1_tangent(self, h1, v0, v1, dh1):
+        return torch.stack([expm_frechet(-self.dt * (h1[s] - v0 - v1) / 2.0, -self.dt * dh1[s] / 2.0)
+                            for s in range(2)]).contiguous()
+
     def __hash__(self) -> int:
         return super().__hash__()
+
+
+def expm_frechet(a: torch.Tensor, da: torch.Tensor) -> torch.Tensor:
+    """Frechet derivative L(a, da) = d/dt expm(a + t da) at t = 0, the upper-right block
+    of expm([[a, da], [0, a]]) (Higham, Functions of Matrices, 2008, thm. 3.6)."""
+    n = a.shape[0]
+    m = torch.zeros(2 * n, 2 * n, dtype=a.dtype, device=a.device)
+    m[:n, :n] = a
+    m[n:, n:] = a
+    m[:n, n:] = da
+    return torch.linalg.matrix_exp(m)[:n, n:].contiguous()
 
 
 def _any_engine(prop_data, trial, ham_data, wave_data, prop):

@@ -19,8 +19,31 @@ from typing import Optional
 import torch
 
 from . import _lib
-from ._engine import as_dev, device, stream_ptr
+from ._engine import _CACHE_KEY, as_dev, device, stream_ptr
 from .propagation import PropData, RngKey
+from .wavefunctions import _sym
+
+
+def h1_direction(observable_op, norb: int) -> torch.Tensor:
+    """observable_op as the [2, norb, norb] direction added to h1, symmetrised per spin as
+    the measurement intermediates symmetrise h1. A [norb, norb] operator acts on both
+    spins."""
+    op = as_dev(observable_op)
+    if op.dim() == 2:
+        op = torch.stack([op, op])
+    if tuple(op.shape) != (2, norb, norb):
+        raise _lib.AfqError(f"observable_op must be [norb, norb] or [2, norb, norb], got {tuple(op.shape)}")
+    return _sym(op)
+
+
+def coupled_ham_data(ham, ham_data: dict, coupling: float, observable_op, prop, trial,
+                     wave_data: dict) -> dict:
+    """ham_data of h1 + coupling * observable_op with the measurement and propagation
+    intermediates rebuilt, the trial held fixed (sampling.py:274-277)."""
+    hd = {k: v for k, v in ham_data.items() if k != _CACHE_KEY}
+    hd["h1"] = as_dev(ham_data["h1"]) + float(coupling) * h1_direction(observable_op, trial.norb)
+    hd = ham.build_measurement_intermediates(hd, trial, wave_data)
+    return ham.build_propagation_intermediates(hd, prop, trial, wave_data)
 
 
 @dataclass
@@ -72,6 +95,87 @@ class sampler:
         dict.__setitem__(prop_data, "block_energies", be)
         dict.__setitem__(prop_data, "block_weights", bw)
         return energy[0], prop_data
+
+    def propagate_phaseless_ad_norot(self, ham, ham_data: dict, coupling: float, observable_op,
+                                     prop, prop_data: PropData, trial, wave_data: dict,
+                                     fields: Optional[torch.Tensor] = None,
+                                     zetas: Optional[torch.Tensor] = None):
+        """(energy, prop_data) of the block with h1 + coupling * observable_op and the
+        trial held fixed (sampling.py:266-285); the value whose derivative
+        propagate_phaseless_ad_norot_jvp returns."""
+        hd = ham_data if coupling == 0.0 else coupled_ham_data(ham, ham_data, coupling, observable_op,
+                                                                prop, trial, wave_data)
+        return self.propagate_phaseless(ham, hd, prop, prop_data, trial, wave_data, fields, zetas)
+
+    def propagate_phaseless_ad_norot_jvp(self, ham, ham_data: dict, observable_op, prop,
+                                         prop_data: PropData, trial, wave_data: dict,
+                                         coupling: float = 0.0, do_sr: bool = True,
+                                         fields: Optional[torch.Tensor] = None,
+                                         zetas: Optional[torch.Tensor] = None):
+        """Forward-mode derivative of propagate_phaseless_ad_norot (do_sr=False:
+        propagate_phaseless_ad_nosr_norot, sampling.py:287-317) along observable_op at
+        `coupling`, with a zero tangent on prop_data: what driver.py:207-215 computes with
+        jax.jvp. Returns (energy, d energy / d coupling, prop_data), both 0-d CUDA tensors;
+        prop_data also gets "block_energies", "block_weights", "dblock_energies",
+        "dblock_weights". FP64 (complex128) walkers only."""
+        hd = ham_data if coupling == 0.0 else coupled_ham_data(ham, ham_data, coupling, observable_op,
+                                                                prop, trial, wave_data)
+        eng = prop._engine(trial, hd, wave_data, prop_data["walkers"])
+        if eng.precision != _lib.AFQ_PREC_FP64:
+            raise _lib.AfqError("the derivative path needs FP64 (complex128) walkers")
+        dict.__setitem__(prop_data, "_engine", eng)
+        n_sr = self.n_sr_blocks if do_sr else 1
+        nblk = n_sr * self.n_ene_blocks
+        dh1 = h1_direction(observable_op, trial.norb)
+        dexp = prop.exp_h1_tangent(hd, trial, wave_data, dh1)
+        drot = trial.rot_h1_tangent(dh1, wave_data)
+        if dexp.dim() == 3:
+            dexp_up, dexp_dn = dexp[0].contiguous(), dexp[1].contiguous()
+        else:
+            dexp_up, dexp_dn = dexp, None
+        if isinstance(drot, list):
+            drot_up, drot_dn = drot
+        else:
+            drot_up, drot_dn = drot, None
+        want = (n_sr, self.n_ene_blocks, self.n_prop_steps, eng.nw, eng.nchol)
+        if fields is None:
+            f = torch.empty(want, dtype=torch.float64, device=device())
+            key: RngKey = prop_data["key"]
+            _lib.call("afq_fill_normal", f.data_ptr(), f.numel(), key.seed, key.take(f.numel()),
+                      stream_ptr())
+        else:
+            f = as_dev(fields)
+        if f.numel() != nblk * self.n_prop_steps * eng.nw * eng.nchol:
+            raise _lib.AfqError(f"fields must have shape {want}")
+        if do_sr:
+            z = self.draw_zetas(prop_data, n_sr) if zetas is None else as_dev(zetas)
+            if z.numel() != n_sr:
+                raise _lib.AfqError(f"zetas must have {n_sr} entries")
+        else:
+            z = None
+        tws = getattr(eng, "tangent_workspace", None)
+        nbytes = eng.lib.afq_tangent_workspace_size(ctypes.byref(eng.dims))
+        if nbytes == 0:
+            raise _lib.AfqError("afq_tangent_workspace_size: " + eng.lib.afq_last_error().decode())
+        if tws is None or tws.numel() < nbytes + 256:
+            tws = torch.empty(nbytes + 256, dtype=torch.uint8, device=device())
+            eng.tangent_workspace = tws
+        tptr = tws.data_ptr() + (-tws.data_ptr()) % 256
+        out = torch.empty(4 * nblk + 2, dtype=torch.float64, device=device())
+        be, bw, dbe, dbw = (out[i * nblk:(i + 1) * nblk] for i in range(4))
+        energy, denergy = out[4 * nblk:4 * nblk + 1], out[4 * nblk + 1:]
+        st = prop_data.state(eng)
+        _lib.call("afq_propagate_phaseless_jvp", eng.ctx, ctypes.byref(st), dexp_up.data_ptr(),
+                  None if dexp_dn is None else dexp_dn.data_ptr(), drot_up.data_ptr(),
+                  None if drot_dn is None else drot_dn.data_ptr(), tptr, nbytes, f.data_ptr(),
+                  None if z is None else z.data_ptr(), self.n_prop_steps, self.n_ene_blocks, n_sr,
+                  0 if do_sr else _lib.AFQ_JVP_NO_SR, be.data_ptr(), bw.data_ptr(), dbe.data_ptr(),
+                  dbw.data_ptr(), energy.data_ptr(), denergy.data_ptr(), stream_ptr())
+        dict.__setitem__(prop_data, "block_energies", be)
+        dict.__setitem__(prop_data, "block_weights", bw)
+        dict.__setitem__(prop_data, "dblock_energies", dbe)
+        dict.__setitem__(prop_data, "dblock_weights", dbw)
+        return energy[0], denergy[0], prop_data
 
     def __hash__(self) -> int:
         return hash((self.n_prop_steps, self.n_ene_blocks, self.n_sr_blocks, self.n_blocks))

@@ -132,6 +132,12 @@ class rhf(wave_function):
         ham_data["rot_chol"] = torch.einsum("pi,gij->gpj", mo.T, chol).contiguous()
         return ham_data
 
+    def rot_h1_tangent(self, dh1, wave_data: dict) -> torch.Tensor:
+        """d rot_h1 / d lambda for h1 -> h1 + lambda dh1 (dh1 symmetrised per spin)."""
+        mo = as_dev(wave_data["mo_coeff"])
+        dh1 = as_dev(dh1)
+        return (mo.T @ ((dh1[0] + dh1[1]) / 2.0)).contiguous()
+
     def __hash__(self) -> int:
         return super().__hash__()
 
@@ -163,6 +169,13 @@ class uhf(wave_function):
         ham_data["rot_chol"] = [torch.einsum("pi,gij->gpj", a.T, chol).contiguous(),
                                 torch.einsum("pi,gij->gpj", b.T, chol).contiguous()]
         return ham_data
+
+    def rot_h1_tangent(self, dh1, wave_data: dict) -> list:
+        """d rot_h1 / d lambda per spin for h1 -> h1 + lambda dh1 (dh1 symmetrised per spin)."""
+        mo = wave_data["mo_coeff"]
+        a, b = as_dev(mo[0]), as_dev(mo[1])
+        dh1 = as_dev(dh1)
+        return [(a.T @ dh1[0]).contiguous(), (b.T @ dh1[1]).contiguous()]
 
     def __hash__(self) -> int:
         return super().__hash__()

@@ -184,6 +184,40 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
 int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, const double* zeta,
                   double* block_weight, void* stream);
 
+/* ---- forward-mode derivative of the block (differentiation pattern, FP64) ------------ */
+
+/* Bytes of device tangent workspace afq_propagate_phaseless_jvp needs. 0 on bad sizes. */
+size_t afq_tangent_workspace_size(const afq_dims* dims);
+
+/* flags of afq_propagate_phaseless_jvp */
+enum {
+  AFQ_JVP_NO_SR = 1 /* no local SR after the energy blocks (the _nosr variants,
+                       sampling.py:221-254, 287-317); needs n_sr_blocks == 1, zetas may be NULL */
+};
+
+/* afq_propagate_phaseless together with its derivative with respect to a coupling lambda of
+ * h1 + lambda * D, the trial held fixed: the jvp that driver.py:207-215 takes of
+ * sampler.propagate_phaseless_ad_norot (sampling.py:266-285) with tangent 1 on the
+ * coupling and zero on prop_data. The only inputs with a tangent are the propagator's
+ * exp_h1 and the measurement intermediate rot_h1, whose derivatives the caller passes:
+ * dexp_h1_up/dn float64 [norb, norb] (d expm(-dt h1_mod/2) / d lambda; dn NULL for
+ * restricted walkers) and drot_h1_up/dn with the layout of rot_h1_up/dn (dn NULL for the
+ * RHF trial). Values (walkers, weights, overlaps, scalars, block_energy, block_weight,
+ * energy) are those of afq_propagate_phaseless on the same draws; dblock_energy,
+ * dblock_weight ([n_sr_blocks * n_ene_blocks]) and denergy ([1]) are their derivatives.
+ * Clamped quantities (weights set to 0, local energies replaced by e_estimate) have a zero
+ * derivative, as jnp.where's jvp gives. tangent_workspace: 256-B aligned device memory of
+ * afq_tangent_workspace_size(dims) bytes, cleared by the call. FP64 contexts only. */
+int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const double* dexp_h1_up,
+                                const double* dexp_h1_dn, const double* drot_h1_up,
+                                const double* drot_h1_dn, void* tangent_workspace,
+                                size_t tangent_workspace_bytes, const double* fields,
+                                const double* zetas, int32_t n_prop_steps, int32_t n_ene_blocks,
+                                int32_t n_sr_blocks, int32_t flags, double* block_energy,
+                                double* block_weight, double* dblock_energy,
+                                double* dblock_weight, double* energy, double* denergy,
+                                void* stream);
+
 /* ---- correlated sampling (ad_afqmc/corr_sample/corr_sample.py) ---------------------- */
 
 /* One correlated-sampling block of one system with the given fields (float64

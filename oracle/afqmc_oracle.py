@@ -416,9 +416,11 @@ class Sampler:
         prop_data["pop_control_ene_shift"] = 0.9 * prop_data["pop_control_ene_shift"] + 0.1 * be
         return prop_data, be, bw
 
-    def propagate_phaseless(self, prop, trial, ham_data, prop_data, mo, fields, zetas):
+    def propagate_phaseless(self, prop, trial, ham_data, prop_data, mo, fields, zetas, do_sr=True):
         """fields [n_sr_blocks, n_ene_blocks, n_prop_steps, nw, G]; zetas [n_sr_blocks]
-        (sampling.py:126-144, 319-341). Returns (energy, prop_data, block_e, block_w)."""
+        (sampling.py:126-144, 319-341). do_sr=False: the no-SR block of
+        propagate_phaseless_ad_nosr (sampling.py:287-317; n_sr_blocks 1). Returns (energy,
+        prop_data, block_e, block_w)."""
         prop_data["overlaps"] = trial.overlap(prop_data["walkers"], mo)
         prop_data["n_killed_walkers"] = 0
         prop_data["pop_control_ene_shift"] = prop_data["e_estimate"]
@@ -428,6 +430,8 @@ class Sampler:
                 prop_data, be, bw = self.block_scan(prop, trial, ham_data, prop_data, mo, fields[s, b])
                 be_all.append(be)
                 bw_all.append(bw)
+            if not do_sr:
+                continue
             prop_data = prop.stochastic_reconfiguration(prop_data, zetas[s])
             prop_data["overlaps"] = trial.overlap(prop_data["walkers"], mo)
         prop_data["n_killed_walkers"] /= self.n_sr_blocks * self.n_ene_blocks * prop.n_walkers
@@ -508,6 +512,36 @@ def cs_steps_scan(sampler: "Sampler", sys1: tuple, sys2: tuple, fields: np.ndarr
                     np.sum(e2 * pd2["weights"]), np.sum(pd2["weights"])))
     out = np.array(out)
     return pd1, pd2, out[:, 0], out[:, 1], out[:, 2], out[:, 3]
+
+
+def phaseless_derivative_fd(sampler: "Sampler", prop: "Propagator", trial: "Trial", ham_data: dict,
+                            direction: np.ndarray, rdm1: np.ndarray, mo, prop_data: dict,
+                            fields: np.ndarray, zetas, restricted: bool, h: float = 1e-3,
+                            do_sr: bool = True):
+    """d/d lambda of the blocked energy and of each block's (energy, weight) for
+    h1 + lambda * direction (direction [2, norb, norb]) with the trial, prop_data, fields
+    and SR uniforms held fixed: the quantity that driver.py:207-215 takes with jax.jvp of
+    sampling.py:266-285 (norot) or 287-317 (nosr_norot). ham_data is the raw
+    {h0, h1, chol}; intermediates are rebuilt at each lambda. Central differences at h and
+    h/2, Richardson-extrapolated (error O(h^4)). Returns (energy, d energy, block_e,
+    d block_e, block_w, d block_w) at lambda = 0."""
+    import copy
+
+    def run(lam):
+        hd = {"h0": ham_data["h0"], "h1": np.asarray(ham_data["h1"]) + lam * direction,
+              "chol": ham_data["chol"]}
+        hd = trial.build_measurement_intermediates(hd, mo)
+        hd = build_propagation_intermediates(hd, rdm1, trial.norb, trial.nelec, prop.dt, restricted)
+        e, _, be, bw = sampler.propagate_phaseless(prop, trial, hd, copy.deepcopy(prop_data), mo,
+                                                   fields, zetas, do_sr=do_sr)
+        return np.concatenate([[e], be, bw])
+
+    v0 = run(0.0)
+    d1 = (run(h) - run(-h)) / (2 * h)
+    d2 = (run(h / 2) - run(-h / 2)) / h
+    d = (4 * d2 - d1) / 3
+    nb = (len(v0) - 1) // 2
+    return v0[0], d[0], v0[1:1 + nb], d[1:1 + nb], v0[1 + nb:], d[1 + nb:]
 
 
 def blocking_analysis(weights: np.ndarray, energies: np.ndarray, neql: int = 0):

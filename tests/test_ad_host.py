@@ -1,0 +1,75 @@
+"""Host-side pieces of the forward-mode derivative, on the CPU: the Frechet derivative of
+expm that gives d exp_h1 / d lambda, and the oracle's finite-difference derivative of the
+blocked energy (its convergence in h)."""
+
+import numpy as np
+import pytest
+import scipy.linalg
+import torch
+
+from oracle import afqmc_oracle as O
+
+
+def test_expm_frechet_matches_scipy():
+    from cs_afqmc_gb300.propagation import expm_frechet
+    rng = np.random.default_rng(1)
+    for n in (1, 5, 24):
+        a = rng.standard_normal((n, n)) * 0.3
+        e = rng.standard_normal((n, n))
+        want = scipy.linalg.expm_frechet(a, e, compute_expm=False)
+        got = expm_frechet(torch.as_tensor(a), torch.as_tensor(e)).numpy()
+        assert np.max(np.abs(got - want)) < 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+def test_expm_frechet_is_the_derivative():
+    from cs_afqmc_gb300.propagation import expm_frechet
+    rng = np.random.default_rng(2)
+    a = rng.standard_normal((8, 8)) * 0.05
+    e = rng.standard_normal((8, 8))
+    h = 1e-5
+    fd = (scipy.linalg.expm(a + h * e) - scipy.linalg.expm(a - h * e)) / (2 * h)
+    got = expm_frechet(torch.as_tensor(a), torch.as_tensor(e)).numpy()
+    assert np.max(np.abs(got - fd)) < 1e-8
+
+
+def _small_system(kind="rhf", restricted=True, norb=6, nelec=(2, 2), nchol=8, nw=4, seed=5):
+    from cs_afqmc_gb300 import synthetic
+    s = synthetic.molecular(norb, nelec, nchol, seed=seed, kind=kind)
+    rng = np.random.default_rng(seed + 100)
+    trial = O.Trial(kind, norb, nelec)
+    ham = {"h0": s.h0, "h1": s.h1.copy(), "chol": s.chol.copy()}
+    hd = trial.build_measurement_intermediates(dict(ham), s.mo_coeff)
+    dt = 0.005
+    hd = O.build_propagation_intermediates(hd, s.rdm1, norb, nelec, dt, restricted)
+    prop = O.Propagator(dt=dt, n_walkers=nw, n_exp_terms=6)
+    if restricted:
+        w = np.repeat(s.mo_coeff[None].astype(np.complex128), nw, 0)
+        w = w + 0.2 * (rng.standard_normal(w.shape) + 1j * rng.standard_normal(w.shape))
+    else:
+        mos = [s.mo_coeff[:, : nelec[0]], s.mo_coeff[:, : nelec[1]]] if kind == "rhf" else s.mo_coeff
+        w = [np.repeat(m[None].astype(np.complex128), nw, 0) for m in mos]
+        w = [x + 0.2 * (rng.standard_normal(x.shape) + 1j * rng.standard_normal(x.shape)) for x in w]
+    pd = O.init_prop_data(prop, trial, hd, s.mo_coeff, w)
+    return s, trial, ham, prop, pd
+
+
+@pytest.mark.parametrize("kind,restricted", [("rhf", True), ("uhf", False)])
+def test_oracle_fd_converges(kind, restricted):
+    """The Richardson-extrapolated central difference agrees with itself at h and h/4 (the
+    derivative is smooth in lambda for these draws: no clamp or SR index changes)."""
+    s, trial, ham, prop, pd = _small_system(kind=kind, restricted=restricted)
+    samp = O.Sampler(n_prop_steps=2, n_ene_blocks=2, n_sr_blocks=1)
+    rng = np.random.default_rng(3)
+    fields = rng.standard_normal((1, 2, 2, prop.n_walkers, s.chol.shape[0]))
+    zetas = rng.uniform(size=1)
+    D = rng.standard_normal((2, s.norb, s.norb)) * 0.1
+    a = O.phaseless_derivative_fd(samp, prop, trial, ham, D, s.rdm1, s.mo_coeff, pd, fields, zetas,
+                                  restricted, h=1e-3)
+    b = O.phaseless_derivative_fd(samp, prop, trial, ham, D, s.rdm1, s.mo_coeff, pd, fields, zetas,
+                                  restricted, h=2.5e-4)
+    assert abs(a[1] - b[1]) < 1e-8 * max(1.0, abs(a[1]))
+    assert np.max(np.abs(a[3] - b[3])) < 1e-8 * max(1.0, np.max(np.abs(a[3])))
+    # zero direction: zero derivative, values unchanged
+    z = O.phaseless_derivative_fd(samp, prop, trial, ham, 0 * D, s.rdm1, s.mo_coeff, pd, fields, zetas,
+                                  restricted, h=1e-3)
+    assert z[1] == 0.0 and z[0] == a[0]
