@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--serving-norb-max", type=int, default=128)
     ap.add_argument("--serving-slots", type=int, default=16)
     ap.add_argument("--cs-derivative", action="store_true",
-                    help="correlated-sampling derivative dE/dlambda on the UHF workload")
+                    help="dE/dlambda on the UHF workload: correlated sampling and forward mode")
     ap.add_argument("--cs-blocks", type=int, default=10)
     ap.add_argument("--energy-sync", action="store_true",
                     help="with --energy-only: per-block comparison from the FP64 run's states")
@@ -589,7 +589,8 @@ def cs_derivative(args) -> dict:
     systems at lambda = +-1e-4 on identical fields (cs_steps_scan), for the UHF workload
     (norb 60, 10+8 electrons, 300 Cholesky vectors, 512 walkers, 50 steps per block).
     D is a seeded symmetric N(0, 0.05) matrix. Run in the mixed and the FP64 precision on
-    the same draws; reports the per-block derivative statistics and walker-steps/s."""
+    the same draws; reports the per-block derivative statistics and walker-steps/s, then
+    the forward-mode derivative of the same D (ad_derivative)."""
     import numpy as np
     import torch
 
@@ -647,7 +648,88 @@ def cs_derivative(args) -> dict:
         del systems, p1, p2, h1, h2, pr1, pr2
         torch.cuda.empty_cache()
     res["mixed_minus_fp64"] = res["mixed"]["dE_dlambda"] - res["fp64"]["dE_dlambda"]
+    res["forward_mode_fp64"] = ad_derivative(w, name, d, steps, n_prop)
     return res
+
+
+def ad_derivative(w: dict, name: str, d, steps: int, n_prop: int) -> dict:
+    """The same derivative by forward mode, FP64: driver.run_blocks_ad (per driver block the
+    jvp of sampler.propagate_phaseless_ad_norot over one 50-step energy block with its
+    local SR, then QR, global SR and the e_estimate update), `steps` blocks after one
+    warm-up block; its cost against driver.run_blocks on the same draws; and, on the first
+    block, the jvp against a central difference of the FP64 value path at coupling +-1e-4
+    on identical draws (a check at the full workload size)."""
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import driver, hamiltonian, propagation, sampling, synthetic, wavefunctions
+    from cs_afqmc_gb300.propagation import RngKey
+
+    norb = w["norb"]
+    s = synthetic.molecular(norb, w["nelec"], w["nchol"], seed=1, kind=w["kind"])
+    ham = hamiltonian.hamiltonian(norb)
+    trial = wavefunctions.uhf(norb, w["nelec"])
+    wave = {"mo_coeff": s.mo_coeff, "rdm1": s.rdm1}
+    hd = {"h0": s.h0, "h1": s.h1, "chol": s.chol, "ene0": 0.0}
+    hd = ham.build_measurement_intermediates(hd, trial, wave)
+    prop = propagation.propagator_unrestricted(dt=w["dt"], n_walkers=w["n_walkers"], n_exp_terms=6,
+                                               n_batch=1, precision="fp64")
+    hd = ham.build_propagation_intermediates(hd, prop, trial, wave)
+    samp = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=1, n_sr_blocks=1)
+    op = np.stack([d, d])
+
+    def fresh(seed=777):
+        pd = prop.init_prop_data(trial, wave, hd, init_walkers=s.init_walkers(w["n_walkers"], False))
+        pd["key"] = RngKey(seed)
+        return pd
+
+    # check on the first block: jvp against the value path's central difference
+    pd = fresh()
+    f0 = samp.draw_fields(prop, pd, int(hd["chol"].shape[0]))
+    z0 = samp.draw_zetas(pd, 1)
+    _, de0, _ = samp.propagate_phaseless_ad_norot_jvp(ham, hd, op, prop, fresh(), trial, wave,
+                                                     fields=f0, zetas=z0)
+    lam = 1e-4
+    ev = [samp.propagate_phaseless_ad_norot(ham, hd, c, op, prop, fresh(), trial, wave,
+                                            fields=f0, zetas=z0)[0].item()
+          for c in (lam, -lam, lam / 2, -lam / 2)]
+    fd = (4 * (ev[2] - ev[3]) / lam - (ev[0] - ev[1]) / (2 * lam)) / 3
+    check = {"jvp": de0.item(), "central_difference": fd, "abs_diff": abs(de0.item() - fd),
+             "lambda": lam, "richardson": True}
+
+    def timed(ad: bool):
+        pd = fresh()
+        run = (lambda k, p: driver.run_blocks_ad(samp, ham, hd, prop, p, trial, wave, k, observable=(op, 0.0))) \
+            if ad else (lambda k, p: driver.run_blocks(samp, ham, hd, prop, p, trial, wave, k))
+        out = run(1, pd)  # warm-up block
+        pd = out[-1]
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        out = run(steps, pd)
+        t1.record()
+        torch.cuda.synchronize()
+        return out, t0.elapsed_time(t1) / 1e3
+
+    (be, bo, bw, _), sec = timed(True)
+    (be_v, bw_v, _), sec_v = timed(False)
+    be, bo, bw = (x.cpu().numpy() for x in (be, bo, bw))
+    obs = float(np.sum(bo * bw) / np.sum(bw))
+    return {
+        "dE_dlambda": obs,
+        "per_block_mean": float(bo.mean()),
+        "per_block_stderr": float(bo.std(ddof=1) / np.sqrt(len(bo))) if len(bo) > 1 else None,
+        "energy": float(np.sum(be * bw) / np.sum(bw)),
+        "energy_equals_value_driver": bool(np.allclose(be, be_v.cpu().numpy(), rtol=1e-9, atol=0)),
+        "walker_steps_per_s": steps * n_prop * w["n_walkers"] / sec,
+        "value_fp64_walker_steps_per_s": steps * n_prop * w["n_walkers"] / sec_v,
+        "cost_vs_value": sec / sec_v,
+        "per_block": [round(float(x), 6) for x in bo],
+        "first_block_check": check,
+        "estimator": "driver forward mode: block observable = d(block energy)/dlambda with SR per "
+                     "block; clamped quantities have zero derivative",
+    }
 
 
 def serving_bench(args) -> dict:
