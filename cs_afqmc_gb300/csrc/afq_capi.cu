@@ -46,8 +46,8 @@ struct afq_ctx {
   int32_t* sr_idx;
   double* cum;
   afq::TcState tc;  // tensor-core (mixed precision) operands and plans
-  // Inside afq_propagate_phaseless only (mixed path): what the scratch buffers hold for the
-  // current walkers. 0 nothing, 1 S^-1 and the walker operand, 2 also G and its operands.
+  // Inside afq_propagate_phaseless only (mixed path): 1 when the operand buffers already
+  // hold G, its operands and the walker operand of the current walkers, else 0.
   int gstate;
 };
 
@@ -170,13 +170,13 @@ bool is_fp64(const afq_ctx* c) { return c->d.precision == AFQ_PREC_FP64; }
 
 // Green's function + overlap. FP64: G into c->green. Mixed: the 16-bit operands of the
 // force-bias, energy and exp_h1 contractions (wg) and/or the overlap.
-// chain (mixed path, inside afq_propagate_phaseless): keep S^-1 and record in c->gstate what
-// the next propagation step can reuse.
+// chain (mixed path, inside afq_propagate_phaseless): the walkers are propagated next, so
+// the same launch also forms G and the operands; c->gstate records that for the next step.
 int green(afq_ctx* c, const void* wu, const void* wd, double2* g, double2* ovl, bool wg, cudaStream_t st,
           bool chain = false) {
   if (is_fp64(c)) return afq::launch_green<double>(c->dev, wu, wd, g, ovl, wg, st);
   CHECK(afq::tc_green(c->tc, c->dev, wu, wd, ovl, wg, st, chain));
-  c->gstate = chain ? (wg ? 2 : 1) : 0;
+  c->gstate = chain ? 1 : 0;
   return 0;
 }
 
@@ -214,9 +214,7 @@ int propagate_impl(afq_ctx* c, afq_walker_state* s, const double* fields, cudaSt
   const afq_ctx_dev& d = c->dev;
   if (!is_fp64(c)) {
     // mixed: operands -> fused force bias / field shifts -> exp_h1, vhs + Taylor, exp_h1
-    const int have = chain ? c->gstate : 0;
-    if (have == 0) CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, nullptr, true, st));
-    else if (have == 1) CHECK(afq::tc_green_from_inverse(c->tc, d, s->walkers_up, s->walkers_dn, st));
+    if (!(chain && c->gstate == 1)) CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, nullptr, true, st));
     CHECK(afq::tc_field_shifts(c->tc, d, fields, st));
     CHECK(afq::tc_propagate_walkers(c->tc, d, s->walkers_up, s->walkers_dn, st));
     CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, c->ovl_new, false, st, chain));

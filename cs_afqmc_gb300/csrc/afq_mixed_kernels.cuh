@@ -49,19 +49,6 @@ struct MixedDev {
   double2* ene1;
 };
 
-// ======================================================================================
-// Green's function, overlap and operand packing, in three kernels
-// (wavefunctions.py:478-501 rhf, 658-692 uhf):
-//   k_green_s   one CTA per walker, thread p <-> orbital p: S_s = C_s^T W_s (FP32) into a
-//               scratch buffer, plus the walker operand of the exp_h1 products;
-//   k_green_inv one warp per walker: in-place Gauss-Jordan with partial pivoting on S_s in
-//               registers (lane r <-> row r), the determinant as the FP64 signed product of
-//               the pivots (over both spins; squared for restricted walkers), S_s^-1 back to
-//               the scratch buffer (or the determinant alone);
-//   k_green_g   one CTA per walker, thread p: G_s[:, p] = (W_s S_s^-1)^T[:, p] (FP32), the
-//               per-walker power-of-two scale, the 16-bit operands and ene1 = sum G * rot_h1.
-// ======================================================================================
-
 constexpr int kGreenMaxO = 32;
 
 // dst[map(e)] = src[e] for e < n by a block of NT threads, 8 independent loads in flight per
@@ -83,57 +70,124 @@ __device__ __forceinline__ void copy_batched(T* dst, const T* __restrict__ src, 
   }
 }
 
-// Row stride (complex elements) of the walker copy in k_green_s: a multiple of 4 columns
+// Row stride (complex elements) of the walker copy in k_green_fused: a multiple of 4 columns
 // rounded so that stride / 2 is odd (16-byte aligned rows; the row-per-thread reads of the
 // operand packing then hit each shared-memory bank at most twice per half warp).
 __host__ __device__ constexpr int green_s_ld(int o) {
   return ((((o + 3) & ~3) >> 1) & 1) ? ((o + 3) & ~3) : ((o + 3) & ~3) + 2;
 }
 
-__global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2* __restrict__ wu,
-                                                 const float2* __restrict__ wd,
-                                                 float2* __restrict__ sbuf, int write_ops) {
+// ======================================================================================
+// Green's function, overlap and operands in one kernel, one CTA (NT = 128 or 256 threads)
+// per walker (wavefunctions.py:478-501 rhf, 658-692 uhf). Per slab: the walker and trial
+// copied to shared memory; S = C^T W (FP32, the orbital sum split over the NT / 128 thread
+// groups); Gauss-Jordan with partial pivoting on S, double-buffered in shared memory with one
+// barrier per pivot, thread (row group g = warp, column c = lane) updating rows g, g + NW, ..
+// of column c (NW warps); the determinant as the FP64 signed product of the pivots (squared
+// for restricted walkers); then, with kGreenG, G = (W S^-1)^T, its power-of-two scale, the
+// 16-bit operands and ene1 = sum G * rot_h1, with thread (p = tid % 128, h = tid / 128) on
+// orbital p and share h of the occupied columns.
+// kGreenWT also writes the walker operand of the exp_h1 products.
+// Pivoting is implicit, as in a row-per-lane register version: no rows move; the pivot of
+// step j is the unused row with the largest |re| + |im| in column j (ties to the lower row).
+// The working matrix ends as P^T S^-1 P^T for the pivot order P: its row r is row step(r)
+// of S^-1 and its column c is column piv(c); det(S) = sign(P) * prod(pivots).
+// ======================================================================================
+
+constexpr int kGreenWT = 1, kGreenG = 2;
+constexpr int kGfThreads = 128;  // threads per walker CTA (128 or 256; 128 measured faster)
+
+__host__ __device__ constexpr size_t green_fused_smem(int n, int omax, int om, int gtot, bool g) {
+  return (((size_t)n * green_s_ld(omax) * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15) +
+         (size_t)om * kGreenMaxO * 8 + (g ? (size_t)gtot * n * 8 : 0);
+}
+
+// dst[(e / o) * ld + e % o] = src[e] for e < n * o, 8 loads in flight per thread, the row and
+// column advanced incrementally (no division per element)
+template <int NT>
+__device__ __forceinline__ void copy_rows(float2* dst, const float2* __restrict__ src, int n, int o, int ld) {
+  const int total = n * o, dq = NT / o, dr = NT - dq * o;
+  int p = threadIdx.x / o, k = threadIdx.x - p * o;
+  for (int base = threadIdx.x; base < total; base += 8 * NT) {
+    float2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * NT;
+      if (e < total) v[u] = src[e];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * NT;
+      if (e < total) dst[p * ld + k] = v[u];
+      p += dq;
+      k += dr;
+      if (k >= o) {
+        k -= o;
+        ++p;
+      }
+    }
+  }
+}
+
+template <int OM, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md, const float2* __restrict__ wu,
+                                                               const float2* __restrict__ wd,
+                                                               double2* __restrict__ ovl, int flags) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const int w = blockIdx.x, tid = threadIdx.x, n = md.n;
+  constexpr int NW = NT / 32, NH = NT / 128;  // warps; thread groups of 128 (orbital rows)
+  constexpr int RPT = (OM + NW - 1) / NW;     // rows of S per thread in the Gauss-Jordan phase
+  const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = md.n;
+  const int p = tid & 127, h = tid >> 7;
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
   const int ldmax = green_s_ld(omax);
-  float2* Ws = reinterpret_cast<float2*>(sm);                   // [n][ld] (columns >= o zero)
+  const bool do_g = (flags & kGreenG) != 0;
+  const int gtot = md.o_blk[0] + md.o_blk[1];
+  float2* Ws = reinterpret_cast<float2*>(sm);                    // [n][ld] (columns >= o zero)
   float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * ldmax);  // [n][o]
+  float2* Si = reinterpret_cast<float2*>(
+      sm + (((size_t)n * ldmax * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15));  // [OM][kGreenMaxO]
+  float2* Gs = Si + OM * kGreenMaxO;                             // [gtot][n]
+  __shared__ float2 Ssh[2][OM][OM + 1];  // S (partials), then the double-buffered working matrix
+  __shared__ float2 pivv[OM];
+  __shared__ int piv_s[OM], step_s[OM];
+  __shared__ float2 e1w[NW], e1l[NW];
+  __shared__ float fred[NW];
   const bool bf = md.bf16 != 0;
+  const bool prow_ok = p < n;
+  double2 det = c2(1.0, 0.0);  // thread 0
   for (int s = 0; s < md.nslab; ++s) {
     const int o = md.o_slab[s], o4 = (o + 3) & ~3, ld = green_s_ld(o);
     const float2* W = (s == 0 ? wu : wd) + (size_t)w * n * o;
-    const float* C = md.trial32[s];
-    // coalesced copies; W rows padded to a multiple of 4 columns for 16-byte loads
     if (o4 != o)
-      for (int e = tid; e < n * (o4 - o); e += 128) {
-        const int pp = e / (o4 - o), k = o + e - pp * (o4 - o);
-        Ws[pp * ld + k] = make_float2(0.f, 0.f);
-      }
-    copy_batched<128>(Ws, W, n * o, [o, ld](int e) { return (e / o) * ld + e % o; });
-    copy_batched<128>(Cs, C, n * o, [](int e) { return e; });
+      for (int pp = tid; pp < n; pp += NT)
+        for (int k = o; k < o4; ++k) Ws[pp * ld + k] = make_float2(0.f, 0.f);
+    copy_rows<NT>(Ws, W, n, o, ld);
+    copy_batched<NT>(Cs, md.trial32[s], n * o, [](int e) { return e; });
     __syncthreads();
-    if (write_ops && tid < n) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
-      uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + tid;
-      uint16_t* lo = md.wt[s][1] + (size_t)w * md.R[s] * md.nk + tid;
-      for (int k = 0; k < o; ++k) {
-        const float2 v = Ws[tid * ld + k];
-        uint16_t h, l;
-        split16(v.x, bf, h, l);
-        hi[(size_t)(2 * k) * md.nk] = h;
+    if ((flags & kGreenWT) && prow_ok) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
+      uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + p;
+      uint16_t* lo = md.wt[s][1] + (size_t)w * md.R[s] * md.nk + p;
+      for (int k = h; k < o; k += NH) {
+        const float2 v = Ws[p * ld + k];
+        uint16_t hh, l;
+        split16(v.x, bf, hh, l);
+        hi[(size_t)(2 * k) * md.nk] = hh;
         lo[(size_t)(2 * k) * md.nk] = l;
-        split16(v.y, bf, h, l);
-        hi[(size_t)(2 * k + 1) * md.nk] = h;
+        split16(v.y, bf, hh, l);
+        hi[(size_t)(2 * k + 1) * md.nk] = hh;
         lo[(size_t)(2 * k + 1) * md.nk] = l;
       }
     }
-    // S[i][k..k+3] = sum_p C[p][i] W[p][k..k+3]
-    float2* S = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
-    const int nk4 = o4 / 4;
-    for (int e = tid; e < o * nk4; e += 128) {
-      const int i = e / nk4, k0 = (e - i * nk4) * 4;
+    // S[i][k..k+3] = sum_p C[p][i] W[p][k..k+3], orbitals split in two halves (partials in
+    // Ssh[0] and Ssh[1], then summed)
+    const int nk4 = o4 / 4, nh = (n + NH - 1) / NH;
+    for (int e = tid; e < NH * o * nk4; e += NT) {
+      const int hh = e / (o * nk4), e2 = e - hh * o * nk4;
+      const int i = e2 / nk4, k0 = (e2 - i * nk4) * 4;
       float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
-      for (int pp = 0; pp < n; ++pp) {
+      const int p1 = hh + 1 == NH ? n : (hh + 1) * nh;
+#pragma unroll 4
+      for (int pp = hh * nh; pp < p1; ++pp) {
         const float cv = Cs[pp * o + i];
         const float4 x = *reinterpret_cast<const float4*>(&Ws[pp * ld + k0]);
         const float4 y = *reinterpret_cast<const float4*>(&Ws[pp * ld + k0 + 2]);
@@ -142,129 +196,107 @@ __global__ void __launch_bounds__(128) k_green_s(const MixedDev md, const float2
         a2.x = fmaf(cv, y.x, a2.x); a2.y = fmaf(cv, y.y, a2.y);
         a3.x = fmaf(cv, y.z, a3.x); a3.y = fmaf(cv, y.w, a3.y);
       }
-      float2* Si = S + i * kGreenMaxO + k0;
-      Si[0] = a0;
-      if (k0 + 1 < o) Si[1] = a1;
-      if (k0 + 2 < o) Si[2] = a2;
-      if (k0 + 3 < o) Si[3] = a3;
+      float2* Sr = &Ssh[hh][i][k0];
+      Sr[0] = a0;
+      if (k0 + 1 < o) Sr[1] = a1;
+      if (k0 + 2 < o) Sr[2] = a2;
+      if (k0 + 3 < o) Sr[3] = a3;
     }
     __syncthreads();
-  }
-}
-
-// Gauss-Jordan with partial pivoting, one warp per walker, lane r <-> row r of S in
-// registers. Pivoting is implicit: no rows move; the pivot of step j is the unused row with
-// the largest |re| + |im| in column j (one __reduce_max_sync over a key that orders by that
-// magnitude, ties to the lower row), broadcast to the other lanes. With rows left in place
-// the working matrix ends as P^T S^-1 P^T for the pivot order P, so row r is written to row
-// step(r) and its column c to column piv(c); det(S) = sign(P) * prod(pivots).
-template <int OM>
-__global__ void __launch_bounds__(256) k_green_inv(const MixedDev md, float2* __restrict__ sbuf,
-                                                   double2* __restrict__ ovl, int write_inv) {
-  __shared__ int piv_sm[8][32];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int w = blockIdx.x * 8 + wib;
-  if (w >= md.nw) return;
-  int* piv = piv_sm[wib];
-  double2 det = c2(1.0, 0.0);
-  for (int s = 0; s < md.nslab; ++s) {
-    const int o = md.o_slab[s];
-    float2* S = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
-    float2 a[OM];
+    if (NH == 2) {
+      if (lane < o) {
 #pragma unroll
-    for (int c = 0; c < OM; ++c)
-      a[c] = (lane < o && c < o) ? S[lane * kGreenMaxO + c] : make_float2(0.f, 0.f);
-    bool used = lane >= o;
-    int my_step = -1;
+        for (int m = 0; m < RPT; ++m) {
+          const int r = warp + NW * m;
+          if (r < o) Ssh[0][r][lane] = cadd(Ssh[0][r][lane], Ssh[1][r][lane]);
+        }
+      }
+      __syncthreads();
+    }
+    // Gauss-Jordan, double-buffered in shared memory: step j reads Ssh[j & 1] and writes
+    // Ssh[(j & 1) ^ 1], so one barrier per pivot; thread (warp, lane) updates rows
+    // warp, warp + 8, .. of column lane.
+    bool used = lane >= o;  // row `lane` already pivoted (the same in every warp)
 #pragma unroll 1
     for (int j = 0; j < o; ++j) {
-      float2 aj = make_float2(0.f, 0.f);  // a[j], selected without dynamic register indexing
+      const int b = j & 1;
+      // loads that do not depend on the pivot first: column j (search), own elements, and
+      // the column-j factors of the own rows
+      const float2 v = lane < o ? Ssh[b][lane][j] : make_float2(0.f, 0.f);
+      float2 own[RPT], fj[RPT];
 #pragma unroll
-      for (int c = 0; c < OM; ++c)
-        if (c == j) aj = a[c];
-      const float mag = fabsf(aj.x) + fabsf(aj.y);
+      for (int m = 0; m < RPT; ++m) {
+        const int r = warp + NW * m;
+        own[m] = (r < o && lane < o) ? Ssh[b][r][lane] : make_float2(0.f, 0.f);
+        fj[m] = r < o ? Ssh[b][r][j] : make_float2(0.f, 0.f);
+      }
+      const float mag = fabsf(v.x) + fabsf(v.y);
       const unsigned key = used ? 0u : ((__float_as_uint(mag) & ~31u) | (unsigned)(31 - lane));
       const int pr = 31 - (int)(__reduce_max_sync(0xffffffffu, key) & 31u);
-      if (lane == pr) {
-        used = true;
-        my_step = j;
-      }
-      if (lane == 0) piv[j] = pr;
-      float2 rowp[OM];
+      if (lane == pr) used = true;
+      const float2 pv = Ssh[b][pr][j];
+      const float2 ap = lane < o ? Ssh[b][pr][lane] : make_float2(0.f, 0.f);
+      // 1 / pv = conj(pv) / |pv|^2 with pv scaled by a power of two first (no overflow)
+      int ex;
+      frexpf(fmaxf(fabsf(pv.x), fabsf(pv.y)), &ex);
+      const float px = ldexpf(pv.x, -ex), py = ldexpf(pv.y, -ex);
+      const float dd = ldexpf(__frcp_rn(fmaf(px, px, py * py)), -ex);
+      const float2 inv = make_float2(px * dd, -py * dd);
+      if (lane < o) {
+        const float2 sp = (lane == j) ? inv : cmul(ap, inv);
 #pragma unroll
-      for (int c = 0; c < OM; ++c) {
-        rowp[c].x = __shfl_sync(0xffffffffu, a[c].x, pr);
-        rowp[c].y = __shfl_sync(0xffffffffu, a[c].y, pr);
-      }
-      const float2 pv = make_float2(__shfl_sync(0xffffffffu, aj.x, pr), __shfl_sync(0xffffffffu, aj.y, pr));
-      if (lane == 0) det = cmul(det, c2((double)pv.x, (double)pv.y));
-      const float2 inv = cdiv(make_float2(1.f, 0.f), pv);
-      if (write_inv) {
-#pragma unroll
-        for (int c = 0; c < OM; ++c) rowp[c] = (c == j) ? inv : cmul(rowp[c], inv);
-        if (lane == pr) {
-#pragma unroll
-          for (int c = 0; c < OM; ++c) a[c] = rowp[c];
-        } else {
-#pragma unroll
-          for (int c = 0; c < OM; ++c) a[c] = csub((c == j) ? make_float2(0.f, 0.f) : a[c], cmul(aj, rowp[c]));
+        for (int m = 0; m < RPT; ++m) {
+          const int r = warp + NW * m;
+          if (r < o)
+            Ssh[b ^ 1][r][lane] =
+                (r == pr) ? sp : csub((lane == j) ? make_float2(0.f, 0.f) : own[m], cmul(fj[m], sp));
         }
-      } else if (!used) {  // determinant only: eliminate below the pivots
-        const float2 f = cmul(aj, inv);
+      }
+      if (tid == 0) {
+        pivv[j] = pv;
+        piv_s[j] = pr;
+        step_s[pr] = j;
+      }
+      __syncthreads();
+    }
+    const int fbuf = o & 1;  // buffer holding the final working matrix
+    if (warp == 0) {  // det: FP64 product of the pivots (a shuffle tree), sign of the pivot order
+      int cnt = 0;
+      double2 pd = c2(1.0, 0.0);
+      if (lane < o) {
+        for (int y = lane + 1; y < o; ++y) cnt += piv_s[lane] > piv_s[y] ? 1 : 0;
+        pd = c2((double)pivv[lane].x, (double)pivv[lane].y);
+      }
+      cnt = __reduce_add_sync(0xffffffffu, cnt);
 #pragma unroll
-        for (int c = 0; c < OM; ++c)
-          if (c > j) a[c] = csub(a[c], cmul(f, rowp[c]));
+      for (int off = 16; off > 0; off >>= 1)
+        pd = cmul(pd, c2(__shfl_xor_sync(0xffffffffu, pd.x, off), __shfl_xor_sync(0xffffffffu, pd.y, off)));
+      if (lane == 0) det = cmul(det, (cnt & 1) ? c2(-pd.x, -pd.y) : pd);
+    }
+    if (!do_g) {
+      __syncthreads();  // the next slab rewrites Ws, Cs and Ssh
+      continue;
+    }
+    if (lane < o) {
+#pragma unroll
+      for (int m = 0; m < RPT; ++m) {
+        const int r = warp + NW * m;
+        if (r < o) Si[step_s[r] * kGreenMaxO + piv_s[lane]] = Ssh[fbuf][r][lane];
       }
     }
-    __syncwarp();
-    if (lane == 0) {  // sign of the pivot order: parity of its inversions
-      int inv_count = 0;
-      for (int x = 0; x < o; ++x)
-        for (int y = x + 1; y < o; ++y) inv_count += piv[x] > piv[y] ? 1 : 0;
-      if (inv_count & 1) det = c2(-det.x, -det.y);
-    }
-    if (write_inv && lane < o) {
-#pragma unroll
-      for (int c = 0; c < OM; ++c)
-        if (c < o) S[my_step * kGreenMaxO + piv[c]] = a[c];
-    }
-    __syncwarp();
-  }
-  if (lane == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
-}
-
-__global__ void __launch_bounds__(128) k_green_g(const MixedDev md, const float2* __restrict__ wu,
-                                                 const float2* __restrict__ wd,
-                                                 const float2* __restrict__ sbuf) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = md.n;
-  const int gtot = md.o_blk[0] + md.o_blk[1];
-  float2* Gs = reinterpret_cast<float2*>(sm);                 // [gtot][n]
-  float2* Si = Gs + (((size_t)gtot * n + 1) & ~(size_t)1);     // [kGreenMaxO][kGreenMaxO], 16-B aligned
-  float2* Wsm = Si + kGreenMaxO * kGreenMaxO;                  // [n][o] walker slab
-  __shared__ double red[32];
-  __shared__ float fred[4];
-  const bool bf = md.bf16 != 0;
-  const bool prow = tid < n;
-  for (int s = 0; s < md.nslab; ++s) {
-    const int o = md.o_slab[s];
-    const float2* Ssrc = sbuf + ((size_t)s * md.nw + w) * kGreenMaxO * kGreenMaxO;
-    // the o rows of S^-1 (row stride kGreenMaxO) and the walker slab
-    copy_batched<128>(Si, Ssrc, o * kGreenMaxO, [](int e) { return e; });
-    const float2* Wg = (s == 0 ? wu : wd) + (size_t)w * n * o;
-    copy_batched<128>(Wsm, Wg, n * o, [](int e) { return e; });
     __syncthreads();
-    if (prow) {
-      float2 wr[kGreenMaxO];
+    if (prow_ok) {
+      float2 wr[OM];
 #pragma unroll
-      for (int k = 0; k < kGreenMaxO; ++k) wr[k] = (k < o) ? Wsm[tid * o + k] : make_float2(0.f, 0.f);
+      for (int k = 0; k < OM; ++k) wr[k] = (k < o) ? Ws[p * ld + k] : make_float2(0.f, 0.f);
       const int b = md.nblk == 2 ? s : 0;
       float2* Gb = Gs + (size_t)(b == 0 ? 0 : md.o_blk[0]) * n;
-      // four columns i at a time: independent accumulation chains, 16-byte reads of S^-1
-      for (int i0 = 0; i0 < o; i0 += 4) {
+      // four columns i at a time (this half's groups): independent accumulation chains,
+      // 16-byte reads of S^-1
+      for (int i0 = 4 * h; i0 < o; i0 += 4 * NH) {
         float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
 #pragma unroll
-        for (int k = 0; k < kGreenMaxO; ++k) {
+        for (int k = 0; k < OM; ++k) {
           if (k < o) {
             const float4 s01 = *reinterpret_cast<const float4*>(&Si[k * kGreenMaxO + i0]);
             const float4 s23 = *reinterpret_cast<const float4*>(&Si[k * kGreenMaxO + i0 + 2]);
@@ -280,55 +312,82 @@ __global__ void __launch_bounds__(128) k_green_g(const MixedDev md, const float2
           const int i = i0 + u;
           if (i < o) {
             float2 acc = av[u];
-            if (md.nblk == 1 && s == 1) acc = cadd(acc, Gb[(size_t)i * n + tid]);  // RHF two slabs
-            Gb[(size_t)i * n + tid] = acc;
+            if (md.nblk == 1 && s == 1) acc = cadd(acc, Gb[(size_t)i * n + p]);  // RHF two slabs
+            Gb[(size_t)i * n + p] = acc;
           }
         }
       }
     }
-    __syncthreads();
+    __syncthreads();  // Ws, Cs, Ssh and Si are rewritten by the next slab
   }
+  if (tid == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
+  if (!do_g) return;
   float mx = 0.f;
-  if (prow)
-    for (int i = 0; i < gtot; ++i) {
-      const float2 g = Gs[(size_t)i * n + tid];
+  if (prow_ok)
+    for (int i = h; i < gtot; i += NH) {
+      const float2 g = Gs[(size_t)i * n + p];
       mx = fmaxf(mx, fmaxf(fabsf(g.x), fabsf(g.y)));
     }
   for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
   if (lane == 0) fred[warp] = mx;
   __syncthreads();
-  const float scl = pow2_scale(fmaxf(fmaxf(fred[0], fred[1]), fmaxf(fred[2], fred[3])));
+  float mall = fred[0];
+#pragma unroll
+  for (int q = 1; q < NW; ++q) mall = fmaxf(mall, fred[q]);
+  const float scl = pow2_scale(mall);
   if (tid == 0) md.g_inv[w] = 1.0f / scl;
-  double e1x = 0.0, e1y = 0.0;
-  if (prow) {
-    for (int i = 0; i < gtot; ++i) {
-      const float2 g = Gs[(size_t)i * n + tid];
-      const int e = i * n + tid;
-      uint16_t h, l;
-      split16(g.x * scl, bf, h, l);
-      md.g_fb[0][(size_t)(2 * w) * md.ldfb + e] = h;
+  float e1x = 0.f, e1y = 0.f;  // per-thread partials of <= 32 terms; FP64 across warps
+  if (prow_ok) {
+    for (int i = h; i < gtot; i += NH) {
+      const float2 g = Gs[(size_t)i * n + p];
+      const int e = i * n + p;
+      uint16_t hh, l;
+      split16(g.x * scl, bf, hh, l);
+      md.g_fb[0][(size_t)(2 * w) * md.ldfb + e] = hh;
       md.g_fb[1][(size_t)(2 * w) * md.ldfb + e] = l;
-      split16(g.y * scl, bf, h, l);
-      md.g_fb[0][(size_t)(2 * w + 1) * md.ldfb + e] = h;
+      split16(g.y * scl, bf, hh, l);
+      md.g_fb[0][(size_t)(2 * w + 1) * md.ldfb + e] = hh;
       md.g_fb[1][(size_t)(2 * w + 1) * md.ldfb + e] = l;
       const int b = (md.nblk == 2 && i >= md.o_blk[0]) ? 1 : 0;
       const int eb = e - b * md.o_blk[0] * n;
       if (md.nblk == 2) {  // per-block operand (exchange / Coulomb of each spin separately)
-        split16(g.x * scl, bf, h, l);
-        md.g_blk[b][0][(size_t)(2 * w) * md.ldkb[b] + eb] = h;
+        split16(g.x * scl, bf, hh, l);
+        md.g_blk[b][0][(size_t)(2 * w) * md.ldkb[b] + eb] = hh;
         md.g_blk[b][1][(size_t)(2 * w) * md.ldkb[b] + eb] = l;
-        split16(g.y * scl, bf, h, l);
-        md.g_blk[b][0][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = h;
+        split16(g.y * scl, bf, hh, l);
+        md.g_blk[b][0][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = hh;
         md.g_blk[b][1][(size_t)(2 * w + 1) * md.ldkb[b] + eb] = l;
       }
       const float r1 = md.rh1_32[b][eb];
-      e1x += (double)(g.x * r1);
-      e1y += (double)(g.y * r1);
+      e1x = fmaf(g.x, r1, e1x);
+      e1y = fmaf(g.y, r1, e1y);
     }
   }
-  e1x = block_sum(e1x, red);
-  e1y = block_sum(e1y, red);
-  if (tid == 0) md.ene1[w] = c2(e1x, e1y);
+  // warp sums as unevaluated float pairs (hi + lo, Knuth's TwoSum at every level)
+  float lx = 0.f, ly = 0.f;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float ox = __shfl_xor_sync(0xffffffffu, e1x, off), oy = __shfl_xor_sync(0xffffffffu, e1y, off);
+    const float olx = __shfl_xor_sync(0xffffffffu, lx, off), oly = __shfl_xor_sync(0xffffffffu, ly, off);
+    float sx = e1x + ox, bx = sx - e1x;
+    lx += olx + ((e1x - (sx - bx)) + (ox - bx));
+    e1x = sx;
+    float sy = e1y + oy, by = sy - e1y;
+    ly += oly + ((e1y - (sy - by)) + (oy - by));
+    e1y = sy;
+  }
+  if (lane == 0) {
+    e1w[warp] = make_float2(e1x, e1y);
+    e1l[warp] = make_float2(lx, ly);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double2 t = c2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < NW; ++q)
+      t = c2(t.x + ((double)e1w[q].x + (double)e1l[q].x), t.y + ((double)e1w[q].y + (double)e1l[q].y));
+    md.ene1[w] = t;
+  }
 }
 
 // ======================================================================================

@@ -547,7 +547,7 @@ struct Plan {
   size_t o_rc_fb[2], o_rc_inv, o_lop[2], o_eop[2][2], o_u[2][2], o_rcb[2][2], o_rcb_inv[2], o_utmp;
   size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gblk[2][2];
   size_t o_fbpart;
-  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_sbuf, o_trial32[2], o_rh1[2];
+  size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_trial32[2], o_rh1[2];
 };
 
 int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
@@ -658,7 +658,6 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   P->o_exc = L.take((size_t)t.nw * (t.mt_z[0] + t.mt_z[1]) * 16);
   P->o_status = L.take(256);
   P->o_amax = L.take(256);
-  P->o_sbuf = L.take((size_t)t.nslab * t.nw * 32 * 32 * 8);
   for (int s = 0; s < 2; ++s) P->o_trial32[s] = L.take((size_t)t.n * 64 * 4);
   for (int b = 0; b < 2; ++b) P->o_rh1[b] = L.take((size_t)t.n * 64 * 4);
   P->total = L.off + 1024;
@@ -747,7 +746,6 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   t.c_out = reinterpret_cast<double2*>(base + P.o_cout);
   t.exc_part = reinterpret_cast<double2*>(base + P.o_exc);
   t.status = reinterpret_cast<int*>(base + P.o_status);
-  t.sbuf = reinterpret_cast<float2*>(base + P.o_sbuf);
   for (int s = 0; s < 2; ++s) {
     t.trial32[s] = reinterpret_cast<float*>(base + P.o_trial32[s]);
     t.rh1_32[s] = reinterpret_cast<float*>(base + P.o_rh1[s]);
@@ -899,54 +897,37 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
 }
 
 template <int OM>
-static void launch_green_inv(const MixedDev& md, float2* sbuf, double2* ovl, bool inv, cudaStream_t st) {
-  k_green_inv<OM><<<(md.nw + 7) / 8, 256, 0, st>>>(md, sbuf, ovl, inv ? 1 : 0);
+static void launch_green_fused(const MixedDev& md, size_t smem, const float2* w0, const float2* w1, double2* ovl,
+                               int flags, cudaStream_t st) {
+  cudaFuncSetAttribute(k_green_fused<OM, kGfThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_green_fused<OM, kGfThreads><<<md.nw, kGfThreads, smem, st>>>(md, w0, w1, ovl, flags);
 }
 
 int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl, bool write_ops,
-             cudaStream_t st, bool keep_inverse) {
+             cudaStream_t st, bool for_propagation) {
   MixedDev md = mixed_dev(t, c);
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
   if (omax > kGreenMaxO) {
     afq_set_error("mixed precision path: at most %d electrons per spin", kGreenMaxO);
     return -2;
   }
+  if (t.n > 128) {
+    afq_set_error("mixed precision path: at most %d orbitals", 128);
+    return -2;
+  }
   const float2* w0 = static_cast<const float2*>(wu);
   const float2* w1 = static_cast<const float2*>(wd);
-  const size_t smem_s = (size_t)t.n * green_s_ld(omax) * 8 + (size_t)t.n * omax * 4;
-  cudaFuncSetAttribute(k_green_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s);
+  const int flags = (write_ops || for_propagation) ? (kGreenWT | kGreenG) : 0;
+  const int om = omax <= 8 ? 8 : omax <= 16 ? 16 : omax <= 24 ? 24 : 32;
+  const size_t smem = green_fused_smem(t.n, omax, om, md.o_blk[0] + md.o_blk[1], (flags & kGreenG) != 0);
   {
     ProfScope _ps(K_GREEN, st);
-    k_green_s<<<t.nw, 128, smem_s, st>>>(md, w0, w1, t.sbuf, (write_ops || keep_inverse) ? 1 : 0);
+    if (om == 8) launch_green_fused<8>(md, smem, w0, w1, ovl, flags, st);
+    else if (om == 16) launch_green_fused<16>(md, smem, w0, w1, ovl, flags, st);
+    else if (om == 24) launch_green_fused<24>(md, smem, w0, w1, ovl, flags, st);
+    else launch_green_fused<32>(md, smem, w0, w1, ovl, flags, st);
   }
-  TC_CHECK(launch_check("green_s"));
-  const bool inv = write_ops || keep_inverse;
-  {
-    ProfScope _ps(K_GREEN, st);
-    if (omax <= 8) launch_green_inv<8>(md, t.sbuf, ovl, inv, st);
-    else if (omax <= 16) launch_green_inv<16>(md, t.sbuf, ovl, inv, st);
-    else if (omax <= 24) launch_green_inv<24>(md, t.sbuf, ovl, inv, st);
-    else launch_green_inv<32>(md, t.sbuf, ovl, inv, st);
-  }
-  TC_CHECK(launch_check("green_inv"));
-  if (!write_ops) return 0;
-  return tc_green_from_inverse(t, c, wu, wd, st);
-}
-
-int tc_green_from_inverse(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd,
-                          cudaStream_t st) {
-  MixedDev md = mixed_dev(t, c);
-  const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
-  const float2* w0 = static_cast<const float2*>(wu);
-  const float2* w1 = static_cast<const float2*>(wd);
-  const size_t smem_g = (size_t)(md.o_blk[0] + md.o_blk[1]) * t.n * 8 + 8 + (size_t)kGreenMaxO * kGreenMaxO * 8 +
-                        (size_t)t.n * omax * 8;
-  cudaFuncSetAttribute(k_green_g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g);
-  {
-    ProfScope _ps(K_GREEN, st);
-    k_green_g<<<t.nw, 128, smem_g, st>>>(md, w0, w1, t.sbuf);
-  }
-  return launch_check("green_g");
+  return launch_check("green_fused");
 }
 
 static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, double2* fb_out, cudaStream_t st,

@@ -70,7 +70,6 @@ struct TcState {
   const float* trial32[2];  // [norb][o_s] trial in FP32
   const float* rh1_32[2];   // [o_b][norb] rot_h1 in FP32
   int* status;              // device word: nonzero after a pipeline timeout
-  float2* sbuf;             // [nslab][nw][32][32] overlap matrices / their inverses
   // tensor maps
   GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2], m_z[2];
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
@@ -84,13 +83,10 @@ struct TcState {
 size_t tc_workspace_bytes(const afq_ctx_dev& c, int nw_chunk, int32_t mixed_config);
 int tc_init(TcState* t, const afq_ctx_dev& c, const afq_hamiltonian& h, const double* rccat,
             int nw_chunk, int32_t mixed_config, char* ws, cudaStream_t st);
-// write_ops: S, S^-1 and the walker operand, then G and its 16-bit operands. keep_inverse
-// (without write_ops): S, the walker operand, S^-1 kept in the scratch buffer and the
-// overlap, so that a later tc_green_from_inverse on the same walkers only forms G.
+// Overlap (when ovl is not NULL); with write_ops or for_propagation also G, its 16-bit
+// operands, ene1 and the walker operand of the exp_h1 products, all in one launch.
 int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, double2* ovl,
-             bool write_ops, cudaStream_t st, bool keep_inverse = false);
-int tc_green_from_inverse(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd,
-                          cudaStream_t st);
+             bool write_ops, cudaStream_t st, bool for_propagation = false);
 int tc_force_bias(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st);
 int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st);
 int tc_field_shifts(TcState& t, const afq_ctx_dev& c, const double* fields, cudaStream_t st);
