@@ -116,10 +116,10 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
 // shared memory, acc = sum_m T_m in FP32 registers. The first `split` products use
 // V_hi T_hi + V_hi T_lo + V_lo T_hi. Writes acc as the B operand of the last exp_h1 product.
 //
-// Persistent: one CTA per SM loops over the walkers of the chunk. 8 warps: warp w reads
-// TMEM lanes 32*(w%4).. (thread <-> orbital row p) and owns the output columns of half
-// (w/4) of the walker's orbitals, so the per-product epilogue (TMEM readout, Taylor sum,
-// next B operand) is split over twice the threads. As soon as the last product's MMAs of a
+// Persistent: one CTA per SM loops over the walkers of the chunk. 4 * NT / 16 warps: warp w
+// reads TMEM lanes 32*(w%4).. (thread <-> orbital row p) and owns the 16 output columns
+// 16*(w/4).. (8 orbitals), so the per-product epilogue (TMEM readout, Taylor sum, next B
+// operand) is spread over as many warps as the columns allow. As soon as the last product's MMAs of a
 // walker have completed, the TMA loads of the next walker's V and T_0 are issued, so they
 // overlap that walker's last epilogue and its output.
 // Each K tile of V_hi T_hi, and each correction product, accumulates in its own 64-column
@@ -132,14 +132,15 @@ struct TaylorDev {
   uint16_t* acc_lo;
 };
 
-constexpr int kTaylorThreads = 256;
+constexpr int kTaylorMaxThreads = 512;  // 128 threads per 16 columns of the B operand (NT <= 64)
 
 static inline size_t taylor_smem(int nq, int NT, bool lo) {
   const int KT = 2 * nq / 64;
   return 1024 + (size_t)KT * 128 * 128 * (lo ? 2 : 1) + (size_t)KT * NT * 128 * 2 + 64;
 }
 
-__global__ void __launch_bounds__(kTaylorThreads, 1)
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
     k_taylor_tc(const __grid_constant__ CUtensorMap mv_hi, const __grid_constant__ CUtensorMap mv_lo,
                 const __grid_constant__ CUtensorMap mt_hi, const __grid_constant__ CUtensorMap mt_lo,
                 const TaylorDev td, int* status) {
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(kTaylorThreads, 1)
   uint64_t* mma_bar = bars + 1;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int q = warp & 3, half = warp >> 2;
+  const int q = warp & 3, part = warp >> 2;
   const uint32_t tcols = gemm_tmem_cols((KT + 2) * 64);
   const bool bf = td.bf16 != 0;
   const uint32_t ld_bytes = KT * VT * (has_lo ? 2 : 1) + KT * BT * 2;
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(kTaylorThreads, 1)
   const int p = q * 32 + lane;
   const bool prow = p < td.n;
   const int o2 = 2 * td.o;
-  const int c_begin = half * 32;  // this thread's 32 columns (orbitals k = c_begin/2 ..)
+  const int c_begin = part * 16;  // this thread's 16 columns (orbitals k = c_begin/2 ..)
   const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
   const uint32_t idesc = ptx::idesc_f16(128, td.NT, bf ? 1 : 0);
   const uint32_t sVh = ptx::smem_u32(Vh), sVl = ptx::smem_u32(Vl), sBh = ptx::smem_u32(Bh),
@@ -205,9 +206,9 @@ __global__ void __launch_bounds__(kTaylorThreads, 1)
   int iter = 0, prod = 0;
   for (int wl = blockIdx.x; wl < td.nwc && ok; wl += gridDim.x, ++iter) {
     if (!ptx::mbar_wait(ld_bar, iter & 1)) ok = false;
-    float acc[32];
+    float acc[16];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
+    for (int j = 0; j < 16; ++j) {
       const int r = c_begin + j;
       if (r < o2 && prow) {
         const uint32_t off = kt0 * BT + sw128(r, kc0);
@@ -253,9 +254,9 @@ __global__ void __launch_bounds__(kTaylorThreads, 1)
       const int nreg = KT + ((m <= td.split) ? 2 : 0);
       const float invm = 1.0f / (float)m;
       const bool lo_next = (m + 1) <= td.split;
-#pragma unroll
-      for (int cc = 0; cc < 32; cc += 16) {
-        const int c0 = c_begin + cc;
+      {
+        constexpr int cc = 0;
+        const int c0 = c_begin;
         if (c0 < td.NT) {
           float dd[16];
 #pragma unroll
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kTaylorThreads, 1)
       uint16_t* oh = td.acc_hi + (size_t)wg * td.R * td.nk + p;
       uint16_t* ol = td.acc_lo + (size_t)wg * td.R * td.nk + p;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
+      for (int j = 0; j < 16; ++j) {
         const int r = c_begin + j;
         if (r < o2) {
           uint16_t h, l;
@@ -1077,11 +1078,18 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
       td.acc_hi = t.acc[s][0];
       td.acc_lo = t.acc[s][1];
       const size_t smem = taylor_smem(t.nq, t.NT[s], want_lo);
-      cudaFuncSetAttribute(k_taylor_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      const int threads = 128 * ((t.NT[s] + 15) / 16);
+      if (threads > kTaylorMaxThreads) {
+        afq_set_error("Taylor kernel: B operand of %d rows (at most %d)", t.NT[s], kTaylorMaxThreads / 8);
+        return -2;
+      }
+      // the register budget follows the block size: 384 threads up to 48 rows, else 512
+      auto kfn = threads <= 384 ? k_taylor_tc<384> : k_taylor_tc<kTaylorMaxThreads>;
+      cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       {
         ProfScope _ps(K_TAYLOR, st);
-        k_taylor_tc<<<t.nwc < t.num_sms ? t.nwc : t.num_sms, kTaylorThreads, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0], t.m_t0[s][1], td,
-                                              t.status);
+        kfn<<<t.nwc < t.num_sms ? t.nwc : t.num_sms, threads, smem, st>>>(t.m_vt[s][0], t.m_vt[s][1], t.m_t0[s][0],
+                                                                          t.m_t0[s][1], td, t.status);
       }
       TC_CHECK(launch_check("taylor_tc"));
     }
