@@ -116,10 +116,10 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
 // shared memory, acc = sum_m T_m in FP32 registers. The first `split` products use
 // V_hi T_hi + V_hi T_lo + V_lo T_hi. Writes acc as the B operand of the last exp_h1 product.
 //
-// Persistent: one CTA per SM loops over the walkers of the chunk. 4 * NT / 16 warps: warp w
-// reads TMEM lanes 32*(w%4).. (thread <-> orbital row p) and owns the 16 output columns
-// 16*(w/4).. (8 orbitals), so the per-product epilogue (TMEM readout, Taylor sum, next B
-// operand) is spread over as many warps as the columns allow. As soon as the last product's MMAs of a
+// Persistent: one CTA per SM loops over the walkers of the chunk. 4 * NT / CW warps: warp w
+// reads TMEM lanes 32*(w%4).. (thread <-> orbital row p) and owns the CW output columns
+// CW*(w/4).. (CW / 2 orbitals), so the per-product epilogue (TMEM readout, Taylor sum, next
+// B operand) is spread over several warps per lane quadrant. As soon as the last product's MMAs of a
 // walker have completed, the TMA loads of the next walker's V and T_0 are issued, so they
 // overlap that walker's last epilogue and its output.
 // Each K tile of V_hi T_hi, and each correction product, accumulates in its own 64-column
@@ -132,14 +132,15 @@ struct TaylorDev {
   uint16_t* acc_lo;
 };
 
-constexpr int kTaylorMaxThreads = 512;  // 128 threads per 16 columns of the B operand (NT <= 64)
+constexpr int kTaylorCW = 16;  // B-operand columns per warp of the epilogue (8 or 16; 16 measured faster)
+constexpr int kTaylorMaxThreads = 128 * 64 / kTaylorCW;  // NT <= 64
 
 static inline size_t taylor_smem(int nq, int NT, bool lo) {
   const int KT = 2 * nq / 64;
   return 1024 + (size_t)KT * 128 * 128 * (lo ? 2 : 1) + (size_t)KT * NT * 128 * 2 + 64;
 }
 
-template <int MAXT>
+template <int MAXT, int CW>
 __global__ void __launch_bounds__(MAXT, 1)
     k_taylor_tc(const __grid_constant__ CUtensorMap mv_hi, const __grid_constant__ CUtensorMap mv_lo,
                 const __grid_constant__ CUtensorMap mt_hi, const __grid_constant__ CUtensorMap mt_lo,
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(MAXT, 1)
   const int p = q * 32 + lane;
   const bool prow = p < td.n;
   const int o2 = 2 * td.o;
-  const int c_begin = part * 16;  // this thread's 16 columns (orbitals k = c_begin/2 ..)
+  const int c_begin = part * CW;  // this thread's CW columns (orbitals k = c_begin/2 ..)
   const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
   const uint32_t idesc = ptx::idesc_f16(128, td.NT, bf ? 1 : 0);
   const uint32_t sVh = ptx::smem_u32(Vh), sVl = ptx::smem_u32(Vl), sBh = ptx::smem_u32(Bh),
@@ -206,9 +207,9 @@ __global__ void __launch_bounds__(MAXT, 1)
   int iter = 0, prod = 0;
   for (int wl = blockIdx.x; wl < td.nwc && ok; wl += gridDim.x, ++iter) {
     if (!ptx::mbar_wait(ld_bar, iter & 1)) ok = false;
-    float acc[16];
+    float acc[CW];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
+    for (int j = 0; j < CW; ++j) {
       const int r = c_begin + j;
       if (r < o2 && prow) {
         const uint32_t off = kt0 * BT + sw128(r, kc0);
@@ -258,19 +259,19 @@ __global__ void __launch_bounds__(MAXT, 1)
         constexpr int cc = 0;
         const int c0 = c_begin;
         if (c0 < td.NT) {
-          float dd[16];
+          float dd[CW];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) dd[j] = 0.f;
+          for (int j = 0; j < CW; ++j) dd[j] = 0.f;
 #pragma unroll
           for (int g0 = 0; g0 < 6; g0 += 3) {  // regions in two groups of three
             if (g0 < nreg) {
-              float v[3][16];
+              float v[3][CW];
 #pragma unroll
               for (int rg = 0; rg < 3; ++rg)
-                if (g0 + rg < nreg) ptx::tmem_ld16p(lane_base + (uint32_t)(64 * (g0 + rg) + c0), v[rg]);
+                if (g0 + rg < nreg) ptx::tmem_ldp<CW>(lane_base + (uint32_t)(64 * (g0 + rg) + c0), v[rg]);
               ptx::tmem_ld_wait();
 #pragma unroll
-              for (int j = 0; j < 16; ++j) {
+              for (int j = 0; j < CW; ++j) {
 #pragma unroll
                 for (int rg = 0; rg < 3; ++rg)
                   if (g0 + rg < nreg) dd[j] += v[rg][j];
@@ -278,13 +279,13 @@ __global__ void __launch_bounds__(MAXT, 1)
             }
           }
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < CW; ++j) {
             dd[j] = (c0 + j < o2) ? dd[j] * invm : 0.f;
             acc[cc + j] += dd[j];
           }
           if (!last && prow) {
 #pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
+            for (int kk = 0; kk < CW / 2; ++kk) {
               const int k = c0 / 2 + kk;
               if (k < td.o) {
                 const float tr = dd[2 * kk], ti = dd[2 * kk + 1];
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(MAXT, 1)
       uint16_t* oh = td.acc_hi + (size_t)wg * td.R * td.nk + p;
       uint16_t* ol = td.acc_lo + (size_t)wg * td.R * td.nk + p;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
+      for (int j = 0; j < CW; ++j) {
         const int r = c_begin + j;
         if (r < o2) {
           uint16_t h, l;
@@ -1078,13 +1079,15 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
       td.acc_hi = t.acc[s][0];
       td.acc_lo = t.acc[s][1];
       const size_t smem = taylor_smem(t.nq, t.NT[s], want_lo);
-      const int threads = 128 * ((t.NT[s] + 15) / 16);
+      // one warp per kTaylorCW columns of the B operand and TMEM lane quadrant; the register
+      // budget follows the block size
+      const int threads = 128 * ((t.NT[s] + kTaylorCW - 1) / kTaylorCW);
       if (threads > kTaylorMaxThreads) {
-        afq_set_error("Taylor kernel: B operand of %d rows (at most %d)", t.NT[s], kTaylorMaxThreads / 8);
+        afq_set_error("Taylor kernel: B operand of %d rows (at most %d)", t.NT[s], kTaylorMaxThreads * kTaylorCW / 128);
         return -2;
       }
-      // the register budget follows the block size: 384 threads up to 48 rows, else 512
-      auto kfn = threads <= 384 ? k_taylor_tc<384> : k_taylor_tc<kTaylorMaxThreads>;
+      auto kfn = threads <= kTaylorMaxThreads * 3 / 4 ? k_taylor_tc<kTaylorMaxThreads * 3 / 4, kTaylorCW>
+                                                      : k_taylor_tc<kTaylorMaxThreads, kTaylorCW>;
       cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       {
         ProfScope _ps(K_TAYLOR, st);
