@@ -37,7 +37,9 @@ constexpr int kSplitStages = 2;
 constexpr int kSplitA = 128 * 128;                      // bytes of one A plane per K tile
 constexpr int kSplitB = kSplitBN * 128;                 // bytes of one B plane per K tile
 constexpr int kSplitUnit = 2 * kSplitA + 2 * kSplitB;   // one K tile, four planes
-constexpr int kSplitSmem = 1024 + kSplitStages * kSplitUnit + 256;
+constexpr int kSplitStageRow = 80;                      // bytes per row of an epilogue staging buffer
+constexpr int kSplitStageWarp = 32 * kSplitStageRow;     // one buffer per epilogue warp
+constexpr int kSplitSmem = 1024 + kSplitStages * kSplitUnit + 256 + 8 * kSplitStageWarp;
 
 struct SplitArgs {
   int m_tiles, n_tiles, k_tiles;
@@ -51,7 +53,10 @@ struct SplitArgs {
 
 // Epi::store(params, row, col0, v, ks): row of D (global row index without a_row0), 128
 // consecutive columns col0.. in v[0..127], K range ks; columns >= N must be ignored by the
-// epilogue. With k_splits > 1 each K range produces a partial result.
+// epilogue. With k_splits > 1 each K range produces a partial result. An epilogue with
+// kWarpStore provides store_warp(params, row0, lane, col0, v, ks, stage) instead, called by
+// all 32 lanes of the warp (rows row0 + lane) with a kSplitStageWarp-byte shared-memory
+// buffer of its own.
 template <class Epi>
 __global__ void __launch_bounds__(kSplitThreads, 1)
     k_gemm_split(const __grid_constant__ SplitMaps maps, const SplitArgs g,
@@ -215,7 +220,11 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
         if (lane == 0) ptx::mbar_arrive(&accempty[a]);
       }
       if (!ok) break;
-      Epi::store(ep, m0 + q * 32 + lane, n0 + half * 128, sum, ks);
+      if constexpr (Epi::kWarpStore)
+        Epi::store_warp(ep, m0 + q * 32, lane, n0 + half * 128, sum, ks,
+                        smem + kSplitStages * kSplitUnit + 256 + (warp - 2) * kSplitStageWarp);
+      else
+        Epi::store(ep, m0 + q * 32 + lane, n0 + half * 128, sum, ks);
     }
   }
   if (!ok) atomicOr(status, 4);
@@ -229,6 +238,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
 
 // Plain epilogue for tests: D (fp32, row-major, ldd) clipped to M x N.
 struct SplitStoreF32 {
+  static constexpr bool kWarpStore = false;
   struct Params {
     float* d;
     int M, N;
@@ -244,6 +254,7 @@ struct SplitStoreF32 {
 
 // Partial results of a K-split GEMM: d[ks][row][col] (fp32, row stride ldd, split stride sst).
 struct SplitPartialF32 {
+  static constexpr bool kWarpStore = false;
   struct Params {
     float* d;
     int M, N;

@@ -610,32 +610,50 @@ struct EpiVHS {
 // The same scatter for the persistent split GEMM: row R of the chunk, 128 columns from col0.
 struct EpiVHSSplit {
   using Params = EpiVHS::Params;
-  __device__ __forceinline__ static void store(const Params& p, int R, int col0, const float* v, int) {
-    if (R >= p.rows) return;
-    const int wl = R >> 1, c = R & 1;
+  static constexpr bool kWarpStore = true;
+  // Rows R0 + lane (walker R / 2, real (even R) or imaginary part) and 128 columns col0.. of
+  // vhs, i.e. (orbital pr, q) pairs, into the Taylor operand V = [Vr | Vi] per walker. Per 32
+  // columns each lane converts its row to fp16 hi / lo and stages one plane at a time in
+  // shared memory (80-byte rows), then four lanes store each row's 64 contiguous bytes: a
+  // warp's stores cover 8 rows x 64 B instead of 32 separate 16-byte pieces.
+  __device__ __forceinline__ static void store_warp(const Params& p, int R0, int lane, int col0, const float* v, int,
+                                                    unsigned char* stage) {
+    const int R = R0 + lane;
     const bool bf = p.bf16 != 0;
-    const float scale = c == 0 ? p.sqdt : -p.sqdt;
+    const float scale = (R & 1) == 0 ? p.sqdt : -p.sqdt;
 #pragma unroll
-    for (int c0 = 0; c0 < 128; c0 += 16) {
-      const int col = col0 + c0, pr = col / p.nq, q0 = col % p.nq;
-      if (pr >= p.n) continue;
-      const size_t off = ((size_t)wl * 128 + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0;
-      uint32_t hw[8], lw[8];
+    for (int c32 = 0; c32 < 128; c32 += 32) {
+      const int col = col0 + c32, pr = col / p.nq, q0 = col % p.nq;
+      if (pr >= p.n) continue;  // warp-uniform
+      uint32_t hw[16], lw[16];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
+      for (int j = 0; j < 16; ++j) {
         uint16_t h0, l0, h1, l1;
-        split16(v[c0 + 2 * j] * scale, bf, h0, l0);
-        split16(v[c0 + 2 * j + 1] * scale, bf, h1, l1);
+        split16(v[c32 + 2 * j] * scale, bf, h0, l0);
+        split16(v[c32 + 2 * j + 1] * scale, bf, h1, l1);
         hw[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
         lw[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
       }
-      uint4* dh = reinterpret_cast<uint4*>(p.v_hi + off);
-      dh[0] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-      dh[1] = make_uint4(hw[4], hw[5], hw[6], hw[7]);
-      if (p.want_lo) {
-        uint4* dl = reinterpret_cast<uint4*>(p.v_lo + off);
-        dl[0] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-        dl[1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+#pragma unroll
+      for (int plane = 0; plane < 2; ++plane) {
+        if (plane == 1 && !p.want_lo) break;
+        const uint32_t* src = plane ? lw : hw;
+        uint4* srow = reinterpret_cast<uint4*>(stage + lane * kSplitStageRow);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) srow[u] = make_uint4(src[4 * u], src[4 * u + 1], src[4 * u + 2], src[4 * u + 3]);
+        __syncwarp();
+        uint16_t* base = plane ? p.v_lo : p.v_hi;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = lane + 32 * u, row = t >> 2, part = t & 3, Rr = R0 + row;
+          if (Rr < p.rows) {
+            const int wl = Rr >> 1, c = Rr & 1;
+            const size_t off = ((size_t)wl * 128 + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0 + part * 8;
+            *reinterpret_cast<uint4*>(base + off) =
+                *reinterpret_cast<const uint4*>(stage + row * kSplitStageRow + part * 16);
+          }
+        }
+        __syncwarp();
       }
     }
   }
