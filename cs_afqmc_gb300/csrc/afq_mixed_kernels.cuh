@@ -97,9 +97,11 @@ __host__ __device__ constexpr int green_s_ld(int o) {
 constexpr int kGreenWT = 1, kGreenG = 2;
 constexpr int kGfThreads = 128;  // threads per walker CTA (128 or 256; 128 measured faster)
 
-__host__ __device__ constexpr size_t green_fused_smem(int n, int omax, int om, int gtot, bool g) {
+// G lives in its own region when two slabs contribute to it; with one slab it overwrites the
+// walker copy once G's inputs are in registers
+__host__ __device__ constexpr size_t green_fused_smem(int n, int omax, int om, int gtot, bool g, int nslab) {
   return (((size_t)n * green_s_ld(omax) * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15) +
-         (size_t)om * kGreenMaxO * 8 + (g ? (size_t)gtot * n * 8 : 0);
+         (size_t)om * kGreenMaxO * 8 + ((g && nslab == 2) ? (size_t)gtot * n * 8 : 0);
 }
 
 // dst[(e / o) * ld + e % o] = src[e] for e < n * o, 8 loads in flight per thread, the row and
@@ -146,7 +148,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * ldmax);  // [n][o]
   float2* Si = reinterpret_cast<float2*>(
       sm + (((size_t)n * ldmax * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15));  // [OM][kGreenMaxO]
-  float2* Gs = Si + OM * kGreenMaxO;                             // [gtot][n]
+  // [gtot][n]: after the walker copy's last use when there is one slab (ld >= o = gtot)
+  float2* Gs = md.nslab == 1 ? Ws : Si + OM * kGreenMaxO;
   __shared__ float2 Ssh[2][OM][OM + 1];  // S (partials), then the double-buffered working matrix
   __shared__ float2 pivv[OM];
   __shared__ int piv_s[OM], step_s[OM];
@@ -285,10 +288,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
       }
     }
     __syncthreads();
-    if (prow_ok) {
-      float2 wr[OM];
+    float2 wr[OM];
 #pragma unroll
-      for (int k = 0; k < OM; ++k) wr[k] = (k < o) ? Ws[p * ld + k] : make_float2(0.f, 0.f);
+    for (int k = 0; k < OM; ++k) wr[k] = (prow_ok && k < o) ? Ws[p * ld + k] : make_float2(0.f, 0.f);
+    if (md.nslab == 1) __syncthreads();  // G overwrites the walker copy
+    if (prow_ok) {
       const int b = md.nblk == 2 ? s : 0;
       float2* Gb = Gs + (size_t)(b == 0 ? 0 : md.o_blk[0]) * n;
       // four columns i at a time (this half's groups): independent accumulation chains,

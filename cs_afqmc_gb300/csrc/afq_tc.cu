@@ -921,7 +921,8 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   const float2* w1 = static_cast<const float2*>(wd);
   const int flags = (write_ops || for_propagation) ? (kGreenWT | kGreenG) : 0;
   const int om = omax <= 8 ? 8 : omax <= 16 ? 16 : omax <= 24 ? 24 : 32;
-  const size_t smem = green_fused_smem(t.n, omax, om, md.o_blk[0] + md.o_blk[1], (flags & kGreenG) != 0);
+  const size_t smem =
+      green_fused_smem(t.n, omax, om, md.o_blk[0] + md.o_blk[1], (flags & kGreenG) != 0, md.nslab);
   {
     ProfScope _ps(K_GREEN, st);
     if (om == 8) launch_green_fused<8>(md, smem, w0, w1, ovl, flags, st);
