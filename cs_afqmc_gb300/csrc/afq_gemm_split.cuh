@@ -253,19 +253,37 @@ struct SplitStoreF32 {
 };
 
 // Partial results of a K-split GEMM: d[ks][row][col] (fp32, row stride ldd, split stride sst).
+// K-split partials: D_ks (fp32, row-major, ldd; partial ks at d + ks * sst), rows < M, groups
+// of 4 columns starting below N (ldd covers the last group). Per 16 columns the warp stages its 32 rows in shared memory, then four
+// lanes store each row's 64 contiguous bytes.
 struct SplitPartialF32 {
-  static constexpr bool kWarpStore = false;
+  static constexpr bool kWarpStore = true;
   struct Params {
     float* d;
     int M, N;
     long ldd, sst;
   };
-  __device__ __forceinline__ static void store(const Params& p, int row, int col0, const float* v, int ks) {
-    if (row >= p.M) return;
-    float* dst = p.d + (long)ks * p.sst + (long)row * p.ldd + col0;
+  __device__ __forceinline__ static void store_warp(const Params& p, int row0, int lane, int col0, const float* v,
+                                                    int ks, unsigned char* stage) {
+    float* base = p.d + (long)ks * p.sst;
 #pragma unroll
-    for (int j = 0; j < 128; j += 4)
-      if (col0 + j < p.N) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+    for (int c16 = 0; c16 < 128; c16 += 16) {
+      if (col0 + c16 >= p.N) break;  // warp-uniform
+      float4* srow = reinterpret_cast<float4*>(stage + lane * kSplitStageRow);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        srow[u] = make_float4(v[c16 + 4 * u], v[c16 + 4 * u + 1], v[c16 + 4 * u + 2], v[c16 + 4 * u + 3]);
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = lane + 32 * u, row = t >> 2, part = t & 3;
+        const int r = row0 + row, c = col0 + c16 + 4 * part;
+        if (r < p.M && c < p.N)
+          *reinterpret_cast<float4*>(base + (long)r * p.ldd + c) =
+              *reinterpret_cast<const float4*>(stage + row * kSplitStageRow + 16 * part);
+      }
+      __syncwarp();
+    }
   }
 };
 
