@@ -132,6 +132,9 @@ struct TaylorDev {
   uint16_t* acc_lo;
 };
 
+constexpr int kTaylorDrain = 2;  // K tiles accumulated per TMEM region of the main product
+// TMEM regions read per product: the main product's (K <= 256: at most 4 K tiles) + 2 corrections
+constexpr int kTaylorRegions = (4 + kTaylorDrain - 1) / kTaylorDrain + 2;
 constexpr int kTaylorCW = 16;  // B-operand columns per warp of the epilogue (8 or 16; 16 measured faster)
 constexpr int kTaylorMaxThreads = 128 * 64 / kTaylorCW;  // NT <= 64
 
@@ -162,7 +165,8 @@ __global__ void __launch_bounds__(MAXT, 1)
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3, part = warp >> 2;
-  const uint32_t tcols = gemm_tmem_cols((KT + 2) * 64);
+  const int KR = (KT + kTaylorDrain - 1) / kTaylorDrain;  // TMEM regions of the main product
+  const uint32_t tcols = gemm_tmem_cols((KR + 2) * 64);
   const bool bf = td.bf16 != 0;
   const uint32_t ld_bytes = KT * VT * (has_lo ? 2 : 1) + KT * BT * 2;
   bool ok = true;
@@ -235,12 +239,12 @@ __global__ void __launch_bounds__(MAXT, 1)
           const uint32_t ba = gi == 1 ? sBl : sBh;
           for (int kt = 0; kt < KT; ++kt) {
             // region: one per K tile for the main product, one per correction product
-            const uint32_t dreg = tmem + (uint32_t)(64 * (gi == 0 ? kt : KT + gi - 1));
+            const uint32_t dreg = tmem + (uint32_t)(64 * (gi == 0 ? kt / kTaylorDrain : KR + gi - 1));
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
               ptx::mma_f16(dreg, ptx::desc_kmajor_sw128(va + kt * VT + kk * 32),
                            ptx::desc_kmajor_sw128(ba + kt * BT + kk * 32), idesc,
-                           (kk > 0 || (gi > 0 && kt > 0)) ? 1u : 0u);
+                           (kk > 0 || (gi == 0 ? kt % kTaylorDrain != 0 : kt > 0)) ? 1u : 0u);
           }
         }
         ptx::mma_commit(mma_bar);
@@ -252,7 +256,7 @@ __global__ void __launch_bounds__(MAXT, 1)
       const bool last = m + 1 == td.nterms;
       // the smem operands are free once the last product's MMAs are done: fetch the next walker
       if (last && tid == 0 && wl + gridDim.x < td.nwc) issue_loads(wl + gridDim.x);
-      const int nreg = KT + ((m <= td.split) ? 2 : 0);
+      const int nreg = KR + ((m <= td.split) ? 2 : 0);
       const float invm = 1.0f / (float)m;
       const bool lo_next = (m + 1) <= td.split;
       {
@@ -263,17 +267,17 @@ __global__ void __launch_bounds__(MAXT, 1)
 #pragma unroll
           for (int j = 0; j < CW; ++j) dd[j] = 0.f;
 #pragma unroll
-          for (int g0 = 0; g0 < 6; g0 += 3) {  // regions in two groups of three
+          for (int g0 = 0; g0 < kTaylorRegions; g0 += 2) {  // regions in groups of two
             if (g0 < nreg) {
-              float v[3][CW];
+              float v[2][CW];
 #pragma unroll
-              for (int rg = 0; rg < 3; ++rg)
+              for (int rg = 0; rg < 2; ++rg)
                 if (g0 + rg < nreg) ptx::tmem_ldp<CW>(lane_base + (uint32_t)(64 * (g0 + rg) + c0), v[rg]);
               ptx::tmem_ld_wait();
 #pragma unroll
               for (int j = 0; j < CW; ++j) {
 #pragma unroll
-                for (int rg = 0; rg < 3; ++rg)
+                for (int rg = 0; rg < 2; ++rg)
                   if (g0 + rg < nreg) dd[j] += v[rg][j];
               }
             }
