@@ -28,7 +28,7 @@
 namespace afq {
 
 struct SplitMaps {
-  CUtensorMap a_hi, a_lo, b_hi, b_lo;  // A boxes 64 x 128 rows, B boxes 64 x 256 rows
+  CUtensorMap a_hi, a_lo, b_hi, b_lo;  // A boxes 64 x 128 rows, B boxes 64 x kSplitBBox rows
 };
 
 constexpr int kSplitThreads = 320;
@@ -36,6 +36,7 @@ constexpr int kSplitBN = 256;
 constexpr int kSplitStages = 2;
 constexpr int kSplitA = 128 * 128;                      // bytes of one A plane per K tile
 constexpr int kSplitB = kSplitBN * 128;                 // bytes of one B plane per K tile
+constexpr int kSplitBBox = 128;                         // rows per B TMA box (half a tile)
 constexpr int kSplitUnit = 2 * kSplitA + 2 * kSplitB;   // one K tile, four planes
 constexpr int kSplitStageRow = 80;                      // bytes per row of an epilogue staging buffer
 constexpr int kSplitStageWarp = 32 * kSplitStageRow;     // one buffer per epilogue warp
@@ -57,10 +58,15 @@ struct SplitArgs {
 // kWarpStore provides store_warp(params, row0, lane, col0, v, ks, stage) instead, called by
 // all 32 lanes of the warp (rows row0 + lane) with a kSplitStageWarp-byte shared-memory
 // buffer of its own.
-template <class Epi>
+// CL = 2: clusters of two CTAs take M tiles 2i and 2i + 1 of the same (N tile, K range); each
+// CTA loads its own A tile and one 128-row half of the B tile, multicast to both, so every
+// CTA reads half of B from L2. A stage is refilled once both CTAs' MMAs have consumed it
+// (each MMA warp's commit arrives on the empty barrier of both). Requires m_tiles % CL == 0.
+template <class Epi, int CL>
 __global__ void __launch_bounds__(kSplitThreads, 1)
     k_gemm_split(const __grid_constant__ SplitMaps maps, const SplitArgs g,
                  const __grid_constant__ typename Epi::Params ep, int* status) {
+  static_assert(CL == 1 || CL == 2, "cluster size");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -72,14 +78,17 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = g.m_tiles * g.n_tiles * g.k_splits;
+  const int rank = CL == 2 ? (int)ptx::cluster_ctarank() : 0;
+  const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;  // cluster index and count
+  const int mt = g.m_tiles / CL;                           // M tile groups
+  const int ntiles = mt * g.n_tiles * g.k_splits;
   const int kps = (g.k_tiles + g.k_splits - 1) / g.k_splits;  // K tiles per split
   const uint32_t tx_bytes = kSplitA * (g.has_alo ? 2 : 1) + kSplitB * (g.has_blo ? 2 : 1);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSplitStages; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], 1);
+      ptx::mbar_init(&empty[s], CL);
     }
     for (int a = 0; a < 2; ++a) {
       ptx::mbar_init(&accfull[a], 1);
@@ -93,7 +102,10 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     ptx::tmem_relinquish();
   }
   ptx::tc_fence_before();
-  __syncthreads();
+  if constexpr (CL == 2)
+    ptx::cluster_sync();  // barrier inits visible to the partner before its multicasts
+  else
+    __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
   bool ok = true;
@@ -105,9 +117,9 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       if (g.has_alo) ptx::prefetch_tmap(&maps.a_lo);
       if (g.has_blo) ptx::prefetch_tmap(&maps.b_lo);
       int it = 0;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int m0 = (tile % g.m_tiles) * 128, n0 = ((tile / g.m_tiles) % g.n_tiles) * kSplitBN;
-        const int ks = tile / (g.m_tiles * g.n_tiles);
+      for (int tile = cid; tile < ntiles && ok; tile += ncl) {
+        const int m0 = ((tile % mt) * CL + rank) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
+        const int ks = tile / (mt * g.n_tiles);
         const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
         for (int kt = ka; kt < kb; ++kt, ++it) {
           const int s = it % kSplitStages, r = it / kSplitStages;
@@ -119,8 +131,21 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
           ptx::mbar_expect_tx(&full[s], tx_bytes);
           ptx::tma_load_2d(u, &maps.a_hi, &full[s], kt * 64, g.a_row0 + m0);
           if (g.has_alo) ptx::tma_load_2d(u + kSplitA, &maps.a_lo, &full[s], kt * 64, g.a_row0 + m0);
-          ptx::tma_load_2d(u + 2 * kSplitA, &maps.b_hi, &full[s], kt * 64, n0);
-          if (g.has_blo) ptx::tma_load_2d(u + 2 * kSplitA + kSplitB, &maps.b_lo, &full[s], kt * 64, n0);
+          if constexpr (CL == 2) {  // this CTA's half of B, to both CTAs
+            const int hb = rank * kSplitBBox * 128;
+            ptx::tma_load_2d_mc(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, n0 + rank * kSplitBBox, 3);
+            if (g.has_blo)
+              ptx::tma_load_2d_mc(u + 2 * kSplitA + kSplitB + hb, &maps.b_lo, &full[s], kt * 64,
+                                  n0 + rank * kSplitBBox, 3);
+          } else {
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const int hb = hh * kSplitBBox * 128;
+              ptx::tma_load_2d(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, n0 + hh * kSplitBBox);
+              if (g.has_blo)
+                ptx::tma_load_2d(u + 2 * kSplitA + kSplitB + hb, &maps.b_lo, &full[s], kt * 64, n0 + hh * kSplitBBox);
+            }
+          }
         }
       }
       // never leave a copy in flight: wait for the last round issued on each stage
@@ -130,8 +155,8 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       int it = 0, grun = 0;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int ks = tile / (g.m_tiles * g.n_tiles);
+      for (int tile = cid; tile < ntiles && ok; tile += ncl) {
+        const int ks = tile / (mt * g.n_tiles);
         const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
         const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
         for (int run = 0; run < runs_per_tile && ok; ++run, ++grun) {
@@ -176,7 +201,10 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
                            g.idesc, first ? 0u : 1u);
               first = false;
             }
-            ptx::mma_commit(&empty[s]);
+            if constexpr (CL == 2)
+              ptx::mma_commit_mc(&empty[s], 3);  // the stage is free here and in the partner
+            else
+              ptx::mma_commit(&empty[s]);
           }
           ptx::mma_commit(&accfull[a]);
         }
@@ -189,9 +217,9 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     const int q = warp & 3, half = (warp - 2) >> 2;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     int grun = 0;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int m0 = (tile % g.m_tiles) * 128, n0 = ((tile / g.m_tiles) % g.n_tiles) * kSplitBN;
-      const int ks = tile / (g.m_tiles * g.n_tiles);
+    for (int tile = cid; tile < ntiles && ok; tile += ncl) {
+      const int m0 = ((tile % mt) * CL + rank) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
+      const int ks = tile / (mt * g.n_tiles);
       const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
       const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
       float sum[128];
@@ -229,7 +257,12 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   }
   if (!ok) atomicOr(status, 4);
   ptx::tc_fence_before();
-  __syncthreads();
+  // with CL == 2 neither CTA leaves while the partner may still multicast into its shared
+  // memory or arrive on its barriers
+  if constexpr (CL == 2)
+    ptx::cluster_sync();
+  else
+    __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, 512);

@@ -91,7 +91,9 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
   return launch_check("gemm_tc");
 }
 
-// persistent split-precision GEMM (afq_gemm_split.cuh): one CTA per SM, at most one per tile
+// persistent split-precision GEMM (afq_gemm_split.cuh): one CTA per SM, at most one per tile.
+// With an even number of M tiles, clusters of two CTAs share each B tile (multicast); the grid
+// is then the number of co-resident clusters (or of tile pairs, if fewer) times two.
 template <class Epi>
 static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms,
                         const typename Epi::Params& ep, int* status, cudaStream_t st) {
@@ -100,7 +102,41 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
     afq_set_error("split gemm: bad sizes");
     return -1;
   }
-  auto kfn = k_gemm_split<Epi>;
+  if (g.m_tiles % 2 == 0) {
+    auto kfn = k_gemm_split<Epi, 2>;
+    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kSplitThreads);
+    cfg.dynamicSmemBytes = kSplitSmem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(num_sms - (num_sms & 1));
+    int maxc = 0;
+    if (cudaOccupancyMaxActiveClusters(&maxc, kfn, &cfg) != cudaSuccess || maxc < 1) {
+      cudaGetLastError();
+      maxc = num_sms / 2;
+    }
+    const int pairs = ntiles / 2;
+    const int ncl = pairs < maxc ? pairs : maxc;
+    cfg.gridDim = dim3(2 * ncl);
+    cudaError_t e;
+    {
+      ProfScope _ps(cls, st);
+      e = cudaLaunchKernelEx(&cfg, kfn, maps, g, ep, status);
+    }
+    if (e != cudaSuccess) {
+      afq_set_error("gemm_split (clusters of 2): %s", cudaGetErrorString(e));
+      return (int)e;
+    }
+    return launch_check("gemm_split");
+  }
+  auto kfn = k_gemm_split<Epi, 1>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
   const int grid = ntiles < num_sms ? ntiles : num_sms;
   {
@@ -817,15 +853,15 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   {  // force-bias planes for the persistent split GEMM
     TC_CHECK(mk(&t.m_fb_split.a_hi, t.g_fb[0], 2 * t.nw, t.kfb, t.ldfb, 128));
     TC_CHECK(mk(&t.m_fb_split.a_lo, t.g_fb[1], 2 * t.nw, t.kfb, t.ldfb, 128));
-    TC_CHECK(mk(&t.m_fb_split.b_hi, t.rc_fb[0], c.nchol, t.kfb, t.ldfb, kSplitBN));
-    TC_CHECK(mk(&t.m_fb_split.b_lo, t.rc_fb[1], c.nchol, t.kfb, t.ldfb, kSplitBN));
+    TC_CHECK(mk(&t.m_fb_split.b_hi, t.rc_fb[0], c.nchol, t.kfb, t.ldfb, kSplitBBox));
+    TC_CHECK(mk(&t.m_fb_split.b_lo, t.rc_fb[1], c.nchol, t.kfb, t.ldfb, kSplitBBox));
   }
   {  // vhs planes for the persistent split GEMM (B boxes of 256 rows)
     const uint64_t nrows = (uint64_t)t.n * t.nq;
     TC_CHECK(mk(&t.m_vhs_split.a_hi, t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
     TC_CHECK(mk(&t.m_vhs_split.a_lo, t.xt[1], 2 * t.nw, c.nchol, t.ldg, 128));
-    TC_CHECK(mk(&t.m_vhs_split.b_hi, t.lop[0], nrows, c.nchol, t.ldg, kSplitBN));
-    TC_CHECK(mk(&t.m_vhs_split.b_lo, t.lop[1], nrows, c.nchol, t.ldg, kSplitBN));
+    TC_CHECK(mk(&t.m_vhs_split.b_hi, t.lop[0], nrows, c.nchol, t.ldg, kSplitBBox));
+    TC_CHECK(mk(&t.m_vhs_split.b_lo, t.lop[1], nrows, c.nchol, t.ldg, kSplitBBox));
     int dev = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&t.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || t.num_sms < 1)
@@ -1173,8 +1209,8 @@ extern "C" int afq_test_gemm_split(const void* a_hi, const void* a_lo, const voi
   memset(&maps, 0, sizeof(maps));
   int e = make_tmap_16(&maps.a_hi, a_hi, M, K, lda, 128, bf16 != 0);
   if (!e && a_lo) e = make_tmap_16(&maps.a_lo, a_lo, M, K, lda, 128, bf16 != 0);
-  if (!e) e = make_tmap_16(&maps.b_hi, b_hi, N, K, ldb, kSplitBN, bf16 != 0);
-  if (!e && b_lo) e = make_tmap_16(&maps.b_lo, b_lo, N, K, ldb, kSplitBN, bf16 != 0);
+  if (!e) e = make_tmap_16(&maps.b_hi, b_hi, N, K, ldb, kSplitBBox, bf16 != 0);
+  if (!e && b_lo) e = make_tmap_16(&maps.b_lo, b_lo, N, K, ldb, kSplitBBox, bf16 != 0);
   if (e) return e;
   SplitArgs g;
   g.k_tiles = (K + 63) / 64;
