@@ -540,16 +540,23 @@ __global__ void __launch_bounds__(256) k_fb_reduce(const FbReduce r) {
     }
   }
   if (r.fb_out) return;
-  // the four sums reduced together: warp shuffles, then one shared-memory pass
-  double v[4] = {(double)shx, (double)shy, (double)fbx, (double)fby};
+  // the four sums reduced together: warp shuffles on unevaluated float pairs (hi + lo,
+  // Knuth's TwoSum at every level: no FP64 on the shuffle path), then one FP64 pass over the
+  // warps in shared memory
+  float v[4] = {shx, shy, fbx, fby}, vl[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], off);
+    for (int j = 0; j < 4; ++j) {
+      const float o = __shfl_xor_sync(0xffffffffu, v[j], off), ol = __shfl_xor_sync(0xffffffffu, vl[j], off);
+      const float sum = v[j] + o, bb = sum - v[j];
+      vl[j] += ol + ((v[j] - (sum - bb)) + (o - bb));
+      v[j] = sum;
+    }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   if (lane == 0)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) red[4 * wid + j] = v[j];
+    for (int j = 0; j < 4; ++j) red[4 * wid + j] = (double)v[j] + (double)vl[j];
   __syncthreads();
   if (threadIdx.x < 4) {
     double t = 0.0;

@@ -336,11 +336,14 @@ __global__ void k_weights(int nw, double dt, double2 h0_prop, const double2* __r
     sh = cadd(sh, shift[(size_t)w * ntiles + t]);
     fb = cadd(fb, fbt[(size_t)w * ntiles + t]);
   }
-  double2 arg = c2(-sqdt * sh.x + fb.x + dt * (pcs + h0_prop.x), -sqdt * sh.y + fb.y + dt * h0_prop.y);
-  double2 imp = cmul(cexp_(arg), ratio);
-  double2 ph = cmul(cexp_(c2(-sqdt * sh.x, -sqdt * sh.y)), ratio);
-  double theta = atan2(ph.y, ph.x);
-  double v = hypot(imp.x, imp.y) * cos(theta);
+  // |I| cos(angle(ph)) with I = exp(arg) O'/O and ph = exp(-sqrt(dt) shift) O'/O equals
+  // exp(Re arg) Re(exp(i Im(-sqrt(dt) shift)) O'/O): one exp and one sincos instead of two
+  // complex exponentials, atan2, hypot and cos (the same quantity; FP64 transcendentals are
+  // slow on this part)
+  const double re_arg = -sqdt * sh.x + fb.x + dt * (pcs + h0_prop.x);
+  double sn, cs;
+  sincos(-sqdt * sh.y, &sn, &cs);
+  double v = exp(re_arg) * (cs * ratio.x - sn * ratio.y);
   if (isnan(v)) v = 0.0;
   if (v < 1.0e-3) v = 0.0;
   if (v > 100.0) v = 0.0;
@@ -895,8 +898,9 @@ int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fb
                    cudaStream_t st) {
   {
     ProfScope _ps(K_WEIGHTS, st);
-    k_weights<<<(c.nw + 31) / 32, 32, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt,
-                                               ntiles, ovl_new, ovl, weights, scalars);
+    // FP64 transcendentals per walker: 8 walkers per CTA spread them over the SMs' FP64 units
+    k_weights<<<(c.nw + 7) / 8, 8, 0, st>>>(c.nw, c.dt, c2(c.h0_prop_re, c.h0_prop_im), shift, fbt, ntiles,
+                                            ovl_new, ovl, weights, scalars);
   }
   {
     ProfScope _ps(K_WEIGHTS, st);
