@@ -675,13 +675,39 @@ struct EpiVHSSplit {
 // LAPACK Householder factorisation (zgeqr2) and explicit Q (zung2r), one warp per slab with
 // the slab in shared memory (row stride k | 1: conflict-free column walks) and only
 // warp-level synchronisation. Column sums (the reflector applied to the trailing columns)
-// are owned by lane = column; the rank-1 updates by lane = row. The squared norm below
-// the diagonal is accumulated in FP64, as in the block-per-walker kernel.
+// are owned by lanes per column (qr_colsum); the rank-1 updates by lane = row. The squared
+// norm below the diagonal is accumulated as a float pair.
 // ======================================================================================
 
 constexpr int kQrWarps = 4;
 
 __host__ __device__ constexpr int qr_ld(int k) { return k | 1; }
+
+// y[c] = sum_{r >= j} conj(A[r][c]) A[r][j] for c in (j, k) by one warp: lpc = the largest
+// power of two with lpc * (k - j - 1) <= 32 lanes per column, each summing every lpc-th row,
+// combined by shuffles (the rows of a column are the serial part otherwise).
+__device__ __forceinline__ void qr_colsum(const float2* A, int ld, int m, int k, int j, int lane, float2* y) {
+  const int nc = k - j - 1;
+  if (nc <= 0) return;
+  int lpc = 1;
+  while (lpc * 2 * nc <= 32) lpc *= 2;
+  const int col = j + 1 + lane / lpc, part = lane % lpc;
+  const bool active = lane < lpc * nc;
+  float yx = 0.f, yy = 0.f;
+  if (active) {
+#pragma unroll 4
+    for (int r = j + part; r < m; r += lpc) {
+      const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
+      yx += pr.x;
+      yy += pr.y;
+    }
+  }
+  for (int off = 1; off < lpc; off <<= 1) {  // lpc is warp-uniform
+    yx += __shfl_xor_sync(0xffffffffu, yx, off);
+    yy += __shfl_xor_sync(0xffffffffu, yy, off);
+  }
+  if (active && part == 0) y[col] = make_float2(yx, yy);
+}
 
 __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k, float2* __restrict__ wbase) {
   extern __shared__ __align__(16) unsigned char qsm_raw[];
@@ -700,11 +726,22 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
   __syncwarp();
   // ---- factorisation
   for (int j = 0; j < k; ++j) {
-    double xnd = 0.0;
-    for (int r = j + 1 + lane; r < m; r += 32) xnd += (double)cabs2(A[r * ld + j]);
-    xnd = warp_sum(xnd);
+    // squared norm below the diagonal as an unevaluated float pair (TwoSum per term and per
+    // shuffle level): FP64-class accuracy without the FP64 pipe
+    float xh = 0.f, xl = 0.f;
+    for (int r = j + 1 + lane; r < m; r += 32) {
+      const float a2 = cabs2(A[r * ld + j]), sum = xh + a2, bb = sum - xh;
+      xl += (xh - (sum - bb)) + (a2 - bb);
+      xh = sum;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const float o = __shfl_xor_sync(0xffffffffu, xh, off), ol = __shfl_xor_sync(0xffffffffu, xl, off);
+      const float sum = xh + o, bb = sum - xh;
+      xl += ol + ((xh - (sum - bb)) + (o - bb));
+      xh = sum;
+    }
     const float2 alpha = A[j * ld + j];
-    const float xn = (float)xnd;
+    const float xn = xh + xl;
     float2 t, scl, beta;
     if (xn == 0.f && alpha.y == 0.f) {
       t = make_float2(0.f, 0.f);
@@ -724,17 +761,7 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
       tau[j] = t;
     }
     __syncwarp();
-    const int col = j + 1 + lane;
-    if (col < k) {
-      float yx = 0.f, yy = 0.f;
-#pragma unroll 8
-      for (int r = j; r < m; ++r) {
-        const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
-        yx += pr.x;
-        yy += pr.y;
-      }
-      y[col] = make_float2(yx, yy);
-    }
+    qr_colsum(A, ld, m, k, j, lane, y);
     __syncwarp();
     const float2 ct = make_float2(t.x, -t.y);
     for (int r = j + lane; r < m; r += 32) {
@@ -753,17 +780,7 @@ __global__ void __launch_bounds__(32 * kQrWarps) k_qr_warp(int nw, int m, int k,
     if (j < k - 1) {
       if (lane == 0) A[j * ld + j] = make_float2(1.f, 0.f);
       __syncwarp();
-      const int col = j + 1 + lane;
-      if (col < k) {
-        float yx = 0.f, yy = 0.f;
-#pragma unroll 8
-        for (int r = j; r < m; ++r) {
-          const float2 pr = cmulc(A[r * ld + col], A[r * ld + j]);
-          yx += pr.x;
-          yy += pr.y;
-        }
-        y[col] = make_float2(yx, yy);
-      }
+      qr_colsum(A, ld, m, k, j, lane, y);
       __syncwarp();
       for (int r = j + lane; r < m; r += 32) {
         const float2 v = A[r * ld + j];
