@@ -45,6 +45,7 @@ struct afq_ctx {
   void* wcopy;
   int32_t* sr_idx;
   double* cum;
+  double2* free_scr;  // free projection: spin constants and QR norm factors [4][nw]
   afq::TcState tc;  // tensor-core (mixed precision) operands and plans
   // Inside afq_propagate_phaseless only (mixed path): 1 when the operand buffers already
   // hold G, its operands and the walker operand of the current walkers, else 0.
@@ -63,7 +64,7 @@ struct Layout {
 };
 
 struct Sizes {
-  size_t green, fb, xt, shift, fbt, vhs, ovl_new, ene, epart, rccat, wcopy, sr_idx, cum, tc, total;
+  size_t green, fb, xt, shift, fbt, vhs, ovl_new, ene, epart, rccat, wcopy, sr_idx, cum, free_scr, tc, total;
 };
 
 int derive(const afq_dims* d, afq_ctx_dev* c, int* nw_chunk, int* e_chunks, int* e_gchunk,
@@ -152,6 +153,7 @@ Sizes sizes_for(const afq_dims* d, const afq_ctx_dev& c, int nw_chunk, int e_chu
   s.wcopy = L->take(nw * c.norb * (c.kslab[0] + c.kslab[1]) * welem);
   s.sr_idx = L->take(nw * sizeof(int32_t));
   s.cum = L->take(nw * sizeof(double));
+  s.free_scr = L->take(4 * nw * C16);
   s.tc = L->take(d->precision == AFQ_PREC_MIXED ? afq::tc_workspace_bytes(c, nw_chunk, d->mixed_config)
                                                 : 256);
   s.total = L->off;
@@ -254,6 +256,45 @@ int sr_impl(afq_ctx* c, afq_walker_state* s, const double* zeta, int32_t* indice
     cudaError_t e = cudaMemcpyAsync(indices, c->sr_idx, sizeof(int32_t) * c->dev.nw,
                                     cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) { afq_set_error("sr index copy: %s", cudaGetErrorString(e)); return (int)e; }
+  }
+  return 0;
+}
+
+// One free-projection step (propagation.py:436-462), FP64 unrestricted walkers.
+int free_step(afq_ctx* c, afq_walker_state* s, const double* fields, double ene0, double2* norms, double2* normed,
+              cudaStream_t st) {
+  const afq_ctx_dev& d = c->dev;
+  double2* consts = c->free_scr;
+  double2* rdiag = c->free_scr + 2 * (size_t)d.nw;
+  double2* ovl = reinterpret_cast<double2*>(s->overlaps);
+  CHECK(afq::launch_free_prep(d, fields, ene0, c->xt, consts, st));
+  const int nb = d.nw / c->nw_chunk;
+  const long nn = (long)d.norb * d.norb;
+  for (int b = 0; b < nb; ++b) {
+    const int w0 = b * c->nw_chunk;
+    CHECK(afq::launch_gemm_cr(true, c->nw_chunk, d.norb * d.norb, d.nchol, c->xt + (size_t)w0 * d.nchol, d.nchol,
+                              c->h.chol, nn, c->vhs, nn, c2(0.0, sqrt(d.dt)), st));
+    CHECK(afq::launch_taylor_f64<double>(d, w0, c->nw_chunk, c->vhs, s->walkers_up, s->walkers_dn, st));
+  }
+  CHECK(afq::launch_free_scale(d, consts, s->walkers_up, s->walkers_dn, st));
+  CHECK(afq::launch_qr<double>(d, s->walkers_up, s->walkers_dn, st, rdiag));
+  CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, ovl, false, st));
+  CHECK(afq::launch_free_finish(d.nw, rdiag, norms, ovl, st));
+  // normed overlaps: the walkers through the QR once more, on a copy
+  const size_t e0 = (size_t)d.nw * d.norb * d.kslab[0], e1 = (size_t)d.nw * d.norb * d.kslab[1];
+  double2* cu = static_cast<double2*>(c->wcopy);
+  double2* cd = cu + e0;
+  cudaError_t e = cudaMemcpyAsync(cu, s->walkers_up, e0 * sizeof(double2), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cd, s->walkers_dn, e1 * sizeof(double2), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) { afq_set_error("walker copy: %s", cudaGetErrorString(e)); return (int)e; }
+  CHECK(afq::launch_qr<double>(d, cu, cd, st));
+  return green(c, cu, cd, nullptr, normed, false, st);
+}
+
+int check_free(const afq_ctx* c) {
+  if (!is_fp64(c) || c->dev.nslab != 2) {
+    afq_set_error("free projection needs an FP64 context with unrestricted walkers");
+    return -1;
   }
   return 0;
 }
@@ -403,6 +444,7 @@ int afq_ctx_create(const afq_dims* dims, const afq_hamiltonian* ham, void* works
   c->wcopy = ws + sz.wcopy;
   c->sr_idx = reinterpret_cast<int32_t*>(ws + sz.sr_idx);
   c->cum = reinterpret_cast<double*>(ws + sz.cum);
+  c->free_scr = reinterpret_cast<double2*>(ws + sz.free_scr);
   cudaStream_t st = S(stream);
   if (uhf) {
     // rccat[g] = [rot_chol_up[g] | rot_chol_dn[g]]
@@ -624,6 +666,42 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
   CHECK(afq::launch_phaseless_end(blk, (double)n_sr_blocks * n_ene_blocks * d.nw, block_energy, block_weight,
                                   state->scalars, energy, st));
   return afq::t_launch_end(blk, block_energy, block_weight, t, nullptr, denergy, st);
+}
+
+int afq_propagate_free(afq_ctx* ctx, afq_walker_state* state, const double* fields, double ene0, double* norms,
+                       double* normed_overlaps, void* stream) {
+  if (!ctx || !fields || !norms || !normed_overlaps) { afq_set_error("NULL argument"); return -1; }
+  CHECK(check_state(ctx, state));
+  CHECK(check_free(ctx));
+  return free_step(ctx, state, fields, ene0, reinterpret_cast<double2*>(norms),
+                   reinterpret_cast<double2*>(normed_overlaps), S(stream));
+}
+
+int afq_propagate_free_blocks(afq_ctx* ctx, afq_walker_state* state, const double* fields, int32_t n_prop_steps,
+                              int32_t n_blocks, double ene0, double* norms, double* normed_overlaps,
+                              double* block_energy, double* block_weight, void* stream) {
+  if (!ctx || !fields || !norms || !normed_overlaps || !block_energy || !block_weight) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (n_prop_steps < 1 || n_blocks < 1) { afq_set_error("block counts must be >= 1"); return -1; }
+  CHECK(check_state(ctx, state));
+  CHECK(check_free(ctx));
+  cudaStream_t st = S(stream);
+  const afq_ctx_dev& d = ctx->dev;
+  double2* ovl = reinterpret_cast<double2*>(state->overlaps);
+  CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+  const size_t step_elems = (size_t)d.nw * d.nchol;
+  for (int b = 0; b < n_blocks; ++b) {
+    for (int p = 0; p < n_prop_steps; ++p)
+      CHECK(free_step(ctx, state, fields + ((size_t)b * n_prop_steps + p) * step_elems, ene0,
+                      reinterpret_cast<double2*>(norms), reinterpret_cast<double2*>(normed_overlaps), st));
+    CHECK(green(ctx, state->walkers_up, state->walkers_dn, ctx->green, nullptr, true, st));
+    CHECK(energy_from_green(ctx, ctx->ene, st));
+    CHECK(afq::launch_free_block_stats(d.nw, ctx->ene, ovl, reinterpret_cast<double2*>(block_energy) + b,
+                                       reinterpret_cast<double2*>(block_weight) + b, st));
+  }
+  return 0;
 }
 
 int afq_field_block(afq_ctx* ctx, afq_walker_state* state, const double* fields, int32_t n_prop_steps,

@@ -39,8 +39,9 @@ int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fb
                    cudaStream_t st);
 int launch_energy_f64(const afq_ctx_dev& c, int nchunks, int gchunk, const double2* green,
                       double2* epart, double2* energy, cudaStream_t st);
+// rdiag (optional, [nslab][nw] complex): prod(diag R) per walker slab
 template <typename WT>
-int launch_qr(const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st);
+int launch_qr(const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st, double2* rdiag = nullptr);
 template <typename WT>
 int launch_sr(const afq_ctx_dev& c, const double* zeta, double* weights, double* cum, int32_t* idx,
               void* wu, void* wd, void* wcopy, cudaStream_t st);
@@ -55,6 +56,13 @@ int launch_phaseless_end(int nblk, double denom, const double* be, const double*
                          double* scalars, double* energy, cudaStream_t st);
 int launch_driver_update(const afq_ctx_dev& c, const double* weights, const double* energy,
                          double* scalars, double* wsum, cudaStream_t st);
+// free projection (afq_free.cu)
+int launch_free_prep(const afq_ctx_dev& c, const double* fields, double ene0, double2* xt, double2* consts,
+                     cudaStream_t st);
+int launch_free_scale(const afq_ctx_dev& c, const double2* consts, void* wu, void* wd, cudaStream_t st);
+int launch_free_finish(int nw, const double2* rdiag, double2* norms, double2* ovl, cudaStream_t st);
+int launch_free_block_stats(int nw, const double2* energy, const double2* ovl, double2* be, double2* bw,
+                            cudaStream_t st);
 int launch_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t st);
 int launch_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t st);
 }  // namespace afq

@@ -497,9 +497,11 @@ AFQ_D float warp_sumf(float v) {
 AFQ_D double warp_sum_t(double v) { return warp_sum(v); }
 AFQ_D float warp_sum_t(float v) { return warp_sumf(v); }
 
+// rdiag (optional, [nslab][nw]): prod(diag R) per walker slab (linalg_utils.py:51-65 returns
+// it as the norm factor; the free-projection step multiplies its norms by it)
 template <typename WT>
 __global__ void __launch_bounds__(256) k_qr_householder(const afq_ctx_dev c, WT* __restrict__ w_up,
-                                                        WT* __restrict__ w_dn) {
+                                                        WT* __restrict__ w_dn, double2* __restrict__ rdiag) {
   using CT = typename CplxOf<WT>::type;  // compute in the storage precision
   using R = typename QrT<CT>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -514,6 +516,7 @@ __global__ void __launch_bounds__(256) k_qr_householder(const afq_ctx_dev c, WT*
   __shared__ CT sc_sh, beta_sh;
   CT* W = reinterpret_cast<CT*>(s == 0 ? w_up : w_dn) + (size_t)wlk * m * k;
   for (int i = tid; i < m * k; i += nt) A[i] = W[i];
+  double2 rprod = c2(1.0, 0.0);  // thread 0
   __syncthreads();
   // ---- factorisation
   for (int j = 0; j < k; ++j) {
@@ -562,9 +565,13 @@ __global__ void __launch_bounds__(256) k_qr_householder(const afq_ctx_dev c, WT*
       }
     }
     __syncthreads();
-    if (tid == 0) A[j * k + j] = beta_sh;
+    if (tid == 0) {
+      A[j * k + j] = beta_sh;
+      rprod = cmul(rprod, c2((double)beta_sh.x, (double)beta_sh.y));
+    }
     __syncthreads();
   }
+  if (tid == 0 && rdiag) rdiag[(size_t)s * c.nw + wlk] = rprod;
   // ---- form Q (zung2r): columns from last to first
   for (int j = k - 1; j >= 0; --j) {
     if (j < k - 1) {
@@ -927,13 +934,13 @@ int launch_energy_f64(const afq_ctx_dev& c, int nchunks, int gchunk, const doubl
 }
 
 template <typename WT>
-int launch_qr(const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
+int launch_qr(const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st, double2* rdiag) {
   size_t smem = ((size_t)c.norb * c.kmax + 2 * c.kmax) * sizeof(typename CplxOf<WT>::type);
   auto kfn = k_qr_householder<WT>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   {
     ProfScope _ps(K_QR, st);
-    kfn<<<dim3(c.nw, c.nslab), 256, smem, st>>>(c, (WT*)wu, (WT*)wd);
+    kfn<<<dim3(c.nw, c.nslab), 256, smem, st>>>(c, (WT*)wu, (WT*)wd, rdiag);
   }
   return launch_err("qr_householder");
 }
@@ -1045,8 +1052,8 @@ template int launch_green<double>(const afq_ctx_dev&, const void*, const void*, 
 template int launch_green<float>(const afq_ctx_dev&, const void*, const void*, double2*, double2*, bool, cudaStream_t);
 template int launch_taylor_f64<double>(const afq_ctx_dev&, int, int, const double2*, void*, void*, cudaStream_t);
 template int launch_taylor_f64<float>(const afq_ctx_dev&, int, int, const double2*, void*, void*, cudaStream_t);
-template int launch_qr<double>(const afq_ctx_dev&, void*, void*, cudaStream_t);
-template int launch_qr<float>(const afq_ctx_dev&, void*, void*, cudaStream_t);
+template int launch_qr<double>(const afq_ctx_dev&, void*, void*, cudaStream_t, double2*);
+template int launch_qr<float>(const afq_ctx_dev&, void*, void*, cudaStream_t, double2*);
 template int launch_sr<double>(const afq_ctx_dev&, const double*, double*, double*, int32_t*, void*, void*, void*, cudaStream_t);
 template int launch_sr<float>(const afq_ctx_dev&, const double*, double*, double*, int32_t*, void*, void*, void*, cudaStream_t);
 

@@ -154,6 +154,11 @@ class propagator_restricted:
         _lib.call("afq_propagate", eng.ctx, ctypes.byref(st), f.data_ptr(), stream_ptr())
         return prop_data
 
+    def propagate_free(self, trial, ham_data: dict, prop_data: PropData, fields,
+                       wave_data: dict) -> PropData:
+        """Free projection is defined for unrestricted walkers only (propagation.py:166-188)."""
+        raise NotImplementedError("Free projection not implemented for this propagator.")
+
     def orthonormalize_walkers(self, prop_data: PropData, trial=None, ham_data=None,
                                wave_data=None) -> PropData:
         """Q of the reduced QR of every walker (propagation.py:251-253, 422-424)."""
@@ -240,12 +245,55 @@ class propagator_unrestricted(propagator_restricted):
         return torch.stack([torch.linalg.matrix_exp(-self.dt * (h1[0] - v0 - v1) / 2.0),
                             torch.linalg.matrix_exp(-self.dt * (h1[1] - v0 - v1) / 2.0)]).contiguous()
 
+    def _build_propagation_intermediates(self, ham_data: dict, trial, wave_data: dict) -> dict:
+        """Also the free-projection intermediates mf_shifts_fp and h0_prop_fp
+        (propagation.py:473-486)."""
+        ham_data = super()._build_propagation_intermediates(ham_data, trial, wave_data)
+        mf = ham_data["mf_shifts"]
+        n_up, n_dn = trial.nelec
+        ham_data["mf_shifts_fp"] = torch.stack([mf / n_up / 2.0, mf / n_dn / 2.0])
+        h0p = ham_data["h0_prop"] + float(np.real(_engine._scalar(ham_data.get("ene0", 0.0))))
+        ham_data["h0_prop_fp"] = [h0p / n_up / 2.0, h0p / n_dn / 2.0]
+        return ham_data
+
+    def propagate_free(self, trial, ham_data: dict, prop_data: PropData, fields,
+                       wave_data: dict) -> PropData:
+        """One free-projection step with unshifted fields [nw, nchol] (propagation.py:436-462):
+        updates walkers, prop_data["norms"], ["overlaps"] (overlap * norms) and
+        ["normed_overlaps"]. FP64 (complex128) walkers."""
+        eng = self._engine(trial, ham_data, wave_data, prop_data["walkers"])
+        f = as_dev(fields)
+        if tuple(f.shape) != (eng.nw, eng.nchol):
+            raise _lib.AfqError(f"fields must be [{eng.nw}, {eng.nchol}], got {tuple(f.shape)}")
+        dict.__setitem__(prop_data, "_engine", eng)
+        norms, normed = _free_state(prop_data, eng.nw)
+        st = prop_data.state(eng)
+        ene0 = float(np.real(_engine._scalar(ham_data.get("ene0", 0.0))))
+        _lib.call("afq_propagate_free", eng.ctx, ctypes.byref(st), f.data_ptr(), ene0, norms.data_ptr(),
+                  normed.data_ptr(), stream_ptr())
+        return prop_data
+
     def _exp_h1_tangent(self, h1, v0, v1, dh1):
         return torch.stack([expm_frechet(-self.dt * (h1[s] - v0 - v1) / 2.0, -self.dt * dh1[s] / 2.0)
                             for s in range(2)]).contiguous()
 
     def __hash__(self) -> int:
         return super().__hash__()
+
+
+def _free_state(prop_data: PropData, nw: int):
+    """prop_data["norms"] and ["normed_overlaps"] as complex128 device tensors of their own
+    (init_prop_data starts normed_overlaps as the overlaps themselves)."""
+    out = []
+    for key in ("norms", "normed_overlaps"):
+        t = prop_data.get(key)
+        t = torch.ones(nw, dtype=torch.complex128, device=device()) if t is None else as_dev(t, torch.complex128)
+        if key == "normed_overlaps" and t.data_ptr() == prop_data["overlaps"].data_ptr():
+            t = t.clone()
+        t = t.contiguous()
+        dict.__setitem__(prop_data, key, t)
+        out.append(t)
+    return out
 
 
 def expm_frechet(a: torch.Tensor, da: torch.Tensor) -> torch.Tensor:

@@ -19,7 +19,7 @@ from typing import Optional
 import torch
 
 from . import _lib
-from ._engine import _CACHE_KEY, as_dev, device, stream_ptr
+from ._engine import _CACHE_KEY, _scalar, as_dev, device, stream_ptr
 from .propagation import PropData, RngKey
 from .wavefunctions import _sym
 
@@ -95,6 +95,35 @@ class sampler:
         dict.__setitem__(prop_data, "block_energies", be)
         dict.__setitem__(prop_data, "block_weights", bw)
         return energy[0], prop_data
+
+    def propagate_free(self, ham, ham_data: dict, prop, prop_data: PropData, trial, wave_data: dict,
+                       fields: Optional[torch.Tensor] = None):
+        """n_blocks free-projection blocks of n_prop_steps steps (sampling.py:95-124, 344-360),
+        unrestricted FP64 walkers. fields: [n_blocks, n_prop_steps, nw, nchol] or drawn from
+        prop_data["key"]. Returns (prop_data, block_energy, block_weight, key) with complex128
+        CUDA tensors [n_blocks]; prop_data is the final state (the reference returns the
+        per-block trajectory)."""
+        from .propagation import _free_state
+        eng = prop._engine(trial, ham_data, wave_data, prop_data["walkers"])
+        dict.__setitem__(prop_data, "_engine", eng)
+        want = (self.n_blocks, self.n_prop_steps, eng.nw, eng.nchol)
+        if fields is None:
+            f = torch.empty(want, dtype=torch.float64, device=device())
+            key: RngKey = prop_data["key"]
+            _lib.call("afq_fill_normal", f.data_ptr(), f.numel(), key.seed, key.take(f.numel()), stream_ptr())
+        else:
+            f = as_dev(fields)
+        if f.numel() != self.n_blocks * self.n_prop_steps * eng.nw * eng.nchol:
+            raise _lib.AfqError(f"fields must have shape {want}")
+        norms, normed = _free_state(prop_data, eng.nw)
+        be = torch.empty(self.n_blocks, dtype=torch.complex128, device=device())
+        bw = torch.empty(self.n_blocks, dtype=torch.complex128, device=device())
+        st = prop_data.state(eng)
+        ene0 = float(complex(_scalar(ham_data.get("ene0", 0.0))).real)
+        _lib.call("afq_propagate_free_blocks", eng.ctx, ctypes.byref(st), f.data_ptr(), self.n_prop_steps,
+                  self.n_blocks, ene0, norms.data_ptr(), normed.data_ptr(), be.data_ptr(), bw.data_ptr(),
+                  stream_ptr())
+        return prop_data, be, bw, prop_data.get("key")
 
     def propagate_phaseless_ad_norot(self, ham, ham_data: dict, coupling: float, observable_op,
                                      prop, prop_data: PropData, trial, wave_data: dict,

@@ -184,6 +184,29 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
 int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, const double* zeta,
                   double* block_weight, void* stream);
 
+/* ---- free projection (FP64, unrestricted walkers) ------------------------------------ */
+
+/* One free-projection step with unshifted fields (float64 [nw, nchol]): no force bias, no
+ * phaseless constraint. Each slab s times exp(-sqrt(dt) sum_g x_g mf_g / (2 n_s))
+ * exp(dt (h0_prop + ene0) / (2 n_s)) after exp(vhs) between the exp_h1 half steps; QR of both
+ * slabs with norms (complex128 [nw]) *= prod(diag R_up) prod(diag R_dn); state->overlaps =
+ * overlap of the new walkers * norms; normed_overlaps (complex128 [nw]) = overlap of the walkers
+ * QR-ed once more. Replaces propagator_unrestricted.propagate_free (propagation.py:436-462,
+ * intermediates 464-490). Weights and scalars are not used. */
+int afq_propagate_free(afq_ctx* ctx, afq_walker_state* state, const double* fields, double ene0,
+                       double* norms, double* normed_overlaps, void* stream);
+
+/* n_blocks free-projection blocks of n_prop_steps steps (fields float64
+ * [n_blocks, n_prop_steps, nw, nchol]), starting from state->overlaps = overlap(walkers):
+ * after each block the complex local energies E and block_energy[b] = sum E O / sum O,
+ * block_weight[b] = sum O (complex128 [n_blocks], O = state->overlaps). Replaces
+ * sampler.propagate_free / _block_scan_free (sampling.py:95-124, 344-360); the per-block
+ * prop_data trajectory the reference returns is not kept. */
+int afq_propagate_free_blocks(afq_ctx* ctx, afq_walker_state* state, const double* fields,
+                              int32_t n_prop_steps, int32_t n_blocks, double ene0, double* norms,
+                              double* normed_overlaps, double* block_energy,
+                              double* block_weight, void* stream);
+
 /* ---- forward-mode derivative of the block (differentiation pattern, FP64) ------------ */
 
 /* Bytes of device tangent workspace afq_propagate_phaseless_jvp needs. 0 on bad sizes. */

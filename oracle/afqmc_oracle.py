@@ -348,6 +348,33 @@ class Propagator:
         prop_data["overlaps"] = overlaps_new
         return prop_data
 
+    def propagate_free(self, trial: Trial, ham_data: dict, prop_data: dict, fields: np.ndarray, mo,
+                       ene0: float = 0.0):
+        """One free-projection step, unrestricted walkers (propagation.py:436-462, intermediates
+        464-490): no force bias; shift_term_s = sum_g x_g mf_g / (2 n_s); each slab times
+        exp(-sqrt(dt) shift_term_s) exp(dt (h0_prop + ene0) / (2 n_s)); QR of both slabs with
+        norms *= prod(diag R_up) prod(diag R_dn); overlaps = overlap(walkers) * norms;
+        normed_overlaps = overlap of the walkers QR-ed once more."""
+        dt, sdt = self.dt, math.sqrt(self.dt)
+        nel = trial.nelec
+        mf = ham_data["mf_shifts"]
+        s = fields @ mf  # [nw]
+        h0p = ham_data["h0_prop"] + ene0
+        consts = [np.exp(-sdt * s / (2.0 * nel[i])) * np.exp(dt * h0p / (2.0 * nel[i])) for i in range(2)]
+        w = apply_trotprop(ham_data, prop_data["walkers"], fields.astype(np.complex128), dt, trial.norb,
+                           self.n_exp_terms)
+        w = [consts[0][:, None, None] * w[0], consts[1][:, None, None] * w[1]]
+        qs, norms = [], np.ones(fields.shape[0], dtype=np.complex128)
+        for x in w:
+            q, r = np.linalg.qr(x)
+            qs.append(q)
+            norms = norms * np.prod(np.diagonal(r, axis1=1, axis2=2), axis=1)
+        prop_data["walkers"] = qs
+        prop_data["norms"] = prop_data["norms"] * norms
+        prop_data["overlaps"] = trial.overlap(qs, mo) * prop_data["norms"]
+        prop_data["normed_overlaps"] = trial.overlap([np.linalg.qr(x)[0] for x in qs], mo)
+        return prop_data
+
     def orthonormalize_walkers(self, prop_data: dict) -> dict:
         """Q of the reduced QR of each walker (propagation.py:251-253, 422-424 ->
         linalg_utils.py:51-65). LAPACK Householder convention, as jnp.linalg.qr."""
@@ -415,6 +442,26 @@ class Sampler:
         be = np.sum(e * prop_data["weights"]) / bw
         prop_data["pop_control_ene_shift"] = 0.9 * prop_data["pop_control_ene_shift"] + 0.1 * be
         return prop_data, be, bw
+
+    def block_scan_free(self, prop, trial, ham_data, prop_data, mo, fields, ene0=0.0):
+        """fields [n_prop_steps, nw, G] (sampling.py:95-124): free steps, then the complex
+        local energies and block_energy = sum E O / sum O, block_weight = sum O."""
+        for st in range(self.n_prop_steps):
+            prop_data = prop.propagate_free(trial, ham_data, prop_data, fields[st], mo, ene0)
+        e = trial.energy(prop_data["walkers"], ham_data, mo)
+        o = prop_data["overlaps"]
+        return prop_data, np.sum(e * o) / np.sum(o), np.sum(o)
+
+    def propagate_free(self, prop, trial, ham_data, prop_data, mo, fields, ene0=0.0):
+        """n_blocks free-projection blocks (sampling.py:344-360); fields
+        [n_blocks, n_prop_steps, nw, G]. Returns (prop_data, block_energy, block_weight)."""
+        prop_data["overlaps"] = trial.overlap(prop_data["walkers"], mo)
+        be, bw = [], []
+        for b in range(fields.shape[0]):
+            prop_data, e, wt = self.block_scan_free(prop, trial, ham_data, prop_data, mo, fields[b], ene0)
+            be.append(e)
+            bw.append(wt)
+        return prop_data, np.array(be), np.array(bw)
 
     def propagate_phaseless(self, prop, trial, ham_data, prop_data, mo, fields, zetas, do_sr=True):
         """fields [n_sr_blocks, n_ene_blocks, n_prop_steps, nw, G]; zetas [n_sr_blocks]

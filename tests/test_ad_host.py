@@ -73,3 +73,26 @@ def test_oracle_fd_converges(kind, restricted):
     z = O.phaseless_derivative_fd(samp, prop, trial, ham, 0 * D, s.rdm1, s.mo_coeff, pd, fields, zetas,
                                   restricted, h=1e-3)
     assert z[1] == 0.0 and z[0] == a[0]
+
+
+def test_oracle_free_projection_norm_bookkeeping():
+    """After free steps, overlap(Q) * norms equals the overlap of the walkers propagated without
+    any QR (the norms carry exactly what the orthonormalisation removed)."""
+    s, trial, ham, prop, pd = _small_system(kind="uhf", restricted=False)
+    hd = trial.build_measurement_intermediates(dict(ham), s.mo_coeff)
+    hd = O.build_propagation_intermediates(hd, s.rdm1, s.norb, s.nelec, prop.dt, False)
+    pd["norms"] = np.ones(prop.n_walkers, dtype=np.complex128)
+    raw = [w.copy() for w in pd["walkers"]]
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        f = rng.standard_normal((prop.n_walkers, s.chol.shape[0]))
+        pd = prop.propagate_free(trial, hd, pd, f, s.mo_coeff)
+        # the same step on the raw walkers, without the QR
+        sdt = np.sqrt(prop.dt)
+        sh = f @ hd["mf_shifts"]
+        raw = O.apply_trotprop(hd, raw, f.astype(np.complex128), prop.dt, s.norb, prop.n_exp_terms)
+        for i in range(2):
+            c = np.exp(-sdt * sh / (2.0 * s.nelec[i])) * np.exp(prop.dt * hd["h0_prop"] / (2.0 * s.nelec[i]))
+            raw[i] = c[:, None, None] * raw[i]
+    want = trial.overlap(raw, s.mo_coeff)
+    assert np.max(np.abs(pd["overlaps"] - want)) < 1e-10 * np.max(np.abs(want))

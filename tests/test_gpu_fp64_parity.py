@@ -165,3 +165,56 @@ def test_errors_are_loud():
     u = wavefunctions.uhf(12, (3, 3))
     with pytest.raises(_lib.AfqError):
         u.calc_overlap(case.gpu_walkers(), {"mo_coeff": [case.sys.mo_coeff, case.sys.mo_coeff]})
+
+
+FREE_CASES = [
+    dict(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=5),
+    dict(kind="rhf", restricted=False, norb=10, nelec=(4, 4), nchol=17, nw=6),
+]
+
+
+@pytest.mark.parametrize("cfg", FREE_CASES, ids=["uhf", "rhf-u"])
+def test_free_projection_steps(cfg):
+    """Free-projection steps (propagation.py:436-462) against the oracle: walkers, norms,
+    overlaps and normed overlaps on identical fields."""
+    import torch
+    case = Case(**cfg)
+    rng = np.random.default_rng(41)
+    fields = rng.standard_normal((3, case.nw, case.nchol))
+    po = case.oracle_prop_data()
+    po["norms"] = np.ones(case.nw, dtype=np.complex128)
+    pg = case.gpu_prop_data()
+    for f in fields:
+        po = case.o_prop.propagate_free(case.o_trial, case.o_ham, po, f, case.sys.mo_coeff)
+        pg = case.prop.propagate_free(case.trial, case.ham_data, pg, f, case.wave_data)
+    torch.cuda.synchronize()
+    assert rel_err(_flat(to_np(pg["walkers"])), _flat(po["walkers"])) < 1e-9
+    assert rel_err(to_np(pg["norms"]), po["norms"]) < 1e-9
+    assert rel_err(to_np(pg["overlaps"]), po["overlaps"]) < 1e-9
+    assert rel_err(to_np(pg["normed_overlaps"]), po["normed_overlaps"]) < 1e-9
+
+
+def test_free_projection_blocks():
+    """sampler.propagate_free (sampling.py:344-360): complex block energies and weights of
+    3 blocks x 2 steps against the oracle."""
+    from cs_afqmc_gb300 import sampling
+    case = Case(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=5)
+    rng = np.random.default_rng(43)
+    fields = rng.standard_normal((3, 2, case.nw, case.nchol))
+    samp_o = O.Sampler(n_prop_steps=2)
+    po = case.oracle_prop_data()
+    po["norms"] = np.ones(case.nw, dtype=np.complex128)
+    po, be_o, bw_o = samp_o.propagate_free(case.o_prop, case.o_trial, case.o_ham, po, case.sys.mo_coeff, fields)
+    samp = sampling.sampler(n_prop_steps=2, n_blocks=3)
+    pg, be, bw, _ = samp.propagate_free(case.ham, case.ham_data, case.prop, case.gpu_prop_data(), case.trial,
+                                        case.wave_data, fields=fields)
+    assert rel_err(to_np(be), be_o) < 1e-9
+    assert rel_err(to_np(bw), bw_o) < 1e-9
+    assert rel_err(to_np(pg["norms"]), po["norms"]) < 1e-9
+
+
+def test_free_projection_rejects_restricted():
+    case = Case(kind="rhf", restricted=True, norb=10, nelec=(3, 3), nchol=12, nw=4)
+    with pytest.raises(NotImplementedError):
+        case.prop.propagate_free(case.trial, case.ham_data, case.gpu_prop_data(),
+                                 np.zeros((case.nw, case.nchol)), case.wave_data)
