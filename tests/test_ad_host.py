@@ -1,6 +1,6 @@
-"""Host-side pieces of the forward-mode derivative, on the CPU: the Frechet derivative of
-expm that gives d exp_h1 / d lambda, and the oracle's finite-difference derivative of the
-blocked energy (its convergence in h)."""
+"""Host-side pieces on the CPU: the Frechet derivative of expm that gives d exp_h1 / d lambda,
+the oracle's finite-difference derivative of the blocked energy (its convergence in h), and
+the norm bookkeeping of the oracle's free-projection step."""
 
 import numpy as np
 import pytest
