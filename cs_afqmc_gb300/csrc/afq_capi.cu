@@ -749,6 +749,31 @@ int afq_block_end(afq_ctx* ctx, afq_walker_state* state, const double* energy, c
   return sr_impl(ctx, state, zeta, nullptr, st);
 }
 
+int afq_cpmc_init(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, const double* trial_up,
+                  const double* trial_dn, double* walkers_up, double* walkers_dn, double* overlaps, double* greens,
+                  void* stream) {
+  if (!trial_up || !trial_dn || !walkers_up || !walkers_dn || !overlaps || !greens) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  return afq::launch_cpmc(norb, n_up, n_dn, n_walkers, 1.0, 0.0, nullptr, nullptr, trial_up, trial_dn, walkers_up,
+                          walkers_dn, nullptr, overlaps, greens, nullptr, nullptr, 0, S(stream));
+}
+
+int afq_cpmc_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, double dt, double u,
+                       const double* exp_h1_up, const double* exp_h1_dn, const double* trial_up,
+                       const double* trial_dn, double* walkers_up, double* walkers_dn, double* weights,
+                       double* overlaps, double* greens, double* scalars, const double* gaussian, void* stream) {
+  if (!exp_h1_up || !exp_h1_dn || !trial_up || !trial_dn || !walkers_up || !walkers_dn || !weights || !overlaps ||
+      !greens || !scalars || !gaussian) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (!(dt > 0.0)) { afq_set_error("dt must be positive"); return -1; }
+  return afq::launch_cpmc(norb, n_up, n_dn, n_walkers, dt, u, exp_h1_up, exp_h1_dn, trial_up, trial_dn, walkers_up,
+                          walkers_dn, weights, overlaps, greens, scalars, gaussian, 1, S(stream));
+}
+
 int afq_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream) {
   if (!out && n > 0) { afq_set_error("NULL argument"); return -1; }
   return afq::launch_fill_normal(out, n, seed, offset, S(stream));

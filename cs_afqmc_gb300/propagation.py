@@ -307,6 +307,57 @@ def expm_frechet(a: torch.Tensor, da: torch.Tensor) -> torch.Tensor:
     return torch.linalg.matrix_exp(m)[:n, n:].contiguous()
 
 
+@dataclass
+class propagator_cpmc(propagator_unrestricted):
+    """CPMC for the Hubbard model with on-site U (propagation.py:515-657), FP64 with real
+    walkers. ham_data needs "u" and the unrestricted propagation intermediates (exp_h1);
+    the trial is wavefunctions.uhf_cpmc."""
+
+    def init_prop_data(self, trial, wave_data: dict, ham_data: dict, init_walkers=None) -> PropData:
+        """The unrestricted initial state, then real walkers and overlaps, the full Green's
+        functions and hs_constant (propagation.py:518-537)."""
+        from .wavefunctions import cpmc_overlap_green
+        pd = super().init_prop_data(trial, wave_data, ham_data, init_walkers)
+        w = [pd["walkers"][0].real.contiguous(), pd["walkers"][1].real.contiguous()]
+        dict.__setitem__(pd, "walkers", w)
+        ovl, greens = cpmc_overlap_green(trial, w, wave_data)
+        dict.__setitem__(pd, "overlaps", ovl)
+        dict.__setitem__(pd, "greens", greens)
+        u = float(np.real(_engine._scalar(ham_data["u"])))
+        gamma = math.acosh(math.exp(self.dt * u / 2))
+        c = math.exp(-self.dt * u / 2)
+        dict.__setitem__(pd, "hs_constant", torch.tensor(
+            [[c * math.exp(gamma), c * math.exp(-gamma)], [c * math.exp(-gamma), c * math.exp(gamma)]],
+            dtype=torch.float64, device=device()))
+        return pd
+
+    def propagate(self, trial, ham_data: dict, prop_data: PropData, gaussian_rns,
+                  wave_data: dict) -> PropData:
+        """One CPMC step with Gaussians [nw, norb] turned into uniforms (propagation.py:565-657)."""
+        norb, (n_up, n_dn) = trial.norb, trial.nelec
+        w = prop_data["walkers"]
+        g = as_dev(gaussian_rns).contiguous()
+        if tuple(g.shape) != (self.n_walkers, norb):
+            raise _lib.AfqError(f"gaussian_rns must be [{self.n_walkers}, {norb}], got {tuple(g.shape)}")
+        e = ham_data["exp_h1"]
+        e = e if isinstance(e, torch.Tensor) else torch.as_tensor(np.asarray(e))
+        eu, ed = as_dev(e[0]).contiguous(), as_dev(e[1]).contiguous()
+        mo = wave_data["mo_coeff"]
+        cu, cd = as_dev(mo[0]).contiguous(), as_dev(mo[1]).contiguous()
+        for t in (w[0], w[1], prop_data["weights"], prop_data["overlaps"], prop_data["greens"]):
+            if t.dtype != torch.float64 or not t.is_contiguous():
+                raise _lib.AfqError("CPMC state must be contiguous float64 (init_prop_data of this class)")
+        u = float(np.real(_engine._scalar(ham_data["u"])))
+        _lib.call("afq_cpmc_propagate", norb, n_up, n_dn, self.n_walkers, float(self.dt), u, eu.data_ptr(),
+                  ed.data_ptr(), cu.data_ptr(), cd.data_ptr(), w[0].data_ptr(), w[1].data_ptr(),
+                  prop_data["weights"].data_ptr(), prop_data["overlaps"].data_ptr(),
+                  prop_data["greens"].data_ptr(), prop_data["_scalars"].data_ptr(), g.data_ptr(), stream_ptr())
+        return prop_data
+
+    def __hash__(self) -> int:
+        return super().__hash__()
+
+
 def _any_engine(prop_data, trial, ham_data, wave_data, prop):
     """QR and SR need only sizes: reuse the engine that last propagated these walkers."""
     eng = prop_data.get("_engine") if isinstance(prop_data, dict) else None

@@ -179,3 +179,33 @@ class uhf(wave_function):
 
     def __hash__(self) -> int:
         return super().__hash__()
+
+
+@dataclass
+class uhf_cpmc(uhf):
+    """UHF trial of the CPMC propagator (wavefunctions.py:848-955): real walkers and full
+    Green's functions G_s = (W_s (C_s^T W_s)^-1 C_s^T)^T."""
+
+    kind = "uhf"
+
+    def calc_full_green_vmap(self, walkers, wave_data: dict) -> torch.Tensor:
+        """[nw, 2, norb, norb] (wavefunctions.py:894-914)."""
+        return cpmc_overlap_green(self, walkers, wave_data)[1]
+
+    def __hash__(self) -> int:
+        return super().__hash__()
+
+
+def cpmc_overlap_green(trial, walkers, wave_data: dict):
+    """(overlaps [nw] float64, greens [nw, 2, norb, norb] float64) of real walkers
+    ([nw, norb, n_up], [nw, norb, n_dn]) for a real UHF trial, on the device."""
+    wu = as_dev(walkers[0]).contiguous()
+    wd = as_dev(walkers[1]).contiguous()
+    mo = wave_data["mo_coeff"]
+    cu, cd = as_dev(mo[0]).contiguous(), as_dev(mo[1]).contiguous()
+    nw, norb = int(wu.shape[0]), trial.norb
+    ovl = torch.empty(nw, dtype=torch.float64, device=device())
+    greens = torch.empty(nw, 2, norb, norb, dtype=torch.float64, device=device())
+    _lib.call("afq_cpmc_init", norb, trial.nelec[0], trial.nelec[1], nw, cu.data_ptr(), cd.data_ptr(),
+              wu.data_ptr(), wd.data_ptr(), ovl.data_ptr(), greens.data_ptr(), stream_ptr())
+    return ovl, greens

@@ -207,6 +207,34 @@ int afq_propagate_free_blocks(afq_ctx* ctx, afq_walker_state* state, const doubl
                               double* normed_overlaps, double* block_energy,
                               double* block_weight, void* stream);
 
+/* ---- CPMC, Hubbard model with on-site U (FP64, real walkers) ------------------------- */
+
+/* Overlaps det(C_up^T W_up) det(C_dn^T W_dn) (float64 [nw]) and full Green's functions
+ * greens (float64 [nw][2][norb][norb], G_s = (W_s (C_s^T W_s)^-1 C_s^T)^T) of real walkers
+ * ([nw][norb][n_up], [nw][norb][n_dn]) for the real UHF trial C_up [norb, n_up], C_dn
+ * [norb, n_dn]: the part of propagator_cpmc.init_prop_data that needs the walkers
+ * (propagation.py:518-537, uhf_cpmc.calc_full_green wavefunctions.py:894-914). No context;
+ * norb <= 64, n_up, n_dn <= 32. */
+int afq_cpmc_init(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers,
+                  const double* trial_up, const double* trial_dn, double* walkers_up,
+                  double* walkers_dn, double* overlaps, double* greens, void* stream);
+
+/* One CPMC step (propagator_cpmc.propagate, propagation.py:565-657): exp_h1 half step with
+ * the overlap-ratio weight update (weights < 1e-8 -> 0), then for every site x a discrete
+ * Hubbard-Stratonovich field, field f chosen with probability proportional to
+ * (1 + (c_f,up - 1) G_up[x,x]) (1 + (c_f,dn - 1) G_dn[x,x]) (ratios < 1e-8 -> 0; uniforms
+ * (erf(g / sqrt 2) + 1) / 2 of gaussian [nw][norb]), c = exp(-dt u / 2) exp(+-gamma),
+ * cosh(gamma) = exp(dt u / 2); walker rows x scaled, rank-one Green's-function updates
+ * (wavefunctions.py:916-945), overlaps * ratio, weights * normalisation; exp_h1 half step;
+ * weights * exp(dt pop_control_ene_shift), > 100 -> 0; scalars[AFQ_S_POP_CONTROL_SHIFT] =
+ * e_estimate - 0.1 log(sum w / nw) / dt. exp_h1_up / exp_h1_dn: float64 [norb, norb].
+ * greens as in afq_cpmc_init, updated. */
+int afq_cpmc_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, double dt,
+                       double u, const double* exp_h1_up, const double* exp_h1_dn,
+                       const double* trial_up, const double* trial_dn, double* walkers_up,
+                       double* walkers_dn, double* weights, double* overlaps, double* greens,
+                       double* scalars, const double* gaussian, void* stream);
+
 /* ---- forward-mode derivative of the block (differentiation pattern, FP64) ------------ */
 
 /* Bytes of device tangent workspace afq_propagate_phaseless_jvp needs. 0 on bad sizes. */

@@ -405,6 +405,129 @@ class Propagator:
         return prop_data
 
 
+# ----------------------------------------------------------------------------------------
+# CPMC for the Hubbard model with on-site U (propagation.py:515-657, slow form 660-773;
+# uhf_cpmc trial wavefunctions.py:848-955)
+# ----------------------------------------------------------------------------------------
+
+
+def cpmc_full_green(walkers, mo):
+    """[nw, 2, norb, norb]: G_s = (W_s (C_s^T W_s)^-1 C_s^T)^T (wavefunctions.py:894-914)."""
+    out = []
+    for w, c in zip(walkers, mo):
+        a = w @ np.linalg.inv(np.einsum("pi,wpk->wik", c, w))
+        out.append(np.transpose(a @ c.T, (0, 2, 1)))
+    return np.stack(out, axis=1)
+
+
+def cpmc_overlap(walkers, mo):
+    return np.linalg.det(np.einsum("pi,wpk->wik", mo[0], walkers[0])) * \
+        np.linalg.det(np.einsum("pi,wpk->wik", mo[1], walkers[1]))
+
+
+def cpmc_hs_constant(dt: float, u: float) -> np.ndarray:
+    """[[up, dn] for field 0, [up, dn] for field 1] (propagation.py:532-536)."""
+    gamma = np.arccosh(np.exp(dt * u / 2))
+    const = np.exp(-dt * u / 2)
+    return const * np.array([[np.exp(gamma), np.exp(-gamma)], [np.exp(-gamma), np.exp(gamma)]])
+
+
+def cpmc_init(walkers, mo, weights=None):
+    """Real walkers and overlaps, full Green's functions (propagation.py:518-537)."""
+    w = [np.real(walkers[0]).copy(), np.real(walkers[1]).copy()]
+    nw = w[0].shape[0]
+    return {"walkers": w, "overlaps": np.real(cpmc_overlap(w, mo)),
+            "weights": np.ones(nw) if weights is None else weights.copy(),
+            "greens": cpmc_full_green(w, mo)}
+
+
+def _cpmc_one_body(exp_h1, pd, mo):
+    """propagation.py:539-563."""
+    pd["walkers"] = [np.einsum("ij,wjk->wik", exp_h1[0], pd["walkers"][0]),
+                     np.einsum("ij,wjk->wik", exp_h1[1], pd["walkers"][1])]
+    ov = cpmc_overlap(pd["walkers"], mo)
+    pd["weights"] = pd["weights"] * np.real(ov / pd["overlaps"])
+    pd["weights"] = np.where(pd["weights"] < 1.0e-8, 0.0, pd["weights"])
+    pd["overlaps"] = ov
+    pd["greens"] = cpmc_full_green(pd["walkers"], mo)
+    return pd
+
+
+def cpmc_propagate(exp_h1, dt: float, u: float, pd: dict, gaussian, mo, e_estimate: float,
+                   pop_control_ene_shift: float, n_walkers: int, slow: bool = False):
+    """One CPMC step (propagation.py:565-657): one-body half step, for every site x a discrete
+    Hubbard-Stratonovich field chosen with probabilities from the overlap ratios (uniforms
+    (erf(g / sqrt 2) + 1) / 2 of the given Gaussians [nw, norb]), the rank-one updates of the
+    Green's functions, one-body half step, weights * exp(dt E_pc), the > 100 clamp and the new
+    pop-control shift. slow: the ratios from determinants (propagation.py:660-773) instead of
+    the Green's function. Returns (pd, new pop_control_ene_shift)."""
+    import scipy.special
+    hs = cpmc_hs_constant(dt, u)
+    norb = pd["walkers"][0].shape[1]
+    pd = _cpmc_one_body(exp_h1, pd, mo)
+    uni = (scipy.special.erf(gaussian / 2 ** 0.5) + 1) / 2
+    for x in range(norb):
+        if slow:
+            rat = []
+            cand = []
+            for f in range(2):
+                wu = pd["walkers"][0].copy()
+                wd = pd["walkers"][1].copy()
+                wu[:, x, :] *= hs[f, 0]
+                wd[:, x, :] *= hs[f, 1]
+                ov = cpmc_overlap([wu, wd], mo)
+                r = np.real(ov / pd["overlaps"]) / 2.0
+                rat.append(np.where(r < 1.0e-8, 0.0, r))
+                cand.append((wu, wd, ov))
+            norm = rat[0] + rat[1]
+            p0 = rat[0] / norm
+            m = uni[:, x] < p0
+            pd["walkers"] = [np.where(m[:, None, None], cand[0][0], cand[1][0]),
+                             np.where(m[:, None, None], cand[0][1], cand[1][1])]
+            pd["overlaps"] = np.where(m, cand[0][2], cand[1][2])
+            pd["weights"] = pd["weights"] * norm
+            continue
+        g = pd["greens"]
+        rats = []
+        for f in range(2):
+            c = hs[f] - 1
+            r = (1 + c[0] * g[:, 0, x, x]) * (1 + c[1] * g[:, 1, x, x])
+            rats.append(np.where(r < 1.0e-8, 0.0, r))
+        p0, p1 = rats[0] / 2.0, rats[1] / 2.0
+        norm = p0 + p1
+        p0 = p0 / norm
+        m = uni[:, x] < p0
+        consts = np.where(m[:, None], hs[0][None, :], hs[1][None, :])  # [nw, 2]
+        pd["walkers"][0] = pd["walkers"][0].copy()
+        pd["walkers"][1] = pd["walkers"][1].copy()
+        pd["walkers"][0][:, x, :] *= consts[:, 0:1]
+        pd["walkers"][1][:, x, :] *= consts[:, 1:2]
+        ratios = np.where(m, rats[0], rats[1])
+        uc = consts - 1
+        # wavefunctions.py:916-945 with update indices (0, x), (1, x): different spins, so
+        # g_ij = g_ji = 0 and the second update sees the first spin block unchanged
+        gn = g.copy()
+        sg_i = g[:, 0, x, :].copy()
+        sg_i[:, x] -= 1
+        sg_j = g[:, 1, x, :].copy()
+        sg_j[:, x] -= 1
+        g_ii, g_jj = g[:, 0, x, x], g[:, 1, x, x]
+        fac_i = uc[:, 0] / ratios
+        gn[:, 0] += fac_i[:, None, None] * np.einsum(
+            "wi,wj->wij", g[:, 0, :, x], uc[:, 1:2] * (-g_jj[:, None] * sg_i) - sg_i)
+        fac_j = uc[:, 1] / ratios
+        gn[:, 1] += fac_j[:, None, None] * np.einsum(
+            "wi,wj->wij", g[:, 1, :, x], uc[:, 0:1] * (-g_ii[:, None] * sg_j) - sg_j)
+        pd["greens"] = gn
+        pd["overlaps"] = ratios * pd["overlaps"]
+        pd["weights"] = pd["weights"] * norm
+    pd = _cpmc_one_body(exp_h1, pd, mo)
+    pd["weights"] = pd["weights"] * np.exp(dt * pop_control_ene_shift)
+    pd["weights"] = np.where(pd["weights"] > 100.0, 0.0, pd["weights"])
+    pcs = e_estimate - 0.1 * np.log(np.sum(pd["weights"]) / n_walkers) / dt
+    return pd, pcs
+
+
 def init_prop_data(prop: Propagator, trial: Trial, ham_data: dict, mo, walkers) -> dict:
     """weights 1, e_estimate = mean real energy, overlaps (propagation.py:210-232, 333-357)."""
     pd = {"weights": np.ones(prop.n_walkers), "walkers": walkers}
