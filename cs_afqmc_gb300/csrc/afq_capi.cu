@@ -774,6 +774,21 @@ int afq_cpmc_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walke
                           walkers_dn, weights, overlaps, greens, scalars, gaussian, 1, S(stream));
 }
 
+int afq_cpmc_continuous_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, double dt,
+                                  double hs_constant, const double* exp_h1_up, const double* exp_h1_dn,
+                                  const double* trial_up, const double* trial_dn, double* walkers_up,
+                                  double* walkers_dn, double* weights, double* overlaps, double* scalars,
+                                  const double* gaussian, void* stream) {
+  if (!exp_h1_up || !exp_h1_dn || !trial_up || !trial_dn || !walkers_up || !walkers_dn || !weights || !overlaps ||
+      !scalars || !gaussian) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (!(dt > 0.0)) { afq_set_error("dt must be positive"); return -1; }
+  return afq::launch_cpmc(norb, n_up, n_dn, n_walkers, dt, hs_constant, exp_h1_up, exp_h1_dn, trial_up, trial_dn,
+                          walkers_up, walkers_dn, weights, overlaps, nullptr, scalars, gaussian, 2, S(stream));
+}
+
 int afq_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, void* stream) {
   if (!out && n > 0) { afq_set_error("NULL argument"); return -1; }
   return afq::launch_fill_normal(out, n, seed, offset, S(stream));

@@ -2,7 +2,8 @@
 // uhf_cpmc trial wavefunctions.py:848-955), FP64 with real walkers, one CTA per walker:
 // one-body half step, overlap and full Green's functions, a sweep over the sites choosing a
 // discrete Hubbard-Stratonovich field per site from the overlap ratios with rank-one
-// Green's-function updates, one-body half step, weights and the pop-control shift.
+// Green's-function updates, one-body half step, weights and the pop-control shift; and the
+// continuous-field variant (propagation.py:1595-1675).
 
 #include <math.h>
 
@@ -38,7 +39,7 @@ static size_t cpmc_smem(int n, int kmax) {
 // det; A = W S^-1 into T; G_s = C_s A^T. Returns the product of both determinants
 // (thread 0's value is the one used).
 __device__ double cpmc_one_body(const CpmcDev& d, double* G, double* Ws, double* T, double* Aug, int kmax,
-                                bool apply_exp) {
+                                bool apply_exp, bool need_det = true, bool need_green = true) {
   __shared__ double colj[kCpmcMaxOcc];
   __shared__ int piv_sh;
   __shared__ double det_sh;
@@ -60,6 +61,7 @@ __device__ double cpmc_one_body(const CpmcDev& d, double* G, double* Ws, double*
       for (int e = tid; e < n * o; e += nt) W[e] = T[e];
       __syncthreads();
     }
+    if (!need_det) continue;
     for (int e = tid; e < o * o; e += nt) {  // Aug = [S | I]
       const int i = e / o, k = e % o;
       double a = 0.0;
@@ -106,6 +108,10 @@ __device__ double cpmc_one_body(const CpmcDev& d, double* G, double* Ws, double*
       __syncthreads();
     }
     det *= det_sh;
+    if (!need_green) {
+      __syncthreads();  // det_sh and Aug are rewritten for the next spin
+      continue;
+    }
     for (int e = tid; e < n * o; e += nt) {  // A = W S^-1
       const int p = e / o, i = e % o;
       double a = 0.0;
@@ -125,7 +131,8 @@ __device__ double cpmc_one_body(const CpmcDev& d, double* G, double* Ws, double*
   return det;
 }
 
-// mode 0: overlaps and Green's functions of the given walkers; mode 1: one CPMC step
+// mode 0: overlaps and Green's functions of the given walkers; mode 1: one CPMC step;
+// mode 2: one step of the continuous-field variant (no Green's functions)
 __global__ void __launch_bounds__(kCpmcThreads) k_cpmc(const CpmcDev d, int mode) {
   extern __shared__ __align__(16) double csm[];
   __shared__ double colx[2][64], rowx[2][64];
@@ -147,6 +154,32 @@ __global__ void __launch_bounds__(kCpmcThreads) k_cpmc(const CpmcDev d, int mode
   if (mode == 0) {
     const double det = cpmc_one_body(d, G, Ws, T, Aug, kmax, false);
     if (tid == 0) d.overlaps[wl] = det;
+  } else if (mode == 2) {
+    // continuous fields (propagator_cpmc_continuous, propagation.py:1595-1675; its force bias
+    // is multiplied by zero): exp_h1, rows i times exp(+-x_i hs), exp_h1, overlap ratio
+    cpmc_one_body(d, G, Ws, T, Aug, kmax, true, false, false);
+    const double hs = d.hs[0][0];
+    for (int e = tid; e < n * (d.no[0] + d.no[1]); e += nt) {
+      const int s = e < n * d.no[0] ? 0 : 1;
+      const int ee = s == 0 ? e : e - n * d.no[0], i = ee / d.no[s];
+      const double x = d.gauss[(size_t)wl * n + i];
+      Ws[(size_t)s * n * kmax + ee] *= exp(s == 0 ? x * hs : -x * hs);
+    }
+    __syncthreads();
+    const double det = cpmc_one_body(d, G, Ws, T, Aug, kmax, true, true, false);
+    if (tid == 0) {
+      w *= exp(d.dt * d.scalars[AFQ_S_POP_CONTROL_SHIFT]) * det / ov;
+      if (w < 1.0e-8) w = 0.0;
+      if (w > 100.0) w = 0.0;
+      d.weights[wl] = w;
+      d.overlaps[wl] = det;
+    }
+    for (int s = 0; s < 2; ++s) {
+      const int o = d.no[s];
+      double* dst = d.w[s] + (size_t)wl * n * o;
+      for (int e = tid; e < n * o; e += nt) dst[e] = Ws[(size_t)s * n * kmax + e];
+    }
+    return;
   } else {
     // one-body half step (propagation.py:539-563)
     double det = cpmc_one_body(d, G, Ws, T, Aug, kmax, true);
@@ -246,11 +279,15 @@ int launch_cpmc(int norb, int n_up, int n_dn, int nw, double dt, double u, const
   d.no[1] = n_dn;
   d.nw = nw;
   d.dt = dt;
-  const double gamma = acosh(exp(dt * u / 2.0)), cst = exp(-dt * u / 2.0);
-  d.hs[0][0] = cst * exp(gamma);
-  d.hs[0][1] = cst * exp(-gamma);
-  d.hs[1][0] = cst * exp(-gamma);
-  d.hs[1][1] = cst * exp(gamma);
+  if (mode == 2) {  // u is the continuous constant ham_data["hs_constant"]
+    d.hs[0][0] = d.hs[0][1] = d.hs[1][0] = d.hs[1][1] = u;
+  } else {
+    const double gamma = acosh(exp(dt * u / 2.0)), cst = exp(-dt * u / 2.0);
+    d.hs[0][0] = cst * exp(gamma);
+    d.hs[0][1] = cst * exp(-gamma);
+    d.hs[1][0] = cst * exp(-gamma);
+    d.hs[1][1] = cst * exp(gamma);
+  }
   d.exph[0] = exp_up;
   d.exph[1] = exp_dn;
   d.trial[0] = trial_up;
@@ -268,7 +305,7 @@ int launch_cpmc(int norb, int n_up, int n_dn, int nw, double dt, double u, const
   {
     ProfScope _ps(K_WEIGHTS, st);
     k_cpmc<<<nw, kCpmcThreads, smem, st>>>(d, mode);
-    if (mode == 1) k_cpmc_pop_control<<<1, 1024, 0, st>>>(nw, dt, weights, scalars);
+    if (mode != 0) k_cpmc_pop_control<<<1, 1024, 0, st>>>(nw, dt, weights, scalars);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -358,6 +358,36 @@ class propagator_cpmc(propagator_unrestricted):
         return super().__hash__()
 
 
+@dataclass
+class propagator_cpmc_continuous(propagator_cpmc):
+    """Continuous-field CPMC (propagation.py:1595-1675): ham_data["hs_constant"] scales the
+    Gaussian fields; no discrete sweep and no Green's functions. Real walkers, as
+    propagator_cpmc keeps them (the reference's unrestricted state is complex with zero
+    imaginary parts for real inputs)."""
+
+    def propagate(self, trial, ham_data: dict, prop_data: PropData, gaussian_rns,
+                  wave_data: dict) -> PropData:
+        norb, (n_up, n_dn) = trial.norb, trial.nelec
+        w = prop_data["walkers"]
+        g = as_dev(gaussian_rns).contiguous()
+        if tuple(g.shape) != (self.n_walkers, norb):
+            raise _lib.AfqError(f"gaussian_rns must be [{self.n_walkers}, {norb}], got {tuple(g.shape)}")
+        e = ham_data["exp_h1"]
+        e = e if isinstance(e, torch.Tensor) else torch.as_tensor(np.asarray(e))
+        eu, ed = as_dev(e[0]).contiguous(), as_dev(e[1]).contiguous()
+        mo = wave_data["mo_coeff"]
+        cu, cd = as_dev(mo[0]).contiguous(), as_dev(mo[1]).contiguous()
+        hs = float(np.real(_engine._scalar(ham_data["hs_constant"])))
+        _lib.call("afq_cpmc_continuous_propagate", norb, n_up, n_dn, self.n_walkers, float(self.dt), hs,
+                  eu.data_ptr(), ed.data_ptr(), cu.data_ptr(), cd.data_ptr(), w[0].data_ptr(), w[1].data_ptr(),
+                  prop_data["weights"].data_ptr(), prop_data["overlaps"].data_ptr(),
+                  prop_data["_scalars"].data_ptr(), g.data_ptr(), stream_ptr())
+        return prop_data
+
+    def __hash__(self) -> int:
+        return super().__hash__()
+
+
 def _any_engine(prop_data, trial, ham_data, wave_data, prop):
     """QR and SR need only sizes: reuse the engine that last propagated these walkers."""
     eng = prop_data.get("_engine") if isinstance(prop_data, dict) else None

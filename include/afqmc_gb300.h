@@ -235,6 +235,19 @@ int afq_cpmc_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walke
                        double* walkers_dn, double* weights, double* overlaps, double* greens,
                        double* scalars, const double* gaussian, void* stream);
 
+/* One step of the continuous-field CPMC variant (propagator_cpmc_continuous,
+ * propagation.py:1595-1675, whose force bias is multiplied by zero): exp_h1 half step; rows i
+ * of the up / down slab times exp(+x_i hs_constant) / exp(-x_i hs_constant) with the
+ * Gaussians x = gaussian[w] (float64 [nw][norb]); exp_h1 half step; weights *=
+ * exp(dt pop_control_ene_shift) O'/O (< 1e-8 -> 0, > 100 -> 0); overlaps = O'; then the
+ * pop-control shift as in afq_cpmc_propagate. Real walkers, no Green's functions. */
+int afq_cpmc_continuous_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers,
+                                  double dt, double hs_constant, const double* exp_h1_up,
+                                  const double* exp_h1_dn, const double* trial_up,
+                                  const double* trial_dn, double* walkers_up, double* walkers_dn,
+                                  double* weights, double* overlaps, double* scalars,
+                                  const double* gaussian, void* stream);
+
 /* ---- forward-mode derivative of the block (differentiation pattern, FP64) ------------ */
 
 /* Bytes of device tangent workspace afq_propagate_phaseless_jvp needs. 0 on bad sizes. */

@@ -528,6 +528,23 @@ def cpmc_propagate(exp_h1, dt: float, u: float, pd: dict, gaussian, mo, e_estima
     return pd, pcs
 
 
+def cpmc_continuous_propagate(exp_h1, dt: float, hs: float, pd: dict, gaussian, mo, e_estimate: float,
+                              pop_control_ene_shift: float, n_walkers: int):
+    """One step of the continuous-field CPMC variant (propagation.py:1595-1675; the force bias
+    and fb_term there are multiplied by zero). Returns (pd, new pop_control_ene_shift)."""
+    w = [np.einsum("ij,wjk->wik", exp_h1[0], pd["walkers"][0]),
+         np.einsum("ij,wjk->wik", exp_h1[1], pd["walkers"][1])]
+    w = [np.exp(gaussian * hs)[:, :, None] * w[0], np.exp(-gaussian * hs)[:, :, None] * w[1]]
+    w = [np.einsum("ij,wjk->wik", exp_h1[0], w[0]), np.einsum("ij,wjk->wik", exp_h1[1], w[1])]
+    ov = cpmc_overlap(w, mo)
+    imp = np.exp(dt * pop_control_ene_shift) * ov / pd["overlaps"]
+    wt = pd["weights"] * np.real(imp)
+    wt = np.where(wt < 1.0e-8, 0.0, wt)
+    wt = np.where(wt > 100.0, 0.0, wt)
+    pd = {"walkers": w, "overlaps": ov, "weights": wt, "greens": pd.get("greens")}
+    return pd, e_estimate - 0.1 * np.log(np.sum(wt) / n_walkers) / dt
+
+
 def init_prop_data(prop: Propagator, trial: Trial, ham_data: dict, mo, walkers) -> dict:
     """weights 1, e_estimate = mean real energy, overlaps (propagation.py:210-232, 333-357)."""
     pd = {"weights": np.ones(prop.n_walkers), "walkers": walkers}

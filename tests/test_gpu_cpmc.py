@@ -74,3 +74,26 @@ def test_cpmc_oracle_fast_equals_slow():
         b, pb = O.cpmc_propagate(exp_h1, prop.dt, 4.0, b, g, mo, -5.0, -5.0, prop.n_walkers, slow=True)
     assert np.allclose(a["walkers"][0], b["walkers"][0]) and np.allclose(a["weights"], b["weights"])
     assert np.allclose(a["overlaps"], b["overlaps"])
+
+
+def test_cpmc_continuous_steps():
+    import torch
+    from cs_afqmc_gb300 import propagation
+    s, trial, wave, hd, prop, pd, w0, mo = _system(lx=4, ly=4, nelec=(7, 5))
+    cprop = propagation.propagator_cpmc_continuous(dt=prop.dt, n_walkers=prop.n_walkers, precision="fp64")
+    hd["hs_constant"] = 0.3
+    exp_h1 = to_np(hd["exp_h1"])
+    po = O.cpmc_init(w0, mo)
+    e_est = pd["e_estimate"].item()
+    pcs = pd["pop_control_ene_shift"].item()
+    rng = np.random.default_rng(8)
+    for _ in range(4):
+        g = rng.standard_normal((prop.n_walkers, s.norb))
+        po, pcs = O.cpmc_continuous_propagate(exp_h1, prop.dt, 0.3, po, g, mo, e_est, pcs, prop.n_walkers)
+        pd = cprop.propagate(trial, hd, pd, g, wave)
+    torch.cuda.synchronize()
+    assert rel_err(to_np(pd["walkers"][0]), po["walkers"][0]) < 1e-9
+    assert rel_err(to_np(pd["walkers"][1]), po["walkers"][1]) < 1e-9
+    assert rel_err(to_np(pd["weights"]), po["weights"]) < 1e-9
+    assert rel_err(to_np(pd["overlaps"]), po["overlaps"]) < 1e-9
+    assert abs(pd["pop_control_ene_shift"].item() - pcs) < 1e-9 * max(1.0, abs(pcs))
