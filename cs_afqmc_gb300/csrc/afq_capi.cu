@@ -211,15 +211,17 @@ int check_state(const afq_ctx* c, const afq_walker_state* s) {
 
 // chain: a step inside afq_propagate_phaseless, where the Green's-function work of the
 // previous overlap evaluation on the same walkers (c->gstate) is reused.
+// next_g (with chain): the next operation propagates the same walkers again, so the overlap
+// evaluation after the step also forms G and the operands (not before a QR).
 int propagate_impl(afq_ctx* c, afq_walker_state* s, const double* fields, cudaStream_t st,
-                   bool chain = false) {
+                   bool chain = false, bool next_g = true) {
   const afq_ctx_dev& d = c->dev;
   if (!is_fp64(c)) {
     // mixed: operands -> fused force bias / field shifts -> exp_h1, vhs + Taylor, exp_h1
     if (!(chain && c->gstate == 1)) CHECK(afq::tc_green(c->tc, d, s->walkers_up, s->walkers_dn, nullptr, true, st));
     CHECK(afq::tc_field_shifts(c->tc, d, fields, st));
     CHECK(afq::tc_propagate_walkers(c->tc, d, s->walkers_up, s->walkers_dn, st));
-    CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, c->ovl_new, false, st, chain));
+    CHECK(green(c, s->walkers_up, s->walkers_dn, nullptr, c->ovl_new, false, st, chain && next_g));
     return afq::tc_weights(c->tc, d, c->ovl_new, reinterpret_cast<double2*>(s->overlaps), s->weights,
                            s->scalars, st);
   }
@@ -540,7 +542,7 @@ int afq_propagate_phaseless(afq_ctx* ctx, afq_walker_state* state, const double*
     for (int eb = 0; eb < n_ene_blocks; ++eb, ++blk) {
       for (int p = 0; p < n_prop_steps; ++p) {
         const double* f = fields + ((size_t)blk * n_prop_steps + p) * step_elems;
-        CHECK(propagate_impl(ctx, state, f, st, true));
+        CHECK(propagate_impl(ctx, state, f, st, true, p + 1 < n_prop_steps));
       }
       ctx->gstate = 0;
       CHECK(qr_impl(ctx, state, st));
