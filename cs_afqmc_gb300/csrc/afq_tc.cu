@@ -973,9 +973,11 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   return launch_check("green_fused");
 }
 
+// energy (with maps == nullptr): the Coulomb contraction of the local energy on the split
+// path (RHF: the same operands as the force bias), with the energy's split-term options
 static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, double2* fb_out, cudaStream_t st,
                    const GemmMaps* maps = nullptr, const float* rc_inv = nullptr, float alpha = 0.f,
-                   int kdim = 0) {
+                   int kdim = 0, bool energy = false) {
   EpiFB::Params ep;
   memset(&ep, 0, sizeof(ep));
   ep.fields = fields;
@@ -1004,13 +1006,14 @@ static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, doubl
     sa.k_tiles = kt;
     sa.k_splits = t.fb_ks;
     sa.a_row0 = 0;
-    sa.has_alo = (t.cfg & kFbDyn) ? 1 : 0;
-    sa.has_blo = (t.cfg & kFbStat) ? 1 : 0;
+    sa.has_alo = (t.cfg & (energy ? kEneDyn : kFbDyn)) ? 1 : 0;
+    sa.has_blo = (t.cfg & (energy ? kEneStat : kFbStat)) ? 1 : 0;
     sa.drain = t.drain > 0 ? t.drain : kt;
     sa.idesc = ptx::idesc_f16(128, kSplitBN, t.bf16 ? 1 : 0);
     const long ldp = t.fb_npad, sst = (long)mt * 128 * t.fb_npad;
     SplitPartialF32::Params pp{t.fb_part, 2 * t.nw, c.nchol, ldp, sst};
-    TC_CHECK(launch_split<SplitPartialF32>(K_FB, t.m_fb_split, sa, t.num_sms, pp, t.status, st));
+    const int cls = energy ? K_ENERGY : K_FB;
+    TC_CHECK(launch_split<SplitPartialF32>(cls, t.m_fb_split, sa, t.num_sms, pp, t.status, st));
     FbReduce r;
     r.part = t.fb_part;
     r.ksplit = t.fb_ks;
@@ -1032,7 +1035,7 @@ static int fb_gemm(TcState& t, const afq_ctx_dev& c, const double* fields, doubl
     r.part_fbt = t.part_fbt;
     r.fb_out = fb_out;
     {
-      ProfScope _ps(K_FB, st);
+      ProfScope _ps(cls, st);
       k_fb_reduce<<<t.nw, 256, 0, st>>>(r);
     }
     return launch_check("fb_reduce");
@@ -1152,8 +1155,11 @@ int tc_weights(TcState& t, const afq_ctx_dev& c, const double2* ovl_new, double2
 // exchange from the U GEMM, both per spin block; ene1 comes from the Green kernel.
 int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
   for (int b = 0; b < t.nblk; ++b) {
-    TC_CHECK(fb_gemm(t, c, nullptr, t.c_out + (size_t)b * t.nw * c.nchol, st, &t.m_c[b], t.rc_blk_inv[b], 1.0f,
-                     t.kb[b]));
+    if (t.nblk == 1)  // RHF: the force-bias operands, on the persistent split GEMM
+      TC_CHECK(fb_gemm(t, c, nullptr, t.c_out, st, nullptr, nullptr, 1.0f, 0, true));
+    else
+      TC_CHECK(fb_gemm(t, c, nullptr, t.c_out + (size_t)b * t.nw * c.nchol, st, &t.m_c[b], t.rc_blk_inv[b], 1.0f,
+                       t.kb[b]));
     EpiExc::Params ep;
     ep.g_hi = t.g_blk[b][0];
     ep.g_lo = t.g_blk[b][1];
