@@ -82,6 +82,11 @@ _SIGS = {
                                                    _vp, ctypes.c_size_t, _vp, _vp, ctypes.c_int32,
                                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _vp, _vp,
                                                    _vp, _vp, _vp, _vp, _vp]),
+    "afq_vjp_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(Dims), ctypes.c_int32, ctypes.c_int32,
+                                                 ctypes.c_int32]),
+    "afq_propagate_phaseless_vjp": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_size_t, _vp,
+                                                   _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                   ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "afq_field_block": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_int32, _vp, _vp,
                                        _vp, _vp]),
     "afq_cs_outlier_removal": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_double, _vp,

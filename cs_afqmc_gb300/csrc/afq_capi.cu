@@ -9,6 +9,7 @@
 #include <new>
 
 #include "afq_common.cuh"
+#include "afq_adjoint.cuh"
 #include "afq_kernels.cuh"
 #include "afq_tangent.cuh"
 #include "afq_tc.cuh"
@@ -367,6 +368,101 @@ int copy_d2d(void* dst, const void* src, size_t bytes, cudaStream_t st, const ch
   return 0;
 }
 
+// Workspace of afq_propagate_phaseless_vjp: the recorded forward sweep (snapshots of the
+// walker state before every step, after the last step of an energy block and after its QR;
+// shifted fields and shift terms of every step; local energies of every block; SR indices)
+// followed by the backward sweep's cotangents.
+struct AdjSizes {
+  size_t snap_w, snap_wt, snap_ov, snap_sc, t_xt, t_sh, t_fbt, t_ene, t_idx;
+  size_t wb, wb2, wbar, lbar, lbar2, gpend, gene, fbb, xtb, shb, fbtb, vbar, tay, ebar, scal, beb, bwb, total;
+  size_t wslab;  // walker elements of one snapshot, both slabs
+  int nblk, nsteps, nsnap;
+};
+
+AdjSizes adjoint_sizes(const afq_ctx_dev& c, int nw_chunk, int n_prop, int n_ene, int n_sr, Layout* L) {
+  AdjSizes s;
+  const size_t nw = c.nw, C16 = sizeof(double2), nk = (size_t)c.norb * (c.kslab[0] + c.kslab[1]);
+  s.nblk = n_ene * n_sr;
+  s.nsteps = s.nblk * n_prop;
+  s.nsnap = s.nblk * (n_prop + 2);
+  s.wslab = nw * nk;
+  s.snap_w = L->take((size_t)s.nsnap * s.wslab * C16);
+  s.snap_wt = L->take((size_t)s.nsnap * nw * sizeof(double));
+  s.snap_ov = L->take((size_t)s.nsnap * nw * C16);
+  s.snap_sc = L->take((size_t)s.nsnap * AFQ_NSCALARS * sizeof(double));
+  s.t_xt = L->take((size_t)s.nsteps * nw * c.nchol * C16);
+  s.t_sh = L->take((size_t)s.nsteps * nw * C16);
+  s.t_fbt = L->take((size_t)s.nsteps * nw * C16);
+  s.t_ene = L->take((size_t)s.nblk * nw * C16);
+  s.t_idx = L->take((size_t)n_sr * nw * sizeof(int32_t));
+  s.wb = L->take(s.wslab * C16);
+  s.wb2 = L->take(s.wslab * C16);
+  s.wbar = L->take(nw * sizeof(double));
+  s.lbar = L->take(nw * C16);
+  s.lbar2 = L->take(nw * C16);
+  s.gpend = L->take(nw * c.ktot * C16);
+  s.gene = L->take(nw * c.ktot * C16);
+  s.fbb = L->take(nw * c.nchol * C16);
+  s.xtb = L->take(nw * c.nchol * C16);
+  s.shb = L->take(nw * C16);
+  s.fbtb = L->take(nw * C16);
+  s.vbar = L->take((size_t)nw_chunk * c.norb * c.norb * C16);
+  s.tay = L->take((size_t)nw_chunk * (2 * (c.n_exp_terms - 1) + 2) * nk * C16);
+  s.ebar = L->take(nw * sizeof(double));
+  s.scal = L->take(8 * sizeof(double));
+  s.beb = L->take((size_t)s.nblk * sizeof(double));
+  s.bwb = L->take((size_t)s.nblk * sizeof(double));
+  s.total = L->off;
+  return s;
+}
+
+// Views of the recorded forward sweep. Snapshot i = blk * (n_prop + 2) + j: j < n_prop
+// before step j, j == n_prop after the last step (before the QR), j == n_prop + 1 after
+// the QR and the overlap evaluation.
+struct Tape {
+  char* base;
+  AdjSizes s;
+  const afq_ctx_dev* d;
+  double2* w(int i, int slab) const {
+    return reinterpret_cast<double2*>(base + s.snap_w) + (size_t)i * s.wslab +
+           (slab ? (size_t)d->nw * d->norb * d->kslab[0] : 0);
+  }
+  double* wt(int i) const { return reinterpret_cast<double*>(base + s.snap_wt) + (size_t)i * d->nw; }
+  double2* ov(int i) const { return reinterpret_cast<double2*>(base + s.snap_ov) + (size_t)i * d->nw; }
+  double* sc(int i) const { return reinterpret_cast<double*>(base + s.snap_sc) + (size_t)i * AFQ_NSCALARS; }
+  double2* xt(int step) const {
+    return reinterpret_cast<double2*>(base + s.t_xt) + (size_t)step * d->nw * d->nchol;
+  }
+  double2* sh(int step) const { return reinterpret_cast<double2*>(base + s.t_sh) + (size_t)step * d->nw; }
+  double2* fbt(int step) const { return reinterpret_cast<double2*>(base + s.t_fbt) + (size_t)step * d->nw; }
+  double2* ene(int blk) const { return reinterpret_cast<double2*>(base + s.t_ene) + (size_t)blk * d->nw; }
+  int32_t* idx(int sr) const { return reinterpret_cast<int32_t*>(base + s.t_idx) + (size_t)sr * d->nw; }
+};
+
+int snapshot(const Tape& t, int i, const afq_walker_state* st_, cudaStream_t st) {
+  const afq_ctx_dev& d = *t.d;
+  const size_t e0 = (size_t)d.nw * d.norb * d.kslab[0], e1 = (size_t)d.nw * d.norb * d.kslab[1];
+  CHECK(copy_d2d(t.w(i, 0), st_->walkers_up, e0 * sizeof(double2), st, "walker snapshot"));
+  if (d.nslab == 2) CHECK(copy_d2d(t.w(i, 1), st_->walkers_dn, e1 * sizeof(double2), st, "walker snapshot"));
+  CHECK(copy_d2d(t.wt(i), st_->weights, d.nw * sizeof(double), st, "weight snapshot"));
+  CHECK(copy_d2d(t.ov(i), st_->overlaps, d.nw * sizeof(double2), st, "overlap snapshot"));
+  return copy_d2d(t.sc(i), st_->scalars, AFQ_NSCALARS * sizeof(double), st, "scalar snapshot");
+}
+
+int zero(void* p, size_t bytes, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(p, 0, bytes, st);
+  if (e != cudaSuccess) { afq_set_error("memset: %s", cudaGetErrorString(e)); return (int)e; }
+  return 0;
+}
+
+void swap_slabs(double2* a[2], double2* b[2]) {
+  for (int k = 0; k < 2; ++k) {
+    double2* t = a[k];
+    a[k] = b[k];
+    b[k] = t;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -668,6 +764,178 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
   CHECK(afq::launch_phaseless_end(blk, (double)n_sr_blocks * n_ene_blocks * d.nw, block_energy, block_weight,
                                   state->scalars, energy, st));
   return afq::t_launch_end(blk, block_energy, block_weight, t, nullptr, denergy, st);
+}
+
+size_t afq_vjp_workspace_size(const afq_dims* dims, int32_t n_prop_steps, int32_t n_ene_blocks,
+                              int32_t n_sr_blocks) {
+  afq_ctx_dev c;
+  int nwc, ec, eg;
+  size_t we;
+  if (n_prop_steps < 1 || n_ene_blocks < 1 || n_sr_blocks < 1) return 0;
+  if (derive(dims, &c, &nwc, &ec, &eg, &we)) return 0;
+  Layout L;
+  return adjoint_sizes(c, nwc, n_prop_steps, n_ene_blocks, n_sr_blocks, &L).total;
+}
+
+int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp_workspace,
+                                size_t vjp_workspace_bytes, const double* fields, const double* zetas,
+                                int32_t n_prop_steps, int32_t n_ene_blocks, int32_t n_sr_blocks,
+                                int32_t flags, double* block_energy, double* block_weight,
+                                double* energy, double* gexp_h1_up, double* gexp_h1_dn,
+                                double* grot_h1_up, double* grot_h1_dn, void* stream) {
+  const bool do_sr = !(flags & AFQ_JVP_NO_SR);
+  if (!ctx || !fields || (do_sr && !zetas) || !block_energy || !block_weight || !energy || !gexp_h1_up ||
+      !grot_h1_up) {
+    afq_set_error("NULL argument");
+    return -1;
+  }
+  if (!is_fp64(ctx)) { afq_set_error("the derivative path needs an FP64 context"); return -1; }
+  if (n_prop_steps < 1 || n_ene_blocks < 1 || n_sr_blocks < 1 || (!do_sr && n_sr_blocks != 1)) {
+    afq_set_error("block counts must be >= 1 (n_sr_blocks == 1 without SR)");
+    return -1;
+  }
+  if (flags & ~AFQ_JVP_NO_SR) { afq_set_error("unknown flags 0x%x", (unsigned)flags); return -1; }
+  CHECK(check_state(ctx, state));
+  const afq_ctx_dev& d = ctx->dev;
+  if (d.nslab == 2 && !gexp_h1_dn) { afq_set_error("unrestricted walkers need gexp_h1_dn"); return -1; }
+  if (d.nspin_g == 2 && !grot_h1_dn) { afq_set_error("the UHF trial needs grot_h1_dn"); return -1; }
+  const int P = n_prop_steps, NE = n_ene_blocks;
+  Layout L;
+  const AdjSizes as = adjoint_sizes(d, ctx->nw_chunk, P, NE, n_sr_blocks, &L);
+  if (!vjp_workspace || vjp_workspace_bytes < as.total) {
+    afq_set_error("vjp workspace too small: need %zu bytes, got %zu", as.total, vjp_workspace_bytes);
+    return -1;
+  }
+  if (reinterpret_cast<uintptr_t>(vjp_workspace) & 255) {
+    afq_set_error("vjp workspace must be 256-byte aligned");
+    return -1;
+  }
+  char* base = static_cast<char*>(vjp_workspace);
+  const Tape tp{base, as, &d};
+  afq::AdjointBufs a;
+  const size_t e0 = (size_t)d.nw * d.norb * d.kslab[0];
+  a.wb[0] = reinterpret_cast<double2*>(base + as.wb);
+  a.wb[1] = a.wb[0] + e0;
+  a.wb2[0] = reinterpret_cast<double2*>(base + as.wb2);
+  a.wb2[1] = a.wb2[0] + e0;
+  a.wbar = reinterpret_cast<double*>(base + as.wbar);
+  a.lbar = reinterpret_cast<double2*>(base + as.lbar);
+  a.lbar2 = reinterpret_cast<double2*>(base + as.lbar2);
+  a.gpend = reinterpret_cast<double2*>(base + as.gpend);
+  a.gene = reinterpret_cast<double2*>(base + as.gene);
+  a.fbb = reinterpret_cast<double2*>(base + as.fbb);
+  a.xtb = reinterpret_cast<double2*>(base + as.xtb);
+  a.shb = reinterpret_cast<double2*>(base + as.shb);
+  a.fbtb = reinterpret_cast<double2*>(base + as.fbtb);
+  a.vbar = reinterpret_cast<double2*>(base + as.vbar);
+  a.tay = reinterpret_cast<double2*>(base + as.tay);
+  a.ebar = reinterpret_cast<double*>(base + as.ebar);
+  a.scal = reinterpret_cast<double*>(base + as.scal);
+  a.beb = reinterpret_cast<double*>(base + as.beb);
+  a.bwb = reinterpret_cast<double*>(base + as.bwb);
+  a.gexp[0] = gexp_h1_up;
+  a.gexp[1] = d.nslab == 2 ? gexp_h1_dn : nullptr;
+  a.grot[0] = grot_h1_up;
+  a.grot[1] = d.nspin_g == 2 ? grot_h1_dn : nullptr;
+  cudaStream_t st = S(stream);
+  double2* ovl = reinterpret_cast<double2*>(state->overlaps);
+  const size_t step_elems = (size_t)d.nw * d.nchol;
+
+  // forward sweep: afq_propagate_phaseless's FP64 path, recording the state
+  ctx->gstate = 0;
+  CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+  CHECK(afq::launch_phaseless_begin(state->scalars, st));
+  int blk = 0;
+  for (int sr = 0; sr < n_sr_blocks; ++sr) {
+    for (int eb = 0; eb < NE; ++eb, ++blk) {
+      for (int p = 0; p < P; ++p) {
+        const int step = blk * P + p;
+        CHECK(snapshot(tp, blk * (P + 2) + p, state, st));
+        CHECK(propagate_impl(ctx, state, fields + (size_t)step * step_elems, st));
+        CHECK(copy_d2d(tp.xt(step), ctx->xt, step_elems * sizeof(double2), st, "shifted-field record"));
+        CHECK(copy_d2d(tp.sh(step), ctx->shift, d.nw * sizeof(double2), st, "shift record"));
+        CHECK(copy_d2d(tp.fbt(step), ctx->fbt, d.nw * sizeof(double2), st, "fbt record"));
+      }
+      CHECK(snapshot(tp, blk * (P + 2) + P, state, st));
+      CHECK(qr_impl(ctx, state, st));
+      CHECK(green(ctx, state->walkers_up, state->walkers_dn, ctx->green, ovl, true, st));
+      CHECK(snapshot(tp, blk * (P + 2) + P + 1, state, st));
+      CHECK(energy_from_green(ctx, ctx->ene, st));
+      CHECK(copy_d2d(tp.ene(blk), ctx->ene, d.nw * sizeof(double2), st, "local-energy record"));
+      CHECK(afq::launch_block_stats(d, ctx->ene, state->weights, state->scalars, block_energy + blk,
+                                    block_weight + blk, st));
+    }
+    if (!do_sr) continue;
+    CHECK(sr_impl(ctx, state, zetas + sr, tp.idx(sr), st));
+    CHECK(green(ctx, state->walkers_up, state->walkers_dn, nullptr, ovl, false, st));
+  }
+  CHECK(afq::launch_phaseless_end(blk, (double)n_sr_blocks * NE * d.nw, block_energy, block_weight,
+                                  state->scalars, energy, st));
+
+  // backward sweep, from the sampler total to the start of the first block
+  CHECK(zero(base + as.wb, as.wslab * sizeof(double2), st));
+  CHECK(zero(a.wbar, d.nw * sizeof(double), st));
+  CHECK(zero(a.lbar, d.nw * sizeof(double2), st));
+  CHECK(zero(a.scal, 8 * sizeof(double), st));
+  CHECK(zero(gexp_h1_up, (size_t)d.norb * d.norb * sizeof(double), st));
+  if (d.nslab == 2) CHECK(zero(gexp_h1_dn, (size_t)d.norb * d.norb * sizeof(double), st));
+  CHECK(zero(grot_h1_up, (size_t)d.gocc[0] * d.norb * sizeof(double), st));
+  if (d.nspin_g == 2) CHECK(zero(grot_h1_dn, (size_t)d.gocc[1] * d.norb * sizeof(double), st));
+  CHECK(afq::a_launch_end(blk, block_energy, block_weight, a, st));
+  const int nwc = ctx->nw_chunk, nb = d.nw / nwc;
+  const long nn = (long)d.norb * d.norb;
+  const double sq = sqrt(d.dt);
+  const double* brc = d.nspin_g == 2 ? ctx->rccat : d.rot_chol[0];
+  const double alpha = d.energy_mode == 0 ? 2.0 : 1.0;
+  bool gp = false;  // a.gpend holds the pending G cotangent of the current point
+  for (int b = blk - 1; b >= 0; --b) {
+    if (do_sr && b + 1 < blk && b % NE == NE - 1) {
+      // the SR between blocks b and b + 1: finish the cotangent of its output walkers,
+      // then send it back through the gather
+      const int s0 = (b + 1) * (P + 2);
+      CHECK(afq::a_launch_green(d, tp.w(s0, 0), tp.w(s0, 1), gp ? a.gpend : nullptr, nullptr, a.lbar, a.wb[0],
+                                a.wb[1], st));
+      CHECK(afq::a_launch_sr(d, a, tp.idx(b / NE), st));
+      swap_slabs(a.wb, a.wb2);
+      CHECK(zero(a.lbar, d.nw * sizeof(double2), st));
+      gp = false;
+    }
+    const int sq_i = b * (P + 2) + P + 1, sw_i = b * (P + 2) + P;
+    CHECK(afq::a_launch_block_stats(d, a, b, tp.ene(b), tp.wt(sq_i), tp.sc(sq_i), block_energy, st));
+    CHECK(afq::launch_green<double>(d, tp.w(sq_i, 0), tp.w(sq_i, 1), ctx->green, nullptr, true, st));
+    CHECK(afq::a_launch_energy(d, a, ctx->green, st));
+    CHECK(afq::a_launch_green(d, tp.w(sq_i, 0), tp.w(sq_i, 1), a.gene, gp ? a.gpend : nullptr, a.lbar, a.wb[0],
+                              a.wb[1], st));
+    CHECK(zero(a.lbar, d.nw * sizeof(double2), st));
+    gp = false;
+    CHECK(afq::a_launch_qr(d, tp.w(sw_i, 0), tp.w(sw_i, 1), tp.w(sq_i, 0), tp.w(sq_i, 1), a.wb[0], a.wb[1],
+                           a.wb2[0], a.wb2[1], st));
+    swap_slabs(a.wb, a.wb2);
+    for (int p = P - 1; p >= 0; --p) {
+      const int post = b * (P + 2) + p + 1, start = b * (P + 2) + p, step = b * P + p;
+      CHECK(afq::a_launch_weights(d, a, tp.sh(step), tp.fbt(step), tp.ov(post), tp.ov(start), tp.wt(start),
+                                  tp.wt(post), tp.sc(start), st));
+      CHECK(afq::a_launch_green(d, tp.w(post, 0), tp.w(post, 1), gp ? a.gpend : nullptr, nullptr, a.lbar, a.wb[0],
+                                a.wb[1], st));
+      for (int k = 0; k < nb; ++k) {
+        const int w0 = k * nwc;
+        CHECK(afq::launch_gemm_cr(true, nwc, (int)nn, d.nchol, tp.xt(step) + (size_t)w0 * d.nchol, d.nchol,
+                                  ctx->h.chol, nn, ctx->vhs, nn, c2(0.0, sq), st));
+        CHECK(afq::a_launch_taylor(d, a, w0, nwc, ctx->vhs, tp.w(start, 0), tp.w(start, 1), st));
+        CHECK(afq::launch_gemm_cr(false, nwc, d.nchol, (int)nn, a.vbar, nn, ctx->h.chol, nn,
+                                  a.xtb + (size_t)w0 * d.nchol, d.nchol, c2(0.0, -sq), st));
+      }
+      CHECK(afq::a_launch_field(d, a, tp.xt(step), st));
+      CHECK(afq::launch_gemm_cr(true, d.nw, d.ktot, d.nchol, a.fbb, d.nchol, brc, d.ktot, a.gpend, d.ktot,
+                                c2(alpha, 0.0), st));
+      gp = true;
+      swap_slabs(a.wb, a.wb2);
+      double2* t = a.lbar;
+      a.lbar = a.lbar2;
+      a.lbar2 = t;
+    }
+  }
+  return 0;
 }
 
 int afq_propagate_free(afq_ctx* ctx, afq_walker_state* state, const double* fields, double ene0, double* norms,

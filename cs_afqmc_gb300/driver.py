@@ -41,16 +41,21 @@ def run_blocks(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_da
 
 
 def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_data,
-                  n_blocks: int, observable=None, do_sr: bool = True, fields=None, zetas=None):
-    """Forward-mode branch of driver.py (ad_mode "forward" without orbital rotation,
-    driver.py:165-215, 245-308 on one rank): per block the jvp of
-    sampler.propagate_phaseless_ad_norot (do_sr=False: ..._nosr_norot) along the observable,
-    a non-finite derivative replaced by the trial's value sum(rdm1 * op), then the block
-    weight, QR, global SR and e_estimate update of the non-AD branch. observable:
-    (op, constant) or None for (h1, 0) as driver.py:35-40. fields (optional):
+                  n_blocks: int, observable=None, do_sr: bool = True, fields=None, zetas=None,
+                  ad_mode: str = "forward"):
+    """AD branches of driver.py without orbital rotation (driver.py:165-229, 245-308 on one
+    rank). ad_mode "forward": per block the jvp of sampler.propagate_phaseless_ad_norot
+    (do_sr=False: ..._nosr_norot) along the observable; "reverse": its vjp, the block's
+    one-body density matrix rdm1 = d energy / d h1, and the observable sum(rdm1 * op). A
+    non-finite result is replaced by the trial's value sum(rdm1_T * op) (and rdm1_T), then
+    the block weight, QR, global SR and e_estimate update of the non-AD branch follow.
+    observable: (op, constant) or None for (h1, 0) as driver.py:35-40. fields (optional):
     [n_blocks, n_sr, n_ene, n_prop, nw, G]; zetas (optional): [n_blocks, n_sr + 1].
     Returns device tensors (block_energy, block_observable, block_weight), each
-    [n_blocks], and prop_data."""
+    [n_blocks], and prop_data; in reverse mode prop_data["block_rdm1s"] holds the
+    [n_blocks, 2, norb, norb] density matrices."""
+    if ad_mode not in ("forward", "reverse"):
+        raise ValueError(f"ad_mode must be 'forward' or 'reverse', got {ad_mode!r}")
     if observable is None:
         op, const = torch.as_tensor(ham_data["h1"]), 0.0
     else:
@@ -62,11 +67,21 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
     bo = torch.empty(n_blocks, dtype=torch.float64, device=device())
     bw = torch.empty(n_blocks, dtype=torch.float64, device=device())
     n_sr = sampler.n_sr_blocks if do_sr else 1
+    rdm1s = None
+    if ad_mode == "reverse":
+        rdm1s = torch.empty((n_blocks, 2, trial.norb, trial.norb), dtype=torch.float64, device=device())
     for n in range(n_blocks):
         f = None if fields is None else fields[n]
         z_local = None if (zetas is None or not do_sr) else zetas[n][:n_sr]
-        e, de, prop_data = sampler.propagate_phaseless_ad_norot_jvp(
-            ham, ham_data, op, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f, zetas=z_local)
+        if ad_mode == "forward":
+            e, de, prop_data = sampler.propagate_phaseless_ad_norot_jvp(
+                ham, ham_data, op, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f, zetas=z_local)
+        else:
+            e, r, prop_data = sampler.propagate_phaseless_ad_norot_vjp(
+                ham, ham_data, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f, zetas=z_local)
+            de = torch.sum(r * op)
+            ok = torch.isfinite(de)
+            rdm1s[n].copy_(torch.where(ok, r, rdm1.to(r.dtype)))
         be[n].copy_(e)
         bo[n].copy_(torch.where(torch.isfinite(de), de, trial_observable) + const)
         if zetas is None:
@@ -77,4 +92,6 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
         st = prop_data.state(eng)
         _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), be[n:].data_ptr(), zg.data_ptr(),
                   bw[n:].data_ptr(), stream_ptr())
+    if rdm1s is not None:
+        dict.__setitem__(prop_data, "block_rdm1s", rdm1s)
     return be, bo, bw, prop_data

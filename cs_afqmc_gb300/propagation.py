@@ -222,9 +222,21 @@ class propagator_restricted:
         _, v0, v1 = self._mf_v0_v1(ham_data, trial, wave_data)
         return self._exp_h1_tangent(as_dev(ham_data["h1"]), v0, v1, as_dev(dh1))
 
+    def exp_h1_cotangent(self, ham_data: dict, trial, wave_data: dict, gexp) -> torch.Tensor:
+        """Transpose of exp_h1_tangent: d energy / d h1 per spin [2, norb, norb] (before the
+        symmetrisation) from d energy / d exp_h1. The transpose of the Frechet derivative
+        L(A, .) of expm is L(A^T, .)."""
+        _, v0, v1 = self._mf_v0_v1(ham_data, trial, wave_data)
+        return self._exp_h1_cotangent(as_dev(ham_data["h1"]), v0, v1, gexp)
+
     def _exp_h1(self, h1, v0, v1):
         h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
         return torch.linalg.matrix_exp(-self.dt * h1_mod / 2.0).contiguous()
+
+    def _exp_h1_cotangent(self, h1, v0, v1, gexp):
+        h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
+        g = -self.dt / 4.0 * expm_frechet((-self.dt * h1_mod / 2.0).T.contiguous(), as_dev(gexp))
+        return torch.stack([g, g])
 
     def _exp_h1_tangent(self, h1, v0, v1, dh1):
         h1_mod = (h1[0] + h1[1]) / 2.0 - v0 - v1
@@ -276,6 +288,10 @@ class propagator_unrestricted(propagator_restricted):
     def _exp_h1_tangent(self, h1, v0, v1, dh1):
         return torch.stack([expm_frechet(-self.dt * (h1[s] - v0 - v1) / 2.0, -self.dt * dh1[s] / 2.0)
                             for s in range(2)]).contiguous()
+
+    def _exp_h1_cotangent(self, h1, v0, v1, gexp):
+        return torch.stack([-self.dt / 2.0 * expm_frechet((-self.dt * (h1[s] - v0 - v1) / 2.0).T.contiguous(),
+                                                          as_dev(gexp[s])) for s in range(2)])
 
     def __hash__(self) -> int:
         return super().__hash__()

@@ -166,22 +166,7 @@ class sampler:
             drot_up, drot_dn = drot
         else:
             drot_up, drot_dn = drot, None
-        want = (n_sr, self.n_ene_blocks, self.n_prop_steps, eng.nw, eng.nchol)
-        if fields is None:
-            f = torch.empty(want, dtype=torch.float64, device=device())
-            key: RngKey = prop_data["key"]
-            _lib.call("afq_fill_normal", f.data_ptr(), f.numel(), key.seed, key.take(f.numel()),
-                      stream_ptr())
-        else:
-            f = as_dev(fields)
-        if f.numel() != nblk * self.n_prop_steps * eng.nw * eng.nchol:
-            raise _lib.AfqError(f"fields must have shape {want}")
-        if do_sr:
-            z = self.draw_zetas(prop_data, n_sr) if zetas is None else as_dev(zetas)
-            if z.numel() != n_sr:
-                raise _lib.AfqError(f"zetas must have {n_sr} entries")
-        else:
-            z = None
+        f, z = self._ad_draws(eng, prop_data, n_sr, do_sr, fields, zetas)
         tws = getattr(eng, "tangent_workspace", None)
         nbytes = eng.lib.afq_tangent_workspace_size(ctypes.byref(eng.dims))
         if nbytes == 0:
@@ -205,6 +190,76 @@ class sampler:
         dict.__setitem__(prop_data, "dblock_energies", dbe)
         dict.__setitem__(prop_data, "dblock_weights", dbw)
         return energy[0], denergy[0], prop_data
+
+    def _ad_draws(self, eng, prop_data: PropData, n_sr: int, do_sr: bool, fields, zetas):
+        """Fields [n_sr, n_ene, n_prop, nw, nchol] and SR uniforms [n_sr] of one AD block,
+        drawn from prop_data["key"] where not given."""
+        nblk = n_sr * self.n_ene_blocks
+        want = (n_sr, self.n_ene_blocks, self.n_prop_steps, eng.nw, eng.nchol)
+        if fields is None:
+            f = torch.empty(want, dtype=torch.float64, device=device())
+            key: RngKey = prop_data["key"]
+            _lib.call("afq_fill_normal", f.data_ptr(), f.numel(), key.seed, key.take(f.numel()),
+                      stream_ptr())
+        else:
+            f = as_dev(fields)
+        if f.numel() != nblk * self.n_prop_steps * eng.nw * eng.nchol:
+            raise _lib.AfqError(f"fields must have shape {want}")
+        if do_sr:
+            z = self.draw_zetas(prop_data, n_sr) if zetas is None else as_dev(zetas)
+            if z.numel() != n_sr:
+                raise _lib.AfqError(f"zetas must have {n_sr} entries")
+        else:
+            z = None
+        return f, z
+
+    def propagate_phaseless_ad_norot_vjp(self, ham, ham_data: dict, prop, prop_data: PropData, trial,
+                                         wave_data: dict, do_sr: bool = True,
+                                         fields: Optional[torch.Tensor] = None,
+                                         zetas: Optional[torch.Tensor] = None):
+        """Reverse-mode derivative of propagate_phaseless_ad_norot (do_sr=False:
+        propagate_phaseless_ad_nosr_norot): what driver.py:217-224 computes with jax.vjp at
+        coupling 1 and a zero rdm_op, i.e. the gradient of the block energy with respect to
+        h1, the block's one-body density matrix estimate. Returns (energy 0-d, rdm1
+        [2, norb, norb], prop_data), CUDA tensors; prop_data also gets "block_energies" and
+        "block_weights". FP64 (complex128) walkers only."""
+        eng = prop._engine(trial, ham_data, wave_data, prop_data["walkers"])
+        if eng.precision != _lib.AFQ_PREC_FP64:
+            raise _lib.AfqError("the derivative path needs FP64 (complex128) walkers")
+        dict.__setitem__(prop_data, "_engine", eng)
+        n_sr = self.n_sr_blocks if do_sr else 1
+        nblk = n_sr * self.n_ene_blocks
+        f, z = self._ad_draws(eng, prop_data, n_sr, do_sr, fields, zetas)
+        nbytes = eng.lib.afq_vjp_workspace_size(ctypes.byref(eng.dims), self.n_prop_steps,
+                                                self.n_ene_blocks, n_sr)
+        if nbytes == 0:
+            raise _lib.AfqError("afq_vjp_workspace_size: " + eng.lib.afq_last_error().decode())
+        vws = getattr(eng, "vjp_workspace", None)
+        if vws is None or vws.numel() < nbytes + 256:
+            vws = torch.empty(nbytes + 256, dtype=torch.uint8, device=device())
+            eng.vjp_workspace = vws
+        vptr = vws.data_ptr() + (-vws.data_ptr()) % 256
+        norb = trial.norb
+        out = torch.empty(2 * nblk + 1, dtype=torch.float64, device=device())
+        be, bw, energy = out[:nblk], out[nblk:2 * nblk], out[2 * nblk:]
+        gexp = torch.empty((2, norb, norb), dtype=torch.float64, device=device())
+        n_up, n_dn = trial.nelec
+        uhf_trial = isinstance(wave_data["mo_coeff"], (list, tuple))
+        grot = ([torch.empty((n_up, norb), dtype=torch.float64, device=device()),
+                 torch.empty((n_dn, norb), dtype=torch.float64, device=device())] if uhf_trial
+                else [torch.empty((n_up, norb), dtype=torch.float64, device=device()), None])
+        st = prop_data.state(eng)
+        _lib.call("afq_propagate_phaseless_vjp", eng.ctx, ctypes.byref(st), vptr, nbytes, f.data_ptr(),
+                  None if z is None else z.data_ptr(), self.n_prop_steps, self.n_ene_blocks, n_sr,
+                  0 if do_sr else _lib.AFQ_JVP_NO_SR, be.data_ptr(), bw.data_ptr(), energy.data_ptr(),
+                  gexp[0].data_ptr(), gexp[1].data_ptr() if not prop.restricted else None,
+                  grot[0].data_ptr(), None if grot[1] is None else grot[1].data_ptr(), stream_ptr())
+        g_exp = prop.exp_h1_cotangent(ham_data, trial, wave_data, gexp if not prop.restricted else gexp[0])
+        g_rot = trial.rot_h1_cotangent(grot if uhf_trial else grot[0], wave_data)
+        rdm1 = _sym(g_exp + g_rot)  # the transpose of the per-spin symmetrisation is itself
+        dict.__setitem__(prop_data, "block_energies", be)
+        dict.__setitem__(prop_data, "block_weights", bw)
+        return energy[0], rdm1, prop_data
 
     def __hash__(self) -> int:
         return hash((self.n_prop_steps, self.n_ene_blocks, self.n_sr_blocks, self.n_blocks))

@@ -138,6 +138,13 @@ class rhf(wave_function):
         dh1 = as_dev(dh1)
         return (mo.T @ ((dh1[0] + dh1[1]) / 2.0)).contiguous()
 
+    def rot_h1_cotangent(self, grot, wave_data: dict) -> torch.Tensor:
+        """Transpose of rot_h1_tangent: d energy / d h1 per spin [2, norb, norb] (before the
+        symmetrisation) from d energy / d rot_h1 [nocc, norb]."""
+        mo = as_dev(wave_data["mo_coeff"])
+        g = mo @ as_dev(grot) / 2.0
+        return torch.stack([g, g])
+
     def __hash__(self) -> int:
         return super().__hash__()
 
@@ -176,6 +183,12 @@ class uhf(wave_function):
         a, b = as_dev(mo[0]), as_dev(mo[1])
         dh1 = as_dev(dh1)
         return [(a.T @ dh1[0]).contiguous(), (b.T @ dh1[1]).contiguous()]
+
+    def rot_h1_cotangent(self, grot, wave_data: dict) -> torch.Tensor:
+        """Transpose of rot_h1_tangent: [2, norb, norb] from the per-spin d energy / d rot_h1."""
+        mo = wave_data["mo_coeff"]
+        a, b = as_dev(mo[0]), as_dev(mo[1])
+        return torch.stack([a @ as_dev(grot[0]), b @ as_dev(grot[1])])
 
     def __hash__(self) -> int:
         return super().__hash__()

@@ -253,7 +253,7 @@ int afq_cpmc_continuous_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int3
 /* Bytes of device tangent workspace afq_propagate_phaseless_jvp needs. 0 on bad sizes. */
 size_t afq_tangent_workspace_size(const afq_dims* dims);
 
-/* flags of afq_propagate_phaseless_jvp */
+/* flags of afq_propagate_phaseless_jvp and afq_propagate_phaseless_vjp */
 enum {
   AFQ_JVP_NO_SR = 1 /* no local SR after the energy blocks (the _nosr variants,
                        sampling.py:221-254, 287-317); needs n_sr_blocks == 1, zetas may be NULL */
@@ -281,6 +281,36 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
                                 double* block_weight, double* dblock_energy,
                                 double* dblock_weight, double* energy, double* denergy,
                                 void* stream);
+
+/* ---- reverse-mode derivative of the block (differentiation pattern, FP64) ------------ */
+
+/* Bytes of device workspace afq_propagate_phaseless_vjp needs for these block counts (the
+ * recorded forward sweep grows with n_prop_steps * n_ene_blocks * n_sr_blocks). 0 on bad
+ * sizes. */
+size_t afq_vjp_workspace_size(const afq_dims* dims, int32_t n_prop_steps, int32_t n_ene_blocks,
+                              int32_t n_sr_blocks);
+
+/* afq_propagate_phaseless together with the gradient of its energy with respect to the
+ * propagator's exp_h1 and the measurement intermediate rot_h1, the trial held fixed: the
+ * reverse pass of the vjp that driver.py:217-229 takes of
+ * sampler.propagate_phaseless_ad_norot (sampling.py:266-285; with AFQ_JVP_NO_SR in flags the
+ * _nosr_norot variant, 287-317) with cotangent 1 on the energy. The caller maps the two
+ * gradients to d energy / d h1 (the block's one-body density matrix estimate) through the
+ * transposed Frechet derivative of expm and the trial's rotation. Outputs (device, float64,
+ * overwritten): gexp_h1_up/dn [norb, norb] per walker slab (dn NULL for restricted walkers)
+ * and grot_h1_up/dn with the layout of rot_h1_up/dn (dn NULL for the RHF trial). Values
+ * (walkers, weights, overlaps, scalars, block_energy, block_weight, energy) are those of
+ * afq_propagate_phaseless on the same draws. Clamped quantities (weights set to 0, local
+ * energies replaced by e_estimate) pass no gradient, as jnp.where's transpose gives.
+ * vjp_workspace: 256-B aligned device memory of afq_vjp_workspace_size(dims, ...) bytes; it
+ * records the forward sweep (walkers, weights, overlaps and shifts before every step and
+ * around every QR) and holds the backward sweep's cotangents. FP64 contexts only. */
+int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp_workspace,
+                                size_t vjp_workspace_bytes, const double* fields, const double* zetas,
+                                int32_t n_prop_steps, int32_t n_ene_blocks, int32_t n_sr_blocks,
+                                int32_t flags, double* block_energy, double* block_weight,
+                                double* energy, double* gexp_h1_up, double* gexp_h1_dn,
+                                double* grot_h1_up, double* grot_h1_dn, void* stream);
 
 /* ---- correlated sampling (ad_afqmc/corr_sample/corr_sample.py) ---------------------- */
 

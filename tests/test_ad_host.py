@@ -32,6 +32,19 @@ def test_expm_frechet_is_the_derivative():
     assert np.max(np.abs(got - fd)) < 1e-8
 
 
+def test_expm_frechet_transpose():
+    """<G, L(A, E)> = <L(A^T, G), E>: the transpose the reverse mode applies to the
+    exp_h1 cotangent (A non-symmetric here, so the transpose is exercised)."""
+    from cs_afqmc_gb300.propagation import expm_frechet
+    rng = np.random.default_rng(4)
+    a = torch.as_tensor(rng.standard_normal((7, 7)) * 0.2)
+    e = torch.as_tensor(rng.standard_normal((7, 7)))
+    g = torch.as_tensor(rng.standard_normal((7, 7)))
+    lhs = float(torch.sum(g * expm_frechet(a, e)))
+    rhs = float(torch.sum(expm_frechet(a.T.contiguous(), g) * e))
+    assert abs(lhs - rhs) < 1e-12 * max(1.0, abs(lhs))
+
+
 def _small_system(kind="rhf", restricted=True, norb=6, nelec=(2, 2), nchol=8, nw=4, seed=5):
     from cs_afqmc_gb300 import synthetic
     s = synthetic.molecular(norb, nelec, nchol, seed=seed, kind=kind)
