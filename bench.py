@@ -720,10 +720,17 @@ def ad_derivative(w: dict, name: str, d, steps: int, n_prop: int) -> dict:
     check = {"jvp": de0.item(), "central_difference": fd, "abs_diff": abs(de0.item() - fd),
              "lambda": lam, "richardson": True}
 
-    def timed(ad: bool):
+    _, r0, _ = samp.propagate_phaseless_ad_norot_vjp(ham, hd, prop, fresh(), trial, wave, fields=f0, zetas=z0)
+    check["vjp_sum_rdm1_op"] = float(torch.sum(r0 * torch.as_tensor(op, device=r0.device)))
+    check["vjp_minus_jvp"] = abs(check["vjp_sum_rdm1_op"] - de0.item())
+
+    def timed(mode: str):
         pd = fresh()
-        run = (lambda k, p: driver.run_blocks_ad(samp, ham, hd, prop, p, trial, wave, k, observable=(op, 0.0))) \
-            if ad else (lambda k, p: driver.run_blocks(samp, ham, hd, prop, p, trial, wave, k))
+        if mode == "value":
+            run = lambda k, p: driver.run_blocks(samp, ham, hd, prop, p, trial, wave, k)
+        else:
+            run = lambda k, p: driver.run_blocks_ad(samp, ham, hd, prop, p, trial, wave, k, observable=(op, 0.0),
+                                                    ad_mode=mode)
         out = run(1, pd)  # warm-up block
         pd = out[-1]
         torch.cuda.synchronize()
@@ -735,9 +742,11 @@ def ad_derivative(w: dict, name: str, d, steps: int, n_prop: int) -> dict:
         torch.cuda.synchronize()
         return out, t0.elapsed_time(t1) / 1e3
 
-    (be, bo, bw, _), sec = timed(True)
-    (be_v, bw_v, _), sec_v = timed(False)
+    (be, bo, bw, _), sec = timed("forward")
+    (be_r, bo_r, bw_r, _), sec_r = timed("reverse")
+    (be_v, bw_v, _), sec_v = timed("value")
     be, bo, bw = (x.cpu().numpy() for x in (be, bo, bw))
+    bo_r = bo_r.cpu().numpy()
     obs = float(np.sum(bo * bw) / np.sum(bw))
     return {
         "dE_dlambda": obs,
@@ -752,6 +761,14 @@ def ad_derivative(w: dict, name: str, d, steps: int, n_prop: int) -> dict:
         "first_block_check": check,
         "estimator": "driver forward mode: block observable = d(block energy)/dlambda with SR per "
                      "block; clamped quantities have zero derivative",
+        "reverse_mode": {
+            "walker_steps_per_s": steps * n_prop * w["n_walkers"] / sec_r,
+            "cost_vs_value": sec_r / sec_v,
+            "energy_equals_value_driver": bool(np.allclose(be_r.cpu().numpy(), be_v.cpu().numpy(), rtol=1e-9,
+                                                           atol=0)),
+            "max_abs_diff_vs_forward_per_block": float(np.max(np.abs(bo_r - bo))),
+            "output": "rdm1 = d(block energy)/d h1 [2, norb, norb] per block; observable sum(rdm1 * D)",
+        },
     }
 
 
