@@ -77,6 +77,9 @@ _SIGS = {
     "afq_cpmc_continuous_propagate": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                      ctypes.c_int32, ctypes.c_double, ctypes.c_double, _vp,
                                                      _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "afq_cpmc_nn_propagate": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int32,
+                                             _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "afq_tangent_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(Dims)]),
     "afq_propagate_phaseless_jvp": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp, _vp, _vp,
                                                    _vp, ctypes.c_size_t, _vp, _vp, ctypes.c_int32,

@@ -1044,6 +1044,22 @@ int afq_cpmc_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walke
                           walkers_dn, weights, overlaps, greens, scalars, gaussian, 1, S(stream));
 }
 
+int afq_cpmc_nn_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, double dt, double u,
+                          double u_1, const int32_t* neighbors, int32_t n_pairs, const double* exp_h1_up,
+                          const double* exp_h1_dn, const double* trial_up, const double* trial_dn,
+                          double* walkers_up, double* walkers_dn, double* weights, double* overlaps,
+                          double* greens, double* scalars, const double* uniforms, void* stream) {
+  if (!exp_h1_up || !exp_h1_dn || !trial_up || !trial_dn || !walkers_up || !walkers_dn || !weights || !overlaps ||
+      !greens || !scalars || !uniforms || (n_pairs > 0 && !neighbors) || n_pairs < 0) {
+    afq_set_error("NULL argument or negative n_pairs");
+    return -1;
+  }
+  if (!(dt > 0.0)) { afq_set_error("dt must be positive"); return -1; }
+  return afq::launch_cpmc(norb, n_up, n_dn, n_walkers, dt, u, exp_h1_up, exp_h1_dn, trial_up, trial_dn, walkers_up,
+                          walkers_dn, weights, overlaps, greens, scalars, nullptr, 3, S(stream), u_1, neighbors,
+                          n_pairs, uniforms);
+}
+
 int afq_cpmc_continuous_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, double dt,
                                   double hs_constant, const double* exp_h1_up, const double* exp_h1_dn,
                                   const double* trial_up, const double* trial_dn, double* walkers_up,

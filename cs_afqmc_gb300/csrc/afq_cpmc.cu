@@ -2,8 +2,10 @@
 // uhf_cpmc trial wavefunctions.py:848-955), FP64 with real walkers, one CTA per walker:
 // one-body half step, overlap and full Green's functions, a sweep over the sites choosing a
 // discrete Hubbard-Stratonovich field per site from the overlap ratios with rank-one
-// Green's-function updates, one-body half step, weights and the pop-control shift; and the
-// continuous-field variant (propagation.py:1595-1675).
+// Green's-function updates, one-body half step, weights and the pop-control shift; the
+// variant with a nearest-neighbour interaction (propagation.py:889-1230), whose neighbour
+// sweep makes two-entry updates within one spin as well; and the continuous-field variant
+// (propagation.py:1595-1675).
 
 #include <math.h>
 
@@ -19,7 +21,11 @@ constexpr int kCpmcMaxOcc = 32;
 struct CpmcDev {
   int norb, no[2], nw;
   double dt;
-  double hs[2][2];  // [field][spin] Hubbard-Stratonovich constants
+  double hs[2][2];   // [field][spin] Hubbard-Stratonovich constants
+  double hsn[2][2];  // [field][entry] constants of the neighbour interaction
+  const int32_t* nbr;  // [npairs][2] neighbour sites
+  int npairs;
+  const double* unif;  // [nw][norb + 4 npairs] uniforms of the neighbour variant
   const double* exph[2];
   const double* trial[2];
   double* w[2];
@@ -131,12 +137,79 @@ __device__ double cpmc_one_body(const CpmcDev& d, double* G, double* Ws, double*
   return det;
 }
 
+// Two-entry discrete-field update at (spin si, site i), (spin sj, site j)
+// (wavefunctions.py:873-945 with propagation.py:949-1220): ratios of both fields from G,
+// the field chosen with probability r0 / (r0 + r1) against `uni`, the walker rows scaled,
+// overlap * ratio, weight * (r0 + r1) / 2 (thread 0's ov and w), and G updated with both
+// steps built from G before the update: the exact rank-two update when si == sj (the
+// reference's code reads column j after its first step, which is not; its test checks the
+// fast form against the determinant form, which this one matches). Neighbour pairs have
+// i != j, so the two scaled rows never coincide.
+__device__ void cpmc_pair_update(const CpmcDev& d, double* G, double* Ws, int kmax, int si, int i, int sj, int j,
+                                 bool nn, double uni, double& ov, double& w, double* sc, double* coli,
+                                 double* colj, double* sgi, double* sgj) {
+  const int n = d.norb, tid = threadIdx.x, nt = blockDim.x;
+  double* Gi = G + (size_t)si * n * n;
+  double* Gj = G + (size_t)sj * n * n;
+  const bool same = si == sj;
+  if (tid == 0) {
+    const double gii = Gi[i * n + i], gjj = Gj[j * n + j];
+    const double gij = same ? Gi[i * n + j] : 0.0, gji = same ? Gj[j * n + i] : 0.0;
+    double r[2];
+    for (int f = 0; f < 2; ++f) {
+      const double c0 = (nn ? d.hsn[f][0] : d.hs[f][0]) - 1.0, c1 = (nn ? d.hsn[f][1] : d.hs[f][1]) - 1.0;
+      r[f] = (1.0 + c0 * gii) * (1.0 + c1 * gjj) - c0 * c1 * gij * gji;
+      if (r[f] < 1.0e-8) r[f] = 0.0;
+    }
+    double p0 = r[0] / 2.0;
+    const double p1 = r[1] / 2.0, norm = p0 + p1;
+    p0 /= norm;
+    const int f = uni < p0 ? 0 : 1;
+    sc[0] = nn ? d.hsn[f][0] : d.hs[f][0];
+    sc[1] = nn ? d.hsn[f][1] : d.hs[f][1];
+    sc[2] = r[f];
+    sc[3] = gii;
+    sc[4] = gjj;
+    sc[5] = gij;
+    sc[6] = gji;
+    ov *= r[f];
+    w *= norm;
+  }
+  for (int e = tid; e < n; e += nt) {
+    coli[e] = Gi[(size_t)e * n + i];
+    colj[e] = Gj[(size_t)e * n + j];
+    sgi[e] = Gi[(size_t)i * n + e] - (e == i ? 1.0 : 0.0);
+    sgj[e] = Gj[(size_t)j * n + e] - (e == j ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  const double c0 = sc[0], c1 = sc[1], ratio = sc[2], gii = sc[3], gjj = sc[4], gij = sc[5], gji = sc[6];
+  const double uc0 = c0 - 1.0, uc1 = c1 - 1.0, fi = uc0 / ratio, fj = uc1 / ratio;
+  const int oi = d.no[si], oj = d.no[sj];
+  for (int e = tid; e < oi + oj; e += nt) {
+    if (e < oi) Ws[(size_t)si * n * kmax + (size_t)i * oi + e] *= c0;
+    else Ws[(size_t)sj * n * kmax + (size_t)j * oj + (e - oi)] *= c1;
+  }
+  for (int e = tid; e < n * n; e += nt) {
+    const int a = e / n, b = e % n;
+    const double vi = uc1 * (gij * sgj[b] - gjj * sgi[b]) - sgi[b];
+    const double vj = uc0 * (gji * sgi[b] - gii * sgj[b]) - sgj[b];
+    if (same) {
+      Gi[e] += fi * coli[a] * vi + fj * colj[a] * vj;
+    } else {
+      Gi[e] += fi * coli[a] * vi;
+      Gj[e] += fj * colj[a] * vj;
+    }
+  }
+  __syncthreads();
+}
+
 // mode 0: overlaps and Green's functions of the given walkers; mode 1: one CPMC step;
-// mode 2: one step of the continuous-field variant (no Green's functions)
+// mode 2: one step of the continuous-field variant (no Green's functions); mode 3: one step
+// with the nearest-neighbour interaction
 __global__ void __launch_bounds__(kCpmcThreads) k_cpmc(const CpmcDev d, int mode) {
   extern __shared__ __align__(16) double csm[];
   __shared__ double colx[2][64], rowx[2][64];
-  __shared__ double sc_sh[6];
+  __shared__ double sc_sh[8];
   const int wl = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, n = d.norb;
   const int kmax = d.no[0] > d.no[1] ? d.no[0] : d.no[1];
   double* G = csm;                             // [2][n][n]
@@ -188,8 +261,25 @@ __global__ void __launch_bounds__(kCpmcThreads) k_cpmc(const CpmcDev d, int mode
       if (w < 1.0e-8) w = 0.0;
       ov = det;
     }
+    if (mode == 3) {
+      // on-site sweep, then four two-entry updates per neighbour pair (propagation.py:944-1218)
+      const double* un = d.unif + (size_t)wl * (n + 4 * d.npairs);
+      for (int x = 0; x < n; ++x)
+        cpmc_pair_update(d, G, Ws, kmax, 0, x, 1, x, false, un[x], ov, w, sc_sh, colx[0], colx[1], rowx[0],
+                         rowx[1]);
+      for (int p = 0; p < d.npairs; ++p) {
+        const int i = d.nbr[2 * p], j = d.nbr[2 * p + 1];
+        if (i < 0 || i >= n || j < 0 || j >= n || i == j) {  // checked on the host as well
+          if (tid == 0) d.scalars[AFQ_S_STATUS] = 3.0;
+          continue;
+        }
+        for (int k = 0; k < 4; ++k)
+          cpmc_pair_update(d, G, Ws, kmax, k >> 1, i, k & 1, j, true, un[n + k * d.npairs + p], ov, w, sc_sh,
+                           colx[0], colx[1], rowx[0], rowx[1]);
+      }
+    }
     // sweep over the sites (propagation.py:594-648)
-    for (int x = 0; x < n; ++x) {
+    for (int x = 0; x < (mode == 1 ? n : 0); ++x) {
       if (tid == 0) {
         const double guu = G[(size_t)x * n + x], gdd = G[(size_t)n * n + (size_t)x * n + x];
         double r[2];
@@ -267,7 +357,7 @@ __global__ void k_cpmc_pop_control(int nw, double dt, const double* __restrict__
 int launch_cpmc(int norb, int n_up, int n_dn, int nw, double dt, double u, const double* exp_up,
                 const double* exp_dn, const double* trial_up, const double* trial_dn, double* w_up, double* w_dn,
                 double* weights, double* overlaps, double* greens, double* scalars, const double* gauss, int mode,
-                cudaStream_t st) {
+                cudaStream_t st, double u1, const int32_t* neighbors, int npairs, const double* uniforms) {
   if (norb < 1 || norb > 64 || n_up < 1 || n_dn < 1 || n_up > kCpmcMaxOcc || n_dn > kCpmcMaxOcc || n_up > norb ||
       n_dn > norb || nw < 1) {
     afq_set_error("cpmc: sizes out of range (norb <= 64, 1 <= n_up, n_dn <= min(32, norb))");
@@ -288,6 +378,22 @@ int launch_cpmc(int norb, int n_up, int n_dn, int nw, double dt, double u, const
     d.hs[1][0] = cst * exp(-gamma);
     d.hs[1][1] = cst * exp(gamma);
   }
+  if (mode == 3) {
+    if (npairs < 0 || (npairs > 0 && !neighbors) || !uniforms) {
+      afq_set_error("cpmc: neighbour variant needs the neighbour list and the uniforms");
+      return -1;
+    }
+    const double g1 = acosh(exp(dt * u1 / 2.0)), c1 = exp(-dt * u1 / 2.0);
+    d.hsn[0][0] = c1 * exp(g1);
+    d.hsn[0][1] = c1 * exp(-g1);
+    d.hsn[1][0] = c1 * exp(-g1);
+    d.hsn[1][1] = c1 * exp(g1);
+  } else {
+    d.hsn[0][0] = d.hsn[0][1] = d.hsn[1][0] = d.hsn[1][1] = 0.0;
+  }
+  d.nbr = neighbors;
+  d.npairs = mode == 3 ? npairs : 0;
+  d.unif = uniforms;
   d.exph[0] = exp_up;
   d.exph[1] = exp_dn;
   d.trial[0] = trial_up;

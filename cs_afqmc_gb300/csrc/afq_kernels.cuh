@@ -63,11 +63,13 @@ int launch_free_scale(const afq_ctx_dev& c, const double2* consts, void* wu, voi
 int launch_free_finish(int nw, const double2* rdiag, double2* norms, double2* ovl, cudaStream_t st);
 int launch_free_block_stats(int nw, const double2* energy, const double2* ovl, double2* be, double2* bw,
                             cudaStream_t st);
-// CPMC, Hubbard on-site U (afq_cpmc.cu); mode 0: overlaps and Green's functions, 1: one step
+// CPMC, Hubbard on-site U (afq_cpmc.cu); mode 0: overlaps and Green's functions, 1: one step,
+// 2: continuous fields, 3: one step with the nearest-neighbour interaction
 int launch_cpmc(int norb, int n_up, int n_dn, int nw, double dt, double u, const double* exp_up,
                 const double* exp_dn, const double* trial_up, const double* trial_dn, double* w_up, double* w_dn,
                 double* weights, double* overlaps, double* greens, double* scalars, const double* gauss, int mode,
-                cudaStream_t st);
+                cudaStream_t st, double u1 = 0.0, const int32_t* neighbors = nullptr, int npairs = 0,
+                const double* uniforms = nullptr);
 int launch_fill_normal(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t st);
 int launch_fill_uniform(double* out, int64_t n, uint64_t seed, uint64_t offset, cudaStream_t st);
 }  // namespace afq

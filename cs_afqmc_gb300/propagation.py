@@ -375,6 +375,82 @@ class propagator_cpmc(propagator_unrestricted):
 
 
 @dataclass
+class propagator_cpmc_nn(propagator_cpmc):
+    """CPMC with on-site U and a nearest-neighbour interaction ham_data["u_1"]
+    (propagator_cpmc_nn, propagation.py:889-1230), FP64 with real walkers. neighbors: a
+    tuple of site pairs (i, j), i != j. The two-entry updates within one spin use the exact
+    rank-two Green's-function update (the reference's fast form reads a column after its
+    first step; its test checks that form against the determinant form, which this one
+    matches)."""
+
+    neighbors: Optional[tuple] = None
+
+    def init_prop_data(self, trial, wave_data: dict, ham_data: dict, init_walkers=None) -> PropData:
+        """propagator_cpmc's state plus hs_constant_onsite and hs_constant_nn
+        (propagation.py:893-918)."""
+        pd = super().init_prop_data(trial, wave_data, ham_data, init_walkers)
+        dict.__setitem__(pd, "hs_constant_onsite", pd["hs_constant"])
+        u1 = float(np.real(_engine._scalar(ham_data["u_1"])))
+        gamma = math.acosh(math.exp(self.dt * u1 / 2))
+        c = math.exp(-self.dt * u1 / 2)
+        dict.__setitem__(pd, "hs_constant_nn", torch.tensor(
+            [[c * math.exp(gamma), c * math.exp(-gamma)], [c * math.exp(-gamma), c * math.exp(gamma)]],
+            dtype=torch.float64, device=device()))
+        return pd
+
+    def _neighbor_array(self, norb: int) -> torch.Tensor:
+        nb = getattr(self, "_nbr_dev", None)
+        if nb is None or nb[0] != (norb, self.neighbors):
+            pairs = np.asarray(self.neighbors if self.neighbors is not None else (), dtype=np.int64).reshape(-1, 2)
+            if pairs.size and (pairs.min() < 0 or pairs.max() >= norb or np.any(pairs[:, 0] == pairs[:, 1])):
+                raise _lib.AfqError(f"neighbors must be pairs of distinct sites in [0, {norb})")
+            t = torch.as_tensor(pairs.astype(np.int32)).contiguous().to(device())
+            object.__setattr__(self, "_nbr_dev", ((norb, self.neighbors), t))
+            return t
+        return nb[1]
+
+    def propagate(self, trial, ham_data: dict, prop_data: PropData, _gaussian_rns, wave_data: dict,
+                  uniforms: Optional[torch.Tensor] = None) -> PropData:
+        """One step (propagation.py:920-1226). The reference ignores the Gaussians and draws
+        its uniforms from prop_data["key"]; here too, unless `uniforms`
+        [nw, norb + 4 npairs] is given (column x for site x, then norb + k npairs + p for
+        update k of pair p)."""
+        norb, (n_up, n_dn) = trial.norb, trial.nelec
+        nbr = self._neighbor_array(norb)
+        npairs = int(nbr.shape[0])
+        ncol = norb + 4 * npairs
+        if uniforms is None:
+            uni = torch.empty((self.n_walkers, ncol), dtype=torch.float64, device=device())
+            key: RngKey = prop_data["key"]
+            _lib.call("afq_fill_uniform", uni.data_ptr(), uni.numel(), key.seed, key.take(uni.numel()),
+                      stream_ptr())
+        else:
+            uni = as_dev(uniforms).contiguous()
+        if tuple(uni.shape) != (self.n_walkers, ncol):
+            raise _lib.AfqError(f"uniforms must be [{self.n_walkers}, {ncol}], got {tuple(uni.shape)}")
+        w = prop_data["walkers"]
+        e = ham_data["exp_h1"]
+        e = e if isinstance(e, torch.Tensor) else torch.as_tensor(np.asarray(e))
+        eu, ed = as_dev(e[0]).contiguous(), as_dev(e[1]).contiguous()
+        mo = wave_data["mo_coeff"]
+        cu, cd = as_dev(mo[0]).contiguous(), as_dev(mo[1]).contiguous()
+        for t in (w[0], w[1], prop_data["weights"], prop_data["overlaps"], prop_data["greens"]):
+            if t.dtype != torch.float64 or not t.is_contiguous():
+                raise _lib.AfqError("CPMC state must be contiguous float64 (init_prop_data of this class)")
+        u = float(np.real(_engine._scalar(ham_data["u"])))
+        u1 = float(np.real(_engine._scalar(ham_data["u_1"])))
+        _lib.call("afq_cpmc_nn_propagate", norb, n_up, n_dn, self.n_walkers, float(self.dt), u, u1,
+                  nbr.data_ptr() if npairs else None, npairs, eu.data_ptr(), ed.data_ptr(), cu.data_ptr(),
+                  cd.data_ptr(), w[0].data_ptr(), w[1].data_ptr(), prop_data["weights"].data_ptr(),
+                  prop_data["overlaps"].data_ptr(), prop_data["greens"].data_ptr(), prop_data["_scalars"].data_ptr(),
+                  uni.data_ptr(), stream_ptr())
+        return prop_data
+
+    def __hash__(self) -> int:
+        return hash((self.dt, self.n_walkers, self.neighbors))
+
+
+@dataclass
 class propagator_cpmc_continuous(propagator_cpmc):
     """Continuous-field CPMC (propagation.py:1595-1675): ham_data["hs_constant"] scales the
     Gaussian fields; no discrete sweep and no Green's functions. Real walkers, as

@@ -248,6 +248,23 @@ int afq_cpmc_continuous_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int3
                                   double* weights, double* overlaps, double* scalars,
                                   const double* gaussian, void* stream);
 
+/* One CPMC step with on-site U and a nearest-neighbour interaction u_1 (propagator_cpmc_nn,
+ * propagation.py:889-1230): one-body half step, the on-site sweep of
+ * afq_cpmc_propagate, then for every neighbour pair (i, j) four two-entry updates with the
+ * Hubbard-Stratonovich constants of u_1 on (up i, up j), (up i, dn j), (dn i, up j),
+ * (dn i, dn j), one-body half step, weights * exp(dt shift), the > 100 clamp and the new
+ * pop-control shift. neighbors: device int32 [n_pairs][2], sites in [0, norb), i != j (a
+ * bad pair is skipped and sets scalars[AFQ_S_STATUS] = 3). uniforms: device float64
+ * [n_walkers][norb + 4 n_pairs], column x for site x, then column norb + k n_pairs + p for
+ * update k of pair p (the reference draws both sets from its key). The two-entry updates
+ * within one spin use the exact rank-two Green's-function update. Other arguments as in
+ * afq_cpmc_propagate. */
+int afq_cpmc_nn_propagate(int32_t norb, int32_t n_up, int32_t n_dn, int32_t n_walkers, double dt, double u,
+                          double u_1, const int32_t* neighbors, int32_t n_pairs, const double* exp_h1_up,
+                          const double* exp_h1_dn, const double* trial_up, const double* trial_dn,
+                          double* walkers_up, double* walkers_dn, double* weights, double* overlaps,
+                          double* greens, double* scalars, const double* uniforms, void* stream);
+
 /* ---- forward-mode derivative of the block (differentiation pattern, FP64) ------------ */
 
 /* Bytes of device tangent workspace afq_propagate_phaseless_jvp needs. 0 on bad sizes. */

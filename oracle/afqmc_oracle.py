@@ -528,6 +528,92 @@ def cpmc_propagate(exp_h1, dt: float, u: float, pd: dict, gaussian, mo, e_estima
     return pd, pcs
 
 
+def _cpmc_pair_update(pd: dict, hs_pair, si: int, i: int, sj: int, j: int, uni, mo, slow: bool):
+    """One two-entry discrete-field update at (spin si, site i), (spin sj, site j) with the
+    constants hs_pair [field][entry] (propagation.py:949-1220). Fast: the ratio and the
+    two-step Green's-function update of uhf_cpmc (wavefunctions.py:873-945) with both steps
+    built from the Green's function before the update. (The reference's code reads column j
+    of the once-updated array in its second step; for two entries of one spin that is not
+    the exact rank-two update, and its own test asserts agreement with the slow form, which
+    the exact update gives.) Slow: determinant ratios (propagation.py:1263-1591)."""
+    w = pd["walkers"]
+    if slow:
+        cand, rat = [], []
+        for f in range(2):
+            wn = [w[0].copy(), w[1].copy()]
+            wn[si][:, i, :] *= hs_pair[f, 0]
+            wn[sj][:, j, :] *= hs_pair[f, 1]
+            ov = cpmc_overlap(wn, mo)
+            r = np.real(ov / pd["overlaps"]) / 2.0
+            rat.append(np.where(r < 1.0e-8, 0.0, r))
+            cand.append((wn, ov))
+        norm = rat[0] + rat[1]
+        m = uni < rat[0] / norm
+        pd["walkers"] = [np.where(m[:, None, None], cand[0][0][s], cand[1][0][s]) for s in range(2)]
+        pd["overlaps"] = np.where(m, cand[0][1], cand[1][1])
+        pd["weights"] = pd["weights"] * norm
+        return pd
+    g = pd["greens"]
+    same = 1.0 if si == sj else 0.0
+    rats = []
+    for f in range(2):
+        c = hs_pair[f] - 1
+        r = (1 + c[0] * g[:, si, i, i]) * (1 + c[1] * g[:, sj, j, j]) \
+            - same * c[0] * c[1] * g[:, si, i, j] * g[:, sj, j, i]
+        rats.append(np.where(r < 1.0e-8, 0.0, r))
+    p0, p1 = rats[0] / 2.0, rats[1] / 2.0
+    norm = p0 + p1
+    m = uni < p0 / norm
+    consts = np.where(m[:, None], hs_pair[0][None, :], hs_pair[1][None, :])
+    wn = [w[0].copy(), w[1].copy()]
+    wn[si][:, i, :] *= consts[:, 0:1]
+    wn[sj][:, j, :] *= consts[:, 1:2]
+    ratios = np.where(m, rats[0], rats[1])
+    uc = consts - 1
+    sg_i = g[:, si, i, :].copy()
+    sg_i[:, i] -= 1
+    sg_j = g[:, sj, j, :].copy()
+    sg_j[:, j] -= 1
+    g_ii, g_jj = g[:, si, i, i], g[:, sj, j, j]
+    g_ij, g_ji = same * g[:, si, i, j], same * g[:, sj, j, i]
+    gn = g.copy()
+    gn[:, si] += (uc[:, 0] / ratios)[:, None, None] * np.einsum(
+        "wa,wb->wab", g[:, si, :, i], uc[:, 1:2] * (g_ij[:, None] * sg_j - g_jj[:, None] * sg_i) - sg_i)
+    gn[:, sj] += (uc[:, 1] / ratios)[:, None, None] * np.einsum(
+        "wa,wb->wab", g[:, sj, :, j], uc[:, 0:1] * (g_ji[:, None] * sg_i - g_ii[:, None] * sg_j) - sg_j)
+    pd["walkers"] = wn
+    pd["greens"] = gn
+    pd["overlaps"] = ratios * pd["overlaps"]
+    pd["weights"] = pd["weights"] * norm
+    return pd
+
+
+def cpmc_nn_propagate(exp_h1, dt: float, u: float, u1: float, neighbors, pd: dict, uniforms, mo,
+                      e_estimate: float, pop_control_ene_shift: float, n_walkers: int, slow: bool = False):
+    """One step of CPMC with on-site U and nearest-neighbour V = u1 (propagator_cpmc_nn,
+    propagation.py:889-1230; slow: propagator_cpmc_nn_slow, 1232-1591): one-body half step,
+    the on-site sweep (fields from hs(u) on (up, x), (dn, x)), then for every neighbour pair
+    (i, j) four two-entry updates with hs(u1) on (up i, up j), (up i, dn j), (dn i, up j),
+    (dn i, dn j), one-body half step, weights * exp(dt E_pc), the > 100 clamp and the new
+    shift. uniforms [nw, norb + 4 npairs]: column x for site x, then norb + k npairs + p for
+    update k of pair p (the reference draws both sets from its key). Returns (pd, shift)."""
+    hs0 = cpmc_hs_constant(dt, u)
+    hs1 = cpmc_hs_constant(dt, u1)
+    norb = pd["walkers"][0].shape[1]
+    npairs = len(neighbors)
+    pd = _cpmc_one_body(exp_h1, pd, mo)
+    for x in range(norb):
+        pd = _cpmc_pair_update(pd, hs0, 0, x, 1, x, uniforms[:, x], mo, slow)
+    for p, (i, j) in enumerate(neighbors):
+        for k, (si, sj) in enumerate(((0, 0), (0, 1), (1, 0), (1, 1))):
+            pd = _cpmc_pair_update(pd, hs1, si, i, sj, j, uniforms[:, norb + k * npairs + p], mo, slow)
+    pd = _cpmc_one_body(exp_h1, pd, mo)
+    pd["weights"] = pd["weights"] * np.exp(dt * pop_control_ene_shift)
+    pd["weights"] = np.where(pd["weights"] > 100.0, 0.0, pd["weights"])
+    pcs = e_estimate - 0.1 * np.log(np.sum(pd["weights"]) / n_walkers) / dt
+    return pd, pcs
+
+
 def cpmc_continuous_propagate(exp_h1, dt: float, hs: float, pd: dict, gaussian, mo, e_estimate: float,
                               pop_control_ene_shift: float, n_walkers: int):
     """One step of the continuous-field CPMC variant (propagation.py:1595-1675; the force bias

@@ -97,3 +97,59 @@ def test_cpmc_continuous_steps():
     assert rel_err(to_np(pd["weights"]), po["weights"]) < 1e-9
     assert rel_err(to_np(pd["overlaps"]), po["overlaps"]) < 1e-9
     assert abs(pd["pop_control_ene_shift"].item() - pcs) < 1e-9 * max(1.0, abs(pcs))
+
+
+def _neighbors(lx, ly):
+    pairs = {tuple(sorted((x + lx * y, (x + 1) % lx + lx * y))) for y in range(ly) for x in range(lx)} | \
+        {tuple(sorted((x + lx * y, x + lx * ((y + 1) % ly)))) for y in range(ly) for x in range(lx)}
+    return tuple(p for p in sorted(pairs) if p[0] != p[1])
+
+
+@pytest.mark.parametrize("lx,ly,nelec", [(4, 2, (3, 3)), (4, 4, (7, 5))], ids=["4x2", "4x4"])
+def test_cpmc_nn_steps(lx, ly, nelec):
+    """propagator_cpmc_nn (propagation.py:889-1230) against the oracle's fast form on
+    identical uniforms: walkers, weights, overlaps, Green's functions and the shift."""
+    import torch
+    from cs_afqmc_gb300 import propagation
+    s, trial, wave, hd, prop, pd, w0, mo = _system(lx=lx, ly=ly, nelec=nelec)
+    nbr = _neighbors(lx, ly)
+    nprop = propagation.propagator_cpmc_nn(dt=prop.dt, n_walkers=prop.n_walkers, precision="fp64", neighbors=nbr)
+    hd["u_1"] = 1.0
+    pd = nprop.init_prop_data(trial, wave, hd, init_walkers=w0)
+    n = s.norb
+    exp_h1 = to_np(hd["exp_h1"])
+    po = O.cpmc_init(w0, mo)
+    e_est = pd["e_estimate"].item()
+    pcs = pd["pop_control_ene_shift"].item()
+    rng = np.random.default_rng(11)
+    for _ in range(3):
+        uni = rng.uniform(size=(prop.n_walkers, n + 4 * len(nbr)))
+        po, pcs = O.cpmc_nn_propagate(exp_h1, prop.dt, 4.0, 1.0, nbr, po, uni, mo, e_est, pcs, prop.n_walkers)
+        pd = nprop.propagate(trial, hd, pd, None, wave, uniforms=uni)
+    torch.cuda.synchronize()
+    assert pd["_scalars"][5].item() == 0.0  # no bad neighbour pair
+    assert rel_err(to_np(pd["walkers"][0]), po["walkers"][0]) < 1e-9
+    assert rel_err(to_np(pd["walkers"][1]), po["walkers"][1]) < 1e-9
+    assert rel_err(to_np(pd["weights"]), po["weights"]) < 1e-9
+    assert rel_err(to_np(pd["overlaps"]), po["overlaps"]) < 1e-9
+    assert rel_err(to_np(pd["greens"]), po["greens"]) < 1e-9
+    assert abs(pd["pop_control_ene_shift"].item() - pcs) < 1e-9 * max(1.0, abs(pcs))
+
+
+def test_cpmc_nn_draws_and_bad_pairs():
+    """Uniforms drawn from prop_data["key"] when not given; pairs outside the lattice or of
+    one site are refused on the host."""
+    from cs_afqmc_gb300 import _lib, propagation
+    from cs_afqmc_gb300.propagation import RngKey
+    s, trial, wave, hd, prop, pd, w0, mo = _system()
+    hd["u_1"] = 1.0
+    nprop = propagation.propagator_cpmc_nn(dt=prop.dt, n_walkers=prop.n_walkers, precision="fp64",
+                                           neighbors=_neighbors(4, 2))
+    pd = nprop.init_prop_data(trial, wave, hd, init_walkers=w0)
+    pd["key"] = RngKey(5)
+    pd = nprop.propagate(trial, hd, pd, None, wave)
+    assert np.all(np.isfinite(to_np(pd["weights"])))
+    for bad in (((0, 0),), ((0, s.norb),)):
+        p2 = propagation.propagator_cpmc_nn(dt=prop.dt, n_walkers=prop.n_walkers, precision="fp64", neighbors=bad)
+        with pytest.raises(_lib.AfqError):
+            p2.propagate(trial, hd, pd, None, wave)
