@@ -213,11 +213,23 @@ def engine_for(trial, ham_data: Optional[dict], wave_data: dict, walkers, *, dt:
         h0p = 0.0
     if restricted:
         a.pop("exp_h1_dn", None)
+    if prec == _lib.AFQ_PREC_MIXED and ham_data is not None and have_prop and \
+            not (int(mixed_config) & _lib.MIXED_EXPLICIT) and _diagonal_chol(a["chol"], norb):
+        # on-site lattice terms: the library replaces the vhs GEMM and the Taylor products by
+        # a per-row polynomial scale (and checks the diagonality itself)
+        mixed_config = (int(mixed_config) or _lib.MIXED_DEFAULT) | _lib.MIXED_DIAG_CHOL
     eng = Engine(norb=norb, nelec=nelec, nchol=nchol, n_walkers=nw, restricted=restricted, uhf=uhf,
                  precision=prec, dt=dt, n_exp_terms=n_exp_terms, n_batch=n_batch, arrays=a, h0=h0,
                  h0_prop=h0p, mixed_config=mixed_config)
     cache[key] = eng
     return eng
+
+
+def _diagonal_chol(chol: torch.Tensor, norb: int) -> bool:
+    """True when every Cholesky vector [norb, norb] is a diagonal matrix."""
+    c = chol.reshape(-1, norb, norb)
+    off = c - torch.diag_embed(torch.diagonal(c, dim1=1, dim2=2))
+    return bool(torch.count_nonzero(off).item() == 0)
 
 
 def _scalar(x):

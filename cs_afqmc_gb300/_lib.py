@@ -21,6 +21,9 @@ AFQ_S_E_ESTIMATE, AFQ_S_POP_CONTROL_SHIFT, AFQ_S_N_KILLED = 0, 1, 2
 AFQ_S_BLOCK_ENERGY, AFQ_S_BLOCK_WEIGHT, AFQ_S_STATUS = 3, 4, 5
 AFQ_NSCALARS = 8
 AFQ_JVP_NO_SR = 1
+MIXED_DEFAULT = 767          # the library's default accuracy options (afq_dims.mixed_config)
+MIXED_DIAG_CHOL = 1 << 15    # every Cholesky vector diagonal: per-row exp(vhs), no Taylor MMA
+MIXED_EXPLICIT = 1 << 30     # the caller's configuration as given (no automatic diagonal path)
 
 _vp = ctypes.c_void_p
 

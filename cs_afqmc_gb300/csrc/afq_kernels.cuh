@@ -34,9 +34,10 @@ template <typename WT>
 int launch_taylor_f64(const afq_ctx_dev& c, int w0, int nwc, const double2* vhs, void* wu, void* wd,
                       cudaStream_t st);
 // shift / fbt: per-walker partial sums [nw][ntiles] (summed here)
+// status (may be NULL): a device guard word folded into scalars[AFQ_S_STATUS]
 int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt, int ntiles,
                    const double2* ovl_new, double2* ovl, double* weights, double* scalars,
-                   cudaStream_t st);
+                   cudaStream_t st, const int* status = nullptr);
 int launch_energy_f64(const afq_ctx_dev& c, int nchunks, int gchunk, const double2* green,
                       double2* epart, double2* energy, cudaStream_t st);
 // rdiag (optional, [nslab][nw] complex): prod(diag R) per walker slab

@@ -354,14 +354,19 @@ __global__ void k_weights(int nw, double dt, double2 h0_prop, const double2* __r
 }
 
 // pop_control_ene_shift = e_estimate - 0.1 log(sum w / nw) / dt (propagation.py:161-163)
+// status (mixed path, may be NULL): the tensor-core pipeline's guard word, folded into
+// scalars[AFQ_S_STATUS] so that callers see a timeout or a bad operand in the state
 __global__ void k_pop_control(int nw, double dt, const double* __restrict__ weights,
-                              double* __restrict__ scalars) {
+                              double* __restrict__ scalars, const int* __restrict__ status) {
   __shared__ double red[32];
   double sum = 0.0;
   for (int w = threadIdx.x; w < nw; w += blockDim.x) sum += weights[w];
   sum = block_sum(sum, red);
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
     scalars[AFQ_S_POP_CONTROL_SHIFT] = scalars[AFQ_S_E_ESTIMATE] - 0.1 * log(sum / (double)nw) / dt;
+    if (status && *status != 0)
+      scalars[AFQ_S_STATUS] = (double)((int)scalars[AFQ_S_STATUS] | *status);
+  }
 }
 
 // ======================================================================================
@@ -902,7 +907,7 @@ int launch_taylor_f64(const afq_ctx_dev& c, int w0, int nwc, const double2* vhs,
 
 int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fbt, int ntiles,
                    const double2* ovl_new, double2* ovl, double* weights, double* scalars,
-                   cudaStream_t st) {
+                   cudaStream_t st, const int* status) {
   {
     ProfScope _ps(K_WEIGHTS, st);
     // FP64 transcendentals per walker: 8 walkers per CTA spread them over the SMs' FP64 units
@@ -911,7 +916,7 @@ int launch_weights(const afq_ctx_dev& c, const double2* shift, const double2* fb
   }
   {
     ProfScope _ps(K_WEIGHTS, st);
-    k_pop_control<<<1, 1024, 0, st>>>(c.nw, c.dt, weights, scalars);
+    k_pop_control<<<1, 1024, 0, st>>>(c.nw, c.dt, weights, scalars, status);
   }
   return launch_err("weights");
 }

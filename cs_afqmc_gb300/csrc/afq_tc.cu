@@ -491,6 +491,95 @@ __global__ void k_prep_lop(const double* __restrict__ chol, int nchol, int n, in
   }
 }
 
+// kDiagChol: the diagonal of every Cholesky vector in FP32 ([nchol][n]); an off-diagonal
+// nonzero sets status bit 4 (the caller promised diagonal vectors). CTA per vector.
+__global__ void k_prep_diag(const double* __restrict__ chol, int n, float* __restrict__ d, int* status) {
+  const int g = blockIdx.x;
+  const double* L = chol + (size_t)g * n * n;
+  bool off = false;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int p = e / n, q = e % n;
+    if (p == q) d[(size_t)g * n + p] = (float)L[e];
+    else if (L[e] != 0.0) off = true;
+  }
+  if (off) atomicOr(status, 4);
+}
+
+// exp(vhs) W1 for diagonal Cholesky vectors (propagation.py:67-92 with a diagonal V):
+// vhs = i sqrt(dt) diag(v), v_p = sum_g xt_g d_g[p], so sum_m vhs^m W1 / m! scales row p of
+// W1 by the Taylor polynomial of i sqrt(dt) v_p (Horner form). Reads the first exp_h1
+// product's Taylor operand (t0: row 2k = [Tr | -Ti], row 2k+1 = [Ti | Tr]) and writes the
+// last product's operand (acc: rows 2k + re/im, cols p), both fp16 hi + lo. CTA per
+// (walker, slab); HBM-bound.
+struct TaylorDiag {
+  const float* dchol;
+  const uint16_t *xt_hi, *xt_lo;
+  const uint16_t *t0_hi[2], *t0_lo[2];
+  uint16_t *acc_hi[2], *acc_lo[2];
+  int nchol, ldg, n, o[2], nq, NT[2], R[2], nk, nterms, bf16;
+  float sqdt;
+};
+
+constexpr int kDiagSplit = 8;  // partial sums over g per orbital (256 threads: 8 x 32 orbitals)
+
+__global__ void __launch_bounds__(256) k_taylor_diag(const TaylorDiag td) {
+  __shared__ float2 poly[128];
+  __shared__ float2 part[kDiagSplit][128];
+  const int w = blockIdx.x, s = blockIdx.y, n = td.n, tid = threadIdx.x;
+  const bool bf = td.bf16 != 0;
+  // v_p = sum_g xt_g d_g[p]: thread (j, lane) takes orbitals lane, lane + 32, ... and every
+  // kDiagSplit-th g from j; xt_g is a broadcast load, d_g[p] coalesced over the warp
+  {
+    const int j = tid >> 5, lane = tid & 31;
+    const size_t r0 = (size_t)(2 * w) * td.ldg, r1 = r0 + td.ldg;
+    for (int p0 = 0; p0 < n; p0 += 32) {
+      const int p = p0 + lane;
+      float vr = 0.f, vi = 0.f;
+      if (p < n)
+        for (int g = j; g < td.nchol; g += kDiagSplit) {
+          const float dg = td.dchol[(size_t)g * n + p];
+          vr = fmaf(h2f(td.xt_hi[r0 + g], bf) + h2f(td.xt_lo[r0 + g], bf), dg, vr);
+          vi = fmaf(h2f(td.xt_hi[r1 + g], bf) + h2f(td.xt_lo[r1 + g], bf), dg, vi);
+        }
+      if (p < n) part[j][p] = make_float2(vr, vi);
+    }
+  }
+  __syncthreads();
+  for (int p = tid; p < n; p += blockDim.x) {
+    float vr = 0.f, vi = 0.f;
+    for (int j = 0; j < kDiagSplit; ++j) {
+      vr += part[j][p].x;
+      vi += part[j][p].y;
+    }
+    const float ar = -td.sqdt * vi, ai = td.sqdt * vr;  // i sqrt(dt) v
+    float pr = 1.f, pi = 0.f;
+    for (int m = td.nterms - 1; m >= 1; --m) {  // P <- 1 + a P / m
+      const float inv = 1.f / (float)m;
+      const float qr = (ar * pr - ai * pi) * inv, qi = (ar * pi + ai * pr) * inv;
+      pr = 1.f + qr;
+      pi = qi;
+    }
+    poly[p] = make_float2(pr, pi);
+  }
+  __syncthreads();
+  const int o = td.o[s];
+  const size_t tb = (size_t)w * td.NT[s] * 2 * td.nq, ab = (size_t)w * td.R[s] * td.nk;
+  for (int e = tid; e < n * o; e += blockDim.x) {
+    const int k = e / n, p = e % n;
+    const size_t ir = tb + (size_t)(2 * k) * 2 * td.nq + p, ii = ir + 2 * td.nq;
+    const float tr = h2f(td.t0_hi[s][ir], bf) + h2f(td.t0_lo[s][ir], bf);
+    const float ti = h2f(td.t0_hi[s][ii], bf) + h2f(td.t0_lo[s][ii], bf);
+    const float2 c = poly[p];
+    uint16_t h, l;
+    split16(c.x * tr - c.y * ti, bf, h, l);
+    td.acc_hi[s][ab + (size_t)(2 * k) * td.nk + p] = h;
+    td.acc_lo[s][ab + (size_t)(2 * k) * td.nk + p] = l;
+    split16(c.x * ti + c.y * tr, bf, h, l);
+    td.acc_hi[s][ab + (size_t)(2 * k + 1) * td.nk + p] = h;
+    td.acc_lo[s][ab + (size_t)(2 * k + 1) * td.nk + p] = l;
+  }
+}
+
 // exp_h1 A operand: E - I -> [128][nk]
 __global__ void k_prep_eop(const double* __restrict__ e, int n, int nk, int bf16, uint16_t* __restrict__ hi,
                            uint16_t* __restrict__ lo) {
@@ -590,6 +679,7 @@ struct Plan {
   size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gblk[2][2];
   size_t o_fbpart;
   size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_trial32[2], o_rh1[2];
+  size_t o_dchol;
 };
 
 int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
@@ -700,6 +790,7 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   P->o_exc = L.take((size_t)t.nw * (t.mt_z[0] + t.mt_z[1]) * 16);
   P->o_status = L.take(256);
   P->o_amax = L.take(256);
+  P->o_dchol = L.take((cfg & kDiagChol) ? (size_t)c.nchol * t.n * 4 : 256);
   for (int s = 0; s < 2; ++s) P->o_trial32[s] = L.take((size_t)t.n * 64 * 4);
   for (int b = 0; b < 2; ++b) P->o_rh1[b] = L.take((size_t)t.n * 64 * 4);
   P->total = L.off + 1024;
@@ -788,6 +879,7 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   t.c_out = reinterpret_cast<double2*>(base + P.o_cout);
   t.exc_part = reinterpret_cast<double2*>(base + P.o_exc);
   t.status = reinterpret_cast<int*>(base + P.o_status);
+  t.dchol = reinterpret_cast<float*>(base + P.o_dchol);
   for (int s = 0; s < 2; ++s) {
     t.trial32[s] = reinterpret_cast<float*>(base + P.o_trial32[s]);
     t.rh1_32[s] = reinterpret_cast<float*>(base + P.o_rh1[s]);
@@ -800,6 +892,7 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   }
   const int bf = t.bf16 ? 1 : 0;
   ProfScope _ps(K_PREP, st);
+  if (t.cfg & kDiagChol) k_prep_diag<<<c.nchol, 256, 0, st>>>(h.chol, t.n, t.dchol, t.status);
   for (int s = 0; s < t.nslab; ++s) {
     k_to_f32<<<64, 256, 0, st>>>(c.trial[s], const_cast<float*>(t.trial32[s]), (long)t.n * t.o_slab[s]);
     k_prep_eop<<<64, 256, 0, st>>>(c.exp_h1[s], t.n, t.nk, bf, t.eop[s][0], t.eop[s][1]);
@@ -1083,6 +1176,40 @@ static int exp_gemm(TcState& t, const afq_ctx_dev& c, int s, bool last, float2* 
 int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
   float2* W[2] = {static_cast<float2*>(wu), static_cast<float2*>(wd)};
   for (int s = 0; s < t.nslab; ++s) TC_CHECK(exp_gemm(t, c, s, false, W[s], st));
+  if (t.cfg & kDiagChol) {
+    if (t.n > 128) {
+      afq_set_error("diagonal Cholesky path: norb <= 128");
+      return -2;
+    }
+    TaylorDiag td;
+    td.dchol = t.dchol;
+    td.xt_hi = t.xt[0];
+    td.xt_lo = t.xt[1];
+    for (int s = 0; s < 2; ++s) {
+      td.t0_hi[s] = t.t0[s][0];
+      td.t0_lo[s] = t.t0[s][1];
+      td.acc_hi[s] = t.acc[s][0];
+      td.acc_lo[s] = t.acc[s][1];
+      td.o[s] = t.o_slab[s];
+      td.NT[s] = t.NT[s];
+      td.R[s] = t.R[s];
+    }
+    td.nchol = c.nchol;
+    td.ldg = t.ldg;
+    td.n = t.n;
+    td.nq = t.nq;
+    td.nk = t.nk;
+    td.nterms = c.n_exp_terms;
+    td.bf16 = t.bf16 ? 1 : 0;
+    td.sqdt = (float)sqrt(c.dt);
+    {
+      ProfScope _ps(K_TAYLOR, st);
+      k_taylor_diag<<<dim3(t.nw, t.nslab), 256, 0, st>>>(td);
+    }
+    TC_CHECK(launch_check("taylor_diag"));
+    for (int s = 0; s < t.nslab; ++s) TC_CHECK(exp_gemm(t, c, s, true, W[s], st));
+    return 0;
+  }
   const int nchunks = t.nw / t.nwc;
   const bool want_lo = t.taylor_split > 0;
   for (int ch = 0; ch < nchunks; ++ch) {
@@ -1148,7 +1275,7 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
 int tc_weights(TcState& t, const afq_ctx_dev& c, const double2* ovl_new, double2* ovl, double* weights,
                double* scalars, cudaStream_t st) {
   // the force-bias reduction leaves one shift_term / fb_term sum per walker
-  return launch_weights(c, t.part_shift, t.part_fbt, 1, ovl_new, ovl, weights, scalars, st);
+  return launch_weights(c, t.part_shift, t.part_fbt, 1, ovl_new, ovl, weights, scalars, st, t.status);
 }
 
 // local energy (wavefunctions.py:529-561, 711-743): Coulomb c_g from a force-bias-like GEMM,

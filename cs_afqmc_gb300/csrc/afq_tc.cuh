@@ -34,6 +34,8 @@ enum MixedBits : int32_t {
   kUseBf16 = 1 << 11,   // bf16 operands instead of fp16
   kDrainShift = 12,     // bits 12..14: K tiles per truncated accumulation run in the force
                         // bias, vhs and exchange GEMMs (0: default, 7: no draining)
+  kDiagChol = 1 << 15,  // every Cholesky vector is a diagonal matrix (on-site lattice terms):
+                        // exp(vhs) W1 is a per-row polynomial scale, no vhs GEMM / Taylor MMA
   kExplicit = 1 << 30,  // set by callers that pass an explicit configuration
 };
 constexpr int kDrainDefault = 2;  // K tiles per drained run unless the configuration says
@@ -69,7 +71,9 @@ struct TcState {
   double2* exc_part;        // [nblk][nw][mt_z]
   const float* trial32[2];  // [norb][o_s] trial in FP32
   const float* rh1_32[2];   // [o_b][norb] rot_h1 in FP32
-  int* status;              // device word: nonzero after a pipeline timeout
+  int* status;              // device word: nonzero after a pipeline timeout (2, 1) or a
+                            // non-diagonal Cholesky vector under kDiagChol (4)
+  float* dchol;             // kDiagChol: [nchol][n] diagonals of the Cholesky vectors
   // tensor maps
   GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2], m_z[2];
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)

@@ -63,7 +63,11 @@ typedef struct afq_dims {
                            rot_chol (energy); bits 8..10: Taylor products with split
                            operands; bit 11: bf16 instead of fp16; bits 12..14: K tiles per
                            drained accumulation run of the force-bias, vhs and exchange
-                           GEMMs (0 = default, 7 = undrained) */
+                           GEMMs (0 = default, 7 = undrained); bit 15: every Cholesky
+                           vector is a diagonal matrix (on-site lattice terms), so exp(vhs)
+                           W1 is a per-row polynomial scale and the vhs GEMM and Taylor
+                           products are skipped (checked on the device: an off-diagonal
+                           nonzero ors 4 into scalars[AFQ_S_STATUS]) */
   double dt;
 } afq_dims;
 

@@ -12,13 +12,18 @@ from oracle import afqmc_oracle as O
 class Case:
     def __init__(self, kind="rhf", norb=12, nelec=(3, 3), nchol=30, nw=8, dt=0.005,
                  restricted=True, precision="fp64", seed=5, perturb=0.2, n_batch=1,
-                 orthonormal=False, h1_shift=None):
+                 orthonormal=False, h1_shift=None, hubbard=None):
         import torch
         from cs_afqmc_gb300 import hamiltonian, propagation, wavefunctions
 
         self.kind, self.norb, self.nelec, self.nchol, self.nw = kind, norb, nelec, nchol, nw
         self.dt, self.restricted = dt, restricted
-        s = synthetic.molecular(norb, nelec, nchol, seed=seed, kind=kind)
+        if hubbard is not None:  # (lx, ly, u): periodic lattice, diagonal Cholesky vectors
+            lx, ly, u = hubbard
+            s = synthetic.hubbard_2d(lx=lx, ly=ly, u=u, nelec=nelec, real_trial=True)
+            assert kind == "rhf" and s.norb == norb and s.chol.shape[0] == nchol
+        else:
+            s = synthetic.molecular(norb, nelec, nchol, seed=seed, kind=kind)
         if h1_shift is not None:  # a second Hamiltonian on the same trial (correlated sampling)
             s.h1 = s.h1 + h1_shift
         self.sys = s
