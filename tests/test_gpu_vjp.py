@@ -157,3 +157,19 @@ def test_vjp_rejects_mixed_precision():
     with pytest.raises(_lib.AfqError):
         samp.propagate_phaseless_ad_norot_vjp(case.ham, case.ham_data, case.prop, case.gpu_prop_data(),
                                               case.trial, case.wave_data)
+
+
+def test_vjp_chunked_vhs():
+    """n_batch 2: the backward sweep recomputes vhs and runs the Taylor adjoint per walker
+    chunk; the result equals the unchunked call's."""
+    from cs_afqmc_gb300 import sampling
+    a = Case(kind="rhf", restricted=False, norb=9, nelec=(3, 3), nchol=17, nw=6)
+    b = Case(kind="rhf", restricted=False, norb=9, nelec=(3, 3), nchol=17, nw=6, n_batch=2)
+    fields, zetas = _draws(a, N_SR, seed=51)
+    samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=N_SR)
+    ea, ra, _ = samp.propagate_phaseless_ad_norot_vjp(a.ham, a.ham_data, a.prop, a.gpu_prop_data(), a.trial,
+                                                      a.wave_data, fields=fields, zetas=zetas)
+    eb, rb, _ = samp.propagate_phaseless_ad_norot_vjp(b.ham, b.ham_data, b.prop, b.gpu_prop_data(), b.trial,
+                                                      b.wave_data, fields=fields, zetas=zetas)
+    assert rel_err(eb.item(), ea.item()) < 1e-12
+    assert rel_err(to_np(rb), to_np(ra)) < 1e-10
