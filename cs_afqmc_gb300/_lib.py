@@ -47,6 +47,11 @@ class Hamiltonian(ctypes.Structure):
     ]
 
 
+class JvpInputs(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("dexp_h1_up", "dexp_h1_dn", "drot_h1_up", "drot_h1_dn",
+                                              "dtrial_up", "dtrial_dn", "drot_chol_up", "drot_chol_dn")]
+
+
 class WalkerState(ctypes.Structure):
     _fields_ = [("walkers_up", _vp), ("walkers_dn", _vp), ("weights", _vp),
                 ("overlaps", _vp), ("scalars", _vp)]
@@ -88,6 +93,10 @@ _SIGS = {
                                                    _vp, ctypes.c_size_t, _vp, _vp, ctypes.c_int32,
                                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _vp, _vp,
                                                    _vp, _vp, _vp, _vp, _vp]),
+    "afq_propagate_phaseless_jvp_ex": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, _vp,
+                                                      ctypes.c_size_t, _vp, _vp, ctypes.c_int32, ctypes.c_int32,
+                                                      ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp,
+                                                      _vp, _vp]),
     "afq_vjp_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(Dims), ctypes.c_int32, ctypes.c_int32,
                                                  ctypes.c_int32]),
     "afq_propagate_phaseless_vjp": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_size_t, _vp,

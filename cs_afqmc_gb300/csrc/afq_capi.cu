@@ -305,7 +305,7 @@ int check_free(const afq_ctx* c) {
 // Tangent workspace of afq_propagate_phaseless_jvp, carved like the main workspace.
 struct TSizes {
   size_t dw[2], wold[2], dgreen, dfb, dxt, dshift, dfbt, dvhs, dlo, dlo_new, dweights, dscalars, dene, dpart,
-      dsum, total;
+      dsum, drccat, total;
 };
 
 TSizes tangent_sizes(const afq_ctx_dev& c, int nw_chunk, int e_chunks, Layout* L) {
@@ -328,6 +328,7 @@ TSizes tangent_sizes(const afq_ctx_dev& c, int nw_chunk, int e_chunks, Layout* L
   s.dene = L->take(nw * C16);
   s.dpart = L->take(nw * e_chunks * 5 * C16);
   s.dsum = L->take(sizeof(double));
+  s.drccat = L->take(c.nspin_g == 2 ? (size_t)c.nchol * c.ktot * sizeof(double) : 256);
   s.total = L->off;
   return s;
 }
@@ -344,6 +345,11 @@ int propagate_jvp(afq_ctx* c, afq_walker_state* s, const afq::TangentBufs& t, co
     const double* B = d.nspin_g == 2 ? c->rccat : d.rot_chol[0];
     CHECK(afq::launch_gemm_cr(false, d.nw, d.nchol, d.ktot, t.dgreen, d.ktot, B, d.ktot, t.dfb, d.nchol, alpha,
                               st));
+    if (t.drccat) {  // orbital rotation: + alpha G dRC^T (t.dxt as scratch, rewritten below)
+      CHECK(afq::launch_gemm_cr(false, d.nw, d.nchol, d.ktot, c->green, d.ktot, t.drccat, d.ktot, t.dxt, d.nchol,
+                                alpha, st));
+      CHECK(afq::t_launch_add((long)d.nw * d.nchol, t.dxt, t.dfb, st));
+    }
   }
   CHECK(afq::t_launch_field_shifts(d, fields, c->fb, t.dfb, c->xt, t.dxt, c->shift, t.dshift, c->fbt, t.dfbt, st));
   const int nb = d.nw / c->nw_chunk;
@@ -672,6 +678,26 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
                                 int32_t n_sr_blocks, int32_t flags, double* block_energy, double* block_weight,
                                 double* dblock_energy, double* dblock_weight, double* energy, double* denergy,
                                 void* stream) {
+  afq_jvp_inputs in;
+  memset(&in, 0, sizeof(in));
+  in.dexp_h1_up = dexp_h1_up;
+  in.dexp_h1_dn = dexp_h1_dn;
+  in.drot_h1_up = drot_h1_up;
+  in.drot_h1_dn = drot_h1_dn;
+  return afq_propagate_phaseless_jvp_ex(ctx, state, &in, tangent_workspace, tangent_workspace_bytes, fields, zetas,
+                                        n_prop_steps, n_ene_blocks, n_sr_blocks, flags, block_energy, block_weight,
+                                        dblock_energy, dblock_weight, energy, denergy, stream);
+}
+
+int afq_propagate_phaseless_jvp_ex(afq_ctx* ctx, afq_walker_state* state, const afq_jvp_inputs* in,
+                                   void* tangent_workspace, size_t tangent_workspace_bytes, const double* fields,
+                                   const double* zetas, int32_t n_prop_steps, int32_t n_ene_blocks,
+                                   int32_t n_sr_blocks, int32_t flags, double* block_energy, double* block_weight,
+                                   double* dblock_energy, double* dblock_weight, double* energy, double* denergy,
+                                   void* stream) {
+  if (!in) { afq_set_error("NULL argument"); return -1; }
+  const double *dexp_h1_up = in->dexp_h1_up, *dexp_h1_dn = in->dexp_h1_dn, *drot_h1_up = in->drot_h1_up,
+               *drot_h1_dn = in->drot_h1_dn;
   const bool do_sr = !(flags & AFQ_JVP_NO_SR);
   if (!ctx || !fields || (do_sr && !zetas) || !block_energy || !block_weight || !dblock_energy || !dblock_weight || !energy ||
       !denergy || !dexp_h1_up || !drot_h1_up) {
@@ -688,6 +714,12 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
   const afq_ctx_dev& d = ctx->dev;
   if (d.nslab == 2 && !dexp_h1_dn) { afq_set_error("unrestricted walkers need dexp_h1_dn"); return -1; }
   if (d.nspin_g == 2 && !drot_h1_dn) { afq_set_error("the UHF trial needs drot_h1_dn"); return -1; }
+  const bool rot = in->dtrial_up || in->drot_chol_up;
+  if (rot && (!in->dtrial_up || !in->drot_chol_up ||
+              (d.nspin_g == 2 && (!in->dtrial_dn || !in->drot_chol_dn)))) {
+    afq_set_error("orbital rotation needs dtrial and drot_chol for every spin of the trial");
+    return -1;
+  }
   Layout L;
   const TSizes ts = tangent_sizes(d, ctx->nw_chunk, ctx->e_chunks, &L);
   if (!tangent_workspace || tangent_workspace_bytes < ts.total) {
@@ -723,11 +755,30 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
   t.dexp[1] = d.nslab == 2 ? dexp_h1_dn : dexp_h1_up;
   t.drot[0] = drot_h1_up;
   t.drot[1] = d.nspin_g == 2 ? drot_h1_dn : drot_h1_up;
+  // the RHF trial serves both walker slabs: one trial tangent for both
+  t.dtrial[0] = rot ? in->dtrial_up : nullptr;
+  t.dtrial[1] = rot ? (d.nspin_g == 2 ? in->dtrial_dn : in->dtrial_up) : nullptr;
+  t.drc[0] = rot ? in->drot_chol_up : nullptr;
+  t.drc[1] = rot && d.nspin_g == 2 ? in->drot_chol_dn : nullptr;
+  t.drccat = nullptr;
   cudaStream_t st = S(stream);
   // walker, weight, overlap and shift tangents start at zero (driver.py:190-200)
   {
     cudaError_t e = cudaMemsetAsync(tangent_workspace, 0, ts.total, st);
     if (e != cudaSuccess) { afq_set_error("tangent workspace clear: %s", cudaGetErrorString(e)); return (int)e; }
+  }
+  if (rot && d.nspin_g == 2) {  // [drot_chol_up[g] | drot_chol_dn[g]], the layout of rccat
+    double* cat = reinterpret_cast<double*>(tw + ts.drccat);
+    const size_t a = (size_t)d.gocc[0] * d.norb, b = (size_t)d.gocc[1] * d.norb;
+    cudaError_t e = cudaMemcpy2DAsync(cat, d.ktot * sizeof(double), in->drot_chol_up, a * sizeof(double),
+                                      a * sizeof(double), d.nchol, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(cat + a, d.ktot * sizeof(double), in->drot_chol_dn, b * sizeof(double),
+                            b * sizeof(double), d.nchol, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) { afq_set_error("drot_chol concat: %s", cudaGetErrorString(e)); return (int)e; }
+    t.drccat = cat;
+  } else if (rot) {
+    t.drccat = in->drot_chol_up;
   }
   double2* ovl = reinterpret_cast<double2*>(state->overlaps);
   const size_t welems[2] = {(size_t)d.nw * d.norb * d.kslab[0], (size_t)d.nw * d.norb * d.kslab[1]};

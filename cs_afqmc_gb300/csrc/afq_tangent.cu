@@ -52,7 +52,9 @@ __global__ void __launch_bounds__(256) k_t_green(const afq_ctx_dev c, const doub
                                                  const double2* __restrict__ dw_up,
                                                  const double2* __restrict__ dw_dn,
                                                  double2* __restrict__ green, double2* __restrict__ dgreen,
-                                                 double2* __restrict__ ovl, double2* __restrict__ dlog_ovl) {
+                                                 double2* __restrict__ ovl, double2* __restrict__ dlog_ovl,
+                                                 const double* __restrict__ dc_up,
+                                                 const double* __restrict__ dc_dn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int wlk = blockIdx.x, norb = c.norb, tid = threadIdx.x, nt = blockDim.x;
   const int km = c.kmax;
@@ -80,6 +82,7 @@ __global__ void __launch_bounds__(256) k_t_green(const afq_ctx_dev c, const doub
       Cs[i] = C[(size_t)p * o + k];
     }
     __syncthreads();
+    const double* dC = s == 0 ? dc_up : dc_dn;  // orbital rotation: dS += dC^T W
     for (int e = tid; e < o * o; e += nt) {
       const int i = e / o, k = e % o;
       double2 a = c2(0, 0), da = c2(0, 0);
@@ -90,6 +93,12 @@ __global__ void __launch_bounds__(256) k_t_green(const afq_ctx_dev c, const doub
         da.x += cv * dWs[p * o + k].x;
         da.y += cv * dWs[p * o + k].y;
       }
+      if (dC)
+        for (int p = 0; p < norb; ++p) {
+          const double dv = dC[(size_t)p * o + i];
+          da.x += dv * Ws[p * o + k].x;
+          da.y += dv * Ws[p * o + k].y;
+        }
       Aug[i * 2 * o + k] = a;
       Aug[i * 2 * o + o + k] = c2(i == k ? 1.0 : 0.0, 0.0);
       dS[i * o + k] = da;
@@ -481,7 +490,9 @@ __global__ void __launch_bounds__(256) k_t_qr(const afq_ctx_dev c, const double2
 __global__ void __launch_bounds__(256) k_t_energy_part(const afq_ctx_dev c, int gchunk,
                                                        const double2* __restrict__ green,
                                                        const double2* __restrict__ dgreen,
-                                                       double2* __restrict__ dpart) {
+                                                       double2* __restrict__ dpart,
+                                                       const double* __restrict__ drc_up,
+                                                       const double* __restrict__ drc_dn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int w = blockIdx.x, ch = blockIdx.y, norb = c.norb, tid = threadIdx.x, nt = blockDim.x;
   const int om = c.kmax;
@@ -506,6 +517,7 @@ __global__ void __launch_bounds__(256) k_t_energy_part(const afq_ctx_dev c, int 
       const size_t base = (size_t)s * c.gocc[0] * norb;
       double2* Fs = F + s * om * om;
       double2* dFs = dF + s * om * om;
+      const double* dRC = s == 0 ? drc_up : drc_dn;  // orbital rotation: dF += dRC G^T
       for (int e = tid; e < o * o; e += nt) {
         const int i = e / o, kk = e % o;
         double2 a = c2(0, 0), da = c2(0, 0);
@@ -517,6 +529,13 @@ __global__ void __launch_bounds__(256) k_t_energy_part(const afq_ctx_dev c, int 
           a.y = fma(rr[p], gg[p].y, a.y);
           da.x = fma(rr[p], dg[p].x, da.x);
           da.y = fma(rr[p], dg[p].y, da.y);
+        }
+        if (dRC) {
+          const double* dr = dRC + (size_t)g * o * norb + (size_t)i * norb;
+          for (int p = 0; p < norb; ++p) {
+            da.x = fma(dr[p], gg[p].x, da.x);
+            da.y = fma(dr[p], gg[p].y, da.y);
+          }
         }
         Fs[e] = a;
         dFs[e] = da;
@@ -680,7 +699,7 @@ int t_launch_green(const afq_ctx_dev& c, const TangentBufs& t, const void* wu, c
   {
     ProfScope _ps(K_GREEN, st);
     k_t_green<<<c.nw, 256, smem, st>>>(c, (const double2*)wu, (const double2*)wd, t.dw[0], t.dw[1], green, dgreen,
-                                       ovl, dlog);
+                                       ovl, dlog, t.dtrial[0], c.nslab == 2 ? t.dtrial[1] : nullptr);
   }
   return t_err("t_green");
 }
@@ -746,7 +765,8 @@ int t_launch_energy(const afq_ctx_dev& c, const TangentBufs& t, int nchunks, int
   cudaFuncSetAttribute(k_t_energy_part, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   {
     ProfScope _ps(K_ENERGY, st);
-    k_t_energy_part<<<dim3(c.nw, nchunks), 256, smem, st>>>(c, gchunk, green, t.dgreen, t.dpart);
+    k_t_energy_part<<<dim3(c.nw, nchunks), 256, smem, st>>>(c, gchunk, green, t.dgreen, t.dpart, t.drc[0],
+                                                            c.nspin_g == 2 ? t.drc[1] : nullptr);
   }
   int e = t_err("t_energy_part");
   if (e) return e;
@@ -755,6 +775,19 @@ int t_launch_energy(const afq_ctx_dev& c, const TangentBufs& t, int nchunks, int
     k_t_energy_final<<<c.nw, 256, 0, st>>>(c, nchunks, green, t.dgreen, t.drot[0], t.drot[1], t.dpart, t.dene);
   }
   return t_err("t_energy_final");
+}
+
+__global__ void k_t_add(long n, const double2* __restrict__ x, double2* __restrict__ y) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = cadd(y[i], x[i]);
+}
+
+int t_launch_add(long n, const double2* x, double2* y, cudaStream_t st) {
+  {
+    ProfScope _ps(K_FB, st);
+    k_t_add<<<256, 256, 0, st>>>(n, x, y);
+  }
+  return t_err("t_add");
 }
 
 int t_launch_block_stats(const afq_ctx_dev& c, const TangentBufs& t, const double2* energy, const double* weights,

@@ -24,6 +24,11 @@ struct TangentBufs {
   double* dbw;         // [n blocks]
   const double* dexp[2];  // d exp_h1 / d lambda per slab
   const double* drot[2];  // d rot_h1 / d lambda per Green block
+  // orbital rotation (NULL: trial fixed): d trial / d lambda per slab [norb][nocc_s] and
+  // d rot_chol / d lambda per Green block (layout of rot_chol) and concatenated [nchol][ktot]
+  const double* dtrial[2];
+  const double* drc[2];
+  const double* drccat;
 };
 
 int t_launch_green(const afq_ctx_dev& c, const TangentBufs& t, const void* wu, const void* wd,
@@ -38,6 +43,8 @@ int t_launch_weights(const afq_ctx_dev& c, const TangentBufs& t, const double2* 
 int t_launch_qr(const afq_ctx_dev& c, const TangentBufs& t, const void* wu, const void* wd, cudaStream_t st);
 int t_launch_energy(const afq_ctx_dev& c, const TangentBufs& t, int nchunks, int gchunk, const double2* green,
                     cudaStream_t st);
+// y += x, complex, n elements
+int t_launch_add(long n, const double2* x, double2* y, cudaStream_t st);
 int t_launch_block_stats(const afq_ctx_dev& c, const TangentBufs& t, const double2* energy, const double* weights,
                          const double* scalars, const double* be, double* dbe, double* dbw, cudaStream_t st);
 int t_launch_sr_pre(const afq_ctx_dev& c, const TangentBufs& t, cudaStream_t st);

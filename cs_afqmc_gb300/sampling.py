@@ -46,6 +46,20 @@ def coupled_ham_data(ham, ham_data: dict, coupling: float, observable_op, prop, 
     return ham.build_propagation_intermediates(hd, prop, trial, wave_data)
 
 
+def rotated_ham_data(ham, ham_data: dict, coupling: float, observable_op, prop, trial, wave_data: dict):
+    """(ham_data, wave_data) of h1 + coupling * observable_op with the trial re-optimised
+    (trial.optimize) and the intermediates rebuilt (sampling.py:187-191). The mean-field
+    shifts follow wave_data["rdm1"], which the driver holds fixed (driver.py:54-56); it is
+    required here so that they do not silently follow the new trial."""
+    if "rdm1" not in wave_data:
+        raise _lib.AfqError("orbital rotation needs wave_data['rdm1'] (the driver sets it to the trial's rdm1)")
+    hd = {k: v for k, v in ham_data.items() if k != _CACHE_KEY}
+    hd["h1"] = as_dev(ham_data["h1"]) + float(coupling) * h1_direction(observable_op, trial.norb)
+    wd = trial.optimize(hd, wave_data)
+    hd = ham.build_measurement_intermediates(hd, trial, wd)
+    return ham.build_propagation_intermediates(hd, prop, trial, wd), wd
+
+
 @dataclass
 class sampler:
     n_prop_steps: int = 50
@@ -167,6 +181,59 @@ class sampler:
         else:
             drot_up, drot_dn = drot, None
         f, z = self._ad_draws(eng, prop_data, n_sr, do_sr, fields, zetas)
+        return self._jvp_call(eng, prop_data, nblk, n_sr, do_sr, f, z, (dexp_up, dexp_dn), (drot_up, drot_dn))
+
+    def propagate_phaseless_ad(self, ham, ham_data: dict, coupling: float, observable_op, prop,
+                               prop_data: PropData, trial, wave_data: dict,
+                               fields: Optional[torch.Tensor] = None, zetas: Optional[torch.Tensor] = None):
+        """(energy, prop_data) of the block with h1 + coupling * observable_op and the trial
+        re-optimised for it (sampling.py:173-196); the value whose derivative
+        propagate_phaseless_ad_jvp returns."""
+        hd, wd = rotated_ham_data(ham, ham_data, coupling, observable_op, prop, trial, wave_data)
+        return self.propagate_phaseless(ham, hd, prop, prop_data, trial, wd, fields, zetas)
+
+    def propagate_phaseless_ad_jvp(self, ham, ham_data: dict, observable_op, prop, prop_data: PropData, trial,
+                                   wave_data: dict, coupling: float = 0.0, do_sr: bool = True,
+                                   fields: Optional[torch.Tensor] = None, zetas: Optional[torch.Tensor] = None):
+        """Forward-mode derivative of propagate_phaseless_ad (do_sr=False:
+        propagate_phaseless_ad_nosr, sampling.py:221-254) along observable_op at `coupling`,
+        with the trial's dependence on the coupling through trial.optimize: what
+        driver.py:207-215 computes with jax.jvp when options["orbital_rotation"] is on (its
+        default). Returns (energy, d energy / d coupling, prop_data) as
+        propagate_phaseless_ad_norot_jvp does. FP64 (complex128) walkers only."""
+        if "rdm1" not in wave_data:
+            raise _lib.AfqError("orbital rotation needs wave_data['rdm1'] (the driver sets it to the trial's rdm1)")
+        dh1 = h1_direction(observable_op, trial.norb)
+        h0 = {k: v for k, v in ham_data.items() if k != _CACHE_KEY}
+        h0["h1"] = as_dev(ham_data["h1"]) + float(coupling) * dh1
+        wd, dmo = trial.optimize_tangent(h0, wave_data, dh1)
+        hd = ham.build_measurement_intermediates(h0, trial, wd)
+        hd = ham.build_propagation_intermediates(hd, prop, trial, wd)
+        eng = prop._engine(trial, hd, wd, prop_data["walkers"])
+        if eng.precision != _lib.AFQ_PREC_FP64:
+            raise _lib.AfqError("the derivative path needs FP64 (complex128) walkers")
+        dict.__setitem__(prop_data, "_engine", eng)
+        n_sr = self.n_sr_blocks if do_sr else 1
+        nblk = n_sr * self.n_ene_blocks
+        dexp = prop.exp_h1_tangent(hd, trial, wd, dh1)
+        dexp_up, dexp_dn = (dexp[0].contiguous(), dexp[1].contiguous()) if dexp.dim() == 3 else (dexp, None)
+        drot, drc = trial.rotation_tangents(hd, wd, dmo, dh1)
+        uhf_trial = isinstance(drot, list)
+        dtr = (dmo[0], dmo[1]) if uhf_trial else (dmo, None)
+        drot_p = (drot[0], drot[1]) if uhf_trial else (drot, None)
+        drc_p = (drc[0], drc[1]) if uhf_trial else (drc, None)
+        f, z = self._ad_draws(eng, prop_data, n_sr, do_sr, fields, zetas)
+        return self._jvp_call(eng, prop_data, nblk, n_sr, do_sr, f, z, (dexp_up, dexp_dn), drot_p, dtr, drc_p)
+
+    def _jvp_call(self, eng, prop_data: PropData, nblk: int, n_sr: int, do_sr: bool, f, z, dexp, drot,
+                  dtrial=(None, None), drc=(None, None)):
+        """afq_propagate_phaseless_jvp_ex with the tangent inputs; returns (energy, d energy,
+        prop_data) and records the per-block values and derivatives in prop_data."""
+        def ptr(x):
+            return None if x is None else x.data_ptr()
+
+        tin = _lib.JvpInputs(ptr(dexp[0]), ptr(dexp[1]), ptr(drot[0]), ptr(drot[1]), ptr(dtrial[0]),
+                             ptr(dtrial[1]), ptr(drc[0]), ptr(drc[1]))
         tws = getattr(eng, "tangent_workspace", None)
         nbytes = eng.lib.afq_tangent_workspace_size(ctypes.byref(eng.dims))
         if nbytes == 0:
@@ -179,10 +246,8 @@ class sampler:
         be, bw, dbe, dbw = (out[i * nblk:(i + 1) * nblk] for i in range(4))
         energy, denergy = out[4 * nblk:4 * nblk + 1], out[4 * nblk + 1:]
         st = prop_data.state(eng)
-        _lib.call("afq_propagate_phaseless_jvp", eng.ctx, ctypes.byref(st), dexp_up.data_ptr(),
-                  None if dexp_dn is None else dexp_dn.data_ptr(), drot_up.data_ptr(),
-                  None if drot_dn is None else drot_dn.data_ptr(), tptr, nbytes, f.data_ptr(),
-                  None if z is None else z.data_ptr(), self.n_prop_steps, self.n_ene_blocks, n_sr,
+        _lib.call("afq_propagate_phaseless_jvp_ex", eng.ctx, ctypes.byref(st), ctypes.byref(tin), tptr, nbytes,
+                  f.data_ptr(), None if z is None else z.data_ptr(), self.n_prop_steps, self.n_ene_blocks, n_sr,
                   0 if do_sr else _lib.AFQ_JVP_NO_SR, be.data_ptr(), bw.data_ptr(), dbe.data_ptr(),
                   dbw.data_ptr(), energy.data_ptr(), denergy.data_ptr(), stream_ptr())
         dict.__setitem__(prop_data, "block_energies", be)

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass
-from typing import Any, List, Sequence, Tuple
+from typing import Optional, Any, List, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -102,6 +102,65 @@ def _sym(h1: torch.Tensor) -> torch.Tensor:
     return torch.stack([(h1[0] + h1[0].T) / 2.0, (h1[1] + h1[1].T) / 2.0])
 
 
+def _eigh_fixed_sign(f: torch.Tensor, df: Optional[torch.Tensor] = None):
+    """eigh with every eigenvector's first largest-magnitude component made non-negative
+    (wavefunctions.py:582-586, 788-792), and with df the eigenvectors' first-order change
+    dV = V (F o V^T df V), F_ij = 1 / (e_j - e_i) off the diagonal (distinct eigenvalues)."""
+    e, v = torch.linalg.eigh(f)
+    n = v.shape[1]
+    ar = torch.arange(n, device=v.device)
+    idx = torch.argmax(torch.abs(v), dim=0)
+    v = v * torch.where(v[idx, ar] < 0, -1.0, 1.0).to(v.dtype)[None, :]
+    if df is None:
+        return e, v, None
+    gap = e[None, :] - e[:, None]
+    off = ~torch.eye(n, dtype=torch.bool, device=v.device)
+    inv = torch.where(off, 1.0 / torch.where(off, gap, torch.ones_like(gap)), torch.zeros_like(gap))
+    return e, v, v @ (inv * (v.T @ df @ v))
+
+
+def _jk(chol3: torch.Tensor, dm: torch.Tensor):
+    """Coulomb and exchange matrices of a density matrix (wavefunctions.py:577-580)."""
+    f = torch.einsum("gij,ik->gjk", chol3, dm)
+    c = torch.einsum("gii->g", f)
+    return torch.einsum("g,gij->ij", c, chol3), torch.einsum("glj,gjk->lk", f, chol3)
+
+
+def _scf(kind: str, h: list, chol3: torch.Tensor, dm0: list, nelec, n_iter: int, dh: Optional[list] = None):
+    """The fixed-point iterations of rhf.optimize (wavefunctions.py:566-600; h = [(h_a + h_b)/2],
+    fock = h + J - K/2, occupation 2) and uhf.optimize (750-813; fock_s = h_s + J_up + J_dn -
+    K_s, occupation 1), with the first-order change along dh when given. Returns the lowest
+    nelec eigenvectors of the last Fock matrix per spin, and their changes."""
+    nsp = 1 if kind == "rhf" else 2
+    occf = 2.0 if kind == "rhf" else 1.0
+    dm = list(dm0)
+    ddm = [torch.zeros_like(x) for x in dm] if dh is not None else None
+    v = dv = None
+    for _ in range(n_iter):
+        jk = [_jk(chol3, dm[s]) for s in range(nsp)]
+        djk = [_jk(chol3, ddm[s]) for s in range(nsp)] if dh is not None else None
+        vj = sum(x[0] for x in jk)
+        dvj = sum(x[0] for x in djk) if dh is not None else None
+        v, dv, ndm, nddm = [], [], [], []
+        for s in range(nsp):
+            kfac = 0.5 if kind == "rhf" else 1.0
+            fock = h[s] + vj - kfac * jk[s][1]
+            dfock = dh[s] + dvj - kfac * djk[s][1] if dh is not None else None
+            e, vs, dvs = _eigh_fixed_sign(fock, dfock)
+            o = torch.argsort(e)[: nelec[s]]
+            occ = vs[:, o]
+            ndm.append(occf * occ @ occ.T)
+            if dh is not None:
+                docc = dvs[:, o]
+                nddm.append(occf * (docc @ occ.T + occ @ docc.T))
+            v.append(vs)
+            dv.append(dvs)
+        dm, ddm = ndm, (nddm if dh is not None else None)
+    mos = [v[s][:, : nelec[s]].contiguous() for s in range(nsp)]
+    dmos = [dv[s][:, : nelec[s]].contiguous() for s in range(nsp)] if dh is not None else None
+    return mos, dmos
+
+
 @dataclass
 class rhf(wave_function):
     """Restricted Hartree-Fock trial; wave_data["mo_coeff"] is [norb, nocc], real
@@ -144,6 +203,40 @@ class rhf(wave_function):
         mo = as_dev(wave_data["mo_coeff"])
         g = mo @ as_dev(grot) / 2.0
         return torch.stack([g, g])
+
+    def optimize(self, ham_data: dict, wave_data: dict) -> dict:
+        """rhf.optimize (wavefunctions.py:566-600): n_opt_iter restricted SCF iterations from
+        dm = 2 C C^T with ham_data["h1"] (spin average, symmetrised) and ham_data["chol"].
+        Returns a copy of wave_data with the new mo_coeff (the other keys, rdm1 included,
+        unchanged)."""
+        return self.optimize_tangent(ham_data, wave_data, None)[0]
+
+    def optimize_tangent(self, ham_data: dict, wave_data: dict, dh1):
+        """(optimize(ham_data, wave_data), d mo_coeff) for h1 -> h1 + lambda dh1
+        ([2, norb, norb]; None: value only)."""
+        h1 = as_dev(ham_data["h1"])
+        h = (h1[0] + h1[1]) / 2.0
+        h = (h + h.T) / 2.0
+        dh = None
+        if dh1 is not None:
+            d = as_dev(dh1)
+            d = (d[0] + d[1]) / 2.0
+            dh = [(d + d.T) / 2.0]
+        chol3 = as_dev(ham_data["chol"]).reshape(-1, self.norb, self.norb)
+        mo = as_dev(wave_data["mo_coeff"])
+        mos, dmos = _scf("rhf", [h], chol3, [2.0 * mo @ mo.T], (self.nelec[0],), self.n_opt_iter, dh)
+        out = dict(wave_data)
+        out["mo_coeff"] = mos[0]
+        return out, (dmos[0] if dmos is not None else None)
+
+    def rotation_tangents(self, ham_data: dict, wave_data: dict, dmo, dh1):
+        """d rot_h1 and d rot_chol for a trial tangent dmo and dh1: rot_h1 = C^T (h_a + h_b)/2
+        and rot_chol_g = C^T L_g of the measurement intermediates (wavefunctions.py:602-619)."""
+        mo, dmo, dh1 = as_dev(wave_data["mo_coeff"]), as_dev(dmo), as_dev(dh1)
+        h1 = _sym(as_dev(ham_data["h1"]))
+        drot = dmo.T @ ((h1[0] + h1[1]) / 2.0) + mo.T @ ((dh1[0] + dh1[1]) / 2.0)
+        chol = as_dev(ham_data["chol"]).reshape(-1, self.norb, self.norb)
+        return drot.contiguous(), torch.einsum("pi,gij->gpj", dmo.T, chol).contiguous()
 
     def __hash__(self) -> int:
         return super().__hash__()
@@ -189,6 +282,36 @@ class uhf(wave_function):
         mo = wave_data["mo_coeff"]
         a, b = as_dev(mo[0]), as_dev(mo[1])
         return torch.stack([a @ as_dev(grot[0]), b @ as_dev(grot[1])])
+
+    def optimize(self, ham_data: dict, wave_data: dict) -> dict:
+        """uhf.optimize (wavefunctions.py:750-813): n_opt_iter unrestricted SCF iterations
+        from the trial's own density matrices. Returns a copy of wave_data with the new
+        mo_coeff (the other keys, rdm1 included, unchanged)."""
+        return self.optimize_tangent(ham_data, wave_data, None)[0]
+
+    def optimize_tangent(self, ham_data: dict, wave_data: dict, dh1):
+        """(optimize(ham_data, wave_data), [d C_a, d C_b]) for h1 -> h1 + lambda dh1."""
+        h1 = _sym(as_dev(ham_data["h1"]))
+        dh = None if dh1 is None else list(_sym(as_dev(dh1)))
+        chol3 = as_dev(ham_data["chol"]).reshape(-1, self.norb, self.norb)
+        mo = wave_data["mo_coeff"]
+        a, b = as_dev(mo[0]), as_dev(mo[1])
+        mos, dmos = _scf("uhf", [h1[0], h1[1]], chol3, [a @ a.T, b @ b.T], self.nelec, self.n_opt_iter, dh)
+        out = dict(wave_data)
+        out["mo_coeff"] = mos
+        return out, dmos
+
+    def rotation_tangents(self, ham_data: dict, wave_data: dict, dmo, dh1):
+        """([d rot_h1_a, d rot_h1_b], [d rot_chol_a, d rot_chol_b]) (wavefunctions.py:817-841)."""
+        mo, dh1 = wave_data["mo_coeff"], _sym(as_dev(dh1))
+        h1 = _sym(as_dev(ham_data["h1"]))
+        chol = as_dev(ham_data["chol"]).reshape(-1, self.norb, self.norb)
+        drot, drc = [], []
+        for s in range(2):
+            c, dc = as_dev(mo[s]), as_dev(dmo[s])
+            drot.append((dc.T @ h1[s] + c.T @ dh1[s]).contiguous())
+            drc.append(torch.einsum("pi,gij->gpj", dc.T, chol).contiguous())
+        return drot, drc
 
     def __hash__(self) -> int:
         return super().__hash__()

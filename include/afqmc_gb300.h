@@ -303,6 +303,33 @@ int afq_propagate_phaseless_jvp(afq_ctx* ctx, afq_walker_state* state, const dou
                                 double* dblock_weight, double* energy, double* denergy,
                                 void* stream);
 
+/* Tangent inputs of afq_propagate_phaseless_jvp_ex (device float64 arrays, NULL where not
+ * applicable). dexp_h1 / drot_h1 as in afq_propagate_phaseless_jvp. With orbital rotation
+ * (sampler.propagate_phaseless_ad, sampling.py:173-196, and its _nosr variant 221-254: the
+ * trial re-optimised for h1 + lambda D by trial.optimize) also the trial's tangent
+ * dtrial_up/dn [norb, n_s] (dn NULL for the RHF trial) and rot_chol's tangent
+ * drot_chol_up/dn (layout of rot_chol_up/dn); all NULL for a fixed trial. The mean-field
+ * shifts do not change (they follow wave_data["rdm1"], which the driver holds fixed). */
+typedef struct afq_jvp_inputs {
+  const double* dexp_h1_up;
+  const double* dexp_h1_dn;
+  const double* drot_h1_up;
+  const double* drot_h1_dn;
+  const double* dtrial_up;
+  const double* dtrial_dn;
+  const double* drot_chol_up;
+  const double* drot_chol_dn;
+} afq_jvp_inputs;
+
+/* afq_propagate_phaseless_jvp with the tangent inputs in a struct, which adds the trial's
+ * tangents of the orbital-rotation variants. The same workspace, flags and outputs. */
+int afq_propagate_phaseless_jvp_ex(afq_ctx* ctx, afq_walker_state* state, const afq_jvp_inputs* in,
+                                   void* tangent_workspace, size_t tangent_workspace_bytes,
+                                   const double* fields, const double* zetas, int32_t n_prop_steps,
+                                   int32_t n_ene_blocks, int32_t n_sr_blocks, int32_t flags,
+                                   double* block_energy, double* block_weight, double* dblock_energy,
+                                   double* dblock_weight, double* energy, double* denergy, void* stream);
+
 /* ---- reverse-mode derivative of the block (differentiation pattern, FP64) ------------ */
 
 /* Bytes of device workspace afq_propagate_phaseless_vjp needs for these block counts (the

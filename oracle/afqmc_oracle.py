@@ -787,26 +787,84 @@ def cs_steps_scan(sampler: "Sampler", sys1: tuple, sys2: tuple, fields: np.ndarr
     return pd1, pd2, out[:, 0], out[:, 1], out[:, 2], out[:, 3]
 
 
+def _eigh_fixed_sign(fock: np.ndarray):
+    """eigh with each eigenvector's largest-magnitude component made non-negative
+    (wavefunctions.py:582-586, 788-792): the first index of the largest |component| decides."""
+    e, v = np.linalg.eigh(fock)
+    idx = np.argmax(np.abs(v), axis=0)
+    sign = np.where(v[idx, np.arange(v.shape[1])] < 0, -1.0, 1.0)
+    return e, v * sign[None, :]
+
+
+def rhf_optimize(h1, chol, mo, nelec: int, n_iter: int = 30) -> np.ndarray:
+    """RHF self-consistent-field iterations of rhf.optimize (wavefunctions.py:566-600):
+    from dm = 2 C C^T, n_iter times fock = h1 + J - K/2, eigh, occupy the lowest nelec; the
+    trial becomes the lowest nelec eigenvectors of the last Fock matrix. h1 [2, n, n] (the
+    spin average is used, symmetrised), chol [G, n, n]."""
+    h = (np.asarray(h1)[0] + np.asarray(h1)[1]) / 2.0
+    h = (h + h.T) / 2.0
+    dm = 2.0 * mo @ mo.T
+    v = None
+    for _ in range(n_iter):
+        f = np.einsum("gij,ik->gjk", chol, dm)
+        c = np.einsum("gii->g", f)
+        vj = np.einsum("g,gij->ij", c, chol)
+        vk = np.einsum("glj,gjk->lk", f, chol)
+        e, v = _eigh_fixed_sign(h + vj - 0.5 * vk)
+        occ = v[:, np.argsort(e)[:nelec]]
+        dm = 2.0 * occ @ occ.T
+    return v[:, :nelec]
+
+
+def uhf_optimize(h1, chol, mo, nelec, n_iter: int = 30):
+    """UHF iterations of uhf.optimize (wavefunctions.py:750-813): fock_s = h1_s + J_up +
+    J_dn - K_s from dm0 = C_s C_s^T (the trial's own rdm1)."""
+    h = [(np.asarray(h1)[s] + np.asarray(h1)[s].T) / 2.0 for s in range(2)]
+    dm = [mo[0] @ mo[0].T, mo[1] @ mo[1].T]
+    vs = [None, None]
+    for _ in range(n_iter):
+        f = [np.einsum("gij,ik->gjk", chol, dm[s]) for s in range(2)]
+        vj = sum(np.einsum("g,gij->ij", np.einsum("gii->g", f[s]), chol) for s in range(2))
+        new = []
+        for s in range(2):
+            vk = np.einsum("glj,gjk->lk", f[s], chol)
+            e, v = _eigh_fixed_sign(h[s] + vj - vk)
+            occ = v[:, np.argsort(e)[:nelec[s]]]
+            new.append(occ @ occ.T)
+            vs[s] = v
+        dm = new
+    return [vs[0][:, :nelec[0]], vs[1][:, :nelec[1]]]
+
+
 def phaseless_derivative_fd(sampler: "Sampler", prop: "Propagator", trial: "Trial", ham_data: dict,
                             direction: np.ndarray, rdm1: np.ndarray, mo, prop_data: dict,
                             fields: np.ndarray, zetas, restricted: bool, h: float = 1e-3,
-                            do_sr: bool = True):
+                            do_sr: bool = True, orbital_rotation: bool = False, n_opt_iter: int = 30):
     """d/d lambda of the blocked energy and of each block's (energy, weight) for
-    h1 + lambda * direction (direction [2, norb, norb]) with the trial, prop_data, fields
-    and SR uniforms held fixed: the quantity that driver.py:207-215 takes with jax.jvp of
-    sampling.py:266-285 (norot) or 287-317 (nosr_norot). ham_data is the raw
-    {h0, h1, chol}; intermediates are rebuilt at each lambda. Central differences at h and
-    h/2, Richardson-extrapolated (error O(h^4)). Returns (energy, d energy, block_e,
+    h1 + lambda * direction (direction [2, norb, norb]) with prop_data, fields and SR
+    uniforms held fixed: the quantity that driver.py:207-215 takes with jax.jvp of
+    sampling.py:266-285 (norot) or 287-317 (nosr_norot); orbital_rotation: of
+    sampling.py:173-196 / 221-254, the trial re-optimised at every lambda (rdm1, and so the
+    mean-field shifts, stay those given, as the driver fixes wave_data["rdm1"]). ham_data is
+    the raw {h0, h1, chol}; intermediates are rebuilt at each lambda. Central differences at
+    h and h/2, Richardson-extrapolated (error O(h^4)). Returns (energy, d energy, block_e,
     d block_e, block_w, d block_w) at lambda = 0."""
     import copy
 
     def run(lam):
         hd = {"h0": ham_data["h0"], "h1": np.asarray(ham_data["h1"]) + lam * direction,
               "chol": ham_data["chol"]}
-        hd = trial.build_measurement_intermediates(hd, mo)
+        m = mo
+        if orbital_rotation:
+            chol3 = np.asarray(ham_data["chol"]).reshape(-1, trial.norb, trial.norb)
+            m = rhf_optimize(hd["h1"], chol3, mo, trial.nelec[0], n_opt_iter) if trial.kind == "rhf" else \
+                uhf_optimize(hd["h1"], chol3, mo, trial.nelec, n_opt_iter)
+        hd = trial.build_measurement_intermediates(hd, m)
         hd = build_propagation_intermediates(hd, rdm1, trial.norb, trial.nelec, prop.dt, restricted)
-        e, _, be, bw = sampler.propagate_phaseless(prop, trial, hd, copy.deepcopy(prop_data), mo,
-                                                   fields, zetas, do_sr=do_sr)
+        pd = copy.deepcopy(prop_data)
+        if orbital_rotation:  # _ad_block recomputes the overlaps with the new trial
+            pd["overlaps"] = trial.overlap(pd["walkers"], m)
+        e, _, be, bw = sampler.propagate_phaseless(prop, trial, hd, pd, m, fields, zetas, do_sr=do_sr)
         return np.concatenate([[e], be, bw])
 
     v0 = run(0.0)

@@ -1,6 +1,7 @@
 """Host-side pieces on the CPU: the Frechet derivative of expm that gives d exp_h1 / d lambda,
 the oracle's finite-difference derivative of the blocked energy (its convergence in h), and
-the norm bookkeeping of the oracle's free-projection step."""
+the norm bookkeeping of the oracle's free-projection step, and the trial optimisation
+(SCF) of the orbital-rotation derivative with its tangent."""
 
 import numpy as np
 import pytest
@@ -109,3 +110,49 @@ def test_oracle_free_projection_norm_bookkeeping():
             raw[i] = c[:, None, None] * raw[i]
     want = trial.overlap(raw, s.mo_coeff)
     assert np.max(np.abs(pd["overlaps"] - want)) < 1e-10 * np.max(np.abs(want))
+
+
+def _scf_system(kind, norb=8, nelec=(3, 3), nchol=12, seed=6):
+    from cs_afqmc_gb300 import synthetic
+    s = synthetic.molecular(norb, nelec, nchol, seed=seed, kind=kind)
+    h1 = np.asarray(s.h1)
+    h1 = np.stack([h1, h1]) if h1.ndim == 2 else h1
+    chol3 = np.asarray(s.chol).reshape(-1, norb, norb)
+    return s, h1, chol3
+
+
+@pytest.mark.parametrize("kind,nelec", [("rhf", (3, 3)), ("uhf", (4, 2))])
+def test_scf_optimize_value_and_tangent(kind, nelec):
+    """The trial optimisation of the orbital-rotation AD variants (rhf/uhf.optimize,
+    wavefunctions.py:566-600, 750-813) on the CPU: the torch iterations equal the oracle's,
+    and their first-order change along dh1 equals a Richardson central difference of the
+    oracle's iterations."""
+    from cs_afqmc_gb300.wavefunctions import _scf
+    norb = 8
+    s, h1, chol3 = _scf_system(kind, norb, nelec)
+    mo = s.mo_coeff
+    rng = np.random.default_rng(8)
+    d = rng.standard_normal((2, norb, norb)) * 0.1
+    d = np.stack([(x + x.T) / 2 for x in d])
+    T = lambda x: torch.as_tensor(np.ascontiguousarray(x))  # noqa: E731
+    if kind == "rhf":
+        h = (h1[0] + h1[1]) / 2
+        h, dh = [T((h + h.T) / 2)], [T((d[0] + d[1]) / 2)]
+        dm0 = [T(2 * mo @ mo.T)]
+        ne = (nelec[0],)
+        ora = lambda lam: [O.rhf_optimize(h1 + lam * d, chol3, mo, nelec[0], 30)]  # noqa: E731
+    else:
+        h, dh = [T(h1[0]), T(h1[1])], [T(d[0]), T(d[1])]
+        dm0 = [T(mo[0] @ mo[0].T), T(mo[1] @ mo[1].T)]
+        ne = nelec
+        ora = lambda lam: O.uhf_optimize(h1 + lam * d, chol3, mo, nelec, 30)  # noqa: E731
+    mos, dmos = _scf(kind, h, T(chol3), dm0, ne, 30, dh)
+    ref = ora(0.0)
+    for a, b in zip(mos, ref):
+        assert np.max(np.abs(a.numpy() - b)) < 1e-10
+    eps = 1e-4
+    d1 = [(p - m) / (2 * eps) for p, m in zip(ora(eps), ora(-eps))]
+    d2 = [(p - m) / eps for p, m in zip(ora(eps / 2), ora(-eps / 2))]
+    for got, a, b in zip(dmos, d1, d2):
+        fd = (4 * b - a) / 3
+        assert np.max(np.abs(got.numpy() - fd)) < 1e-7 * max(1.0, np.max(np.abs(fd))), np.max(np.abs(got.numpy() - fd))

@@ -1,0 +1,109 @@
+"""Forward-mode derivative with orbital rotation (sampler.propagate_phaseless_ad,
+sampling.py:173-196, and _ad_nosr 221-254: the trial re-optimised by trial.optimize for
+h1 + lambda D; the driver's default options["orbital_rotation"]) through the C ABI.
+
+Checks, on identical fields and SR uniforms:
+* the optimised trial equals the oracle's SCF iterations (1e-10);
+* the values of the derivative call equal the value path propagate_phaseless_ad (1e-10)
+  and the oracle's (1e-9);
+* d energy / d lambda and the per-block derivatives equal the oracle's Richardson central
+  difference with the trial re-optimised at every lambda (relative 1e-6, as for the
+  fixed-trial derivative);
+* the driver's forward mode with orbital rotation against its own per-block call.
+(The fixed-trial tests of test_gpu_ad.py go through the same entry point with no trial
+tangents.)
+"""
+
+import numpy as np
+import pytest
+
+from oracle import afqmc_oracle as O
+from tests.helpers import Case, rel_err, to_np
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    dict(kind="rhf", restricted=True, norb=10, nelec=(3, 3), nchol=24, nw=8),
+    dict(kind="rhf", restricted=False, norb=9, nelec=(3, 3), nchol=17, nw=6),
+    dict(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=6),
+]
+IDS = ["rhf-r", "rhf-u", "uhf"]
+N_PROP, N_ENE, N_SR = 3, 2, 2
+
+
+@pytest.fixture(params=list(range(len(CASES))), ids=IDS)
+def case(request):
+    return Case(**CASES[request.param])
+
+
+def _draws(case, n_sr, seed=3):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((n_sr, N_ENE, N_PROP, case.nw, case.nchol)), rng.uniform(size=n_sr)
+
+
+def _direction(case, seed=7):
+    return np.random.default_rng(seed).standard_normal((2, case.norb, case.norb)) * 0.1
+
+
+def test_optimize_matches_oracle(case):
+    wd = case.trial.optimize(case.ham_data, case.wave_data)
+    chol3 = np.asarray(case.sys.chol).reshape(-1, case.norb, case.norb)
+    h1 = np.asarray(case.sys.h1)
+    h1 = np.stack([h1, h1]) if h1.ndim == 2 else h1
+    if case.kind == "rhf":
+        want = [O.rhf_optimize(h1, chol3, case.sys.mo_coeff, case.nelec[0], 30)]
+        got = [to_np(wd["mo_coeff"])]
+    else:
+        want = O.uhf_optimize(h1, chol3, case.sys.mo_coeff, case.nelec, 30)
+        got = to_np(wd["mo_coeff"])
+    for a, b in zip(got, want):
+        assert np.max(np.abs(a - b)) < 1e-10
+    assert wd["rdm1"] is case.wave_data["rdm1"]
+
+
+@pytest.mark.parametrize("do_sr", [True, False], ids=["sr", "nosr"])
+def test_jvp_rot_against_oracle_fd(case, do_sr):
+    from cs_afqmc_gb300 import sampling
+    n_sr = N_SR if do_sr else 1
+    fields, zetas = _draws(case, n_sr)
+    D = _direction(case)
+    samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=n_sr)
+    e, de, pg = samp.propagate_phaseless_ad_jvp(case.ham, case.ham_data, D, case.prop, case.gpu_prop_data(),
+                                                case.trial, case.wave_data, do_sr=do_sr, fields=fields,
+                                                zetas=zetas if do_sr else None)
+    samp_o = O.Sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=n_sr)
+    raw = {"h0": case.sys.h0, "h1": case.sys.h1, "chol": case.sys.chol}
+    e_o, de_o, be_o, dbe_o, bw_o, dbw_o = O.phaseless_derivative_fd(
+        samp_o, case.o_prop, case.o_trial, raw, D, case.sys.rdm1, case.sys.mo_coeff,
+        case.oracle_prop_data(), fields, zetas, case.restricted, h=1e-4, do_sr=do_sr, orbital_rotation=True)
+    assert rel_err(e.item(), e_o) < 1e-9
+    assert rel_err(to_np(pg["block_energies"]), be_o) < 1e-9
+    scale_e = max(abs(de_o), np.max(np.abs(dbe_o)), 1e-3)
+    assert abs(de.item() - de_o) < 1e-6 * scale_e, (de.item(), de_o)
+    assert np.max(np.abs(to_np(pg["dblock_energies"]) - dbe_o)) < 1e-6 * scale_e
+    scale_w = max(np.max(np.abs(dbw_o)), 1e-3)
+    assert np.max(np.abs(to_np(pg["dblock_weights"]) - dbw_o)) < 1e-6 * scale_w
+    if do_sr:
+        e_v, _ = samp.propagate_phaseless_ad(case.ham, case.ham_data, 0.0, D, case.prop, case.gpu_prop_data(),
+                                             case.trial, case.wave_data, fields=fields, zetas=zetas)
+        assert rel_err(e.item(), e_v.item()) < 1e-10
+
+
+def test_driver_forward_rotation():
+    from cs_afqmc_gb300 import driver, sampling
+    case = Case(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=6)
+    nb = 2
+    rng = np.random.default_rng(33)
+    fields = rng.standard_normal((nb, 1, N_ENE, N_PROP, case.nw, case.nchol))
+    zetas = rng.uniform(size=(nb, 2))
+    samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=1)
+    e_a, o_a, w_a, _ = driver.run_blocks_ad(samp, case.ham, case.ham_data, case.prop, case.gpu_prop_data(),
+                                            case.trial, case.wave_data, nb, observable=(case.sys.h1, 0.25),
+                                            fields=fields, zetas=zetas, orbital_rotation=True)
+    _, de, _ = samp.propagate_phaseless_ad_jvp(case.ham, case.ham_data, case.sys.h1, case.prop, case.gpu_prop_data(),
+                                               case.trial, case.wave_data, fields=fields[0], zetas=zetas[0][:1])
+    assert abs(to_np(o_a)[0] - (de.item() + 0.25)) < 1e-10 * max(1.0, abs(de.item()))
+    assert np.all(np.isfinite(to_np(e_a))) and np.all(np.isfinite(to_np(w_a)))
+    with pytest.raises(NotImplementedError):
+        driver.run_blocks_ad(samp, case.ham, case.ham_data, case.prop, case.gpu_prop_data(), case.trial,
+                             case.wave_data, 1, ad_mode="reverse", orbital_rotation=True)
