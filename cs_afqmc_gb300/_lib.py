@@ -52,6 +52,11 @@ class JvpInputs(ctypes.Structure):
                                               "dtrial_up", "dtrial_dn", "drot_chol_up", "drot_chol_dn")]
 
 
+class VjpOutputs(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("gexp_h1_up", "gexp_h1_dn", "grot_h1_up", "grot_h1_dn",
+                                              "gtrial_up", "gtrial_dn", "grot_chol")]
+
+
 class WalkerState(ctypes.Structure):
     _fields_ = [("walkers_up", _vp), ("walkers_dn", _vp), ("weights", _vp),
                 ("overlaps", _vp), ("scalars", _vp)]
@@ -97,6 +102,9 @@ _SIGS = {
                                                       ctypes.c_size_t, _vp, _vp, ctypes.c_int32, ctypes.c_int32,
                                                       ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp,
                                                       _vp, _vp]),
+    "afq_propagate_phaseless_vjp_ex": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_size_t,
+                                                      _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                      ctypes.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "afq_vjp_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(Dims), ctypes.c_int32, ctypes.c_int32,
                                                  ctypes.c_int32]),
     "afq_propagate_phaseless_vjp": (ctypes.c_int, [_vp, ctypes.POINTER(WalkerState), _vp, ctypes.c_size_t, _vp,

@@ -233,7 +233,8 @@ __global__ void k_a_rot(const afq_ctx_dev c, const double2* __restrict__ green, 
 __global__ void __launch_bounds__(256) k_a_green(const afq_ctx_dev c, const double2* __restrict__ w_up,
                                                  const double2* __restrict__ w_dn, const double2* __restrict__ ga,
                                                  const double2* __restrict__ gb, const double2* __restrict__ lbar,
-                                                 double2* __restrict__ wb_up, double2* __restrict__ wb_dn) {
+                                                 double2* __restrict__ wb_up, double2* __restrict__ wb_dn,
+                                                 double* gt_up, double* gt_dn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int wlk = blockIdx.x, norb = c.norb, tid = threadIdx.x, nt = blockDim.x, km = c.kmax;
   double2* Ws = reinterpret_cast<double2*>(smem_raw);  // [norb][km]
@@ -314,6 +315,16 @@ __global__ void __launch_bounds__(256) k_a_green(const afq_ctx_dev c, const doub
       const size_t gi = (size_t)p * ks + j;
       Wb[gi] = cadd(Wb[gi], a);
     }
+    // orbital rotation: S = C^T W, so C-bar[p][i] += Re sum_k W[p][k] conj(S-bar[i][k]) with
+    // S-bar = Z; the RHF trial serves both slabs
+    double* gt = s == 0 ? gt_up : gt_dn;
+    if (gt)
+      for (int e = tid; e < norb * o; e += nt) {
+        const int p = e / o, i = e % o;
+        double a = 0.0;
+        for (int k = 0; k < o; ++k) a += Ws[p * o + k].x * Zs[i * o + k].x + Ws[p * o + k].y * Zs[i * o + k].y;
+        atomicAdd(gt + (size_t)p * o + i, a);
+      }
     __syncthreads();
   }
 }
@@ -746,16 +757,148 @@ int a_launch_energy(const afq_ctx_dev& c, const AdjointBufs& a, const double2* g
 }
 
 int a_launch_green(const afq_ctx_dev& c, const void* wu, const void* wd, const double2* ga, const double2* gb,
-                   const double2* lbar, double2* wbu, double2* wbd, cudaStream_t st) {
+                   const double2* lbar, double2* wbu, double2* wbd, cudaStream_t st, double* const* gt) {
   const size_t km = c.kmax;
   const size_t smem = (3 * (size_t)c.norb * km + 4 * km * km) * sizeof(double2) + (size_t)c.norb * km * sizeof(double);
   if (int e = a_smem(smem, "Green")) return e;
   cudaFuncSetAttribute(k_a_green, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   {
     ProfScope _ps(K_GREEN, st);
-    k_a_green<<<c.nw, 256, smem, st>>>(c, (const double2*)wu, (const double2*)wd, ga, gb, lbar, wbu, wbd);
+    double* gu = gt ? gt[0] : nullptr;
+    double* gd = gt ? (c.nspin_g == 2 ? gt[1] : gt[0]) : nullptr;
+    k_a_green<<<c.nw, 256, smem, st>>>(c, (const double2*)wu, (const double2*)wd, ga, gb, lbar, wbu, wbd, gu,
+                                       c.nslab == 2 ? gd : nullptr);
   }
   return a_err("a_green");
+}
+
+// grc[g][k] += alpha Re sum_w conj(fb-bar[w][g]) G[w][k]: the transpose of fb = alpha rot_chol G
+// with respect to rot_chol. CTA per 32 x 64 output tile, walkers staged 8 at a time.
+__global__ void __launch_bounds__(256) k_a_rc_fb(int nw, int nchol, int ktot, double alpha,
+                                                 const double2* __restrict__ fbb, const double2* __restrict__ green,
+                                                 double* __restrict__ grc) {
+  __shared__ double2 Fs[8][32];
+  __shared__ double2 Gs[8][64];
+  const int g0 = blockIdx.y * 32, k0 = blockIdx.x * 64, tid = threadIdx.x, tk = tid & 63, tg = tid >> 6;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int w0 = 0; w0 < nw; w0 += 8) {
+    for (int e = tid; e < 8 * 32; e += 256) {
+      const int wl = e >> 5, gg = e & 31;
+      Fs[wl][gg] = (w0 + wl < nw && g0 + gg < nchol) ? fbb[(size_t)(w0 + wl) * nchol + g0 + gg] : c2(0, 0);
+    }
+    for (int e = tid; e < 8 * 64; e += 256) {
+      const int wl = e >> 6, kk = e & 63;
+      Gs[wl][kk] = (w0 + wl < nw && k0 + kk < ktot) ? green[(size_t)(w0 + wl) * ktot + k0 + kk] : c2(0, 0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int wl = 0; wl < 8; ++wl) {
+      const double2 gv = Gs[wl][tk];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const double2 f = Fs[wl][tg + 4 * r];
+        acc[r] += f.x * gv.x + f.y * gv.y;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int g = g0 + tg + 4 * r, k = k0 + tk;
+    if (g < nchol && k < ktot) grc[(size_t)g * ktot + k] += alpha * acc[r];
+  }
+}
+
+// Local-energy part of the rot_chol cotangent: with f_g = RC_g G^T and
+// dE / d f_g[i][k] = kappa f_g[k][i] + gamma c delta_ik (as in k_a_energy),
+// RC_g-bar[i][p] += sum_w e-bar_w Re sum_k (kappa f_g[k][i] + gamma c delta_ik) G_w[k][p].
+// CTA per g, walkers in sequence; the (i, p) entries of both Green blocks are owned by the
+// threads (at most kRcPT each).
+constexpr int kRcPT = 16;
+
+__global__ void __launch_bounds__(256) k_a_rc_energy(const afq_ctx_dev c, const double2* __restrict__ green,
+                                                     const double* __restrict__ ebar, double* __restrict__ grc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int g = blockIdx.x, norb = c.norb, tid = threadIdx.x, nt = blockDim.x, om = c.kmax;
+  double2* Gs = reinterpret_cast<double2*>(smem_raw);  // [ktot]
+  double2* F = Gs + c.ktot;                            // [2][om*om]
+  const double kappa = c.energy_mode == 2 ? -1.0 : -2.0;
+  const double gamma = c.energy_mode == 0 ? 4.0 : (c.energy_mode == 1 ? 2.0 : 1.0);
+  double acc[kRcPT];
+#pragma unroll
+  for (int j = 0; j < kRcPT; ++j) acc[j] = 0.0;
+  for (int w = 0; w < c.nw; ++w) {
+    const double eb = ebar[w];
+    if (eb == 0.0) continue;  // uniform over the CTA
+    for (int i = tid; i < c.ktot; i += nt) Gs[i] = green[(size_t)w * c.ktot + i];
+    __syncthreads();
+    for (int s = 0; s < c.nspin_g; ++s) {
+      const int o = c.gocc[s];
+      const double* RC = c.rot_chol[s] + (size_t)g * o * norb;
+      const double2* Gsp = Gs + (size_t)s * c.gocc[0] * norb;
+      for (int e = tid; e < o * o; e += nt) {
+        const int i = e / o, k = e % o;
+        double2 a = c2(0, 0);
+        for (int p = 0; p < norb; ++p) {
+          a.x = fma(RC[(size_t)i * norb + p], Gsp[(size_t)k * norb + p].x, a.x);
+          a.y = fma(RC[(size_t)i * norb + p], Gsp[(size_t)k * norb + p].y, a.y);
+        }
+        F[s * om * om + e] = a;
+      }
+    }
+    __syncthreads();
+    double2 ct = c2(0, 0);
+    for (int s = 0; s < c.nspin_g; ++s)
+      for (int i = 0; i < c.gocc[s]; ++i) ct = cadd(ct, F[s * om * om + i * c.gocc[s] + i]);
+#pragma unroll
+    for (int j = 0; j < kRcPT; ++j) {
+      const int e = tid + j * nt;
+      if (e < c.ktot) {
+        const int s = (c.nspin_g == 2 && e >= c.gocc[0] * norb) ? 1 : 0;
+        const int o = c.gocc[s], el = e - s * c.gocc[0] * norb, i = el / norb, p = el % norb;
+        const double2* Fs = F + s * om * om;
+        const double2* Gsp = Gs + (size_t)s * c.gocc[0] * norb;
+        double a = 0.0;
+        for (int k = 0; k < o; ++k) {
+          double2 m = cscale(Fs[k * o + i], kappa);
+          if (k == i) m = cadd(m, cscale(ct, gamma));
+          a += m.x * Gsp[(size_t)k * norb + p].x - m.y * Gsp[(size_t)k * norb + p].y;
+        }
+        acc[j] += eb * a;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < kRcPT; ++j) {
+    const int e = tid + j * nt;
+    if (e < c.ktot) grc[(size_t)g * c.ktot + e] += acc[j];
+  }
+}
+
+int a_launch_rc_fb(const afq_ctx_dev& c, const AdjointBufs& a, const double2* green, double alpha,
+                   cudaStream_t st) {
+  {
+    ProfScope _ps(K_FB, st);
+    k_a_rc_fb<<<dim3((c.ktot + 63) / 64, (c.nchol + 31) / 32), 256, 0, st>>>(c.nw, c.nchol, c.ktot, alpha, a.fbb,
+                                                                             green, a.grc);
+  }
+  return a_err("a_rc_fb");
+}
+
+int a_launch_rc_energy(const afq_ctx_dev& c, const AdjointBufs& a, const double2* green, cudaStream_t st) {
+  if (c.ktot > kRcPT * 256) {
+    afq_set_error("adjoint rot_chol kernel: nocc * norb <= %d", kRcPT * 256);
+    return -2;
+  }
+  const size_t smem = ((size_t)c.ktot + 2 * (size_t)c.kmax * c.kmax) * sizeof(double2);
+  if (int e = a_smem(smem, "rot_chol")) return e;
+  cudaFuncSetAttribute(k_a_rc_energy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  {
+    ProfScope _ps(K_ENERGY, st);
+    k_a_rc_energy<<<c.nchol, 256, smem, st>>>(c, green, a.ebar, a.grc);
+  }
+  return a_err("a_rc_energy");
 }
 
 int a_launch_qr(const afq_ctx_dev& c, const void* wold_u, const void* wold_d, const void* q_u, const void* q_d,

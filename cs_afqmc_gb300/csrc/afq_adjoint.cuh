@@ -24,14 +24,25 @@ struct AdjointBufs {
   double* bwb;         // block-weight cotangents [n blocks]
   double* gexp[2];     // outputs: d energy / d exp_h1 per slab [norb^2]
   double* grot[2];     // outputs: d energy / d rot_h1 per Green block [gocc * norb]
+  // orbital rotation (NULL: not requested): d energy / d trial per Green block [norb][gocc]
+  // and d energy / d rot_chol in the concatenated layout [nchol][ktot]
+  double* gtrial[2];
+  double* grc;
 };
 
 int a_launch_end(int nblk, const double* be, const double* bw, const AdjointBufs& a, cudaStream_t st);
 int a_launch_block_stats(const afq_ctx_dev& c, const AdjointBufs& a, int blk, const double2* energy,
                          const double* weights, const double* scalars, const double* be, cudaStream_t st);
 int a_launch_energy(const afq_ctx_dev& c, const AdjointBufs& a, const double2* green, cudaStream_t st);
+// gt (may be NULL): the trial cotangents, accumulated (gtrial of AdjointBufs)
 int a_launch_green(const afq_ctx_dev& c, const void* wu, const void* wd, const double2* ga, const double2* gb,
-                   const double2* lbar, double2* wbu, double2* wbd, cudaStream_t st);
+                   const double2* lbar, double2* wbu, double2* wbd, cudaStream_t st,
+                   double* const* gt = nullptr);
+// rot_chol cotangent of the force bias: grc += alpha Re(fb-bar^H G) (G of the step's start)
+int a_launch_rc_fb(const afq_ctx_dev& c, const AdjointBufs& a, const double2* green, double alpha,
+                   cudaStream_t st);
+// rot_chol cotangent of the local energy at a measurement (G of the QR'd walkers)
+int a_launch_rc_energy(const afq_ctx_dev& c, const AdjointBufs& a, const double2* green, cudaStream_t st);
 int a_launch_qr(const afq_ctx_dev& c, const void* wold_u, const void* wold_d, const void* q_u, const void* q_d,
                 const double2* qb_u, const double2* qb_d, double2* ob_u, double2* ob_d, cudaStream_t st);
 int a_launch_weights(const afq_ctx_dev& c, const AdjointBufs& a, const double2* shift, const double2* fbt,

@@ -834,6 +834,25 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
                                 int32_t flags, double* block_energy, double* block_weight,
                                 double* energy, double* gexp_h1_up, double* gexp_h1_dn,
                                 double* grot_h1_up, double* grot_h1_dn, void* stream) {
+  afq_vjp_outputs out;
+  memset(&out, 0, sizeof(out));
+  out.gexp_h1_up = gexp_h1_up;
+  out.gexp_h1_dn = gexp_h1_dn;
+  out.grot_h1_up = grot_h1_up;
+  out.grot_h1_dn = grot_h1_dn;
+  return afq_propagate_phaseless_vjp_ex(ctx, state, vjp_workspace, vjp_workspace_bytes, fields, zetas, n_prop_steps,
+                                        n_ene_blocks, n_sr_blocks, flags, block_energy, block_weight, energy, &out,
+                                        stream);
+}
+
+int afq_propagate_phaseless_vjp_ex(afq_ctx* ctx, afq_walker_state* state, void* vjp_workspace,
+                                   size_t vjp_workspace_bytes, const double* fields, const double* zetas,
+                                   int32_t n_prop_steps, int32_t n_ene_blocks, int32_t n_sr_blocks, int32_t flags,
+                                   double* block_energy, double* block_weight, double* energy,
+                                   const afq_vjp_outputs* out, void* stream) {
+  if (!out) { afq_set_error("NULL argument"); return -1; }
+  double *gexp_h1_up = out->gexp_h1_up, *gexp_h1_dn = out->gexp_h1_dn, *grot_h1_up = out->grot_h1_up,
+         *grot_h1_dn = out->grot_h1_dn;
   const bool do_sr = !(flags & AFQ_JVP_NO_SR);
   if (!ctx || !fields || (do_sr && !zetas) || !block_energy || !block_weight || !energy || !gexp_h1_up ||
       !grot_h1_up) {
@@ -850,6 +869,11 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
   const afq_ctx_dev& d = ctx->dev;
   if (d.nslab == 2 && !gexp_h1_dn) { afq_set_error("unrestricted walkers need gexp_h1_dn"); return -1; }
   if (d.nspin_g == 2 && !grot_h1_dn) { afq_set_error("the UHF trial needs grot_h1_dn"); return -1; }
+  const bool rot = out->gtrial_up || out->grot_chol;
+  if (rot && (!out->gtrial_up || !out->grot_chol || (d.nspin_g == 2 && !out->gtrial_dn))) {
+    afq_set_error("orbital-rotation gradients need gtrial for every spin of the trial and grot_chol");
+    return -1;
+  }
   const int P = n_prop_steps, NE = n_ene_blocks;
   Layout L;
   const AdjSizes as = adjoint_sizes(d, ctx->nw_chunk, P, NE, n_sr_blocks, &L);
@@ -888,6 +912,10 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
   a.gexp[1] = d.nslab == 2 ? gexp_h1_dn : nullptr;
   a.grot[0] = grot_h1_up;
   a.grot[1] = d.nspin_g == 2 ? grot_h1_dn : nullptr;
+  a.gtrial[0] = rot ? out->gtrial_up : nullptr;
+  a.gtrial[1] = rot && d.nspin_g == 2 ? out->gtrial_dn : nullptr;
+  a.grc = rot ? out->grot_chol : nullptr;
+  double* const* gt = rot ? a.gtrial : nullptr;
   cudaStream_t st = S(stream);
   double2* ovl = reinterpret_cast<double2*>(state->overlaps);
   const size_t step_elems = (size_t)d.nw * d.nchol;
@@ -932,6 +960,11 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
   if (d.nslab == 2) CHECK(zero(gexp_h1_dn, (size_t)d.norb * d.norb * sizeof(double), st));
   CHECK(zero(grot_h1_up, (size_t)d.gocc[0] * d.norb * sizeof(double), st));
   if (d.nspin_g == 2) CHECK(zero(grot_h1_dn, (size_t)d.gocc[1] * d.norb * sizeof(double), st));
+  if (rot) {
+    for (int b = 0; b < d.nspin_g; ++b)
+      CHECK(zero(a.gtrial[b], (size_t)d.norb * d.gocc[b] * sizeof(double), st));
+    CHECK(zero(a.grc, (size_t)d.nchol * d.ktot * sizeof(double), st));
+  }
   CHECK(afq::a_launch_end(blk, block_energy, block_weight, a, st));
   const int nwc = ctx->nw_chunk, nb = d.nw / nwc;
   const long nn = (long)d.norb * d.norb;
@@ -945,7 +978,7 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
       // then send it back through the gather
       const int s0 = (b + 1) * (P + 2);
       CHECK(afq::a_launch_green(d, tp.w(s0, 0), tp.w(s0, 1), gp ? a.gpend : nullptr, nullptr, a.lbar, a.wb[0],
-                                a.wb[1], st));
+                                a.wb[1], st, gt));
       CHECK(afq::a_launch_sr(d, a, tp.idx(b / NE), st));
       swap_slabs(a.wb, a.wb2);
       CHECK(zero(a.lbar, d.nw * sizeof(double2), st));
@@ -955,8 +988,9 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
     CHECK(afq::a_launch_block_stats(d, a, b, tp.ene(b), tp.wt(sq_i), tp.sc(sq_i), block_energy, st));
     CHECK(afq::launch_green<double>(d, tp.w(sq_i, 0), tp.w(sq_i, 1), ctx->green, nullptr, true, st));
     CHECK(afq::a_launch_energy(d, a, ctx->green, st));
+    if (rot) CHECK(afq::a_launch_rc_energy(d, a, ctx->green, st));
     CHECK(afq::a_launch_green(d, tp.w(sq_i, 0), tp.w(sq_i, 1), a.gene, gp ? a.gpend : nullptr, a.lbar, a.wb[0],
-                              a.wb[1], st));
+                              a.wb[1], st, gt));
     CHECK(zero(a.lbar, d.nw * sizeof(double2), st));
     gp = false;
     CHECK(afq::a_launch_qr(d, tp.w(sw_i, 0), tp.w(sw_i, 1), tp.w(sq_i, 0), tp.w(sq_i, 1), a.wb[0], a.wb[1],
@@ -967,7 +1001,7 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
       CHECK(afq::a_launch_weights(d, a, tp.sh(step), tp.fbt(step), tp.ov(post), tp.ov(start), tp.wt(start),
                                   tp.wt(post), tp.sc(start), st));
       CHECK(afq::a_launch_green(d, tp.w(post, 0), tp.w(post, 1), gp ? a.gpend : nullptr, nullptr, a.lbar, a.wb[0],
-                                a.wb[1], st));
+                                a.wb[1], st, gt));
       for (int k = 0; k < nb; ++k) {
         const int w0 = k * nwc;
         CHECK(afq::launch_gemm_cr(true, nwc, (int)nn, d.nchol, tp.xt(step) + (size_t)w0 * d.nchol, d.nchol,
@@ -977,6 +1011,10 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
                                   a.xtb + (size_t)w0 * d.nchol, d.nchol, c2(0.0, -sq), st));
       }
       CHECK(afq::a_launch_field(d, a, tp.xt(step), st));
+      if (rot) {  // fb = alpha rot_chol G(W_start): rot_chol-bar += alpha Re(fb-bar^H G)
+        CHECK(afq::launch_green<double>(d, tp.w(start, 0), tp.w(start, 1), ctx->green, nullptr, true, st));
+        CHECK(afq::a_launch_rc_fb(d, a, ctx->green, alpha, st));
+      }
       CHECK(afq::launch_gemm_cr(true, d.nw, d.ktot, d.nchol, a.fbb, d.nchol, brc, d.ktot, a.gpend, d.ktot,
                                 c2(alpha, 0.0), st));
       gp = true;
@@ -986,6 +1024,10 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
       a.lbar2 = t;
     }
   }
+  // the first step's G and the block's initial overlap were evaluated with the trial too
+  if (rot)
+    CHECK(afq::a_launch_green(d, tp.w(0, 0), tp.w(0, 1), gp ? a.gpend : nullptr, nullptr, a.lbar, a.wb[0], a.wb[1], st,
+                              gt));
   return 0;
 }
 

@@ -43,7 +43,7 @@ def run_blocks(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_da
 def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_data,
                   n_blocks: int, observable=None, do_sr: bool = True, fields=None, zetas=None,
                   ad_mode: str = "forward", orbital_rotation: bool = False):
-    """AD branches of driver.py without orbital rotation (driver.py:165-229, 245-308 on one
+    """AD branches of driver.py (driver.py:165-229, 245-308 on one
     rank). ad_mode "forward": per block the jvp of sampler.propagate_phaseless_ad_norot
     (do_sr=False: ..._nosr_norot) along the observable; "reverse": its vjp, the block's
     one-body density matrix rdm1 = d energy / d h1, and the observable sum(rdm1 * op). A
@@ -53,14 +53,12 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
     [n_blocks, n_sr, n_ene, n_prop, nw, G]; zetas (optional): [n_blocks, n_sr + 1].
     Returns device tensors (block_energy, block_observable, block_weight), each
     [n_blocks], and prop_data; in reverse mode prop_data["block_rdm1s"] holds the
-    [n_blocks, 2, norb, norb] density matrices. orbital_rotation (forward mode; the
-    reference's options["orbital_rotation"], default True there): the jvp of
+    [n_blocks, 2, norb, norb] density matrices. orbital_rotation (the reference's
+    options["orbital_rotation"], default True there): the jvp / vjp of
     sampler.propagate_phaseless_ad (_nosr), the trial re-optimised for h1 + lambda D in every
     block; wave_data needs "rdm1", as the driver sets it."""
     if ad_mode not in ("forward", "reverse"):
         raise ValueError(f"ad_mode must be 'forward' or 'reverse', got {ad_mode!r}")
-    if orbital_rotation and ad_mode != "forward":
-        raise NotImplementedError("orbital rotation is built for the forward mode only")
     if observable is None:
         op, const = torch.as_tensor(ham_data["h1"]), 0.0
     else:
@@ -83,8 +81,9 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
             e, de, prop_data = jvp(ham, ham_data, op, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f,
                                    zetas=z_local)
         else:
-            e, r, prop_data = sampler.propagate_phaseless_ad_norot_vjp(
-                ham, ham_data, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f, zetas=z_local)
+            vjp = sampler.propagate_phaseless_ad_vjp if orbital_rotation else sampler.propagate_phaseless_ad_norot_vjp
+            e, r, prop_data = vjp(ham, ham_data, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f,
+                                  zetas=z_local)
             de = torch.sum(r * op)
             ok = torch.isfinite(de)
             rdm1s[n].copy_(torch.where(ok, r, rdm1.to(r.dtype)))

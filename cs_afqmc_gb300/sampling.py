@@ -288,6 +288,64 @@ class sampler:
         h1, the block's one-body density matrix estimate. Returns (energy 0-d, rdm1
         [2, norb, norb], prop_data), CUDA tensors; prop_data also gets "block_energies" and
         "block_weights". FP64 (complex128) walkers only."""
+        energy, g, prop_data = self._vjp_call(prop, prop_data, trial, ham_data, wave_data, do_sr, fields, zetas,
+                                              rotation=False)
+        gexp, grot = g[0], g[1]
+        uhf_trial = isinstance(wave_data["mo_coeff"], (list, tuple))
+        g_exp = prop.exp_h1_cotangent(ham_data, trial, wave_data, gexp if not prop.restricted else gexp[0])
+        g_rot = trial.rot_h1_cotangent(grot if uhf_trial else grot[0], wave_data)
+        rdm1 = _sym(g_exp + g_rot)  # the transpose of the per-spin symmetrisation is itself
+        return energy, rdm1, prop_data
+
+    def propagate_phaseless_ad_vjp(self, ham, ham_data: dict, prop, prop_data: PropData, trial, wave_data: dict,
+                                   do_sr: bool = True, fields: Optional[torch.Tensor] = None,
+                                   zetas: Optional[torch.Tensor] = None):
+        """Reverse-mode derivative of propagate_phaseless_ad (do_sr=False:
+        propagate_phaseless_ad_nosr): the block's one-body density matrix d energy / d h1 with
+        the trial's dependence on h1 through trial.optimize, what driver.py:217-224 computes
+        with jax.vjp under the default options["orbital_rotation"]. The device sweep returns
+        the gradients with respect to exp_h1, rot_h1, the trial and rot_chol; the map from h1
+        to those (the SCF tangent of trial.optimize, the trial rotation, the Frechet
+        derivative of expm) is linear in the direction, so its transpose is taken with torch
+        autograd through the same tangent code the forward mode uses. Returns (energy, rdm1
+        [2, norb, norb], prop_data)."""
+        if "rdm1" not in wave_data:
+            raise _lib.AfqError("orbital rotation needs wave_data['rdm1'] (the driver sets it to the trial's rdm1)")
+        h0 = {k: v for k, v in ham_data.items() if k != _CACHE_KEY}
+        wd = trial.optimize(h0, wave_data)
+        hd = ham.build_measurement_intermediates(h0, trial, wd)
+        hd = ham.build_propagation_intermediates(hd, prop, trial, wd)
+        energy, g, prop_data = self._vjp_call(prop, prop_data, trial, hd, wd, do_sr, fields, zetas, rotation=True)
+        gexp, grot, gtrial, grc = g
+        uhf_trial = isinstance(wd["mo_coeff"], (list, tuple))
+        norb = trial.norb
+        nchol = int(hd["chol"].shape[0])
+        D = torch.zeros((2, norb, norb), dtype=torch.float64, device=device(), requires_grad=True)
+        with torch.enable_grad():
+            dh1 = _sym(D)
+            _, dmo = trial.optimize_tangent(h0, wave_data, dh1)
+            dexp = prop.exp_h1_tangent(hd, trial, wd, dh1)
+            drot, drc = trial.rotation_tangents(hd, wd, dmo, dh1)
+            ge = gexp if not prop.restricted else gexp[0]
+            lin = torch.sum(ge * dexp)
+            if uhf_trial:
+                n_up, n_dn = trial.nelec
+                rc = grc.reshape(nchol, -1)
+                lin = lin + torch.sum(grot[0] * drot[0]) + torch.sum(grot[1] * drot[1])
+                lin = lin + torch.sum(gtrial[0] * dmo[0]) + torch.sum(gtrial[1] * dmo[1])
+                lin = lin + torch.sum(rc[:, :n_up * norb].reshape(drc[0].shape) * drc[0])
+                lin = lin + torch.sum(rc[:, n_up * norb:].reshape(drc[1].shape) * drc[1])
+            else:
+                lin = lin + torch.sum(grot[0] * drot) + torch.sum(gtrial[0] * dmo)
+                lin = lin + torch.sum(grc.reshape(drc.shape) * drc)
+            (rdm1,) = torch.autograd.grad(lin, D)
+        return energy, rdm1.detach(), prop_data
+
+    def _vjp_call(self, prop, prop_data: PropData, trial, ham_data: dict, wave_data: dict, do_sr: bool, fields,
+                  zetas, rotation: bool):
+        """afq_propagate_phaseless_vjp_ex on the engine of (trial, ham_data, wave_data).
+        Returns (energy 0-d, (gexp [2, norb, norb], grot [up, dn or None], gtrial, grot_chol),
+        prop_data); gtrial / grot_chol only with rotation."""
         eng = prop._engine(trial, ham_data, wave_data, prop_data["walkers"])
         if eng.precision != _lib.AFQ_PREC_FP64:
             raise _lib.AfqError("the derivative path needs FP64 (complex128) walkers")
@@ -305,26 +363,33 @@ class sampler:
             eng.vjp_workspace = vws
         vptr = vws.data_ptr() + (-vws.data_ptr()) % 256
         norb = trial.norb
-        out = torch.empty(2 * nblk + 1, dtype=torch.float64, device=device())
+        dev = device()
+        out = torch.empty(2 * nblk + 1, dtype=torch.float64, device=dev)
         be, bw, energy = out[:nblk], out[nblk:2 * nblk], out[2 * nblk:]
-        gexp = torch.empty((2, norb, norb), dtype=torch.float64, device=device())
+        gexp = torch.empty((2, norb, norb), dtype=torch.float64, device=dev)
         n_up, n_dn = trial.nelec
         uhf_trial = isinstance(wave_data["mo_coeff"], (list, tuple))
-        grot = ([torch.empty((n_up, norb), dtype=torch.float64, device=device()),
-                 torch.empty((n_dn, norb), dtype=torch.float64, device=device())] if uhf_trial
-                else [torch.empty((n_up, norb), dtype=torch.float64, device=device()), None])
+        occ = (n_up, n_dn) if uhf_trial else (n_up,)
+        grot = [torch.empty((o, norb), dtype=torch.float64, device=dev) for o in occ] + ([] if uhf_trial else [None])
+        gtrial, grc = [None, None], None
+        if rotation:
+            gtrial = [torch.empty((norb, o), dtype=torch.float64, device=dev) for o in occ] + \
+                ([] if uhf_trial else [None])
+            grc = torch.empty((int(ham_data["chol"].shape[0]), sum(occ) * norb), dtype=torch.float64, device=dev)
+
+        def ptr(x):
+            return None if x is None else x.data_ptr()
+
+        outs = _lib.VjpOutputs(gexp[0].data_ptr(), None if prop.restricted else gexp[1].data_ptr(), ptr(grot[0]),
+                               ptr(grot[1]), ptr(gtrial[0]), ptr(gtrial[1]), ptr(grc))
         st = prop_data.state(eng)
-        _lib.call("afq_propagate_phaseless_vjp", eng.ctx, ctypes.byref(st), vptr, nbytes, f.data_ptr(),
+        _lib.call("afq_propagate_phaseless_vjp_ex", eng.ctx, ctypes.byref(st), vptr, nbytes, f.data_ptr(),
                   None if z is None else z.data_ptr(), self.n_prop_steps, self.n_ene_blocks, n_sr,
                   0 if do_sr else _lib.AFQ_JVP_NO_SR, be.data_ptr(), bw.data_ptr(), energy.data_ptr(),
-                  gexp[0].data_ptr(), gexp[1].data_ptr() if not prop.restricted else None,
-                  grot[0].data_ptr(), None if grot[1] is None else grot[1].data_ptr(), stream_ptr())
-        g_exp = prop.exp_h1_cotangent(ham_data, trial, wave_data, gexp if not prop.restricted else gexp[0])
-        g_rot = trial.rot_h1_cotangent(grot if uhf_trial else grot[0], wave_data)
-        rdm1 = _sym(g_exp + g_rot)  # the transpose of the per-spin symmetrisation is itself
+                  ctypes.byref(outs), stream_ptr())
         dict.__setitem__(prop_data, "block_energies", be)
         dict.__setitem__(prop_data, "block_weights", bw)
-        return energy[0], rdm1, prop_data
+        return energy[0], (gexp, grot, gtrial, grc), prop_data
 
     def __hash__(self) -> int:
         return hash((self.n_prop_steps, self.n_ene_blocks, self.n_sr_blocks, self.n_blocks))

@@ -360,6 +360,31 @@ int afq_propagate_phaseless_vjp(afq_ctx* ctx, afq_walker_state* state, void* vjp
                                 double* energy, double* gexp_h1_up, double* gexp_h1_dn,
                                 double* grot_h1_up, double* grot_h1_dn, void* stream);
 
+/* Outputs of afq_propagate_phaseless_vjp_ex (device float64, overwritten; NULL where not
+ * wanted or not applicable): the gradients of afq_propagate_phaseless_vjp, and for the
+ * orbital-rotation variant (sampler.propagate_phaseless_ad, the trial re-optimised for
+ * h1 + lambda D) also d energy / d trial per spin of the trial (gtrial_up/dn [norb, n_s], dn
+ * NULL for the RHF trial) and d energy / d rot_chol in the layout [nchol][ktot], ktot =
+ * (n_up [+ n_dn for UHF]) * norb, each row the up block followed by the dn block. The caller
+ * maps them to d energy / d h1 through the transposed tangents of trial.optimize. */
+typedef struct afq_vjp_outputs {
+  double* gexp_h1_up;
+  double* gexp_h1_dn;
+  double* grot_h1_up;
+  double* grot_h1_dn;
+  double* gtrial_up;
+  double* gtrial_dn;
+  double* grot_chol;
+} afq_vjp_outputs;
+
+/* afq_propagate_phaseless_vjp with the outputs in a struct (the trial and rot_chol
+ * gradients of the orbital-rotation variant added). */
+int afq_propagate_phaseless_vjp_ex(afq_ctx* ctx, afq_walker_state* state, void* vjp_workspace,
+                                   size_t vjp_workspace_bytes, const double* fields, const double* zetas,
+                                   int32_t n_prop_steps, int32_t n_ene_blocks, int32_t n_sr_blocks,
+                                   int32_t flags, double* block_energy, double* block_weight,
+                                   double* energy, const afq_vjp_outputs* out, void* stream);
+
 /* ---- correlated sampling (ad_afqmc/corr_sample/corr_sample.py) ---------------------- */
 
 /* One correlated-sampling block of one system with the given fields (float64

@@ -1,4 +1,4 @@
-"""Forward-mode derivative with orbital rotation (sampler.propagate_phaseless_ad,
+"""Forward- and reverse-mode derivatives with orbital rotation (sampler.propagate_phaseless_ad,
 sampling.py:173-196, and _ad_nosr 221-254: the trial re-optimised by trial.optimize for
 h1 + lambda D; the driver's default options["orbital_rotation"]) through the C ABI.
 
@@ -9,7 +9,9 @@ Checks, on identical fields and SR uniforms:
 * d energy / d lambda and the per-block derivatives equal the oracle's Richardson central
   difference with the trial re-optimised at every lambda (relative 1e-6, as for the
   fixed-trial derivative);
-* the driver's forward mode with orbital rotation against its own per-block call.
+* the driver's forward mode with orbital rotation against its own per-block call, and its
+  reverse mode against the forward one;
+* the reverse mode (rdm1) against the forward mode along three directions (relative 1e-8).
 (The fixed-trial tests of test_gpu_ad.py go through the same entry point with no trial
 tangents.)
 """
@@ -104,6 +106,39 @@ def test_driver_forward_rotation():
                                                case.trial, case.wave_data, fields=fields[0], zetas=zetas[0][:1])
     assert abs(to_np(o_a)[0] - (de.item() + 0.25)) < 1e-10 * max(1.0, abs(de.item()))
     assert np.all(np.isfinite(to_np(e_a))) and np.all(np.isfinite(to_np(w_a)))
-    with pytest.raises(NotImplementedError):
-        driver.run_blocks_ad(samp, case.ham, case.ham_data, case.prop, case.gpu_prop_data(), case.trial,
-                             case.wave_data, 1, ad_mode="reverse", orbital_rotation=True)
+    e_r, o_r, w_r, pr = driver.run_blocks_ad(samp, case.ham, case.ham_data, case.prop, case.gpu_prop_data(),
+                                             case.trial, case.wave_data, nb, observable=(case.sys.h1, 0.25),
+                                             fields=fields, zetas=zetas, ad_mode="reverse", orbital_rotation=True)
+    assert rel_err(to_np(e_r), to_np(e_a)) < 1e-10
+    assert rel_err(to_np(o_r), to_np(o_a)) < 1e-8
+
+
+@pytest.mark.parametrize("do_sr", [True, False], ids=["sr", "nosr"])
+def test_vjp_rot_is_transpose_of_jvp_rot(case, do_sr):
+    """Reverse mode with orbital rotation: sum(rdm1 * D) equals the rotated forward-mode
+    derivative along three directions (relative 1e-8), and the energy equals
+    propagate_phaseless_ad's."""
+    from cs_afqmc_gb300 import sampling
+    n_sr = N_SR if do_sr else 1
+    fields, zetas = _draws(case, n_sr, seed=19)
+    z = zetas if do_sr else None
+    samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=n_sr)
+    e, rdm1, _ = samp.propagate_phaseless_ad_vjp(case.ham, case.ham_data, case.prop, case.gpu_prop_data(), case.trial,
+                                                 case.wave_data, do_sr=do_sr, fields=fields, zetas=z)
+    r = to_np(rdm1)
+    assert np.all(np.isfinite(r))
+    if do_sr:
+        e_v, _ = samp.propagate_phaseless_ad(case.ham, case.ham_data, 0.0, 0.0 * case.sys.h1, case.prop,
+                                             case.gpu_prop_data(), case.trial, case.wave_data, fields=fields,
+                                             zetas=zetas)
+        assert rel_err(e.item(), e_v.item()) < 1e-10
+    rng = np.random.default_rng(53)
+    got, want = [], []
+    for _ in range(3):
+        D = rng.standard_normal((2, case.norb, case.norb)) * 0.1
+        _, de, _ = samp.propagate_phaseless_ad_jvp(case.ham, case.ham_data, D, case.prop, case.gpu_prop_data(),
+                                                   case.trial, case.wave_data, do_sr=do_sr, fields=fields, zetas=z)
+        got.append(float(np.sum(r * D)))
+        want.append(de.item())
+    scale = max(np.max(np.abs(want)), 1e-3)
+    assert np.max(np.abs(np.array(got) - np.array(want))) < 1e-8 * scale, (got, want)
