@@ -54,7 +54,8 @@ class JvpInputs(ctypes.Structure):
 
 class VjpOutputs(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("gexp_h1_up", "gexp_h1_dn", "grot_h1_up", "grot_h1_dn",
-                                              "gtrial_up", "gtrial_dn", "grot_chol")]
+                                              "gtrial_up", "gtrial_dn", "grot_chol", "gchol", "gmf_shifts",
+                                              "gh0_prop")]
 
 
 class WalkerState(ctypes.Structure):

@@ -450,7 +450,10 @@ __global__ void k_a_weights(int nw, double dt, double2 h0_prop, const double2* _
     sa += dt * a;
   }
   sa = block_sum(sa, red);
-  if (threadIdx.x == 0) scal[0] = sa;
+  if (threadIdx.x == 0) {
+    scal[0] = sa;
+    scal[1] += sa;  // arg holds dt (E_pc + Re h0_prop): the same sum is h0_prop's cotangent
+  }
 }
 
 // ======================================================================================
@@ -672,9 +675,10 @@ __global__ void __launch_bounds__(256) k_a_vbar(const afq_ctx_dev c, const doubl
 // s-bar = -xt-bar + conj(x - s) fbt-bar (x - s = xt), fb-bar = i sqrt(dt) s-bar.
 // ======================================================================================
 
+// gmf (may be NULL): mf-bar += sqrt(dt) s-bar + conj(xt) shift-bar, summed over walkers
 __global__ void k_a_field(int nchol, double sqdt, const double2* __restrict__ xt, const double2* __restrict__ mf,
                           const double2* __restrict__ xtb, const double2* __restrict__ shb,
-                          const double2* __restrict__ fbtb, double2* __restrict__ fbb) {
+                          const double2* __restrict__ fbtb, double2* __restrict__ fbb, double2* gmf) {
   const int w = blockIdx.x;
   const double2 sh = shb[w], ft = fbtb[w];
   for (int g = threadIdx.x; g < nchol; g += blockDim.x) {
@@ -682,7 +686,62 @@ __global__ void k_a_field(int nchol, double sqdt, const double2* __restrict__ xt
     const double2 xb = cadd(xtb[i], cmul(cconj(mf[g]), sh));
     const double2 sb = csub(cmul(cconj(xt[i]), ft), xb);
     fbb[i] = c2(-sqdt * sb.y, sqdt * sb.x);
+    if (gmf) {
+      const double2 m = cadd(cscale(sb, sqdt), cmul(cconj(xt[i]), sh));
+      atomicAdd(&gmf[g].x, m.x);
+      atomicAdd(&gmf[g].y, m.y);
+    }
   }
+}
+
+// chol-bar[g][pq] += sqrt(dt) sum_w (xt.x vbar.y - xt.y vbar.x): the transpose of
+// vhs = i sqrt(dt) xt chol with respect to chol. CTA per 32 x 64 tile, walkers 8 at a time.
+__global__ void __launch_bounds__(256) k_a_chol_grad(int nwc, int nchol, long nn, double sqdt,
+                                                     const double2* __restrict__ xt,
+                                                     const double2* __restrict__ vbar, double* __restrict__ gchol) {
+  __shared__ double2 Xs[8][32];
+  __shared__ double2 Vs[8][64];
+  const int g0 = blockIdx.y * 32, tid = threadIdx.x, tk = tid & 63, tg = tid >> 6;
+  const long k0 = (long)blockIdx.x * 64;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int w0 = 0; w0 < nwc; w0 += 8) {
+    for (int e = tid; e < 8 * 32; e += 256) {
+      const int wl = e >> 5, gg = e & 31;
+      Xs[wl][gg] = (w0 + wl < nwc && g0 + gg < nchol) ? xt[(size_t)(w0 + wl) * nchol + g0 + gg] : c2(0, 0);
+    }
+    for (int e = tid; e < 8 * 64; e += 256) {
+      const int wl = e >> 6, kk = e & 63;
+      Vs[wl][kk] = (w0 + wl < nwc && k0 + kk < nn) ? vbar[(size_t)(w0 + wl) * nn + k0 + kk] : c2(0, 0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int wl = 0; wl < 8; ++wl) {
+      const double2 v = Vs[wl][tk];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const double2 x = Xs[wl][tg + 4 * r];
+        acc[r] += x.x * v.y - x.y * v.x;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int g = g0 + tg + 4 * r;
+    const long k = k0 + tk;
+    if (g < nchol && k < nn) gchol[(size_t)g * nn + k] += sqdt * acc[r];
+  }
+}
+
+int a_launch_chol_grad(const afq_ctx_dev& c, const AdjointBufs& a, int nwc, const double2* xt, cudaStream_t st) {
+  const long nn = (long)c.norb * c.norb;
+  {
+    ProfScope _ps(K_VHS, st);
+    k_a_chol_grad<<<dim3((unsigned)((nn + 63) / 64), (c.nchol + 31) / 32), 256, 0, st>>>(nwc, c.nchol, nn,
+                                                                                         sqrt(c.dt), xt, a.vbar,
+                                                                                         a.gchol);
+  }
+  return a_err("a_chol_grad");
 }
 
 // ======================================================================================
@@ -965,7 +1024,7 @@ int a_launch_taylor(const afq_ctx_dev& c, const AdjointBufs& a, int w0, int nwc,
 int a_launch_field(const afq_ctx_dev& c, const AdjointBufs& a, const double2* xt, cudaStream_t st) {
   {
     ProfScope _ps(K_FIELD, st);
-    k_a_field<<<c.nw, 256, 0, st>>>(c.nchol, sqrt(c.dt), xt, c.mf, a.xtb, a.shb, a.fbtb, a.fbb);
+    k_a_field<<<c.nw, 256, 0, st>>>(c.nchol, sqrt(c.dt), xt, c.mf, a.xtb, a.shb, a.fbtb, a.fbb, a.gmf);
   }
   return a_err("a_field");
 }

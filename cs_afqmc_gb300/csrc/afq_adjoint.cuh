@@ -28,6 +28,11 @@ struct AdjointBufs {
   // and d energy / d rot_chol in the concatenated layout [nchol][ktot]
   double* gtrial[2];
   double* grc;
+  // Cholesky-vector gradients (NULL: not requested): d energy / d chol [nchol][norb^2] (the
+  // vhs contraction), d energy / d mf_shifts [nchol] complex (field shifts) and
+  // d energy / d h0_prop (complex; from the weights, accumulated in scal[1])
+  double* gchol;
+  double2* gmf;
 };
 
 int a_launch_end(int nblk, const double* be, const double* bw, const AdjointBufs& a, cudaStream_t st);
@@ -52,5 +57,7 @@ int a_launch_taylor(const afq_ctx_dev& c, const AdjointBufs& a, int w0, int nwc,
                     const void* wu, const void* wd, cudaStream_t st);
 int a_launch_field(const afq_ctx_dev& c, const AdjointBufs& a, const double2* xt, cudaStream_t st);
 int a_launch_sr(const afq_ctx_dev& c, const AdjointBufs& a, const int32_t* idx, cudaStream_t st);
+// chol-bar[g][pq] += sqrt(dt) Re(i sum_w xt[w][g] conj(vhs-bar[w][pq])) over a walker chunk
+int a_launch_chol_grad(const afq_ctx_dev& c, const AdjointBufs& a, int nwc, const double2* xt, cudaStream_t st);
 
 }  // namespace afq

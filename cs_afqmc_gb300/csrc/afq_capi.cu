@@ -916,6 +916,13 @@ int afq_propagate_phaseless_vjp_ex(afq_ctx* ctx, afq_walker_state* state, void* 
   a.gtrial[1] = rot && d.nspin_g == 2 ? out->gtrial_dn : nullptr;
   a.grc = rot ? out->grot_chol : nullptr;
   double* const* gt = rot ? a.gtrial : nullptr;
+  const bool cg = out->gchol != nullptr;
+  if (cg && (!out->gmf_shifts || !out->gh0_prop)) {
+    afq_set_error("Cholesky-vector gradients need gchol, gmf_shifts and gh0_prop");
+    return -1;
+  }
+  a.gchol = cg ? out->gchol : nullptr;
+  a.gmf = cg ? reinterpret_cast<double2*>(out->gmf_shifts) : nullptr;
   cudaStream_t st = S(stream);
   double2* ovl = reinterpret_cast<double2*>(state->overlaps);
   const size_t step_elems = (size_t)d.nw * d.nchol;
@@ -965,6 +972,10 @@ int afq_propagate_phaseless_vjp_ex(afq_ctx* ctx, afq_walker_state* state, void* 
       CHECK(zero(a.gtrial[b], (size_t)d.norb * d.gocc[b] * sizeof(double), st));
     CHECK(zero(a.grc, (size_t)d.nchol * d.ktot * sizeof(double), st));
   }
+  if (cg) {
+    CHECK(zero(a.gchol, (size_t)d.nchol * d.norb * d.norb * sizeof(double), st));
+    CHECK(zero(a.gmf, (size_t)d.nchol * sizeof(double2), st));
+  }
   CHECK(afq::a_launch_end(blk, block_energy, block_weight, a, st));
   const int nwc = ctx->nw_chunk, nb = d.nw / nwc;
   const long nn = (long)d.norb * d.norb;
@@ -1007,6 +1018,7 @@ int afq_propagate_phaseless_vjp_ex(afq_ctx* ctx, afq_walker_state* state, void* 
         CHECK(afq::launch_gemm_cr(true, nwc, (int)nn, d.nchol, tp.xt(step) + (size_t)w0 * d.nchol, d.nchol,
                                   ctx->h.chol, nn, ctx->vhs, nn, c2(0.0, sq), st));
         CHECK(afq::a_launch_taylor(d, a, w0, nwc, ctx->vhs, tp.w(start, 0), tp.w(start, 1), st));
+        if (cg) CHECK(afq::a_launch_chol_grad(d, a, nwc, tp.xt(step) + (size_t)w0 * d.nchol, st));
         CHECK(afq::launch_gemm_cr(false, nwc, d.nchol, (int)nn, a.vbar, nn, ctx->h.chol, nn,
                                   a.xtb + (size_t)w0 * d.nchol, d.nchol, c2(0.0, -sq), st));
       }
@@ -1028,6 +1040,10 @@ int afq_propagate_phaseless_vjp_ex(afq_ctx* ctx, afq_walker_state* state, void* 
   if (rot)
     CHECK(afq::a_launch_green(d, tp.w(0, 0), tp.w(0, 1), gp ? a.gpend : nullptr, nullptr, a.lbar, a.wb[0], a.wb[1], st,
                               gt));
+  if (cg) {  // h0_prop-bar = (scal[1], 0): only its real part enters the weights
+    CHECK(zero(out->gh0_prop, 2 * sizeof(double), st));
+    CHECK(copy_d2d(out->gh0_prop, a.scal + 1, sizeof(double), st, "h0_prop cotangent"));
+  }
   return 0;
 }
 

@@ -53,12 +53,15 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
     [n_blocks, n_sr, n_ene, n_prop, nw, G]; zetas (optional): [n_blocks, n_sr + 1].
     Returns device tensors (block_energy, block_observable, block_weight), each
     [n_blocks], and prop_data; in reverse mode prop_data["block_rdm1s"] holds the
-    [n_blocks, 2, norb, norb] density matrices. orbital_rotation (the reference's
+    [n_blocks, 2, norb, norb] density matrices; ad_mode "2rdm" (the vjp of
+    sampler.propagate_phaseless_ad_1 with respect to the electron-repulsion tensor, small
+    systems) puts the [n_blocks, norb, norb, norb, norb] two-body density matrices into
+    prop_data["block_rdm2s"] and reports the trial's observable, as driver.py:230-245 does. orbital_rotation (the reference's
     options["orbital_rotation"], default True there): the jvp / vjp of
     sampler.propagate_phaseless_ad (_nosr), the trial re-optimised for h1 + lambda D in every
     block; wave_data needs "rdm1", as the driver sets it."""
-    if ad_mode not in ("forward", "reverse"):
-        raise ValueError(f"ad_mode must be 'forward' or 'reverse', got {ad_mode!r}")
+    if ad_mode not in ("forward", "reverse", "2rdm"):
+        raise ValueError(f"ad_mode must be 'forward', 'reverse' or '2rdm', got {ad_mode!r}")
     if observable is None:
         op, const = torch.as_tensor(ham_data["h1"]), 0.0
     else:
@@ -70,9 +73,14 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
     bo = torch.empty(n_blocks, dtype=torch.float64, device=device())
     bw = torch.empty(n_blocks, dtype=torch.float64, device=device())
     n_sr = sampler.n_sr_blocks if do_sr else 1
-    rdm1s = None
+    rdm1s = rdm2s = rdm2_op = None
     if ad_mode == "reverse":
         rdm1s = torch.empty((n_blocks, 2, trial.norb, trial.norb), dtype=torch.float64, device=device())
+    if ad_mode == "2rdm":  # the electron-repulsion tensor sum_g L_g (x) L_g (driver.py:44-52)
+        n = trial.norb
+        ch = torch.as_tensor(ham_data["chol"], dtype=torch.float64).to(device()).reshape(-1, n * n)
+        rdm2_op = (ch.T @ ch).reshape(n, n, n, n)
+        rdm2s = torch.empty((n_blocks, n, n, n, n), dtype=torch.float64, device=device())
     for n in range(n_blocks):
         f = None if fields is None else fields[n]
         z_local = None if (zetas is None or not do_sr) else zetas[n][:n_sr]
@@ -80,6 +88,11 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
             jvp = sampler.propagate_phaseless_ad_jvp if orbital_rotation else sampler.propagate_phaseless_ad_norot_jvp
             e, de, prop_data = jvp(ham, ham_data, op, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f,
                                    zetas=z_local)
+        elif ad_mode == "2rdm":  # driver.py:230-245: the observable is the trial's value
+            e, r2, prop_data = sampler.propagate_phaseless_ad_1_vjp(ham, ham_data, rdm2_op, prop, prop_data, trial,
+                                                                    wave_data, fields=f, zetas=z_local)
+            rdm2s[n].copy_(r2)
+            de = trial_observable.clone()
         else:
             vjp = sampler.propagate_phaseless_ad_vjp if orbital_rotation else sampler.propagate_phaseless_ad_norot_vjp
             e, r, prop_data = vjp(ham, ham_data, prop, prop_data, trial, wave_data, do_sr=do_sr, fields=f,
@@ -99,4 +112,6 @@ def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave
                   bw[n:].data_ptr(), stream_ptr())
     if rdm1s is not None:
         dict.__setitem__(prop_data, "block_rdm1s", rdm1s)
+    if rdm2s is not None:
+        dict.__setitem__(prop_data, "block_rdm2s", rdm2s)
     return be, bo, bw, prop_data

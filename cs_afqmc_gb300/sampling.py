@@ -60,6 +60,34 @@ def rotated_ham_data(ham, ham_data: dict, coupling: float, observable_op, prop, 
     return ham.build_propagation_intermediates(hd, prop, trial, wd), wd
 
 
+def two_body_ham_data(ham, ham_data: dict, op4, prop, trial, wave_data: dict):
+    """(ham_data, wave_data, parts) with the Cholesky vectors rebuilt from the two-body
+    operator op4 [norb]*4, symmetrised over (ij|kl) = (kl|ij) = (ji|lk) = (lk|ji), by the
+    modified Cholesky decomposition with as many vectors as ham_data["chol"], the trial
+    re-optimised and the intermediates rebuilt (sampling.py:198-224). parts holds the
+    tensors the block depends on (chol, exp_h1, mf, h0_prop), built with torch ops so that
+    autograd reaches op4 through them."""
+    from .linalg_utils import modified_cholesky
+    if "rdm1" not in wave_data:
+        raise _lib.AfqError("the two-body derivative needs wave_data['rdm1'] (the driver sets it to the trial's rdm1)")
+    norb = trial.norb
+    v = as_dev(op4).reshape(norb, norb, norb, norb)
+    v = (v + v.permute(2, 3, 0, 1) + v.permute(1, 0, 3, 2) + v.permute(3, 2, 1, 0)) / 4.0
+    nchol = int(as_dev(ham_data["chol"]).reshape(-1, norb * norb).shape[0])
+    chol = modified_cholesky(v.reshape(norb * norb, norb * norb), norb, nchol)
+    hd = {k: val for k, val in ham_data.items() if k not in (_CACHE_KEY, "rot_chol", "rot_h1", "exp_h1",
+                                                             "mf_shifts", "h0_prop")}
+    hd["chol"] = chol
+    wd = trial.optimize(hd, wave_data)
+    hd = ham.build_measurement_intermediates(hd, trial, wd)
+    hd = ham.build_propagation_intermediates(hd, prop, trial, wd)
+    mf, v0, v1 = prop._mf_v0_v1(hd, trial, wd)
+    exp_h1 = prop._exp_h1(as_dev(hd["h1"]), v0, v1)
+    h0 = float(_scalar(hd["h0"]))
+    parts = {"chol": chol, "exp_h1": exp_h1, "mf": mf, "h0_prop": -h0 - torch.sum(mf * mf) / 2.0}
+    return hd, wd, parts
+
+
 @dataclass
 class sampler:
     n_prop_steps: int = 50
@@ -341,8 +369,67 @@ class sampler:
             (rdm1,) = torch.autograd.grad(lin, D)
         return energy, rdm1.detach(), prop_data
 
+    def propagate_phaseless_ad_1(self, ham, ham_data: dict, coupling: float, observable_op, prop,
+                                 prop_data: PropData, trial, wave_data: dict,
+                                 fields: Optional[torch.Tensor] = None, zetas: Optional[torch.Tensor] = None):
+        """(energy, prop_data) of the block whose Cholesky vectors are rebuilt from the
+        two-body operator observable_op [norb]*4 (symmetrised over its four index
+        permutations, modified Cholesky with as many vectors as ham_data["chol"]), the
+        trial re-optimised (sampling.py:198-229). `coupling` is unused, as in the
+        reference."""
+        with torch.no_grad():
+            hd, wd, _ = two_body_ham_data(ham, ham_data, observable_op, prop, trial, wave_data)
+        return self.propagate_phaseless(ham, hd, prop, prop_data, trial, wd, fields, zetas)
+
+    def propagate_phaseless_ad_1_vjp(self, ham, ham_data: dict, observable_op, prop, prop_data: PropData, trial,
+                                     wave_data: dict, fields: Optional[torch.Tensor] = None,
+                                     zetas: Optional[torch.Tensor] = None):
+        """Reverse-mode derivative of propagate_phaseless_ad_1 with respect to the two-body
+        operator: what driver.py:230-234 takes with jax.vjp in ad_mode "2rdm" (the block's
+        two-body density matrix estimate when observable_op is the electron-repulsion
+        tensor). The device sweep returns the gradients with respect to exp_h1, rot_h1, the
+        trial, rot_chol, chol, the mean-field shifts and h0_prop; torch autograd carries them
+        back through the intermediates, trial.optimize and the modified Cholesky
+        decomposition. Returns (energy, rdm2 [norb]*4, prop_data). FP64 walkers only; the
+        host part holds norb^4-sized tensors and a graph of the decomposition (small
+        systems)."""
+        op = as_dev(observable_op).detach().clone().requires_grad_(True)
+        with torch.enable_grad():
+            hd, wd, parts = two_body_ham_data(ham, ham_data, op, prop, trial, wave_data)
+            plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in hd.items()}
+            plain["rot_chol"] = [x.detach() for x in hd["rot_chol"]] if isinstance(hd["rot_chol"], list) \
+                else hd["rot_chol"].detach()
+            plain["rot_h1"] = [x.detach() for x in hd["rot_h1"]] if isinstance(hd["rot_h1"], list) \
+                else hd["rot_h1"].detach()
+            wplain = dict(wd)
+            wplain["mo_coeff"] = [x.detach() for x in wd["mo_coeff"]] if isinstance(wd["mo_coeff"], list) \
+                else wd["mo_coeff"].detach()
+            energy, g, prop_data = self._vjp_call(prop, prop_data, trial, plain, wplain, True, fields, zetas,
+                                                  rotation=True, chol_grads=True)
+            gexp, grot, gtrial, grc, gchol, gmf, gh0p = g
+            uhf_trial = isinstance(wd["mo_coeff"], (list, tuple))
+            norb = trial.norb
+            nchol = int(parts["chol"].shape[0])
+            exp_h1 = parts["exp_h1"]
+            lin = torch.sum((gexp if exp_h1.dim() == 3 else gexp[0]) * exp_h1)
+            lin = lin + torch.sum(gchol * parts["chol"])
+            mf, h0p = parts["mf"], parts["h0_prop"]
+            lin = lin + torch.sum(gmf.real * mf.real + gmf.imag * mf.imag)
+            lin = lin + gh0p.real * h0p.real + gh0p.imag * h0p.imag
+            if uhf_trial:
+                n_up = trial.nelec[0]
+                rc = grc.reshape(nchol, -1)
+                for s_, (o0, o1) in enumerate(((0, n_up * norb), (n_up * norb, rc.shape[1]))):
+                    lin = lin + torch.sum(rc[:, o0:o1].reshape(hd["rot_chol"][s_].shape) * hd["rot_chol"][s_])
+                    lin = lin + torch.sum(grot[s_] * hd["rot_h1"][s_]) + torch.sum(gtrial[s_] * wd["mo_coeff"][s_])
+            else:
+                lin = lin + torch.sum(grc.reshape(hd["rot_chol"].shape) * hd["rot_chol"])
+                lin = lin + torch.sum(grot[0] * hd["rot_h1"]) + torch.sum(gtrial[0] * wd["mo_coeff"])
+            (rdm2,) = torch.autograd.grad(lin, op)
+        return energy, rdm2.detach(), prop_data
+
     def _vjp_call(self, prop, prop_data: PropData, trial, ham_data: dict, wave_data: dict, do_sr: bool, fields,
-                  zetas, rotation: bool):
+                  zetas, rotation: bool, chol_grads: bool = False):
         """afq_propagate_phaseless_vjp_ex on the engine of (trial, ham_data, wave_data).
         Returns (energy 0-d, (gexp [2, norb, norb], grot [up, dn or None], gtrial, grot_chol),
         prop_data); gtrial / grot_chol only with rotation."""
@@ -372,6 +459,12 @@ class sampler:
         occ = (n_up, n_dn) if uhf_trial else (n_up,)
         grot = [torch.empty((o, norb), dtype=torch.float64, device=dev) for o in occ] + ([] if uhf_trial else [None])
         gtrial, grc = [None, None], None
+        gchol = gmf = gh0p = None
+        if chol_grads:
+            nch = int(ham_data["chol"].shape[0])
+            gchol = torch.empty((nch, norb * norb), dtype=torch.float64, device=dev)
+            gmf = torch.empty(nch, dtype=torch.complex128, device=dev)
+            gh0p = torch.empty(1, dtype=torch.complex128, device=dev)
         if rotation:
             gtrial = [torch.empty((norb, o), dtype=torch.float64, device=dev) for o in occ] + \
                 ([] if uhf_trial else [None])
@@ -381,7 +474,8 @@ class sampler:
             return None if x is None else x.data_ptr()
 
         outs = _lib.VjpOutputs(gexp[0].data_ptr(), None if prop.restricted else gexp[1].data_ptr(), ptr(grot[0]),
-                               ptr(grot[1]), ptr(gtrial[0]), ptr(gtrial[1]), ptr(grc))
+                               ptr(grot[1]), ptr(gtrial[0]), ptr(gtrial[1]), ptr(grc), ptr(gchol), ptr(gmf),
+                               ptr(gh0p))
         st = prop_data.state(eng)
         _lib.call("afq_propagate_phaseless_vjp_ex", eng.ctx, ctypes.byref(st), vptr, nbytes, f.data_ptr(),
                   None if z is None else z.data_ptr(), self.n_prop_steps, self.n_ene_blocks, n_sr,
@@ -389,6 +483,8 @@ class sampler:
                   ctypes.byref(outs), stream_ptr())
         dict.__setitem__(prop_data, "block_energies", be)
         dict.__setitem__(prop_data, "block_weights", bw)
+        if chol_grads:
+            return energy[0], (gexp, grot, gtrial, grc, gchol, gmf, gh0p[0]), prop_data
         return energy[0], (gexp, grot, gtrial, grc), prop_data
 
     def __hash__(self) -> int:

@@ -375,6 +375,13 @@ typedef struct afq_vjp_outputs {
   double* gtrial_up;
   double* gtrial_dn;
   double* grot_chol;
+  /* Cholesky-vector gradients, all three or none (the 2-RDM variant,
+   * sampler.propagate_phaseless_ad_1, sampling.py:198-229, rebuilds chol from a two-body
+   * operator): d energy / d chol [nchol][norb^2] through the vhs contraction, d energy /
+   * d mf_shifts [nchol] complex and d energy / d h0_prop (one complex). */
+  double* gchol;
+  double* gmf_shifts;
+  double* gh0_prop;
 } afq_vjp_outputs;
 
 /* afq_propagate_phaseless_vjp with the outputs in a struct (the trial and rot_chol
