@@ -173,3 +173,27 @@ def test_vjp_chunked_vhs():
                                                       b.wave_data, fields=fields, zetas=zetas)
     assert rel_err(eb.item(), ea.item()) < 1e-12
     assert rel_err(to_np(rb), to_np(ra)) < 1e-10
+
+
+@pytest.mark.parametrize("rotation", [False, True], ids=["fixed", "rotated"])
+def test_autograd_function(rotation):
+    """cs_afqmc_gb300.autograd.phaseless_energy: torch.autograd.grad of the block energy with
+    respect to h1 is the adjoint sweep's rdm1; its contraction with a direction equals the
+    forward-mode derivative (relative 1e-8)."""
+    import torch
+    from cs_afqmc_gb300 import autograd, sampling
+    case = Case(kind="uhf", restricted=False, norb=11, nelec=(4, 2), nchol=23, nw=6)
+    fields, zetas = _draws(case, N_SR, seed=57)
+    samp = sampling.sampler(n_prop_steps=N_PROP, n_ene_blocks=N_ENE, n_sr_blocks=N_SR)
+    h1 = torch.as_tensor(np.asarray(case.ham_data["h1"].cpu()), dtype=torch.float64, device="cuda")
+    h1 = h1.clone().requires_grad_(True)
+    e = autograd.phaseless_energy(h1, samp, case.ham, case.ham_data, case.prop, case.gpu_prop_data(), case.trial,
+                                  case.wave_data, fields=fields, zetas=zetas, orbital_rotation=rotation)
+    (g,) = torch.autograd.grad(2.0 * e, h1)
+    D = np.random.default_rng(59).standard_normal((2, case.norb, case.norb)) * 0.1
+    jvp = samp.propagate_phaseless_ad_jvp if rotation else samp.propagate_phaseless_ad_norot_jvp
+    e_j, de, _ = jvp(case.ham, case.ham_data, D, case.prop, case.gpu_prop_data(), case.trial, case.wave_data,
+                     fields=fields, zetas=zetas)
+    assert rel_err(e.item(), e_j.item()) < 1e-10
+    got = float(np.sum(to_np(g) * D)) / 2.0
+    assert abs(got - de.item()) < 1e-8 * max(abs(de.item()), 1e-3), (got, de.item())
