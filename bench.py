@@ -368,6 +368,7 @@ def run_ours(args, rank, world, local):
     import torch
 
     from cs_afqmc_gb300 import _lib
+    from cs_afqmc_gb300 import replicas
     from cs_afqmc_gb300._engine import stream_ptr
 
     torch.cuda.set_device(local)
@@ -440,10 +441,7 @@ def run_ours(args, rank, world, local):
     ms = t0.elapsed_time(t1)
     prof = _lib.profile_read_all()
     lib.afq_profile_enable(0)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = t.item()
+    ms = replicas.max_over_ranks(ms)  # the job's time is the slowest rank's
     ms_per_step = ms / args.steps
     value = world * ws_per_step * args.steps / (ms / 1e3)
     launches = sum(v[1] for v in prof.values())
@@ -477,10 +475,7 @@ def run_ours(args, rank, world, local):
     t1.record()
     torch.cuda.synchronize()
     ms_e2e = t0.elapsed_time(t1)
-    if dist:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = t.item()
+    ms_e2e = replicas.max_over_ranks(ms_e2e)
     e2e = {"value": world * ws_per_step * args.steps / (ms_e2e / 1e3), "unit": UNIT,
            "h2d_bytes_per_step": int(host_fields[0].numel() * 8 + host_z.numel() * 8),
            "d2h_bytes_per_step": int(out_host[0].numel() * 8)}
