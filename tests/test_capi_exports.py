@@ -55,3 +55,29 @@ def test_workspace_size_and_validation_without_gpu():
     assert b"RHF" in lib.afq_last_error()
     d.n_dn, d.n_batch = 20, 3  # must divide n_walkers
     assert lib.afq_workspace_size(ctypes.byref(d)) == 0
+
+
+def test_derivative_and_cpmc_entry_validation_without_gpu():
+    """The derivative and CPMC entry points refuse NULL or inconsistent arguments before
+    any device work: -1 and a message."""
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    import ctypes
+    lib = _lib.load()
+    d = _lib.Dims(norb=12, n_up=3, n_dn=3, nchol=20, n_walkers=8, walker_type=0, trial_type=0, precision=0,
+                  n_exp_terms=6, n_batch=1, dt=0.005)
+    big = lib.afq_vjp_workspace_size(ctypes.byref(d), 5, 4, 2)
+    small = lib.afq_vjp_workspace_size(ctypes.byref(d), 5, 4, 1)
+    assert big > small > 0  # the recorded sweep grows with the block count
+    assert lib.afq_vjp_workspace_size(ctypes.byref(d), 0, 4, 1) == 0
+    assert lib.afq_tangent_workspace_size(ctypes.byref(d)) > 0
+    outs = _lib.VjpOutputs()
+    assert lib.afq_propagate_phaseless_vjp_ex(None, None, None, 0, None, None, 1, 1, 1, 0, None, None, None,
+                                              ctypes.byref(outs), None) == -1
+    assert b"NULL" in lib.afq_last_error()
+    tin = _lib.JvpInputs()
+    assert lib.afq_propagate_phaseless_jvp_ex(None, None, ctypes.byref(tin), None, 0, None, None, 1, 1, 1, 0,
+                                              None, None, None, None, None, None, None) == -1
+    assert lib.afq_cpmc_nn_propagate(8, 3, 3, 4, 0.01, 4.0, 1.0, None, 2, None, None, None, None, None, None,
+                                     None, None, None, None, None, None) == -1
+    assert b"NULL" in lib.afq_last_error()
