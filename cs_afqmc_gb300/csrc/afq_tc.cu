@@ -564,19 +564,53 @@ __global__ void __launch_bounds__(256) k_taylor_diag(const TaylorDiag td) {
   __syncthreads();
   const int o = td.o[s];
   const size_t tb = (size_t)w * td.NT[s] * 2 * td.nq, ab = (size_t)w * td.R[s] * td.nk;
-  for (int e = tid; e < n * o; e += blockDim.x) {
-    const int k = e / n, p = e % n;
-    const size_t ir = tb + (size_t)(2 * k) * 2 * td.nq + p, ii = ir + 2 * td.nq;
-    const float tr = h2f(td.t0_hi[s][ir], bf) + h2f(td.t0_lo[s][ir], bf);
-    const float ti = h2f(td.t0_hi[s][ii], bf) + h2f(td.t0_lo[s][ii], bf);
-    const float2 c = poly[p];
-    uint16_t h, l;
-    split16(c.x * tr - c.y * ti, bf, h, l);
-    td.acc_hi[s][ab + (size_t)(2 * k) * td.nk + p] = h;
-    td.acc_lo[s][ab + (size_t)(2 * k) * td.nk + p] = l;
-    split16(c.x * ti + c.y * tr, bf, h, l);
-    td.acc_hi[s][ab + (size_t)(2 * k + 1) * td.nk + p] = h;
-    td.acc_lo[s][ab + (size_t)(2 * k + 1) * td.nk + p] = l;
+  // four orbitals per thread: 8-byte loads and stores (rows start on 8-byte boundaries: the
+  // row pitches 2 nq and nk are multiples of 4 elements); a partial last group goes one by one
+  const int ng = (n + 3) / 4;
+  for (int e = tid; e < o * ng; e += blockDim.x) {
+    const int k = e / ng, p0 = (e - k * ng) * 4;
+    const size_t ir = tb + (size_t)(2 * k) * 2 * td.nq + p0, ii = ir + 2 * td.nq;
+    const size_t ar = ab + (size_t)(2 * k) * td.nk + p0, ai = ar + td.nk;
+    if (p0 + 4 <= n) {
+      const uint2 vhr = *reinterpret_cast<const uint2*>(td.t0_hi[s] + ir);
+      const uint2 vlr = *reinterpret_cast<const uint2*>(td.t0_lo[s] + ir);
+      const uint2 vhi = *reinterpret_cast<const uint2*>(td.t0_hi[s] + ii);
+      const uint2 vli = *reinterpret_cast<const uint2*>(td.t0_lo[s] + ii);
+      uint32_t ohr[2] = {0, 0}, olr[2] = {0, 0}, ohi[2] = {0, 0}, oli[2] = {0, 0};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int sh = 16 * (j & 1);
+        const uint32_t whr = j < 2 ? vhr.x : vhr.y, wlr = j < 2 ? vlr.x : vlr.y;
+        const uint32_t whi = j < 2 ? vhi.x : vhi.y, wli = j < 2 ? vli.x : vli.y;
+        const float tr = h2f((uint16_t)(whr >> sh), bf) + h2f((uint16_t)(wlr >> sh), bf);
+        const float ti = h2f((uint16_t)(whi >> sh), bf) + h2f((uint16_t)(wli >> sh), bf);
+        const float2 c = poly[p0 + j];
+        uint16_t h, l;
+        split16(c.x * tr - c.y * ti, bf, h, l);
+        ohr[j >> 1] |= (uint32_t)h << sh;
+        olr[j >> 1] |= (uint32_t)l << sh;
+        split16(c.x * ti + c.y * tr, bf, h, l);
+        ohi[j >> 1] |= (uint32_t)h << sh;
+        oli[j >> 1] |= (uint32_t)l << sh;
+      }
+      *reinterpret_cast<uint2*>(td.acc_hi[s] + ar) = make_uint2(ohr[0], ohr[1]);
+      *reinterpret_cast<uint2*>(td.acc_lo[s] + ar) = make_uint2(olr[0], olr[1]);
+      *reinterpret_cast<uint2*>(td.acc_hi[s] + ai) = make_uint2(ohi[0], ohi[1]);
+      *reinterpret_cast<uint2*>(td.acc_lo[s] + ai) = make_uint2(oli[0], oli[1]);
+    } else {
+      for (int j = 0; j < n - p0; ++j) {
+        const float tr = h2f(td.t0_hi[s][ir + j], bf) + h2f(td.t0_lo[s][ir + j], bf);
+        const float ti = h2f(td.t0_hi[s][ii + j], bf) + h2f(td.t0_lo[s][ii + j], bf);
+        const float2 c = poly[p0 + j];
+        uint16_t h, l;
+        split16(c.x * tr - c.y * ti, bf, h, l);
+        td.acc_hi[s][ar + j] = h;
+        td.acc_lo[s][ar + j] = l;
+        split16(c.x * ti + c.y * tr, bf, h, l);
+        td.acc_hi[s][ai + j] = h;
+        td.acc_lo[s][ai + j] = l;
+      }
+    }
   }
 }
 
