@@ -65,3 +65,18 @@ def test_cpmc_nn_without_pairs_is_onsite_cpmc():
     assert abs(pa - pb) < 1e-12
     assert np.allclose(a["weights"], b["weights"], rtol=1e-13, atol=0)
     assert np.allclose(a["greens"], b["greens"], rtol=1e-12, atol=1e-14)
+
+
+def test_cpmc_nn_zero_coupling_is_onsite_step():
+    """u_1 = 0: the neighbour constants are all 1, every neighbour ratio is 1 and the weights
+    are unchanged, so the step equals the on-site one on the same on-site uniforms."""
+    n, mo, w0, exp_h1, nbr, rng = _lattice()
+    nw = w0[0].shape[0]
+    g = rng.standard_normal((nw, n))
+    uni = np.concatenate([(scipy.special.erf(g / 2 ** 0.5) + 1) / 2, rng.uniform(size=(nw, 4 * len(nbr)))], axis=1)
+    a, pa = O.cpmc_nn_propagate(exp_h1, 0.01, 4.0, 0.0, nbr, O.cpmc_init(w0, mo), uni, mo, -5.0, -5.0, nw)
+    b, pb = O.cpmc_propagate(exp_h1, 0.01, 4.0, O.cpmc_init(w0, mo), g, mo, -5.0, -5.0, nw)
+    assert abs(pa - pb) < 1e-12
+    assert np.allclose(a["weights"], b["weights"], rtol=1e-13, atol=0)
+    for s in range(2):
+        assert np.allclose(a["walkers"][s], b["walkers"][s], rtol=1e-13, atol=0)
