@@ -12,9 +12,11 @@ and copied from pinned host memory every step for `e2e`.
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
        [--precision mixed|fp64] [--workload NAME] [--no-cpu-baseline]
        [--energy-blocks B] [--energy-only [--energy-control | --energy-sync]]
-`energy_check` in the line: B driver blocks of the mixed path and of the FP64 GPU path
-from the same walkers and the same Philox draws, blocked energies compared (the accuracy
-half of the metric) and both paths' walker-steps/s on that work.
+`energy_check` in the line (default B = 50): B driver blocks in which the mixed path and the
+FP64 GPU path each propagate the block from the FP64 run's state on the same Philox draws;
+the blocked energies are compared (the accuracy half of the metric, bar 0.1 mHa) and both
+paths' walker-steps/s on that work are reported. `--energy-only` runs only that comparison
+(`--energy-sync` for this synchronized form, else free-running trajectories).
 Under torchrun (N > 1) every rank runs an independent replica with its own seed (walkers
 only couple through block-end reductions, which a replica does not need); value = total
 walker-steps of all ranks / max time over ranks.
@@ -52,7 +54,7 @@ def parse():
     ap.add_argument("--mixed-config", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-procs", type=int, default=0)
-    ap.add_argument("--energy-blocks", type=int, default=4,
+    ap.add_argument("--energy-blocks", type=int, default=50,
                     help="driver blocks of the mixed-vs-FP64 energy comparison (0: skip)")
     ap.add_argument("--energy-only", action="store_true",
                     help="run only the mixed-vs-FP64 energy comparison and print its line")
@@ -323,7 +325,8 @@ def energy_check_sync(args, n_blocks: int, seed: int = 4242) -> dict:
     ham_f, trial_f, wave_f, hd_f, prop_f, pd_f = wf[2], wf[3], wf[4], wf[5], wf[6], wf[7]
     em, ef, bw = [], [], []
     wsum = torch.zeros(1, dtype=torch.float64, device="cuda")
-    for _ in range(n_blocks):
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(n_blocks)]
+    for ib in range(n_blocks):
         if isinstance(pd_f["walkers"], list):
             for a, b in zip(pd_m["walkers"], pd_f["walkers"]):
                 a.copy_(b.to(a.dtype))
@@ -332,8 +335,11 @@ def energy_check_sync(args, n_blocks: int, seed: int = 4242) -> dict:
         pd_m["weights"].copy_(pd_f["weights"])
         dict.__getitem__(pd_m, "_scalars").copy_(dict.__getitem__(pd_f, "_scalars"))
         pd_m["key"].offset = pd_f["key"].offset
+        ev[ib][0].record()
         e_m, pd_m = samp.propagate_phaseless(ham_m, hd_m, prop_m, pd_m, trial_m, wave_m)
+        ev[ib][1].record()
         e_f, pd_f = samp.propagate_phaseless(ham_f, hd_f, prop_f, pd_f, trial_f, wave_f)
+        ev[ib][2].record()
         zg = samp.draw_zetas(pd_f, 1)
         eng = pd_f["_engine"]
         st = pd_f.state(eng)
@@ -343,11 +349,19 @@ def energy_check_sync(args, n_blocks: int, seed: int = 4242) -> dict:
         em.append(e_m.item())
         ef.append(e_hold.item())
         bw.append(wsum.item())
+    torch.cuda.synchronize()
+    # block 0 includes both contexts' set-up: the rates are over blocks 1..n-1
+    sec_m = sum(e[0].elapsed_time(e[1]) for e in ev[1:]) / 1e3
+    sec_f = sum(e[1].elapsed_time(e[2]) for e in ev[1:]) / 1e3
+    ws = (n_blocks - 1) * N_PROP * N_ENE * N_SR * wm[0]["n_walkers"]
+    vm = ws / sec_m if sec_m > 0 else None
+    vf = ws / sec_f if sec_f > 0 else None
     em, ef, bw = np.array(em), np.array(ef), np.array(bw)
     d = em - ef
     nb = len(d)
     blocked = float(np.sum(bw * d) / np.sum(bw))
     return {
+        "mode": "synchronized",
         "blocks": nb,
         "blocked_energy_fp64": float(np.sum(bw * ef) / np.sum(bw)),
         "blocked_diff_mha": 1e3 * blocked,
@@ -358,7 +372,23 @@ def energy_check_sync(args, n_blocks: int, seed: int = 4242) -> dict:
         "fp64_block_energy_stderr_mha": 1e3 * float(np.std(ef, ddof=1) / np.sqrt(nb)) if nb > 1 else None,
         "within_0p1_mha": bool(abs(blocked) < 1e-4),
         "draws": "every block from the FP64 run's state, identical fields and SR uniforms",
+        "mixed_walker_steps_per_s": vm, "fp64_walker_steps_per_s": vf,
+        "mixed_over_fp64": (vm / vf) if vm and vf else None,
+        "rates": "propagate_phaseless of blocks 1.. (20 steps, 4 QR + energy points each), CUDA events",
     }
+
+
+def bench_config(w: dict, args, world: int) -> dict:
+    """The workload description both arms print (the reference arm times the same workload)."""
+    nw, G = w["n_walkers"], w["nchol"]
+    ws_bytes = nw * G * 8 * N_PROP * N_ENE
+    return {"workload": args.workload, "norb": w["norb"], "nelec": list(w["nelec"]), "nchol": G,
+            "n_walkers": nw, "dt": w["dt"],
+            "step": (f"1 driver block = {N_PROP}x{N_ENE}x{N_SR} propagation steps, QR + energy every "
+                     f"{N_PROP}, local SR, block end"),
+            "walker_steps_per_step": N_PROP * N_ENE * N_SR * nw,
+            "l2": f"inputs larger than L2: fields alone are {ws_bytes / 1e6:.0f} MB per step (> 129 MB L2)",
+            "replicas": "independent replicas per GPU" if world > 1 else "single GPU"}
 
 
 def run_ours(args, rank, world, local):
@@ -424,11 +454,13 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
 
     # ---- timed region: device-resident inputs (fields drawn on the device) ----
+    # per-launch event timing is off here (it records an event pair around every launch);
+    # the launch counter still counts every kernel launch of the library
     clk = ClockSampler(local)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    lib.afq_profile_enable(1)
+    lib.afq_profile_enable(0)  # resets the counters, timing off
     clk.start()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -439,13 +471,21 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     clocks = clk.stop()
     ms = t0.elapsed_time(t1)
-    prof = _lib.profile_read_all()
-    lib.afq_profile_enable(0)
+    launches = sum(v[1] for v in _lib.profile_read_all().values())
     ms = replicas.max_over_ranks(ms)  # the job's time is the slowest rank's
     ms_per_step = ms / args.steps
     value = world * ws_per_step * args.steps / (ms / 1e3)
-    launches = sum(v[1] for v in prof.values())
     block_energy = e_buf.item()
+
+    # ---- per-kernel device time: a second pass of the same steps with an event pair
+    # recorded around every launch on its own stream (shares and the roofline's kernel time)
+    torch.cuda.synchronize()
+    lib.afq_profile_enable(1)
+    for _ in range(args.steps):
+        step_dev()
+    torch.cuda.synchronize()
+    prof = _lib.profile_read_all()
+    lib.afq_profile_enable(0)
 
     # ---- e2e: host fields (pinned) copied in every step, block energy copied out ----
     fshape = (N_SR, N_ENE, N_PROP, nw, G)
@@ -533,9 +573,8 @@ def run_ours(args, rank, world, local):
             cpu_pool.close()
 
     # ---- accuracy at this workload: mixed vs FP64 GPU path on identical draws ----
-    ec = energy_check(args, args.energy_blocks) if args.energy_blocks > 1 and world == 1 else None
+    ec = energy_check_sync(args, args.energy_blocks) if args.energy_blocks > 1 and world == 1 else None
 
-    ws_bytes = nw * G * 8 * N_PROP * N_ENE + nw * w["norb"] * w["nelec"][0] * (8 if args.precision == "mixed" else 16)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
@@ -543,15 +582,13 @@ def run_ours(args, rank, world, local):
         "dtype": ("fp16 tensor-core contractions with hi/lo split, fp32 walkers and small "
                   "linear algebra, fp64 log-determinants/weights/sums") if args.precision == "mixed" else "fp64",
         "data": "synthetic",
-        "config": {"workload": args.workload, "norb": w["norb"], "nelec": list(w["nelec"]),
-                   "nchol": G, "n_walkers": nw, "dt": w["dt"], "precision": args.precision,
-                   "step": f"1 driver block = {N_PROP}x{N_ENE}x{N_SR} propagation steps, QR + energy every {N_PROP}, local SR, block end",
-                   "walker_steps_per_step": ws_per_step, "n_batch": args.n_batch,
-                   "l2": f"inputs larger than L2: fields alone are {ws_bytes/1e6:.0f} MB per step (> 129 MB L2)",
-                   "replicas": "independent replicas per GPU" if world > 1 else "single GPU",
-                   "last_block_energy": block_energy},
+        "config": bench_config(w, args, world),
+        "precision": args.precision, "last_block_energy": block_energy,
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-        "clocks": clocks, "kernels": kernels, "energy_check": ec,
+        "clocks": clocks, "kernels": kernels,
+        "kernels_timing": ("second pass of the same steps with a CUDA-event pair around every launch on "
+                           "its stream (value above is timed without them)"),
+        "energy_check": ec,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -571,7 +608,9 @@ def run_reference(args, rank, world, local):
 
     w = dict(synthetic.WORKLOADS[args.workload])
     procs = args.cpu_procs or (os.cpu_count() or 1)
-    nw_per = max(1, min(16, w["n_walkers"] // procs))
+    # all of the workload's walkers, split evenly over the processes (the reference's CPU layout:
+    # one process per core, walkers divided between ranks)
+    nw_per = -(-w["n_walkers"] // procs)
     pool = CpuPool(procs, w["norb"], w["nelec"][0], w["nchol"], nw_per, w["dt"], kind=w["kind"])
     n_steps, n_meas = 5, 1
     try:
@@ -585,16 +624,17 @@ def run_reference(args, rank, world, local):
     finally:
         pool.close()
     value = tot_ws / tot_s
-    sample = (f"{args.workload}: per step {procs} processes x {nw_per} walkers x {n_steps} "
-              f"propagation steps + {n_meas} QR/energy, FP64 NumPy restatement of the reference "
-              f"(JAX not installed), 1 BLAS thread per process")
+    sample = (f"{args.workload}: per step {procs} processes x {nw_per} walkers (= {procs * nw_per}, the "
+              f"workload's {w['n_walkers']} rounded up to whole processes) x {n_steps} propagation steps "
+              f"+ {n_meas} QR/energy, FP64 NumPy restatement of the reference (JAX not installed), "
+              f"1 BLAS thread per process")
     line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * tot_s / args.steps, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": args.workload, "norb": w["norb"], "nelec": list(w["nelec"]),
-                       "nchol": w["nchol"], "n_walkers": w["n_walkers"], "dt": w["dt"]},
+            "config": bench_config(w, args, world),
+            "timed_walkers": procs * nw_per,
             "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": procs, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,

@@ -58,15 +58,10 @@ struct SplitArgs {
 // kWarpStore provides store_warp(params, row0, lane, col0, v, ks, stage) instead, called by
 // all 32 lanes of the warp (rows row0 + lane) with a kSplitStageWarp-byte shared-memory
 // buffer of its own.
-// CL = 2: clusters of two CTAs take M tiles 2i and 2i + 1 of the same (N tile, K range); each
-// CTA loads its own A tile and one 128-row half of the B tile, multicast to both, so every
-// CTA reads half of B from L2. A stage is refilled once both CTAs' MMAs have consumed it
-// (each MMA warp's commit arrives on the empty barrier of both). Requires m_tiles % CL == 0.
-template <class Epi, int CL>
+template <class Epi>
 __global__ void __launch_bounds__(kSplitThreads, 1)
     k_gemm_split(const __grid_constant__ SplitMaps maps, const SplitArgs g,
                  const __grid_constant__ typename Epi::Params ep, int* status) {
-  static_assert(CL == 1 || CL == 2, "cluster size");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -78,9 +73,8 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rank = CL == 2 ? (int)ptx::cluster_ctarank() : 0;
-  const int cid = blockIdx.x / CL, ncl = gridDim.x / CL;  // cluster index and count
-  const int mt = g.m_tiles / CL;                           // M tile groups
+  const int cid = blockIdx.x, ncl = gridDim.x;
+  const int mt = g.m_tiles;
   const int ntiles = mt * g.n_tiles * g.k_splits;
   const int kps = (g.k_tiles + g.k_splits - 1) / g.k_splits;  // K tiles per split
   const uint32_t tx_bytes = kSplitA * (g.has_alo ? 2 : 1) + kSplitB * (g.has_blo ? 2 : 1);
@@ -88,7 +82,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSplitStages; ++s) {
       ptx::mbar_init(&full[s], 1);
-      ptx::mbar_init(&empty[s], CL);
+      ptx::mbar_init(&empty[s], 1);
     }
     for (int a = 0; a < 2; ++a) {
       ptx::mbar_init(&accfull[a], 1);
@@ -102,10 +96,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     ptx::tmem_relinquish();
   }
   ptx::tc_fence_before();
-  if constexpr (CL == 2)
-    ptx::cluster_sync();  // barrier inits visible to the partner before its multicasts
-  else
-    __syncthreads();
+  __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
   bool ok = true;
@@ -118,7 +109,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       if (g.has_blo) ptx::prefetch_tmap(&maps.b_lo);
       int it = 0;
       for (int tile = cid; tile < ntiles && ok; tile += ncl) {
-        const int m0 = ((tile % mt) * CL + rank) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
+        const int m0 = (tile % mt) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
         const int ks = tile / (mt * g.n_tiles);
         const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
         for (int kt = ka; kt < kb; ++kt, ++it) {
@@ -131,20 +122,12 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
           ptx::mbar_expect_tx(&full[s], tx_bytes);
           ptx::tma_load_2d(u, &maps.a_hi, &full[s], kt * 64, g.a_row0 + m0);
           if (g.has_alo) ptx::tma_load_2d(u + kSplitA, &maps.a_lo, &full[s], kt * 64, g.a_row0 + m0);
-          if constexpr (CL == 2) {  // this CTA's half of B, to both CTAs
-            const int hb = rank * kSplitBBox * 128;
-            ptx::tma_load_2d_mc(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, n0 + rank * kSplitBBox, 3);
-            if (g.has_blo)
-              ptx::tma_load_2d_mc(u + 2 * kSplitA + kSplitB + hb, &maps.b_lo, &full[s], kt * 64,
-                                  n0 + rank * kSplitBBox, 3);
-          } else {
 #pragma unroll
-            for (int hh = 0; hh < 2; ++hh) {
-              const int hb = hh * kSplitBBox * 128;
-              ptx::tma_load_2d(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, n0 + hh * kSplitBBox);
-              if (g.has_blo)
-                ptx::tma_load_2d(u + 2 * kSplitA + kSplitB + hb, &maps.b_lo, &full[s], kt * 64, n0 + hh * kSplitBBox);
-            }
+          for (int hh = 0; hh < 2; ++hh) {
+            const int hb = hh * kSplitBBox * 128;
+            ptx::tma_load_2d(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, n0 + hh * kSplitBBox);
+            if (g.has_blo)
+              ptx::tma_load_2d(u + 2 * kSplitA + kSplitB + hb, &maps.b_lo, &full[s], kt * 64, n0 + hh * kSplitBBox);
           }
         }
       }
@@ -201,10 +184,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
                            g.idesc, first ? 0u : 1u);
               first = false;
             }
-            if constexpr (CL == 2)
-              ptx::mma_commit_mc(&empty[s], 3);  // the stage is free here and in the partner
-            else
-              ptx::mma_commit(&empty[s]);
+            ptx::mma_commit(&empty[s]);
           }
           ptx::mma_commit(&accfull[a]);
         }
@@ -218,7 +198,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     int grun = 0;
     for (int tile = cid; tile < ntiles && ok; tile += ncl) {
-      const int m0 = ((tile % mt) * CL + rank) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
+      const int m0 = (tile % mt) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
       const int ks = tile / (mt * g.n_tiles);
       const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
       const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
@@ -257,12 +237,7 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   }
   if (!ok) atomicOr(status, 4);
   ptx::tc_fence_before();
-  // with CL == 2 neither CTA leaves while the partner may still multicast into its shared
-  // memory or arrive on its barriers
-  if constexpr (CL == 2)
-    ptx::cluster_sync();
-  else
-    __syncthreads();
+  __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
     ptx::tmem_dealloc(tmem, 512);

@@ -23,6 +23,13 @@ struct afq_ctx_dev {
 };
 
 namespace afq {
+// dynamic shared memory of the FP64 Green's-function / overlap kernel (k_green_overlap)
+inline size_t green_f64_smem(int norb, int kmax) {
+  return (size_t)norb * kmax * 16 + (size_t)kmax * 2 * kmax * 16 + (size_t)norb * kmax * 8;
+}
+// 0 when `smem` bytes fit the current device's opt-in shared-memory limit; otherwise the
+// error text names `what` and the limit, and the return is -2
+int check_smem_optin(size_t smem, const char* what);
 template <typename WT>
 int launch_green(const afq_ctx_dev& c, const void* wu, const void* wd, double2* green,
                  double2* ovl, bool write_green, cudaStream_t st);

@@ -11,6 +11,8 @@
 
 #include <mutex>
 
+#include <cuda.h>
+
 #include "afq_common.cuh"
 #include "afq_kernels.cuh"
 
@@ -23,10 +25,32 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// per device: the scratch address and the CUDA context it was looked up in
 void* g_scratch_addr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once per device
-// (host code cannot use the array's name as a device pointer).
+typedef CUresult (*PFN_ctxGetCurrent)(CUcontext*);
+
+// The driver's current context (its handle changes when the primary context is torn down
+// and created again, e.g. after cudaDeviceReset, which also reloads this module's array).
+CUcontext current_context() {
+  static PFN_ctxGetCurrent fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_ctxGetCurrent>(p);
+    cudaGetLastError();
+  }
+  CUcontext ctx = nullptr;
+  if (fn && fn(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+  return ctx;
+}
+
+// Device address of the scratch array on the current device. Host code cannot use the
+// array's name as a device pointer; the address is looked up with cudaGetSymbolAddress the
+// first time a device (and context) is seen, with that device current, and cached.
 int scratch_on_current_device(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -39,7 +63,8 @@ int scratch_on_current_device(void** out) {
     return -1;
   }
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
+  const CUcontext ctx = current_context();
+  if (!g_scratch_addr[dev] || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -47,6 +72,8 @@ int scratch_on_current_device(void** out) {
       return e != cudaSuccess ? (int)e : -1;
     }
     g_scratch_addr[dev] = p;
+    // the context is current now (cudaGetSymbolAddress initialises it if needed)
+    g_scratch_ctx[dev] = current_context();
   }
   *out = g_scratch_addr[dev];
   return 0;
@@ -75,6 +102,10 @@ extern "C" int afq_calc_force_bias_noalloc(int32_t norb, int32_t nocc, int32_t n
     afq_set_error("afq_calc_force_bias_noalloc: NULL argument");
     return -1;
   }
+  // the Green's-function kernel holds the walker, trial and S^-1 in shared memory
+  if (int rc = afq::check_smem_optin(afq::green_f64_smem(norb, nocc),
+                                     "afq_calc_force_bias_noalloc: norb x nocc too large for the Green kernel"))
+    return rc;
   void* scratch = nullptr;
   int rc = scratch_on_current_device(&scratch);
   if (rc) return rc;

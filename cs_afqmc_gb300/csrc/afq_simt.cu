@@ -858,13 +858,31 @@ static inline int launch_err(const char* what) {
   return 0;
 }
 
+int check_smem_optin(size_t smem, const char* what) {
+  int dev = 0, lim = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;  // no limit known here: the launch reports it
+  }
+  if (smem > (size_t)lim) {
+    afq_set_error("%s: needs %zu bytes of shared memory per block, the device allows %d", what, smem, lim);
+    return -2;
+  }
+  return 0;
+}
+
 template <typename WT>
 int launch_green(const afq_ctx_dev& c, const void* wu, const void* wd, double2* green,
                  double2* ovl, bool write_green, cudaStream_t st) {
-  size_t smem = (size_t)c.norb * c.kmax * sizeof(double2) + (size_t)c.kmax * 2 * c.kmax * sizeof(double2) +
-                (size_t)c.norb * c.kmax * sizeof(double);
+  const size_t smem = green_f64_smem(c.norb, c.kmax);
+  if (int rc = check_smem_optin(smem, "green_overlap (norb x occupied orbitals too large)")) return rc;
   auto kfn = k_green_overlap<WT>;
-  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t ea = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ea != cudaSuccess) {
+    afq_set_error("green_overlap: shared-memory attribute: %s", cudaGetErrorString(ea));
+    return (int)ea;
+  }
   {
     ProfScope _ps(K_GREEN, st);
     kfn<<<c.nw, 256, smem, st>>>(c, (const WT*)wu, (const WT*)wd, green, ovl, write_green ? 1 : 0);

@@ -92,8 +92,6 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
 }
 
 // persistent split-precision GEMM (afq_gemm_split.cuh): one CTA per SM, at most one per tile.
-// With an even number of M tiles, clusters of two CTAs share each B tile (multicast); the grid
-// is then the number of co-resident clusters (or of tile pairs, if fewer) times two.
 template <class Epi>
 static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms,
                         const typename Epi::Params& ep, int* status, cudaStream_t st) {
@@ -102,41 +100,7 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
     afq_set_error("split gemm: bad sizes");
     return -1;
   }
-  if (g.m_tiles % 2 == 0) {
-    auto kfn = k_gemm_split<Epi, 2>;
-    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(kSplitThreads);
-    cfg.dynamicSmemBytes = kSplitSmem;
-    cfg.stream = st;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cfg.gridDim = dim3(num_sms - (num_sms & 1));
-    int maxc = 0;
-    if (cudaOccupancyMaxActiveClusters(&maxc, kfn, &cfg) != cudaSuccess || maxc < 1) {
-      cudaGetLastError();
-      maxc = num_sms / 2;
-    }
-    const int pairs = ntiles / 2;
-    const int ncl = pairs < maxc ? pairs : maxc;
-    cfg.gridDim = dim3(2 * ncl);
-    cudaError_t e;
-    {
-      ProfScope _ps(cls, st);
-      e = cudaLaunchKernelEx(&cfg, kfn, maps, g, ep, status);
-    }
-    if (e != cudaSuccess) {
-      afq_set_error("gemm_split (clusters of 2): %s", cudaGetErrorString(e));
-      return (int)e;
-    }
-    return launch_check("gemm_split");
-  }
-  auto kfn = k_gemm_split<Epi, 1>;
+  auto kfn = k_gemm_split<Epi>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
   const int grid = ntiles < num_sms ? ntiles : num_sms;
   {

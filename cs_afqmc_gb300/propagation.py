@@ -12,7 +12,8 @@ device array and read back as 0-d CUDA tensors, so nothing synchronises with the
 JAX PRNG key.
 
 ``precision`` selects the walker dtype: "fp64" -> complex128 walkers and FP64 kernels;
-"mixed" -> complex64 walkers and BF16 tensor-core contractions.
+"mixed" -> complex64 walkers and FP16 tensor-core contractions with hi/lo split operands
+(FP32 accumulation; FP64 log-determinants, weights and sums).
 """
 
 from __future__ import annotations

@@ -94,3 +94,20 @@ def test_phaseless_blocks(case):
                                      case.wave_data, nb, fields=fields, zetas=zetas)
     assert rel_err(to_np(e_g), e_o) < 5e-5
     assert rel_err(to_np(w_g), w_o) < 5e-5
+
+
+@pytest.fixture(scope="module")
+def wide_case():
+    # the benchmark's shapes (norb 120, 20 + 20 electrons, 600 vectors) at 256 walkers: the
+    # vhs and force-bias GEMMs run several 128-row M tiles per launch and the persistent
+    # kernels loop over more walkers than there are SMs' worth of first assignments
+    return Case(precision="mixed", orthonormal=True, perturb=0.05, kind="rhf", restricted=True, norb=120,
+                nelec=(20, 20), nchol=600, nw=256)
+
+
+def test_one_step_many_tiles(wide_case):
+    test_one_step(wide_case)
+
+
+def test_phaseless_blocks_many_tiles(wide_case):
+    test_phaseless_blocks(wide_case)

@@ -1,8 +1,9 @@
 """Cholesky-integral file I/O (cs_afqmc_gb300.integrals) on the CPU: the HDF5 subset reader
 and writer round trip, the FCIDUMP_chol field mapping of _prep_afqmc (mpi_jax.py:39-60), and
-the reader on the reference's own fixture file (tests/FCIDUMP_chol of the reference) when
-that checkout is present: its header and structural identities (symmetric hcore and
-Cholesky vectors, identity / orthogonal trial orbitals) pin the decoding."""
+the reader on the reference's own fixture file (tests/FCIDUMP_chol of the reference, an
+HDF5 file written by h5py; a byte-for-byte copy is kept as tests/golden/FCIDUMP_chol): its
+header and structural identities (symmetric hcore and Cholesky vectors, identity /
+orthogonal trial orbitals) pin the decoding."""
 
 import os
 
@@ -11,7 +12,8 @@ import pytest
 
 from cs_afqmc_gb300 import integrals as I
 
-REF_FCIDUMP = os.environ.get("AFQ_REFERENCE_FCIDUMP", "/root/reference/tests/FCIDUMP_chol")
+REF_FCIDUMP = os.environ.get(
+    "AFQ_REFERENCE_FCIDUMP", os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "FCIDUMP_chol"))
 
 
 def test_h5_round_trip(tmp_path):
@@ -55,7 +57,7 @@ def test_not_hdf5(tmp_path):
         I.read_h5(str(p))
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FCIDUMP), reason="reference checkout not present")
+@pytest.mark.skipif(not os.path.exists(REF_FCIDUMP), reason="fixture file not present")
 def test_reference_fixture():
     f = I.read_fcidump_chol(REF_FCIDUMP)
     assert (f["nelec"], f["nmo"], f["ms"], f["nchol"]) == (6, 6, 0, 15)

@@ -61,3 +61,32 @@ def test_noalloc_rejects_sizes_beyond_the_scratch():
                                          dummy.data_ptr(), dummy.data_ptr(), stream_ptr())
     assert rc < 0
     assert b"static scratch" in lib.afq_last_error()
+
+
+def test_noalloc_at_the_scratch_limit():
+    """n_walkers * nocc * norb exactly at the 2,621,440-element capacity (1024 walkers, 20
+    electrons, 128 orbitals): accepted, and the last walker's force bias - computed from the
+    last bytes of the scratch - equals the context path's; one walker more is rejected."""
+    import torch
+
+    from cs_afqmc_gb300 import _lib
+    from cs_afqmc_gb300._engine import stream_ptr
+
+    case = Case(kind="rhf", restricted=True, norb=128, nelec=(20, 20), nchol=24, nw=1024)
+    assert case.nw * case.nelec[0] * case.norb == 2_621_440
+    w = case.gpu_walkers()
+    ref = to_np(case.trial.calc_force_bias(w, case.ham_data, case.wave_data))
+    out = torch.full((case.nw, case.nchol), float("nan"), dtype=torch.complex128, device="cuda")
+    _noalloc(case, w, out)
+    torch.cuda.synchronize()
+    got = to_np(out)
+    assert rel_err(got, ref) < 1e-10
+    assert rel_err(got[-1], ref[-1]) < 1e-10
+
+    lib = _lib.load()
+    trial = torch.as_tensor(np.ascontiguousarray(case.sys.mo_coeff), dtype=torch.float64, device="cuda")
+    rc = lib.afq_calc_force_bias_noalloc(case.norb, case.nelec[0], case.nchol, case.nw + 1, trial.data_ptr(),
+                                         case.ham_data["rot_chol"].data_ptr(), w.data_ptr(), out.data_ptr(),
+                                         stream_ptr())
+    assert rc < 0
+    assert b"static scratch" in lib.afq_last_error()
