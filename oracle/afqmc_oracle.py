@@ -528,14 +528,18 @@ def cpmc_propagate(exp_h1, dt: float, u: float, pd: dict, gaussian, mo, e_estima
     return pd, pcs
 
 
-def _cpmc_pair_update(pd: dict, hs_pair, si: int, i: int, sj: int, j: int, uni, mo, slow: bool):
+def _cpmc_pair_update(pd: dict, hs_pair, si: int, i: int, sj: int, j: int, uni, mo, slow: bool,
+                      literal: bool = False):
     """One two-entry discrete-field update at (spin si, site i), (spin sj, site j) with the
     constants hs_pair [field][entry] (propagation.py:949-1220). Fast: the ratio and the
     two-step Green's-function update of uhf_cpmc (wavefunctions.py:873-945) with both steps
     built from the Green's function before the update. (The reference's code reads column j
     of the once-updated array in its second step; for two entries of one spin that is not
     the exact rank-two update, and its own test asserts agreement with the slow form, which
-    the exact update gives.) Slow: determinant ratios (propagation.py:1263-1591)."""
+    the exact update gives.) literal=True restates that code as written instead
+    (wavefunctions.py:916-945: the second add's outer-product column green[spin_j, :, j]
+    taken after the first add), to measure how far it is from the slow form. Slow:
+    determinant ratios (propagation.py:1263-1591)."""
     w = pd["walkers"]
     if slow:
         cand, rat = [], []
@@ -579,8 +583,9 @@ def _cpmc_pair_update(pd: dict, hs_pair, si: int, i: int, sj: int, j: int, uni, 
     gn = g.copy()
     gn[:, si] += (uc[:, 0] / ratios)[:, None, None] * np.einsum(
         "wa,wb->wab", g[:, si, :, i], uc[:, 1:2] * (g_ij[:, None] * sg_j - g_jj[:, None] * sg_i) - sg_i)
+    col_j = gn[:, sj, :, j].copy() if literal else g[:, sj, :, j]
     gn[:, sj] += (uc[:, 1] / ratios)[:, None, None] * np.einsum(
-        "wa,wb->wab", g[:, sj, :, j], uc[:, 0:1] * (g_ji[:, None] * sg_i - g_ii[:, None] * sg_j) - sg_j)
+        "wa,wb->wab", col_j, uc[:, 0:1] * (g_ji[:, None] * sg_i - g_ii[:, None] * sg_j) - sg_j)
     pd["walkers"] = wn
     pd["greens"] = gn
     pd["overlaps"] = ratios * pd["overlaps"]
@@ -589,24 +594,27 @@ def _cpmc_pair_update(pd: dict, hs_pair, si: int, i: int, sj: int, j: int, uni, 
 
 
 def cpmc_nn_propagate(exp_h1, dt: float, u: float, u1: float, neighbors, pd: dict, uniforms, mo,
-                      e_estimate: float, pop_control_ene_shift: float, n_walkers: int, slow: bool = False):
+                      e_estimate: float, pop_control_ene_shift: float, n_walkers: int, slow: bool = False,
+                      literal: bool = False):
     """One step of CPMC with on-site U and nearest-neighbour V = u1 (propagator_cpmc_nn,
     propagation.py:889-1230; slow: propagator_cpmc_nn_slow, 1232-1591): one-body half step,
     the on-site sweep (fields from hs(u) on (up, x), (dn, x)), then for every neighbour pair
     (i, j) four two-entry updates with hs(u1) on (up i, up j), (up i, dn j), (dn i, up j),
     (dn i, dn j), one-body half step, weights * exp(dt E_pc), the > 100 clamp and the new
     shift. uniforms [nw, norb + 4 npairs]: column x for site x, then norb + k npairs + p for
-    update k of pair p (the reference draws both sets from its key). Returns (pd, shift)."""
+    update k of pair p (the reference draws both sets from its key). literal: the fast form's
+    Green's-function update as the reference's code writes it (see _cpmc_pair_update).
+    Returns (pd, shift)."""
     hs0 = cpmc_hs_constant(dt, u)
     hs1 = cpmc_hs_constant(dt, u1)
     norb = pd["walkers"][0].shape[1]
     npairs = len(neighbors)
     pd = _cpmc_one_body(exp_h1, pd, mo)
     for x in range(norb):
-        pd = _cpmc_pair_update(pd, hs0, 0, x, 1, x, uniforms[:, x], mo, slow)
+        pd = _cpmc_pair_update(pd, hs0, 0, x, 1, x, uniforms[:, x], mo, slow, literal)
     for p, (i, j) in enumerate(neighbors):
         for k, (si, sj) in enumerate(((0, 0), (0, 1), (1, 0), (1, 1))):
-            pd = _cpmc_pair_update(pd, hs1, si, i, sj, j, uniforms[:, norb + k * npairs + p], mo, slow)
+            pd = _cpmc_pair_update(pd, hs1, si, i, sj, j, uniforms[:, norb + k * npairs + p], mo, slow, literal)
     pd = _cpmc_one_body(exp_h1, pd, mo)
     pd["weights"] = pd["weights"] * np.exp(dt * pop_control_ene_shift)
     pd["weights"] = np.where(pd["weights"] > 100.0, 0.0, pd["weights"])

@@ -80,3 +80,69 @@ def test_cpmc_nn_zero_coupling_is_onsite_step():
     assert np.allclose(a["weights"], b["weights"], rtol=1e-13, atol=0)
     for s in range(2):
         assert np.allclose(a["walkers"][s], b["walkers"][s], rtol=1e-13, atol=0)
+
+
+def _reference_nn_setup():
+    """The inputs of the reference's test_propagate_cpmc_nn (tests/test_propagation.py:12-84,
+    152-179): numpy's legacy RNG after seed 102 in the file's draw order (RHF h0, h1, chol;
+    UHF mo_coeff [10, 5] and [10, 4]; UHF h0, h1 [2, 10, 10], chol [5, 100]), rdm1 = C C^T per
+    spin, exp_h1 of the unrestricted propagator at its default dt = 0.01, walkers = the rdm1
+    natural orbitals (get_init_walkers, wavefunctions.py:298-355) made real, 10 walkers,
+    U = 4, u_1 = 1, ring neighbours (i, i + 1 mod 10). The JAX key's uniforms cannot be
+    reproduced; both forms get the same seeded uniforms instead."""
+    rs = np.random.RandomState(102)
+    norb, nchol, nup, ndn, nw, dt = 10, 5, 5, 4, 10, 0.01
+    rs.rand(1), rs.rand(norb, norb), rs.rand(nchol, norb * norb)  # the RHF part of the file
+    mo = [rs.rand(norb, nup), rs.rand(norb, ndn)]
+    h0 = rs.rand(1)[0]
+    h1 = rs.rand(2, norb, norb)
+    chol = rs.rand(nchol, norb * norb)
+    rdm1 = np.array([mo[0] @ mo[0].T, mo[1] @ mo[1].T])
+    ham = O.build_propagation_intermediates({"h0": h0, "h1": h1, "chol": chol}, rdm1, norb, (nup, ndn), dt,
+                                            restricted=False)
+    nat = [np.linalg.eigh(rdm1[s])[1][:, ::-1][:, :n] for s, n in ((0, nup), (1, ndn))]
+    w0 = [np.repeat(x[None], nw, 0) for x in nat]
+    nbr = [(i, (i + 1) % norb) for i in range(norb)]
+    return norb, mo, w0, list(ham["exp_h1"]), nbr, nw, dt
+
+
+def test_cpmc_nn_literal_update_on_the_references_own_setup_is_vacuous():
+    """On the reference's own test setup (random positive h1 and trial orbitals) every
+    walker's weight is zero after the first step in all three forms - exact, literal and
+    slow - so that test's np.allclose(fast, slow) checks cannot tell the two readings of the
+    update apart: they compare zero weights and identical walkers."""
+    norb, mo, w0, exp_h1, nbr, nw, dt = _reference_nn_setup()
+    uni = np.random.default_rng(7).uniform(size=(nw, norb + 4 * len(nbr)))
+    run = {}
+    with np.errstate(divide="ignore"):
+        for name, kw in (("exact", {}), ("literal", {"literal": True}), ("slow", {"slow": True})):
+            run[name], _ = O.cpmc_nn_propagate(exp_h1, dt, 4.0, 1.0, nbr, O.cpmc_init(w0, mo), uni, mo, -5.0,
+                                               -5.0, nw, **kw)
+    for name in ("exact", "literal", "slow"):
+        assert np.all(run[name]["weights"] == 0.0), name
+    for name in ("exact", "literal"):
+        assert np.allclose(run["slow"]["overlaps"], run[name]["overlaps"])
+        for s in range(2):
+            assert np.allclose(run["slow"]["walkers"][s], run[name]["walkers"][s])
+
+
+def test_cpmc_nn_literal_update_fails_fast_equals_slow():
+    """On a lattice where walkers survive (4 x 2, U = 4, u_1 = 1, 3 steps), the reference's
+    check np.allclose(fast, slow) (tests/test_propagation.py:174-179) passes for the exact
+    rank-two update and fails for the update read literally (wavefunctions.py:916-945, the
+    second add built from the once-updated Green's function): its weights leave the slow
+    form's by ~1e-3 relative within a step. This is why the kernels implement the exact
+    update."""
+    n, mo, w0, exp_h1, nbr, rng = _lattice()
+    nw = w0[0].shape[0]
+    run = {k: O.cpmc_init(w0, mo) for k in ("exact", "literal", "slow")}
+    for _ in range(3):
+        uni = rng.uniform(size=(nw, n + 4 * len(nbr)))
+        for name, kw in (("exact", {}), ("literal", {"literal": True}), ("slow", {"slow": True})):
+            run[name], _ = O.cpmc_nn_propagate(exp_h1, 0.01, 4.0, 1.0, nbr, run[name], uni, mo, -5.0, -5.0, nw,
+                                               **kw)
+        sl, ex, li = run["slow"], run["exact"], run["literal"]
+        assert np.allclose(sl["weights"], ex["weights"]) and np.allclose(sl["overlaps"], ex["overlaps"])
+        assert all(np.allclose(sl["walkers"][s], ex["walkers"][s]) for s in range(2))
+        assert not np.allclose(sl["weights"], li["weights"])
+        assert np.max(np.abs(li["weights"] - sl["weights"])) > 1e-4 * np.max(np.abs(sl["weights"]))
