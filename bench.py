@@ -141,6 +141,7 @@ def flops_per_launch(cls: str, w: dict, n_batch: int) -> float:
     table = {
         "vhs_gemm": 4.0 * G * n * n * nwc,                 # i sqrt(dt) x~ . chol
         "taylor": 5 * 8.0 * n * n * o * nwc,               # 5 products V T
+        "prop_fused": (5 * 8.0 + 2 * 4.0) * n * n * o * nwc,  # exp_h1, 5 products V T, exp_h1
         "exp_h1_gemm": 4.0 * n * n * o * nw,               # (E - I) W, one product
         "force_bias_gemm": 4.0 * G * o * n * nw,           # G . rot_chol
         "energy_gemm": 4.0 * G * n * o * o * nw,           # rot_chol_g G^T for all g

@@ -21,7 +21,7 @@ ClassProf g_prof[K_NCLASS];
 
 const char* kNames[K_NCLASS] = {"green", "force_bias_gemm", "field_shifts", "vhs_gemm", "taylor",
                                 "exp_h1_gemm", "energy_gemm", "energy_reduce", "weights", "qr", "sr",
-                                "block_stats", "rng", "prep"};
+                                "block_stats", "rng", "prep", "prop_fused"};
 
 }  // namespace
 

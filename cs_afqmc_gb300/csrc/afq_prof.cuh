@@ -22,6 +22,7 @@ enum KClass {
   K_STATS,       // block statistics and bookkeeping
   K_RNG,         // Philox draws
   K_PREP,        // one-time operand preparation
+  K_PROP,        // fused exp_h1 * Taylor * exp_h1 walker propagation
   K_NCLASS
 };
 

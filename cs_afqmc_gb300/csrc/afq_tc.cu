@@ -5,6 +5,7 @@
 
 #include "afq_mixed_kernels.cuh"
 #include "afq_prof.cuh"
+#include "afq_prop_fused.cuh"
 
 namespace afq {
 
@@ -994,6 +995,12 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
     TC_CHECK(mk(&t.m_t0[s][0], t.t0[s][0], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
     TC_CHECK(mk(&t.m_t0[s][1], t.t0[s][1], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
   }
+  {  // the fused propagation kernel takes every non-diagonal configuration it has room for
+    int ntmax = 0;
+    for (int s = 0; s < t.nslab; ++s) ntmax = t.NT[s] > ntmax ? t.NT[s] : ntmax;
+    t.fused = !(t.cfg & (kLegacyTaylor | kDiagChol)) && t.n <= 128 && ntmax <= 16 * kPropMaxChains &&
+              prop_fused_smem(t.nq, ntmax) <= 232448 && prop_tmem_cols(t.nq, ntmax) <= 512;
+  }
   for (int b = 0; b < t.nblk; ++b) {
     // Coulomb: c_g = G_b . rot_chol_b (A = Green operand, B = rot_chol operand)
     {
@@ -1050,7 +1057,8 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   }
   const float2* w0 = static_cast<const float2*>(wu);
   const float2* w1 = static_cast<const float2*>(wd);
-  const int flags = (write_ops || for_propagation) ? (kGreenWT | kGreenG) : 0;
+  // the walker operand of the exp_h1 GEMMs is needed only when they run as separate launches
+  const int flags = (write_ops || for_propagation) ? ((t.fused ? 0 : kGreenWT) | kGreenG) : 0;
   const int om = omax <= 8 ? 8 : omax <= 16 ? 16 : omax <= 24 ? 24 : 32;
   const size_t smem =
       green_fused_smem(t.n, omax, om, md.o_blk[0] + md.o_blk[1], (flags & kGreenG) != 0, md.nslab);
@@ -1171,8 +1179,76 @@ static int exp_gemm(TcState& t, const afq_ctx_dev& c, int s, bool last, float2* 
                                      ep, t.status, st);
 }
 
+template <int NP>
+static int launch_prop_fused(const TcState& t, int s, const PropDev& pd, cudaStream_t st) {
+  const size_t smem = prop_fused_smem(t.nq, t.NT[s]);
+  auto kfn = k_prop_fused<NP>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    afq_set_error("prop_fused: shared-memory attribute: %s", cudaGetErrorString(e));
+    return (int)e;
+  }
+  {
+    ProfScope _ps(K_PROP, st);
+    kfn<<<pd.nwc < t.num_sms ? pd.nwc : t.num_sms, 128 * NP + 160, smem, st>>>(
+        t.m_vt[s][0], t.m_vt[s][1], t.eop[s][0], t.eop[s][1], t.nk, pd, t.status);
+  }
+  return launch_check("prop_fused");
+}
+
+// vhs GEMM, then exp_h1 * Taylor * exp_h1 in one kernel per slab, chunk by chunk
+static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, cudaStream_t st) {
+  const int nchunks = t.nw / t.nwc;
+  const bool want_lo = t.taylor_split > 0;
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int w0 = ch * t.nwc;
+    EpiVHS::Params ev;
+    ev.v_hi = t.vbuf[0];
+    ev.v_lo = t.vbuf[1];
+    ev.n = t.n;
+    ev.nq = t.nq;
+    ev.rows = 2 * t.nwc;
+    ev.bf16 = t.bf16 ? 1 : 0;
+    ev.want_lo = want_lo ? 1 : 0;
+    ev.sqdt = (float)sqrt(c.dt);
+    SplitArgs sa;
+    sa.k_tiles = (c.nchol + 63) / 64;
+    sa.k_splits = 1;
+    sa.m_tiles = (2 * t.nwc + 127) / 128;
+    sa.n_tiles = (t.n * t.nq + kSplitBN - 1) / kSplitBN;
+    sa.a_row0 = 2 * w0;
+    sa.has_alo = (t.cfg & kVhsDyn) ? 1 : 0;
+    sa.has_blo = (t.cfg & kVhsStat) ? 1 : 0;
+    sa.drain = t.drain > 0 ? t.drain : sa.k_tiles;
+    sa.idesc = ptx::idesc_f16(128, kSplitBN, t.bf16 ? 1 : 0);
+    if (c.n_exp_terms > 1)
+      TC_CHECK(launch_split<EpiVHSSplit>(K_VHS, t.m_vhs_split, sa, t.num_sms, ev, t.status, st));
+    for (int s = 0; s < t.nslab; ++s) {
+      PropDev pd;
+      pd.n = t.n;
+      pd.o = t.o_slab[s];
+      pd.nq = t.nq;
+      pd.NT = t.NT[s];
+      pd.nterms = c.n_exp_terms;
+      pd.split = t.taylor_split;
+      pd.bf16 = t.bf16 ? 1 : 0;
+      pd.nwc = t.nwc;
+      pd.e_lo = (t.cfg & kExpStat) ? 1 : 0;
+      pd.w_lo = (t.cfg & kExpDyn) ? 1 : 0;
+      pd.w = W[s] + (size_t)w0 * t.n * t.o_slab[s];
+      const int np = t.NT[s] / 16;
+      if (np == 1) TC_CHECK(launch_prop_fused<1>(t, s, pd, st));
+      else if (np == 2) TC_CHECK(launch_prop_fused<2>(t, s, pd, st));
+      else if (np == 3) TC_CHECK(launch_prop_fused<3>(t, s, pd, st));
+      else TC_CHECK(launch_prop_fused<4>(t, s, pd, st));
+    }
+  }
+  return 0;
+}
+
 int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
   float2* W[2] = {static_cast<float2*>(wu), static_cast<float2*>(wd)};
+  if (t.fused) return propagate_fused(t, c, W, st);
   for (int s = 0; s < t.nslab; ++s) TC_CHECK(exp_gemm(t, c, s, false, W[s], st));
   if (t.cfg & kDiagChol) {
     if (t.n > 128) {

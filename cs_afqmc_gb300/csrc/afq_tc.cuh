@@ -36,6 +36,8 @@ enum MixedBits : int32_t {
                         // bias, vhs and exchange GEMMs (0: default, 7: no draining)
   kDiagChol = 1 << 15,  // every Cholesky vector is a diagonal matrix (on-site lattice terms):
                         // exp(vhs) W1 is a per-row polynomial scale, no vhs GEMM / Taylor MMA
+  kLegacyTaylor = 1 << 16,  // separate exp_h1 GEMMs around the Taylor kernel (k_taylor_tc)
+                            // instead of the fused propagation kernel
   kExplicit = 1 << 30,  // set by callers that pass an explicit configuration
 };
 constexpr int kDrainDefault = 2;  // K tiles per drained run unless the configuration says
@@ -78,6 +80,7 @@ struct TcState {
   GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2], m_z[2];
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
+  bool fused;               // fused propagation kernel (norb <= 128, <= 32 orbitals per slab)
   int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;
   int drain;                // K tiles per drained accumulation run (0: not drained)
   int num_sms;              // persistent grid size

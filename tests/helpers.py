@@ -12,7 +12,7 @@ from oracle import afqmc_oracle as O
 class Case:
     def __init__(self, kind="rhf", norb=12, nelec=(3, 3), nchol=30, nw=8, dt=0.005,
                  restricted=True, precision="fp64", seed=5, perturb=0.2, n_batch=1,
-                 orthonormal=False, h1_shift=None, hubbard=None):
+                 orthonormal=False, h1_shift=None, hubbard=None, mixed_config=0):
         import torch
         from cs_afqmc_gb300 import hamiltonian, propagation, wavefunctions
 
@@ -63,7 +63,8 @@ class Case:
         hd = {"h0": s.h0, "h1": s.h1.copy(), "chol": s.chol.copy(), "ene0": 0.0}
         hd = self.ham.build_measurement_intermediates(hd, self.trial, self.wave_data)
         P = propagation.propagator_restricted if restricted else propagation.propagator_unrestricted
-        self.prop = P(dt=dt, n_walkers=nw, n_exp_terms=6, n_batch=n_batch, precision=precision)
+        self.prop = P(dt=dt, n_walkers=nw, n_exp_terms=6, n_batch=n_batch, precision=precision,
+                      mixed_config=mixed_config)
         hd = self.ham.build_propagation_intermediates(hd, self.prop, self.trial, self.wave_data)
         self.ham_data = hd
         self.torch = torch

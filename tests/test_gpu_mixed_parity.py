@@ -111,3 +111,29 @@ def test_one_step_many_tiles(wide_case):
 
 def test_phaseless_blocks_many_tiles(wide_case):
     test_phaseless_blocks(wide_case)
+
+
+@pytest.mark.parametrize("idx", [0, 2, 5], ids=["rhf-r", "uhf", "rhf-120"])
+def test_one_step_legacy_taylor(idx):
+    """The separate exp_h1 GEMMs around the Taylor kernel (the path before the fused
+    propagation kernel, kept behind a configuration bit) against the oracle."""
+    from cs_afqmc_gb300 import _lib
+    case = Case(precision="mixed", orthonormal=True, perturb=0.05,
+                mixed_config=_lib.MIXED_DEFAULT | _lib.MIXED_LEGACY_TAYLOR, **CASES[idx])
+    test_one_step(case)
+
+
+@pytest.mark.parametrize("n_batch", [1, 2])
+def test_fused_matches_legacy_taylor(n_batch):
+    """Fused and separate propagation on the same fields: walkers agree to the mixed path's
+    own accuracy (both against the oracle at 2e-5)."""
+    from cs_afqmc_gb300 import _lib
+    kw = dict(kind="uhf", restricted=False, norb=40, nelec=(9, 7), nchol=70, nw=32, n_batch=n_batch)
+    a = Case(precision="mixed", orthonormal=True, perturb=0.05, **kw)
+    b = Case(precision="mixed", orthonormal=True, perturb=0.05, mixed_config=_lib.MIXED_DEFAULT | _lib.MIXED_LEGACY_TAYLOR,
+             **kw)
+    fields = np.random.default_rng(8).standard_normal((a.nw, a.nchol))
+    pa = a.prop.propagate(a.trial, a.ham_data, a.gpu_prop_data(), fields, a.wave_data)
+    pb = b.prop.propagate(b.trial, b.ham_data, b.gpu_prop_data(), fields, b.wave_data)
+    assert rel_err(_flat(to_np(pa["walkers"])), _flat(to_np(pb["walkers"]))) < 2e-5
+    assert rel_err(to_np(pa["weights"]), to_np(pb["weights"])) < 2e-5
