@@ -1,6 +1,8 @@
 """Single-rank AFQMC block driver (the non-AD branch of ad_afqmc/driver.py:16-492, without
-MPI, file output or equilibration printing): repeated sampler.propagate_phaseless calls
-with the per-block weight record, QR, global SR and e_estimate update kept on the device.
+MPI or file output): the equilibration sweeps (run_equilibration, driver.py:91-133) and
+the sampling blocks (run_blocks, driver.py:245-308), each block a
+sampler.propagate_phaseless call followed by the weight record, QR, global SR and
+e_estimate update, all on the device.
 """
 
 from __future__ import annotations
@@ -38,6 +40,39 @@ def run_blocks(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_da
         _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), be[n:].data_ptr(), zg.data_ptr(),
                   bw[n:].data_ptr(), stream_ptr())
     return be, bw, prop_data
+
+
+def run_equilibration(ham, ham_data, prop, prop_data: PropData, trial, wave_data, n_eql: int,
+                      fields=None, zetas=None, sampler=None):
+    """The equilibration sweeps of driver.py:91-133: n_eql blocks of the equilibration
+    sampler (sampling.sampler(n_prop_steps=50, n_ene_blocks=5, n_sr_blocks=10)), each
+    followed by the block weight record, QR, global SR and e_estimate = 0.9 e_estimate +
+    0.1 E_block (on one rank the population's block energy is the block's own). fields
+    (optional): [n_eql, 10, 5, 50, nw, G]; zetas (optional): [n_eql, 11]. sampler: another
+    equilibration sampler (tests use shorter blocks). Returns device tensors
+    (block_energy [n_eql], block_weight [n_eql]) and prop_data."""
+    from . import sampling
+    samp = sampler if sampler is not None else sampling.sampler(n_prop_steps=50, n_ene_blocks=5, n_sr_blocks=10)
+    return run_blocks(samp, ham, ham_data, prop, prop_data, trial, wave_data, n_eql, fields=fields, zetas=zetas)
+
+
+def afqmc(ham, ham_data, prop, prop_data: PropData, trial, wave_data, sampler, n_eql: int, n_blocks: int):
+    """driver.afqmc's energy path on one rank (driver.py:16-492 without MPI, observables or
+    file output): n_eql equilibration sweeps, then n_blocks sampling blocks of `sampler`.
+    Returns (weighted mean block energy, its standard error from the block values
+    (None for fewer than two blocks), block energies, block weights, prop_data); the
+    reference's blocking analysis and outlier rejection of the block record are host-side
+    statistics left to the caller."""
+    _, _, prop_data = run_equilibration(ham, ham_data, prop, prop_data, trial, wave_data, n_eql)
+    be, bw, prop_data = run_blocks(sampler, ham, ham_data, prop, prop_data, trial, wave_data, n_blocks)
+    e, w = be.double(), bw.double()
+    mean = torch.sum(e * w) / torch.sum(w)
+    err = None
+    if n_blocks > 1:
+        neff = torch.sum(w) ** 2 / torch.sum(w * w)
+        var = torch.sum(w * (e - mean) ** 2) / torch.sum(w)
+        err = float(torch.sqrt(var / (neff - 1)))
+    return float(mean), err, be, bw, prop_data
 
 
 def run_blocks_ad(sampler, ham, ham_data, prop, prop_data: PropData, trial, wave_data,

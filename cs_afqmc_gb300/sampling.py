@@ -428,6 +428,66 @@ class sampler:
             (rdm2,) = torch.autograd.grad(lin, op)
         return energy, rdm2.detach(), prop_data
 
+    def propagate_phaseless_chol_vjp(self, ham, ham_data: dict, prop, prop_data: PropData, trial, wave_data: dict,
+                                     do_sr: bool = True, fields: Optional[torch.Tensor] = None,
+                                     zetas: Optional[torch.Tensor] = None):
+        """Reverse-mode derivative of the block energy of propagate_phaseless with respect to
+        the Cholesky vectors, the trial held fixed: every quantity that depends on them -
+        the vhs operator, the mean-field shifts, h0_prop, exp_h1 (through v0 and the
+        mean-field part of h1_mod) and rot_chol (propagation.py:292-325,
+        wavefunctions.py:602-619) - is rebuilt with torch ops, the device sweep returns the
+        cotangents of each (afq_propagate_phaseless_vjp_ex), and torch autograd carries them
+        back to chol. This is the chain the reference differentiates with jax.vjp when its
+        two-body mode varies the Cholesky vectors (sampling.py:198-229, driver.py:230-245),
+        here without re-optimising the trial. Returns (energy, d energy / d chol
+        [nchol, norb * norb], prop_data). FP64 walkers only."""
+        if "rdm1" not in wave_data:
+            raise _lib.AfqError("the Cholesky derivative needs wave_data['rdm1'] (the driver sets it to the trial's rdm1)")
+        norb = trial.norb
+        chol = as_dev(ham_data["chol"]).reshape(-1, norb * norb).detach().clone().requires_grad_(True)
+        nchol = int(chol.shape[0])
+        with torch.enable_grad():
+            hd = {k: v for k, v in ham_data.items() if k not in (_CACHE_KEY, "rot_chol", "rot_h1", "exp_h1",
+                                                                 "mf_shifts", "h0_prop")}
+            hd["chol"] = chol
+            hd = ham.build_measurement_intermediates(hd, trial, wave_data)
+            hd = ham.build_propagation_intermediates(hd, prop, trial, wave_data)
+            mf, v0, v1 = prop._mf_v0_v1(hd, trial, wave_data)
+            exp_h1 = prop._exp_h1(as_dev(hd["h1"]), v0, v1)
+            h0p = -float(_scalar(hd["h0"])) - torch.sum(mf * mf) / 2.0
+            plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in hd.items()}
+            for key in ("rot_chol", "rot_h1"):
+                plain[key] = [x.detach() for x in hd[key]] if isinstance(hd[key], list) else hd[key].detach()
+            energy, g, prop_data = self._vjp_call(prop, prop_data, trial, plain, wave_data, do_sr, fields, zetas,
+                                                  rotation=True, chol_grads=True)
+            gexp, _, _, grc, gchol, gmf, gh0p = g
+            lin = torch.sum((gexp if exp_h1.dim() == 3 else gexp[0]) * exp_h1)
+            lin = lin + torch.sum(gchol * chol)
+            lin = lin + torch.sum(gmf.real * mf.real + gmf.imag * mf.imag)
+            lin = lin + gh0p.real * h0p.real + gh0p.imag * h0p.imag
+            if isinstance(hd["rot_chol"], list):
+                n_up = trial.nelec[0]
+                rc = grc.reshape(nchol, -1)
+                for s_, (o0, o1) in enumerate(((0, n_up * norb), (n_up * norb, rc.shape[1]))):
+                    lin = lin + torch.sum(rc[:, o0:o1].reshape(hd["rot_chol"][s_].shape) * hd["rot_chol"][s_])
+            else:
+                lin = lin + torch.sum(grc.reshape(hd["rot_chol"].shape) * hd["rot_chol"])
+            (gc,) = torch.autograd.grad(lin, chol)
+        return energy, gc.detach(), prop_data
+
+    def propagate_phaseless_u_vjp(self, ham, ham_data: dict, u: float, prop, prop_data: PropData, trial,
+                                  wave_data: dict, do_sr: bool = True, fields: Optional[torch.Tensor] = None,
+                                  zetas: Optional[torch.Tensor] = None):
+        """d (block energy) / dU for Cholesky vectors proportional to sqrt(U), as in the
+        Hubbard model's L_i = sqrt(U) n_i: dL/dU = L / (2U), so dE/dU = <dE/dL, L> / (2U).
+        Returns (energy, dE/dU, prop_data)."""
+        if not u > 0:
+            raise _lib.AfqError("U must be positive")
+        energy, gc, prop_data = self.propagate_phaseless_chol_vjp(ham, ham_data, prop, prop_data, trial, wave_data,
+                                                                   do_sr, fields, zetas)
+        chol = as_dev(ham_data["chol"]).reshape(gc.shape)
+        return energy, torch.sum(gc * chol) / (2.0 * float(u)), prop_data
+
     def _vjp_call(self, prop, prop_data: PropData, trial, ham_data: dict, wave_data: dict, do_sr: bool, fields,
                   zetas, rotation: bool, chol_grads: bool = False):
         """afq_propagate_phaseless_vjp_ex on the engine of (trial, ham_data, wave_data).

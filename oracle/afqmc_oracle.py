@@ -883,6 +883,31 @@ def phaseless_derivative_fd(sampler: "Sampler", prop: "Propagator", trial: "Tria
     return v0[0], d[0], v0[1:1 + nb], d[1:1 + nb], v0[1 + nb:], d[1 + nb:]
 
 
+def phaseless_chol_derivative_fd(sampler: "Sampler", prop: "Propagator", trial: "Trial", ham_data: dict,
+                                 chol_of: Callable[[float], np.ndarray], theta: float, rdm1: np.ndarray, mo,
+                                 prop_data: dict, fields: np.ndarray, zetas, restricted: bool, h: float = 1e-3,
+                                 do_sr: bool = True):
+    """d/d theta of the blocked energy for Cholesky vectors chol_of(theta) [nchol, norb*norb]
+    (the Hubbard model's sqrt(U) n_i with theta = U), the trial, prop_data, fields and SR
+    uniforms held fixed and every intermediate rebuilt at each theta (the quantity the GPU's
+    Cholesky vjp maps to d/d theta). Central differences at h and h/2, Richardson-extrapolated.
+    Returns (energy, d energy)."""
+    import copy
+
+    def run(t):
+        hd = {"h0": ham_data["h0"], "h1": ham_data["h1"], "chol": chol_of(t)}
+        hd = trial.build_measurement_intermediates(hd, mo)
+        hd = build_propagation_intermediates(hd, rdm1, trial.norb, trial.nelec, prop.dt, restricted)
+        e, _, _, _ = sampler.propagate_phaseless(prop, trial, hd, copy.deepcopy(prop_data), mo, fields, zetas,
+                                                 do_sr=do_sr)
+        return e
+
+    e0 = run(theta)
+    d1 = (run(theta + h) - run(theta - h)) / (2 * h)
+    d2 = (run(theta + h / 2) - run(theta - h / 2)) / h
+    return e0, (4 * d2 - d1) / 3
+
+
 def blocking_analysis(weights: np.ndarray, energies: np.ndarray, neql: int = 0):
     """Weighted mean and plateau error of blocked samples (stat_utils.py:8-52), computed in
     float64 throughout (the reference's blocked arrays are float32)."""
