@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--cs-derivative", action="store_true",
                     help="dE/dlambda on the UHF workload: correlated sampling and forward mode")
     ap.add_argument("--cs-blocks", type=int, default=10)
+    ap.add_argument("--hubbard-derivative", action="store_true",
+                    help="d<E>/dU on the 8x8 Hubbard workload (FP64 reverse mode) with a finite-difference check")
+    ap.add_argument("--hubbard-blocks", type=int, default=10)
     ap.add_argument("--energy-sync", action="store_true",
                     help="with --energy-only: per-block comparison from the FP64 run's states")
     return ap.parse_args()
@@ -708,7 +711,64 @@ def cs_derivative(args) -> dict:
         torch.cuda.empty_cache()
     res["mixed_minus_fp64"] = res["mixed"]["dE_dlambda"] - res["fp64"]["dE_dlambda"]
     res["forward_mode_fp64"] = ad_derivative(w, name, d, steps, n_prop)
+    res["same_trajectory"] = same_trajectory_derivative(w, d, steps, n_prop, lam)
     return res
+
+
+def same_trajectory_derivative(w: dict, d, steps: int, n_prop: int, lam: float) -> dict:
+    """Correlated sampling and forward mode on one trajectory (FP64, UHF workload): `steps`
+    field blocks of n_prop steps from the initial walkers, no SR and no outlier removal,
+    both systems starting from the lambda = 0 state; the central difference of the pair's
+    blocked energy sum_k E_k W_k / sum_k W_k against the jvp of one no-SR block with `steps`
+    energy blocks on the same fields. The two agree to the difference's O(lambda^2) error:
+    the gap between the correlated-sampling number and the driver's forward mode above is
+    the estimator (the driver differentiates each block with the entering walkers held
+    fixed and SR after every block, correlated sampling the whole trajectory without
+    population control), not the arithmetic."""
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import corr_sample, hamiltonian, propagation, sampling, synthetic, wavefunctions
+    from cs_afqmc_gb300.propagation import RngKey
+
+    norb = w["norb"]
+
+    def system(shift):
+        s = synthetic.molecular(norb, w["nelec"], w["nchol"], seed=1, kind=w["kind"])
+        s.h1 = s.h1 + shift * d
+        ham = hamiltonian.hamiltonian(norb)
+        trial = wavefunctions.uhf(norb, w["nelec"])
+        wave = {"mo_coeff": s.mo_coeff, "rdm1": s.rdm1}
+        hd = {"h0": s.h0, "h1": s.h1, "chol": s.chol, "ene0": 0.0}
+        hd = ham.build_measurement_intermediates(hd, trial, wave)
+        prop = propagation.propagator_unrestricted(dt=w["dt"], n_walkers=w["n_walkers"], n_exp_terms=6, n_batch=1,
+                                                   precision="fp64")
+        hd = ham.build_propagation_intermediates(hd, prop, trial, wave)
+        pd = prop.init_prop_data(trial, wave, hd, init_walkers=s.init_walkers(w["n_walkers"], False))
+        pd["key"] = RngKey(4321)
+        return ham, hd, prop, pd, trial, wave
+
+    ham0, hd0, pr0, pd0, tr0, wv0 = system(0.0)
+    sp, sm = system(lam), system(-lam)
+    for sy in (sp, sm):
+        sy[3]["e_estimate"] = pd0["e_estimate"]
+        sy[3]["pop_control_ene_shift"] = pd0["pop_control_ene_shift"]
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(99)
+    fields = torch.empty((steps, n_prop, w["n_walkers"], w["nchol"]), dtype=torch.float64, device="cuda")
+    fields.normal_(generator=gen)
+    samp1 = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=1, n_sr_blocks=1)
+    (_, _), (e1, w1, e2, w2) = corr_sample.cs_steps_scan(
+        steps, sp[3], sp[1], sp[2], sp[4], sp[5], sm[3], sm[1], sm[2], sm[4], sm[5], samp1,
+        fields=fields, z_thresh=float("inf"))
+    e1, w1, e2, w2 = (x.cpu().numpy() for x in (e1, w1, e2, w2))
+    cs = float((e1.sum() / w1.sum() - e2.sum() / w2.sum()) / (2 * lam))
+    sampk = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=steps, n_sr_blocks=1)
+    e, de, _ = sampk.propagate_phaseless_ad_norot_jvp(ham0, hd0, np.stack([d, d]), pr0, pd0, tr0, wv0, do_sr=False,
+                                                      fields=fields[None])
+    return {"correlated_sampling": cs, "forward_mode": de.item(), "abs_diff": abs(cs - de.item()),
+            "energy": e.item(), "blocks": steps, "steps_per_block": n_prop, "lambda": lam,
+            "trajectory": "initial walkers, no SR, no outlier removal, identical fields, FP64"}
 
 
 def ad_derivative(w: dict, name: str, d, steps: int, n_prop: int) -> dict:
@@ -808,6 +868,97 @@ def ad_derivative(w: dict, name: str, d, steps: int, n_prop: int) -> dict:
     }
 
 
+def hubbard_derivative(args) -> dict:
+    """Config 5's derivative: d<E>/dU on the 8 x 8 periodic Hubbard lattice (U = 4, 28 + 28
+    electrons, 2048 walkers, dt 0.01, diagonal Cholesky vectors sqrt(U) n_i), by the FP64
+    reverse-mode sweep per driver block of 50 steps with SR (sampler.propagate_phaseless_u_vjp,
+    then the block end: QR, global SR, e_estimate update), `hubbard_blocks` blocks (500 steps
+    at the default). The first block is also checked against a Richardson central difference
+    of the FP64 value path in U on identical draws (the oracle's restatement of the same check
+    runs on 4 x 4 in tests/test_gpu_hubbard_u.py). The trial is the real free-electron
+    determinant."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from cs_afqmc_gb300 import _lib, hamiltonian, propagation, sampling, synthetic, wavefunctions
+    from cs_afqmc_gb300._engine import stream_ptr
+    from cs_afqmc_gb300.propagation import RngKey
+
+    name = "hubbard_8x8_u4_n28_nw2048"
+    w = dict(synthetic.WORKLOADS[name])
+    u = w["u"]
+    s = synthetic.hubbard_2d(w["lx"], w["ly"], 1.0, u, w["nelec"], real_trial=True)
+    ham = hamiltonian.hamiltonian(s.norb)
+    trial = wavefunctions.rhf(s.norb, w["nelec"])
+    wave = {"mo_coeff": s.mo_coeff, "rdm1": s.rdm1}
+    prop = propagation.propagator_restricted(dt=w["dt"], n_walkers=w["n_walkers"], n_exp_terms=6, n_batch=1,
+                                             precision="fp64")
+
+    def hdata(uu):
+        hd = {"h0": s.h0, "h1": s.h1, "chol": s.chol * np.sqrt(uu / u), "ene0": 0.0}
+        hd = ham.build_measurement_intermediates(hd, trial, wave)
+        return ham.build_propagation_intermediates(hd, prop, trial, wave)
+
+    hd = hdata(u)
+    samp = sampling.sampler(n_prop_steps=50, n_ene_blocks=1, n_sr_blocks=1)
+
+    def fresh(hdx):
+        pd = prop.init_prop_data(trial, wave, hdx, init_walkers=s.init_walkers(w["n_walkers"], True))
+        pd["key"] = RngKey(2025)
+        return pd
+
+    pd = fresh(hd)
+    f0 = samp.draw_fields(prop, pd, s.chol.shape[0])
+    z0 = samp.draw_zetas(pd, 1)
+    e0, du0, _ = samp.propagate_phaseless_u_vjp(ham, hd, u, prop, fresh(hd), trial, wave, fields=f0, zetas=z0)
+    h = 1e-3
+    ev = {}
+    for uu in (u + h, u - h, u + h / 2, u - h / 2):
+        hu = hdata(uu)
+        pu = fresh(hd)  # the block's starting state does not depend on U
+        ev[uu] = samp.propagate_phaseless(ham, hu, prop, pu, trial, wave, fields=f0, zetas=z0)[0].item()
+    fd = (4 * (ev[u + h / 2] - ev[u - h / 2]) / h - (ev[u + h] - ev[u - h]) / (2 * h)) / 3
+    check = {"vjp": du0.item(), "central_difference": fd, "abs_diff": abs(du0.item() - fd), "h": h,
+             "richardson": True, "energy": e0.item()}
+
+    pd = fresh(hd)
+    be, bd, bw = [], [], []
+    wsum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.hubbard_blocks):
+        e, du, pd = samp.propagate_phaseless_u_vjp(ham, hd, u, prop, pd, trial, wave)
+        zg = samp.draw_zetas(pd, 1)
+        eng = pd["_engine"]
+        st = pd.state(eng)
+        eh = e.reshape(1).clone()
+        _lib.call("afq_block_end", eng.ctx, ctypes.byref(st), eh.data_ptr(), zg.data_ptr(), wsum.data_ptr(),
+                  stream_ptr())
+        be.append(eh)
+        bd.append(du.reshape(1).clone())
+        bw.append(wsum.clone())
+    t1.record()
+    torch.cuda.synchronize()
+    sec = t0.elapsed_time(t1) / 1e3
+    be, bd, bw = (torch.cat(x).cpu().numpy() for x in (be, bd, bw))
+    nb = len(be)
+    return {
+        "workload": name, "u": u, "blocks": nb, "steps_per_block": 50, "precision": "fp64",
+        "energy": float(np.sum(be * bw) / np.sum(bw)),
+        "dE_dU": float(np.sum(bd * bw) / np.sum(bw)),
+        "dE_dU_stderr": float(np.std(bd, ddof=1) / np.sqrt(nb)) if nb > 1 else None,
+        "per_block_dE_dU": [round(float(x), 6) for x in bd],
+        "walker_steps_per_s": nb * 50 * w["n_walkers"] / sec,
+        "first_block_check": check,
+        "method": "FP64 reverse-mode sweep; cotangents of chol, mean-field shifts, h0_prop, exp_h1 and rot_chol "
+                  "carried to the Cholesky vectors by torch autograd; dE/dU = <dE/dL, L> / (2U); trial fixed",
+    }
+
+
 def serving_bench(args) -> dict:
     """Serving pattern: a Poisson stream of independent jobs (rate jobs/s for `duration` s,
     norb uniform in [20, norb_max], nocc = norb // 6, nchol = 5 norb, walkers in
@@ -848,6 +999,13 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "serving p50/p99 job latency and aggregate walker-steps/s",
                               "serving": serving_bench(args)}), flush=True)
+        return
+    if args.hubbard_derivative:
+        import torch
+        torch.cuda.set_device(local)
+        if rank == 0:
+            print(json.dumps({"metric": "d<E>/dU, 8x8 Hubbard, FP64 reverse mode",
+                              "hubbard_derivative": hubbard_derivative(args)}), flush=True)
         return
     if args.cs_derivative:
         import torch

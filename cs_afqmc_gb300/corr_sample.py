@@ -78,22 +78,24 @@ def corr_otler_rm(prop_data1: PropData, prop_data2: PropData, z_thresh: float = 
 
 def cs_block_scan(prop_data1, ham_data1, prop1, trial1, wave_data1,
                   prop_data2, ham_data2, prop2, trial2, wave_data2, sampler,
-                  fields=None, sums: Optional[torch.Tensor] = None):
+                  fields=None, sums: Optional[torch.Tensor] = None, z_thresh: float = 5.0):
     """One correlated block: fields from system 1's key (or given), a block of each system,
-    outlier removal (corr_sample.py:596-629)."""
+    outlier removal (corr_sample.py:596-629; z_thresh = inf keeps every walker)."""
     if prop1.n_walkers != prop2.n_walkers:
         raise _lib.AfqError("correlated systems must have the same number of walkers")
     eng1 = prop1._engine(trial1, ham_data1, wave_data1, prop_data1["walkers"])
     f = _draw_fields(prop1, prop_data1, sampler, eng1.nchol) if fields is None else as_dev(fields)
     prop_data1 = field_block_scan(prop_data1, f, ham_data1, prop1, trial1, wave_data1, sampler)
     prop_data2 = field_block_scan(prop_data2, f, ham_data2, prop2, trial2, wave_data2, sampler)
-    return corr_otler_rm(prop_data1, prop_data2, sums=sums)
+    return corr_otler_rm(prop_data1, prop_data2, z_thresh=z_thresh, sums=sums)
 
 
 def cs_steps_scan(steps: int, prop_data1, ham_data1, prop1, trial1, wave_data1,
-                  prop_data2, ham_data2, prop2, trial2, wave_data2, sampler, fields=None):
+                  prop_data2, ham_data2, prop2, trial2, wave_data2, sampler, fields=None,
+                  z_thresh: float = 5.0):
     """`steps` correlated blocks (corr_sample.py:667-694). fields (optional):
-    [steps, n_prop_steps, nw, nchol]. Returns ((prop_data1, prop_data2),
+    [steps, n_prop_steps, nw, nchol]; z_thresh: the outlier cut (inf: none). Returns
+    ((prop_data1, prop_data2),
     (loc_en1, loc_weight1, loc_en2, loc_weight2)): per-step sum E w and sum w of each
     system after outlier removal, CUDA tensors [steps]."""
     sums = torch.empty(steps, 4, dtype=torch.float64, device=device())
@@ -101,5 +103,5 @@ def cs_steps_scan(steps: int, prop_data1, ham_data1, prop1, trial1, wave_data1,
         f = None if fields is None else fields[s]
         prop_data1, prop_data2 = cs_block_scan(prop_data1, ham_data1, prop1, trial1, wave_data1,
                                                prop_data2, ham_data2, prop2, trial2, wave_data2,
-                                               sampler, fields=f, sums=sums[s])
+                                               sampler, fields=f, sums=sums[s], z_thresh=z_thresh)
     return (prop_data1, prop_data2), (sums[:, 0], sums[:, 1], sums[:, 2], sums[:, 3])

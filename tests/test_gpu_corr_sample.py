@@ -79,3 +79,43 @@ def test_outlier_removal_matches_oracle():
     assert r1[7] == 0 and r2[300] == 0 and r1[55] == 0
     ref = [np.sum(e1 * r1), np.sum(r1), np.sum(e2 * r2), np.sum(r2)]
     assert rel_err(to_np(sums), ref) < 1e-13
+
+
+@pytest.mark.parametrize("kind,restricted,nelec", [("rhf", True, (3, 3)), ("uhf", False, (4, 2))])
+def test_cs_derivative_equals_forward_mode_on_the_same_trajectory(kind, restricted, nelec):
+    """Correlated sampling and the forward-mode derivative estimate the same quantity when
+    they follow the same trajectory: K field blocks without SR and without outlier
+    removal (z_thresh = inf) from the same walkers and the same (lambda = 0) starting
+    e_estimate, blocked energy sum_k E_k W_k / sum_k W_k. The central difference of the
+    correlated pair at lambda = +-1e-4 then equals the jvp of
+    propagate_phaseless_ad_nosr_norot with K energy blocks (relative 1e-6: the difference's
+    own O(lambda^2) error). The driver's per-block forward mode differs from both by design:
+    each block's walkers enter with a zero tangent and SR follows every block."""
+    import torch
+    from cs_afqmc_gb300 import corr_sample, sampling
+    norb, nchol, nw = 12, 30, 16
+    rng = np.random.default_rng(17)
+    d = rng.normal(0.0, 0.05, (norb, norb))
+    d = np.triu(d) + np.triu(d, 1).T
+    lam = 1e-4
+    kw = dict(kind=kind, restricted=restricted, norb=norb, nelec=nelec, nchol=nchol, nw=nw, orthonormal=True,
+              perturb=0.05)
+    a, b, c = Case(**kw, h1_shift=lam * d), Case(**kw, h1_shift=-lam * d), Case(**kw)
+    K, n_prop = 3, 4
+    fields = np.random.default_rng(5).standard_normal((K, n_prop, nw, nchol))
+    samp = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=1, n_sr_blocks=1)
+    pc = c.gpu_prop_data()
+    pa, pb = a.gpu_prop_data(), b.gpu_prop_data()
+    for p_ in (pa, pb):  # the starting state does not depend on lambda (the jvp's zero tangent)
+        p_["e_estimate"] = pc["e_estimate"]
+        p_["pop_control_ene_shift"] = pc["pop_control_ene_shift"]
+    (_, _), (e1, w1, e2, w2) = corr_sample.cs_steps_scan(
+        K, pa, a.ham_data, a.prop, a.trial, a.wave_data,
+        pb, b.ham_data, b.prop, b.trial, b.wave_data, samp, fields=fields, z_thresh=float("inf"))
+    e1, w1, e2, w2 = (to_np(x) for x in (e1, w1, e2, w2))
+    fd = (e1.sum() / w1.sum() - e2.sum() / w2.sum()) / (2 * lam)
+    samp_k = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=K, n_sr_blocks=1)
+    e, de, _ = samp_k.propagate_phaseless_ad_norot_jvp(c.ham, c.ham_data, d, c.prop, pc, c.trial, c.wave_data,
+                                                       do_sr=False, fields=torch.as_tensor(fields[None]).cuda())
+    assert abs(e.item() - (e1.sum() / w1.sum() + e2.sum() / w2.sum()) / 2) < 1e-7 * abs(e.item())
+    assert abs(de.item() - fd) < 1e-6 * max(abs(fd), 1e-3), (de.item(), fd)
