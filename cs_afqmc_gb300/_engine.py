@@ -218,6 +218,11 @@ def engine_for(trial, ham_data: Optional[dict], wave_data: dict, walkers, *, dt:
         # on-site lattice terms: the library replaces the vhs GEMM and the Taylor products by
         # a per-row polynomial scale (and checks the diagonality itself)
         mixed_config = (int(mixed_config) or _lib.MIXED_DEFAULT) | _lib.MIXED_DIAG_CHOL
+    elif prec == _lib.AFQ_PREC_MIXED and ham_data is not None and have_prop and \
+            not (int(mixed_config) & _lib.MIXED_EXPLICIT) and _symmetric_chol(a["chol"], norb):
+        # L_g = L_g^T exactly: V is symmetric, so the vhs GEMM computes about two thirds of it
+        # and the propagation kernel mirrors the rest (the same numbers as the full product)
+        mixed_config = (int(mixed_config) or _lib.MIXED_DEFAULT) | _lib.MIXED_SYM_CHOL
     eng = Engine(norb=norb, nelec=nelec, nchol=nchol, n_walkers=nw, restricted=restricted, uhf=uhf,
                  precision=prec, dt=dt, n_exp_terms=n_exp_terms, n_batch=n_batch, arrays=a, h0=h0,
                  h0_prop=h0p, mixed_config=mixed_config)
@@ -230,6 +235,12 @@ def _diagonal_chol(chol: torch.Tensor, norb: int) -> bool:
     c = chol.reshape(-1, norb, norb)
     off = c - torch.diag_embed(torch.diagonal(c, dim1=1, dim2=2))
     return bool(torch.count_nonzero(off).item() == 0)
+
+
+def _symmetric_chol(chol: torch.Tensor, norb: int) -> bool:
+    """True when every Cholesky vector [norb, norb] equals its transpose exactly."""
+    c = chol.reshape(-1, norb, norb)
+    return bool(torch.equal(c, c.transpose(1, 2)))
 
 
 def _scalar(x):

@@ -25,6 +25,7 @@ MIXED_DEFAULT = 767          # the library's default accuracy options (afq_dims.
 MIXED_DIAG_CHOL = 1 << 15    # every Cholesky vector diagonal: per-row exp(vhs), no Taylor MMA
 MIXED_EXPLICIT = 1 << 30     # the caller's configuration as given (no automatic diagonal path)
 MIXED_LEGACY_TAYLOR = 1 << 16  # separate exp_h1 GEMMs and Taylor kernel instead of the fused kernel
+MIXED_SYM_CHOL = 1 << 17     # every Cholesky vector symmetric: packed vhs GEMM, V mirrored on load
 
 _vp = ctypes.c_void_p
 

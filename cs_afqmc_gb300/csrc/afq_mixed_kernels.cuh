@@ -582,6 +582,7 @@ struct EpiVHS {
     uint16_t* v_lo;
     int n, nq, rows, bf16, want_lo;
     float sqdt;
+    int sym;  // split GEMM only: columns are the packed (p, q) pairs of sym_decode
   };
   static constexpr int kSmemBytes = 0;
   __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
@@ -634,7 +635,14 @@ struct EpiVHSSplit {
     const float scale = (R & 1) == 0 ? p.sqdt : -p.sqdt;
 #pragma unroll
     for (int c32 = 0; c32 < 128; c32 += 32) {
-      const int col = col0 + c32, pr = col / p.nq, q0 = col % p.nq;
+      const int col = col0 + c32;
+      int pr, q0;
+      if (p.sym)
+        sym_decode(p.n, p.nq, col, pr, q0);  // the 32 columns stay inside one row run
+      else {
+        pr = col / p.nq;
+        q0 = col % p.nq;
+      }
       if (pr >= p.n) continue;  // warp-uniform
       uint32_t hw[16], lw[16];
 #pragma unroll
@@ -669,6 +677,31 @@ struct EpiVHSSplit {
     }
   }
 };
+
+// vhs B operand for symmetric vectors: chol [nchol][n*n] -> lop[c][g] for the packed columns
+// c = (p, q) of sym_decode, 32 x 32 tiles through shared memory
+__global__ void k_prep_lop_sym(const double* __restrict__ chol, int nchol, int n, int nq, int total, int ldg,
+                               int bf16, uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
+  __shared__ float tile[32][33];
+  const int c0 = blockIdx.x * 32, g0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  int pp = n, qq = 0;
+  if (c0 + tx < total) sym_decode(n, nq, c0 + tx, pp, qq);
+  for (int r = ty; r < 32; r += 8) {
+    const int g = g0 + r;
+    tile[r][tx] = (g < nchol && pp < n && qq < n) ? (float)chol[(size_t)g * n * n + (size_t)pp * n + qq] : 0.f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int c = c0 + r, g = g0 + tx;
+    if (c < total && g < nchol) {
+      uint16_t h, l;
+      split16(tile[tx][r], bf16 != 0, h, l);
+      hi[(size_t)c * ldg + g] = h;
+      lo[(size_t)c * ldg + g] = l;
+    }
+  }
+}
 
 // ======================================================================================
 // QR of the FP32 walker slabs (propagation.py:251-253 -> linalg_utils.py:51-65): the

@@ -39,6 +39,7 @@ namespace afq {
 struct PropDev {
   int n, o, nq, NT, nterms, split, bf16, nwc;
   int e_lo, w_lo;   // exp_h1 products: E_lo * B_hi and E_hi * B_lo terms
+  int sym;          // V is symmetric and stored only for q >= 32 floor(p / 32) (packed vhs)
   float2* w;        // walker slab of the chunk's first walker, [nwc][n][o] complex64
 };
 
@@ -80,7 +81,8 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
   uint64_t* ready = bars + 4;      // B rows written and the accumulators read
   uint64_t* done = bars + 5;       // the step's MMAs completed
   uint64_t* fin = bars + 6;        // every MMA issued has completed (teardown)
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
+  uint64_t* vlofree = bars + 7;    // the walker's last product with V_lo completed (V_lo in TMEM free)
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 8);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr int NT = 16 * NP;
@@ -89,6 +91,9 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
   const bool need_v = pd.nterms > 1;
   const bool v_lo = pd.split > 0;
   const int nsteps = pd.nterms + 1;  // exp_h1, nterms - 1 Taylor products, exp_h1
+  // V_lo is last used by Taylor product `split`: when that is not the last product, the next
+  // walker's V_lo is moved into TMEM as soon as it completes, before the rest of V
+  const bool early_lo = v_lo && pd.split < nsteps - 2;
 
   if (tid == 0) {
     ptx::mbar_init(v_bar, 1);
@@ -98,6 +103,7 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
     ptx::mbar_init(ready, 4 * NP);  // one arrival per epilogue warp
     ptx::mbar_init(done, 1);
     ptx::mbar_init(fin, 1);
+    ptx::mbar_init(vlofree, 1);
     ptx::fence_mbar_init();
   }
   if (warp == kCtrl) {
@@ -183,6 +189,7 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
           ptx::mma_commit(done);
           // the walker's last Taylor products are issued: V in TMEM is free once they complete
           if (ok && need_v && st == nsteps - 2) ptx::mma_commit(vfree);
+          if (ok && early_lo && st == pd.split) ptx::mma_commit(vlofree);
         }
       }
       ptx::mma_commit(fin);
@@ -211,33 +218,70 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(eready);
     }
+    // with symmetric V the staged row p holds only q >= 32 quadrant: the columns below come
+    // from row q, column p (for a fixed q the warp reads 32 consecutive elements of row q)
+    const int q_lo = pd.sym ? 32 * q : 0;
+    const bool pv = p < pd.n;
+    auto copy_plane = [&](int plane) {
+      for (int t = 0; t < 2 * KQ; ++t) {  // tiles: Vr kt = 0..KQ-1, then Vi
+        const unsigned char* tile = Sv + (plane * 2 * KQ + t) * kPropTile + p * 128;
+        const uint32_t col = (plane ? c_vl : c_vh) + (t / KQ) * kw + (t % KQ) * 32;
+        const int k_tile = (t % KQ) * 64;
+        // column p of the part's staged tiles (K tile p / 64 of the same part and plane)
+        const unsigned char* ctile = Sv + (plane * 2 * KQ + (t / KQ) * KQ + (p >> 6)) * kPropTile;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          uint32_t v[16];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {  // 16-byte chunks 4 half + c of the row (swizzled)
+            const int k0 = k_tile + 8 * (4 * half + c);
+            if (k0 >= q_lo) {  // warp-uniform: q_lo and k0 are multiples of 8 and 32
+              const uint4 x = *reinterpret_cast<const uint4*>(tile + (((4 * half + c) ^ (p & 7)) << 4));
+              v[4 * c] = x.x;
+              v[4 * c + 1] = x.y;
+              v[4 * c + 2] = x.z;
+              v[4 * c + 3] = x.w;
+            } else {
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                uint32_t wd = 0;
+                if (pv) {
+#pragma unroll
+                  for (int e = 0; e < 2; ++e) {
+                    const int qq = k0 + 2 * j + e;  // row qq < 32 quadrant <= p
+                    const uint16_t x = *reinterpret_cast<const uint16_t*>(
+                        ctile + qq * 128 + (((((p & 63) >> 3) ^ (qq & 7))) << 4) + ((p & 7) << 1));
+                    wd |= (uint32_t)x << (16 * e);
+                  }
+                }
+                v[4 * c + j] = wd;
+              }
+            }
+          }
+          ptx::tmem_st16u(tmem + lane_off + col + 16 * half, v);
+        }
+      }
+    };
     int it = 0;
     for (int wl = blockIdx.x; need_v && wl < pd.nwc && ok; wl += gridDim.x, ++it) {
       bool w_ok = ptx::mbar_wait(v_bar, it & 1);
+      if (early_lo) {  // V_lo first, once the previous walker's last split product completed
+        if (it > 0) w_ok = w_ok && ptx::mbar_wait(vlofree, (it - 1) & 1);
+        if (!__all_sync(0xffffffffu, w_ok)) {
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        copy_plane(1);
+      }
       if (it > 0) w_ok = w_ok && ptx::mbar_wait(vfree, (it - 1) & 1);
       if (!__all_sync(0xffffffffu, w_ok)) {
         ok = false;
         break;
       }
       ptx::tc_fence_after();
-      for (int plane = 0; plane < (v_lo ? 2 : 1); ++plane)
-        for (int t = 0; t < 2 * KQ; ++t) {  // tiles: Vr kt = 0..KQ-1, then Vi
-          const unsigned char* tile = Sv + (plane * 2 * KQ + t) * kPropTile + p * 128;
-          const uint32_t col = (plane ? c_vl : c_vh) + (t / KQ) * kw + (t % KQ) * 32;
-#pragma unroll
-          for (int half = 0; half < 2; ++half) {
-            uint32_t v[16];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {  // 16-byte chunks 4 half + c of the row (swizzled)
-              const uint4 x = *reinterpret_cast<const uint4*>(tile + (((4 * half + c) ^ (p & 7)) << 4));
-              v[4 * c] = x.x;
-              v[4 * c + 1] = x.y;
-              v[4 * c + 2] = x.z;
-              v[4 * c + 3] = x.w;
-            }
-            ptx::tmem_st16u(tmem + lane_off + col + 16 * half, v);
-          }
-        }
+      copy_plane(0);
+      if (v_lo && !early_lo) copy_plane(1);
       ptx::tmem_st_wait();
       ptx::tc_fence_before();
       __syncwarp();

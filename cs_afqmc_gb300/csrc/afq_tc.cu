@@ -711,6 +711,15 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
       return -2;
     }
   }
+  {  // the fused propagation kernel takes every non-diagonal configuration it has room for
+    int ntmax = 0;
+    for (int s = 0; s < t.nslab; ++s) ntmax = t.NT[s] > ntmax ? t.NT[s] : ntmax;
+    t.fused = !(cfg & (kLegacyTaylor | kDiagChol)) && t.n <= 128 && ntmax <= 16 * kPropMaxChains &&
+              prop_fused_smem(t.nq, ntmax) <= 232448 && prop_tmem_cols(t.nq, ntmax) <= 512;
+    // symmetric vectors: packed vhs columns, mirrored in the fused kernel
+    t.sym = t.fused && (cfg & kSymChol) != 0;
+    t.n_vcols = t.sym ? sym_total(t.n, t.nq) : t.n * t.nq;
+  }
   size_t umax = 0;
   for (int b = 0; b < t.nblk; ++b) {
     t.o_blk[b] = c.gocc[b];
@@ -921,8 +930,12 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
   const double* rcsrc = c.nspin_g == 2 ? rccat : c.rot_chol[0];
   k_row_scale<<<c.nchol, 256, 0, st>>>(rcsrc, t.kfb, t.rc_inv);
   k_prep_rows_scaled<<<c.nchol, 256, 0, st>>>(rcsrc, t.kfb, t.ldfb, bf, t.rc_inv, t.rc_fb[0], t.rc_fb[1]);
-  k_prep_lop<<<dim3((t.n * t.n + 31) / 32, (c.nchol + 31) / 32), 256, 0, st>>>(h.chol, c.nchol, t.n, t.nq,
-                                                                             t.ldg, bf, t.lop[0], t.lop[1]);
+  if (t.sym)
+    k_prep_lop_sym<<<dim3((t.n_vcols + 31) / 32, (c.nchol + 31) / 32), 256, 0, st>>>(
+        h.chol, c.nchol, t.n, t.nq, t.n_vcols, t.ldg, bf, t.lop[0], t.lop[1]);
+  else
+    k_prep_lop<<<dim3((t.n * t.n + 31) / 32, (c.nchol + 31) / 32), 256, 0, st>>>(h.chol, c.nchol, t.n, t.nq,
+                                                                               t.ldg, bf, t.lop[0], t.lop[1]);
   TC_CHECK(launch_check("mixed operand preparation"));
   // ---- tensor maps
   const bool b16 = t.bf16;
@@ -952,8 +965,8 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
     const uint64_t nrows = (uint64_t)t.n * t.nq;
     TC_CHECK(mk(&t.m_vhs_split.a_hi, t.xt[0], 2 * t.nw, c.nchol, t.ldg, 128));
     TC_CHECK(mk(&t.m_vhs_split.a_lo, t.xt[1], 2 * t.nw, c.nchol, t.ldg, 128));
-    TC_CHECK(mk(&t.m_vhs_split.b_hi, t.lop[0], nrows, c.nchol, t.ldg, kSplitBBox));
-    TC_CHECK(mk(&t.m_vhs_split.b_lo, t.lop[1], nrows, c.nchol, t.ldg, kSplitBBox));
+    TC_CHECK(mk(&t.m_vhs_split.b_hi, t.lop[0], (uint64_t)t.n_vcols, c.nchol, t.ldg, kSplitBBox));
+    TC_CHECK(mk(&t.m_vhs_split.b_lo, t.lop[1], (uint64_t)t.n_vcols, c.nchol, t.ldg, kSplitBBox));
     int dev = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&t.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || t.num_sms < 1)
@@ -994,12 +1007,6 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
     TC_CHECK(mk(&t.m_vt[s][1], t.vbuf[1], (uint64_t)nwc * 128, 2 * t.nq, 2 * t.nq, 128));
     TC_CHECK(mk(&t.m_t0[s][0], t.t0[s][0], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
     TC_CHECK(mk(&t.m_t0[s][1], t.t0[s][1], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
-  }
-  {  // the fused propagation kernel takes every non-diagonal configuration it has room for
-    int ntmax = 0;
-    for (int s = 0; s < t.nslab; ++s) ntmax = t.NT[s] > ntmax ? t.NT[s] : ntmax;
-    t.fused = !(t.cfg & (kLegacyTaylor | kDiagChol)) && t.n <= 128 && ntmax <= 16 * kPropMaxChains &&
-              prop_fused_smem(t.nq, ntmax) <= 232448 && prop_tmem_cols(t.nq, ntmax) <= 512;
   }
   for (int b = 0; b < t.nblk; ++b) {
     // Coulomb: c_g = G_b . rot_chol_b (A = Green operand, B = rot_chol operand)
@@ -1211,11 +1218,12 @@ static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, c
     ev.bf16 = t.bf16 ? 1 : 0;
     ev.want_lo = want_lo ? 1 : 0;
     ev.sqdt = (float)sqrt(c.dt);
+    ev.sym = t.sym ? 1 : 0;
     SplitArgs sa;
     sa.k_tiles = (c.nchol + 63) / 64;
     sa.k_splits = 1;
     sa.m_tiles = (2 * t.nwc + 127) / 128;
-    sa.n_tiles = (t.n * t.nq + kSplitBN - 1) / kSplitBN;
+    sa.n_tiles = (t.n_vcols + kSplitBN - 1) / kSplitBN;
     sa.a_row0 = 2 * w0;
     sa.has_alo = (t.cfg & kVhsDyn) ? 1 : 0;
     sa.has_blo = (t.cfg & kVhsStat) ? 1 : 0;
@@ -1235,6 +1243,7 @@ static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, c
       pd.nwc = t.nwc;
       pd.e_lo = (t.cfg & kExpStat) ? 1 : 0;
       pd.w_lo = (t.cfg & kExpDyn) ? 1 : 0;
+      pd.sym = t.sym ? 1 : 0;
       pd.w = W[s] + (size_t)w0 * t.n * t.o_slab[s];
       const int np = t.NT[s] / 16;
       if (np == 1) TC_CHECK(launch_prop_fused<1>(t, s, pd, st));
@@ -1296,6 +1305,7 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.rows = 2 * t.nwc;
     ev.bf16 = t.bf16 ? 1 : 0;
     ev.want_lo = want_lo ? 1 : 0;
+    ev.sym = 0;  // the separate Taylor kernel reads the full V
     ev.sqdt = (float)sqrt(c.dt);
     SplitArgs sa;
     sa.k_tiles = (c.nchol + 63) / 64;

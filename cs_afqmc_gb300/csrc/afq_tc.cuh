@@ -4,7 +4,8 @@
 //   g_fb   [2 nw][ldfb]       rows (w, re/im), cols (spin block, i, p) = G_s[i][p] * 2^e_w
 //   rc_fb  [nchol][ldfb]      rows g, cols (spin block, i, p) = rot_chol_s[g][i][p] * 2^e_g
 //   xt     [2 nw][ldg]        rows (w, re/im), cols g = shifted fields
-//   lop    [norb * nq][ldg]   rows (p, q) (q padded to nq), cols g = chol_g[p][q]
+//   lop    [norb * nq][ldg]   rows (p, q) (q padded to nq), cols g = chol_g[p][q]; with
+//                             symmetric vectors rows are the packed (p, q) pairs of sym_decode
 //   vbuf   [nwc][128][2 nq]   per walker [Vr | Vi] (rows >= norb and q >= norb zero)
 //   eop[s] [128][nk]          exp_h1_s - I (rows >= norb zero)
 //   wt[s], acc[s] [nw * R_s][nk]  rows (w, 2k + re/im), cols p: walker / Taylor sum
@@ -38,11 +39,38 @@ enum MixedBits : int32_t {
                         // exp(vhs) W1 is a per-row polynomial scale, no vhs GEMM / Taylor MMA
   kLegacyTaylor = 1 << 16,  // separate exp_h1 GEMMs around the Taylor kernel (k_taylor_tc)
                             // instead of the fused propagation kernel
+  kSymChol = 1 << 17,   // every Cholesky vector is a symmetric matrix: the vhs GEMM computes
+                        // V only for q >= 32 floor(p / 32) and the fused kernel mirrors the rest
   kExplicit = 1 << 30,  // set by callers that pass an explicit configuration
 };
 constexpr int kDrainDefault = 2;  // K tiles per drained run unless the configuration says
 constexpr int32_t kMixedDefault = kFbDyn | kFbStat | kVhsDyn | kVhsStat | kExpDyn | kExpStat |
                                   kEneDyn | kEneStat | (2 << kTaylorShift);
+
+// Symmetric Cholesky vectors (V = V^T): row p of V, in row blocks of 32 (b = p / 32), keeps
+// the columns q >= 32 b only; the packed column of (p, q) is
+// sym_base(b) + (p - 32 b) (nq - 32 b) + (q - 32 b). Every row run is a multiple of 32 long
+// and starts at a multiple of 32.
+__host__ __device__ inline int sym_rows(int n, int b) { return n - 32 * b < 32 ? n - 32 * b : 32; }
+__host__ __device__ inline int sym_total(int n, int nq) {
+  int t = 0;
+  for (int b = 0; 32 * b < n; ++b) t += sym_rows(n, b) * (nq - 32 * b);
+  return t;
+}
+// (p, q) of packed column c < sym_total(n, nq)
+__host__ __device__ inline void sym_decode(int n, int nq, int c, int& p, int& q) {
+  for (int b = 0; 32 * b < n; ++b) {
+    const int len = nq - 32 * b, size = sym_rows(n, b) * len;
+    if (c < size) {
+      p = 32 * b + c / len;
+      q = 32 * b + c % len;
+      return;
+    }
+    c -= size;
+  }
+  p = n;  // past the end
+  q = 0;
+}
 
 struct TcState {
   int ready;
@@ -81,6 +109,8 @@ struct TcState {
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
   bool fused;               // fused propagation kernel (norb <= 128, <= 32 orbitals per slab)
+  bool sym;                 // symmetric Cholesky vectors on the fused path: packed vhs columns
+  int n_vcols;              // vhs GEMM columns: norb * nq, or the packed count with sym
   int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;
   int drain;                // K tiles per drained accumulation run (0: not drained)
   int num_sms;              // persistent grid size

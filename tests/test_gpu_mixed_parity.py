@@ -137,3 +137,31 @@ def test_fused_matches_legacy_taylor(n_batch):
     pb = b.prop.propagate(b.trial, b.ham_data, b.gpu_prop_data(), fields, b.wave_data)
     assert rel_err(_flat(to_np(pa["walkers"])), _flat(to_np(pb["walkers"]))) < 2e-5
     assert rel_err(to_np(pa["weights"]), to_np(pb["weights"])) < 2e-5
+
+
+@pytest.mark.parametrize("kw", [dict(kind="rhf", restricted=True, norb=120, nelec=(20, 20), nchol=600, nw=32),
+                                dict(kind="uhf", restricted=False, norb=60, nelec=(10, 8), nchol=300, nw=24),
+                                dict(kind="rhf", restricted=True, norb=40, nelec=(9, 9), nchol=70, nw=16)],
+                         ids=["rhf-120", "uhf-60", "rhf-40"])
+def test_symmetric_packing_is_exact(kw):
+    """Symmetric Cholesky vectors (detected by the Python layer): the vhs GEMM computes V only
+    for q >= 32 floor(p / 32) and the propagation kernel mirrors the rest. Each element is the
+    same K sum as in the full product, so walkers and weights after two driver blocks are
+    bitwise those of the full vhs GEMM (the configuration given explicitly, without the bit)."""
+    from cs_afqmc_gb300 import _lib, driver, sampling
+    a = Case(precision="mixed", orthonormal=True, perturb=0.05, **kw)
+    b = Case(precision="mixed", orthonormal=True, perturb=0.05,
+             mixed_config=_lib.MIXED_DEFAULT | _lib.MIXED_EXPLICIT, **kw)
+    rng = np.random.default_rng(12)
+    nb, n_prop, n_ene = 2, 3, 2
+    fields = rng.standard_normal((nb, 1, n_ene, n_prop, a.nw, a.nchol))
+    zetas = rng.uniform(size=(nb, 2))
+    samp = sampling.sampler(n_prop_steps=n_prop, n_ene_blocks=n_ene, n_sr_blocks=1)
+    ea, wa, pa = driver.run_blocks(samp, a.ham, a.ham_data, a.prop, a.gpu_prop_data(), a.trial, a.wave_data, nb,
+                                   fields=fields, zetas=zetas)
+    eb, wb, pb = driver.run_blocks(samp, b.ham, b.ham_data, b.prop, b.gpu_prop_data(), b.trial, b.wave_data, nb,
+                                   fields=fields, zetas=zetas)
+    assert int(pa["_engine"].dims.mixed_config) & _lib.MIXED_SYM_CHOL
+    assert not int(pb["_engine"].dims.mixed_config) & _lib.MIXED_SYM_CHOL
+    assert np.array_equal(_flat(to_np(pa["walkers"])), _flat(to_np(pb["walkers"])))
+    assert np.array_equal(to_np(ea), to_np(eb)) and np.array_equal(to_np(wa), to_np(wb))
