@@ -39,6 +39,7 @@ METRIC = "walker-steps/s at equal energy error vs FP64 GPU path"
 UNIT = "walker-steps/s"
 DEFAULT_WORKLOAD = "rhf_norb120_nocc20_nchol600_nw1024"
 N_PROP, N_ENE, N_SR = 5, 4, 1
+CPU_WALKERS, CPU_STEPS = 48, 30   # CPU baseline sample per process (about 10-20 s of host work)
 L2_BYTES = 129e6
 
 
@@ -66,6 +67,9 @@ def parse():
     ap.add_argument("--serving-duration", type=float, default=10.0)
     ap.add_argument("--serving-norb-max", type=int, default=128)
     ap.add_argument("--serving-slots", type=int, default=16)
+    ap.add_argument("--serving-in-line", type=float, default=5.0,
+                    help="seconds of the serving stream run after the headline measurement and reported "
+                         "in its line under 'serving' (0: skip)")
     ap.add_argument("--cs-derivative", action="store_true",
                     help="dE/dlambda on the UHF workload: correlated sampling and forward mode")
     ap.add_argument("--cs-blocks", type=int, default=10)
@@ -427,7 +431,7 @@ def run_ours(args, rank, world, local):
     cpu_procs = args.cpu_procs or max(1, (os.cpu_count() or 2) - 2)
     if want_cpu:
         from oracle.cpu_bench import CpuPool
-        cpu_pool = CpuPool(cpu_procs, w["norb"], w["nelec"][0], w["nchol"], 16, w["dt"], kind=w["kind"])
+        cpu_pool = CpuPool(cpu_procs, w["norb"], w["nelec"][0], w["nchol"], CPU_WALKERS, w["dt"], kind=w["kind"])
 
     w, s, ham, trial, wave, hd, prop, pd, samp = build_workload(
         args.workload, args.precision, args.n_batch, args.mixed_config, seed=1000 + rank)
@@ -565,9 +569,9 @@ def run_ours(args, rank, world, local):
     if cpu_pool is not None:
         try:
             cpu_pool.run(2, 1)  # warm-up (imports, system build)
-            ws, sec = cpu_pool.run(10, 2)
+            ws, sec = cpu_pool.run(CPU_STEPS, CPU_STEPS // 5)
             cpu = {"value": round(ws / sec, 2), "unit": UNIT, "cores": cpu_procs, "kind": "port",
-                   "sample": (f"{args.workload}: {cpu_procs} processes x 16 walkers x 10 steps "
+                   "sample": (f"{args.workload}: {cpu_procs} processes x {CPU_WALKERS} walkers x {CPU_STEPS} steps "
                               f"(QR + local energy every 5), FP64 NumPy oracle, 1 BLAS thread each, "
                               f"{sec:.1f} s wall")}
         except Exception as ex:  # noqa: BLE001
@@ -578,6 +582,17 @@ def run_ours(args, rank, world, local):
 
     # ---- accuracy at this workload: mixed vs FP64 GPU path on identical draws ----
     ec = energy_check_sync(args, args.energy_blocks) if args.energy_blocks > 1 and world == 1 else None
+
+    # ---- serving pattern on record: a short Poisson stream through the continuous-batching server
+    srv = None
+    if args.serving_in_line > 0 and world == 1:
+        try:
+            import argparse as _ap
+            sa = _ap.Namespace(**vars(args))
+            sa.serving_duration = args.serving_in_line
+            srv = serving_bench(sa)
+        except Exception as ex:  # noqa: BLE001 - the headline line is printed regardless
+            srv = {"error": repr(ex)[:300]}
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -593,6 +608,7 @@ def run_ours(args, rank, world, local):
         "kernels_timing": ("second pass of the same steps with a CUDA-event pair around every launch on "
                            "its stream (value above is timed without them)"),
         "energy_check": ec,
+        "serving": srv,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -97,11 +97,12 @@ __host__ __device__ constexpr int green_s_ld(int o) {
 constexpr int kGreenWT = 1, kGreenG = 2;
 constexpr int kGfThreads = 128;  // threads per walker CTA (128 or 256; 128 measured faster)
 
-// G lives in its own region when two slabs contribute to it; with one slab it overwrites the
-// walker copy once G's inputs are in registers
+// G lives in its own region when two slabs contribute to it or norb > 128 (each thread then
+// owns two orbital rows); with one slab and norb <= 128 it overwrites the walker copy once
+// G's inputs are in registers
 __host__ __device__ constexpr size_t green_fused_smem(int n, int omax, int om, int gtot, bool g, int nslab) {
   return (((size_t)n * green_s_ld(omax) * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15) +
-         (size_t)om * kGreenMaxO * 8 + ((g && nslab == 2) ? (size_t)gtot * n * 8 : 0);
+         (size_t)om * kGreenMaxO * 8 + ((g && (nslab == 2 || n > 128)) ? (size_t)gtot * n * 8 : 0);
 }
 
 // dst[(e / o) * ld + e % o] = src[e] for e < n * o, 8 loads in flight per thread, the row and
@@ -139,7 +140,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   constexpr int NW = NT / 32, NH = NT / 128;  // warps; thread groups of 128 (orbital rows)
   constexpr int RPT = (OM + NW - 1) / NW;     // rows of S per thread in the Gauss-Jordan phase
   const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = md.n;
-  const int p = tid & 127, h = tid >> 7;
+  const int p0 = tid & 127, h = tid >> 7;  // orbital rows p0, p0 + 128 (norb <= 256)
+  const bool overlay = md.nslab == 1 && n <= 128;  // G overwrites the walker copy
   const int omax = md.o_slab[0] > md.o_slab[1] ? md.o_slab[0] : md.o_slab[1];
   const int ldmax = green_s_ld(omax);
   const bool do_g = (flags & kGreenG) != 0;
@@ -148,15 +150,14 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * ldmax);  // [n][o]
   float2* Si = reinterpret_cast<float2*>(
       sm + (((size_t)n * ldmax * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15));  // [OM][kGreenMaxO]
-  // [gtot][n]: after the walker copy's last use when there is one slab (ld >= o = gtot)
-  float2* Gs = md.nslab == 1 ? Ws : Si + OM * kGreenMaxO;
+  // [gtot][n]: after the walker copy's last use when it overlays it (ld >= o = gtot)
+  float2* Gs = overlay ? Ws : Si + OM * kGreenMaxO;
   __shared__ float2 Ssh[2][OM][OM + 1];  // S (partials), then the double-buffered working matrix
   __shared__ float2 pivv[OM];
   __shared__ int piv_s[OM], step_s[OM];
   __shared__ float2 e1w[NW], e1l[NW];
   __shared__ float fred[NW];
   const bool bf = md.bf16 != 0;
-  const bool prow_ok = p < n;
   double2 det = c2(1.0, 0.0);  // thread 0
   for (int s = 0; s < md.nslab; ++s) {
     const int o = md.o_slab[s], o4 = (o + 3) & ~3, ld = green_s_ld(o);
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
     copy_rows<NT>(Ws, W, n, o, ld);
     copy_batched<NT>(Cs, md.trial32[s], n * o, [](int e) { return e; });
     __syncthreads();
-    if ((flags & kGreenWT) && prow_ok) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
+    for (int p = p0; (flags & kGreenWT) && p < n; p += 128) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
       uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + p;
       uint16_t* lo = md.wt[s][1] + (size_t)w * md.R[s] * md.nk + p;
       for (int k = h; k < o; k += NH) {
@@ -288,11 +289,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
       }
     }
     __syncthreads();
-    float2 wr[OM];
+    // overlay: one row per thread and one pass, every thread reaching the barrier; otherwise
+    // rows p0 and p0 + 128, G in its own region
+    for (int p = p0; p < (overlay ? 128 : n); p += 128) {
+      const bool prow_ok = p < n;
+      float2 wr[OM];
 #pragma unroll
-    for (int k = 0; k < OM; ++k) wr[k] = (prow_ok && k < o) ? Ws[p * ld + k] : make_float2(0.f, 0.f);
-    if (md.nslab == 1) __syncthreads();  // G overwrites the walker copy
-    if (prow_ok) {
+      for (int k = 0; k < OM; ++k) wr[k] = (prow_ok && k < o) ? Ws[p * ld + k] : make_float2(0.f, 0.f);
+      if (overlay) __syncthreads();  // G overwrites the walker copy
+      if (!prow_ok) continue;
       const int b = md.nblk == 2 ? s : 0;
       float2* Gb = Gs + (size_t)(b == 0 ? 0 : md.o_blk[0]) * n;
       // four columns i at a time (this half's groups): independent accumulation chains,
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   if (tid == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
   if (!do_g) return;
   float mx = 0.f;
-  if (prow_ok)
+  for (int p = p0; p < n; p += 128)
     for (int i = h; i < gtot; i += NH) {
       const float2 g = Gs[(size_t)i * n + p];
       mx = fmaxf(mx, fmaxf(fabsf(g.x), fabsf(g.y)));
@@ -340,8 +345,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   for (int q = 1; q < NW; ++q) mall = fmaxf(mall, fred[q]);
   const float scl = pow2_scale(mall);
   if (tid == 0) md.g_inv[w] = 1.0f / scl;
-  float e1x = 0.f, e1y = 0.f;  // per-thread partials of <= 32 terms; FP64 across warps
-  if (prow_ok) {
+  float e1x = 0.f, e1y = 0.f;  // per-thread partials of <= 64 terms; FP64 across warps
+  for (int p = p0; p < n; p += 128) {
     for (int i = h; i < gtot; i += NH) {
       const float2 g = Gs[(size_t)i * n + p];
       const int e = i * n + p;
@@ -583,6 +588,7 @@ struct EpiVHS {
     int n, nq, rows, bf16, want_lo;
     float sqdt;
     int sym;  // split GEMM only: columns are the packed (p, q) pairs of sym_decode
+    int mr;   // rows per walker of the V operand (128, or 256 for norb > 128)
   };
   static constexpr int kSmemBytes = 0;
   __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
@@ -597,7 +603,7 @@ struct EpiVHS {
       ptx::tmem_ld_wait();
       const int col = n0 + c0, pr = col / p.nq, q0 = col % p.nq;
       if (R >= p.rows || pr >= p.n) continue;
-      const size_t off = ((size_t)wl * 128 + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0;
+      const size_t off = ((size_t)wl * p.mr + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0;
       uint32_t hw[8], lw[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
@@ -667,7 +673,7 @@ struct EpiVHSSplit {
           const int t = lane + 32 * u, row = t >> 2, part = t & 3, Rr = R0 + row;
           if (Rr < p.rows) {
             const int wl = Rr >> 1, c = Rr & 1;
-            const size_t off = ((size_t)wl * 128 + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0 + part * 8;
+            const size_t off = ((size_t)wl * p.mr + pr) * (2 * p.nq) + (c == 0 ? p.nq : 0) + q0 + part * 8;
             *reinterpret_cast<uint4*>(base + off) =
                 *reinterpret_cast<const uint4*>(stage + row * kSplitStageRow + part * 16);
           }

@@ -6,6 +6,7 @@
 #include "afq_mixed_kernels.cuh"
 #include "afq_prof.cuh"
 #include "afq_prop_fused.cuh"
+#include "afq_prop_wide.cuh"
 
 namespace afq {
 
@@ -688,11 +689,19 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   t.cfg = cfg;
   t.bf16 = (cfg & kUseBf16) != 0;
   t.n = c.norb;
-  if (t.n > 128) {
-    afq_set_error("mixed precision path: norb <= 128 (the Taylor operand lives in shared memory)");
+  if (t.n > 256) {
+    afq_set_error("mixed precision path: norb <= 256");
     return -2;
   }
-  t.nq = t.n <= 64 ? 64 : 128;
+  // norb > 128: two 128-row M tiles in the propagation kernel (k_prop_wide)
+  t.wide = t.n > 128;
+  if (t.wide && (cfg & (kLegacyTaylor | kDiagChol))) {
+    afq_set_error("mixed precision path: norb > 128 runs on the streamed propagation kernel only "
+                  "(no separate Taylor kernel, no diagonal-vector path)");
+    return -2;
+  }
+  t.nq = t.n <= 64 ? 64 : t.n <= 128 ? 128 : 256;
+  t.mr = t.wide ? kWideMR : 128;
   t.nk = rup(t.n, 8);
   t.nw = c.nw;
   t.nwc = nwc;
@@ -768,7 +777,7 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   P->o_rc_inv = L.take((size_t)c.nchol * 4);
   for (int i = 0; i < 2; ++i) P->o_lop[i] = L.take((size_t)t.n * t.nq * t.ldg * H);
   for (int s = 0; s < t.nslab; ++s)
-    for (int i = 0; i < 2; ++i) P->o_eop[s][i] = L.take((size_t)128 * t.nk * H);
+    for (int i = 0; i < 2; ++i) P->o_eop[s][i] = L.take((size_t)t.mr * t.nk * H);
   for (int b = 0; b < t.nblk; ++b) {
     for (int i = 0; i < 2; ++i) P->o_u[b][i] = L.take((size_t)t.kb[b] * t.ldkb[b] * H);
     if (t.nblk == 2) {
@@ -779,7 +788,7 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
   P->o_utmp = L.take(umax * 4);
   for (int i = 0; i < 2; ++i) P->o_gfb[i] = L.take((size_t)2 * t.nw * t.ldfb * H);
   for (int i = 0; i < 2; ++i) P->o_xt[i] = L.take((size_t)2 * t.nw * t.ldg * H);
-  for (int i = 0; i < 2; ++i) P->o_vbuf[i] = L.take((size_t)nwc * 128 * 2 * t.nq * H);
+  for (int i = 0; i < 2; ++i) P->o_vbuf[i] = L.take((size_t)nwc * t.mr * 2 * t.nq * H);
   for (int s = 0; s < t.nslab; ++s)
     for (int i = 0; i < 2; ++i) {
       P->o_wt[s][i] = L.take((size_t)t.nw * t.R[s] * t.nk * H);
@@ -1003,8 +1012,10 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
         TC_CHECK(mk(&m.b[i++], bop[0], rows, t.n, t.nk, t.bn_w[s]));
       }
     }
-    TC_CHECK(mk(&t.m_vt[s][0], t.vbuf[0], (uint64_t)nwc * 128, 2 * t.nq, 2 * t.nq, 128));
-    TC_CHECK(mk(&t.m_vt[s][1], t.vbuf[1], (uint64_t)nwc * 128, 2 * t.nq, 2 * t.nq, 128));
+    TC_CHECK(mk(&t.m_vt[s][0], t.vbuf[0], (uint64_t)nwc * t.mr, 2 * t.nq, 2 * t.nq, 128));
+    TC_CHECK(mk(&t.m_vt[s][1], t.vbuf[1], (uint64_t)nwc * t.mr, 2 * t.nq, 2 * t.nq, 128));
+    TC_CHECK(mk(&t.m_ew[s][0], t.eop[s][0], (uint64_t)t.mr, t.n, t.nk, 128));
+    TC_CHECK(mk(&t.m_ew[s][1], t.eop[s][1], (uint64_t)t.mr, t.n, t.nk, 128));
     TC_CHECK(mk(&t.m_t0[s][0], t.t0[s][0], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
     TC_CHECK(mk(&t.m_t0[s][1], t.t0[s][1], (uint64_t)t.nw * t.NT[s], 2 * t.nq, 2 * t.nq, t.NT[s]));
   }
@@ -1046,6 +1057,7 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
 template <int OM>
 static void launch_green_fused(const MixedDev& md, size_t smem, const float2* w0, const float2* w1, double2* ovl,
                                int flags, cudaStream_t st) {
+  // a refused attribute surfaces as the launch error checked by the caller
   cudaFuncSetAttribute(k_green_fused<OM, kGfThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_green_fused<OM, kGfThreads><<<md.nw, kGfThreads, smem, st>>>(md, w0, w1, ovl, flags);
 }
@@ -1058,17 +1070,16 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
     afq_set_error("mixed precision path: at most %d electrons per spin", kGreenMaxO);
     return -2;
   }
-  if (t.n > 128) {
-    afq_set_error("mixed precision path: at most %d orbitals", 128);
-    return -2;
-  }
   const float2* w0 = static_cast<const float2*>(wu);
   const float2* w1 = static_cast<const float2*>(wd);
   // the walker operand of the exp_h1 GEMMs is needed only when they run as separate launches
-  const int flags = (write_ops || for_propagation) ? ((t.fused ? 0 : kGreenWT) | kGreenG) : 0;
+  const int flags = (write_ops || for_propagation) ? ((t.fused || t.wide ? 0 : kGreenWT) | kGreenG) : 0;
   const int om = omax <= 8 ? 8 : omax <= 16 ? 16 : omax <= 24 ? 24 : 32;
   const size_t smem =
       green_fused_smem(t.n, omax, om, md.o_blk[0] + md.o_blk[1], (flags & kGreenG) != 0, md.nslab);
+  if (int rc = check_smem_optin(smem + sizeof(float2) * 2 * 32 * 33 + 1024,
+                                "mixed Green's-function kernel (norb x electrons too large for one CTA)"))
+    return rc;
   {
     ProfScope _ps(K_GREEN, st);
     if (om == 8) launch_green_fused<8>(md, smem, w0, w1, ovl, flags, st);
@@ -1203,6 +1214,23 @@ static int launch_prop_fused(const TcState& t, int s, const PropDev& pd, cudaStr
   return launch_check("prop_fused");
 }
 
+template <int NP>
+static int launch_prop_wide(const TcState& t, int s, const PropDev& pd, cudaStream_t st) {
+  const size_t smem = prop_wide_smem(t.NT[s]);
+  auto kfn = k_prop_wide<NP>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    afq_set_error("prop_wide: shared-memory attribute: %s", cudaGetErrorString(e));
+    return (int)e;
+  }
+  {
+    ProfScope _ps(K_PROP, st);
+    kfn<<<pd.nwc < t.num_sms ? pd.nwc : t.num_sms, 128 * NP + 64, smem, st>>>(
+        t.m_vt[s][0], t.m_vt[s][1], t.m_ew[s][0], t.m_ew[s][1], pd, t.status);
+  }
+  return launch_check("prop_wide");
+}
+
 // vhs GEMM, then exp_h1 * Taylor * exp_h1 in one kernel per slab, chunk by chunk
 static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, cudaStream_t st) {
   const int nchunks = t.nw / t.nwc;
@@ -1219,6 +1247,7 @@ static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, c
     ev.want_lo = want_lo ? 1 : 0;
     ev.sqdt = (float)sqrt(c.dt);
     ev.sym = t.sym ? 1 : 0;
+    ev.mr = t.mr;
     SplitArgs sa;
     sa.k_tiles = (c.nchol + 63) / 64;
     sa.k_splits = 1;
@@ -1246,6 +1275,13 @@ static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, c
       pd.sym = t.sym ? 1 : 0;
       pd.w = W[s] + (size_t)w0 * t.n * t.o_slab[s];
       const int np = t.NT[s] / 16;
+      if (t.wide) {
+        if (np == 1) TC_CHECK(launch_prop_wide<1>(t, s, pd, st));
+        else if (np == 2) TC_CHECK(launch_prop_wide<2>(t, s, pd, st));
+        else if (np == 3) TC_CHECK(launch_prop_wide<3>(t, s, pd, st));
+        else TC_CHECK(launch_prop_wide<4>(t, s, pd, st));
+        continue;
+      }
       if (np == 1) TC_CHECK(launch_prop_fused<1>(t, s, pd, st));
       else if (np == 2) TC_CHECK(launch_prop_fused<2>(t, s, pd, st));
       else if (np == 3) TC_CHECK(launch_prop_fused<3>(t, s, pd, st));
@@ -1257,7 +1293,7 @@ static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, c
 
 int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
   float2* W[2] = {static_cast<float2*>(wu), static_cast<float2*>(wd)};
-  if (t.fused) return propagate_fused(t, c, W, st);
+  if (t.fused || t.wide) return propagate_fused(t, c, W, st);
   for (int s = 0; s < t.nslab; ++s) TC_CHECK(exp_gemm(t, c, s, false, W[s], st));
   if (t.cfg & kDiagChol) {
     if (t.n > 128) {
@@ -1306,6 +1342,7 @@ int tc_propagate_walkers(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, c
     ev.bf16 = t.bf16 ? 1 : 0;
     ev.want_lo = want_lo ? 1 : 0;
     ev.sym = 0;  // the separate Taylor kernel reads the full V
+    ev.mr = 128;
     ev.sqdt = (float)sqrt(c.dt);
     SplitArgs sa;
     sa.k_tiles = (c.nchol + 63) / 64;
@@ -1397,8 +1434,10 @@ int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
 int tc_orthonormalize(TcState& t, const afq_ctx_dev& c, void* wu, void* wd, cudaStream_t st) {
   for (int s = 0; s < c.nslab; ++s) {
     const int k = c.kslab[s];
-    if (k > 32) return launch_qr<float>(c, wu, wd, st);
     const size_t smem = (size_t)kQrWarps * ((size_t)c.norb * qr_ld(k) + 64) * sizeof(float2);
+    // the warp kernel holds kQrWarps slabs in shared memory; wider or longer slabs take the
+    // one-CTA-per-slab Householder kernel
+    if (k > 32 || smem > 227 * 1024) return launch_qr<float>(c, wu, wd, st);
     cudaFuncSetAttribute(k_qr_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     {
       ProfScope _ps(K_QR, st);

@@ -6,8 +6,9 @@
 //   xt     [2 nw][ldg]        rows (w, re/im), cols g = shifted fields
 //   lop    [norb * nq][ldg]   rows (p, q) (q padded to nq), cols g = chol_g[p][q]; with
 //                             symmetric vectors rows are the packed (p, q) pairs of sym_decode
-//   vbuf   [nwc][128][2 nq]   per walker [Vr | Vi] (rows >= norb and q >= norb zero)
-//   eop[s] [128][nk]          exp_h1_s - I (rows >= norb zero)
+//   vbuf   [nwc][mr][2 nq]    per walker [Vr | Vi] (rows >= norb and q >= norb zero); mr = 128,
+//                             or 256 for norb > 128
+//   eop[s] [mr][nk]           exp_h1_s - I (rows >= norb zero)
 //   wt[s], acc[s] [nw * R_s][nk]  rows (w, 2k + re/im), cols p: walker / Taylor sum
 //   t0[s]  [nw][NT_s][2 nq]   Taylor B operand: row 2k = [Tr | -Ti], row 2k+1 = [Ti | Tr]
 //   u[b]   [kb][ldkb]         rows (i, q), cols (k, p): sum_g rot_chol_b[g,i,p] rot_chol_b[g,k,q]
@@ -110,6 +111,9 @@ struct TcState {
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
   bool fused;               // fused propagation kernel (norb <= 128, <= 32 orbitals per slab)
   bool sym;                 // symmetric Cholesky vectors on the fused path: packed vhs columns
+  bool wide;                // norb > 128: streamed propagation kernel (k_prop_wide)
+  int mr;                   // rows of the per-walker V and exp_h1 - I operands (128 or 256)
+  CUtensorMap m_ew[2][2];   // wide propagation: exp_h1[s] - I hi/lo, boxes of 128 rows
   int n_vcols;              // vhs GEMM columns: norb * nq, or the packed count with sym
   int n_fb_terms, n_vhs_terms, n_e_terms, n_en_terms, taylor_split;
   int drain;                // K tiles per drained accumulation run (0: not drained)

@@ -2,6 +2,9 @@
 FP32 small dense algebra, FP64 log-determinants/weights/sums) against the FP64 oracle on
 identical inputs, through the C ABI.
 
+Cases up to norb 200 cover the wide propagation kernel (two 128-row M tiles, A operands
+streamed from L2) and the Green's-function kernel with two orbital rows per thread.
+
 Tolerances (relative to the largest magnitude of each compared array):
   overlaps 2e-5, force bias 1e-5, local energies 2e-5,
   one-step walkers / weights 2e-5, QR 1e-5, two driver blocks: energies 5e-5.
@@ -23,8 +26,12 @@ CASES = [
     dict(kind="rhf", restricted=True, norb=40, nelec=(9, 9), nchol=70, nw=14),
     dict(kind="rhf", restricted=True, norb=120, nelec=(20, 20), nchol=600, nw=16),
     dict(kind="uhf", restricted=False, norb=60, nelec=(10, 8), nchol=300, nw=12),
+    # norb > 128: two 128-row M tiles, operands streamed through the wide propagation kernel
+    dict(kind="rhf", restricted=True, norb=150, nelec=(25, 25), nchol=300, nw=6),
+    dict(kind="uhf", restricted=False, norb=140, nelec=(12, 9), nchol=200, nw=5),
+    dict(kind="rhf", restricted=True, norb=200, nelec=(32, 32), nchol=400, nw=4),
 ]
-IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40", "rhf-120", "uhf-60"]
+IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40", "rhf-120", "uhf-60", "rhf-150", "uhf-140", "rhf-200"]
 
 
 @pytest.fixture(params=list(range(len(CASES))), ids=IDS)
