@@ -65,7 +65,7 @@ def parse():
                     help="serving pattern: Poisson stream of jobs through the server")
     ap.add_argument("--serving-rate", type=float, default=20.0)
     ap.add_argument("--serving-duration", type=float, default=10.0)
-    ap.add_argument("--serving-norb-max", type=int, default=128)
+    ap.add_argument("--serving-norb-max", type=int, default=200)
     ap.add_argument("--serving-slots", type=int, default=16)
     ap.add_argument("--serving-in-line", type=float, default=5.0,
                     help="seconds of the serving stream run after the headline measurement and reported "

@@ -49,7 +49,7 @@ struct MixedDev {
   double2* ene1;
 };
 
-constexpr int kGreenMaxO = 32;
+constexpr int kGreenMaxO = 40;  // occupied orbitals per slab (S is at most 40 x 40)
 
 // dst[map(e)] = src[e] for e < n by a block of NT threads, 8 independent loads in flight per
 // thread before the shared-memory stores (the copies are latency-bound otherwise)
@@ -139,6 +139,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   extern __shared__ __align__(16) unsigned char sm[];
   constexpr int NW = NT / 32, NH = NT / 128;  // warps; thread groups of 128 (orbital rows)
   constexpr int RPT = (OM + NW - 1) / NW;     // rows of S per thread in the Gauss-Jordan phase
+  constexpr int CPL = (OM + 31) / 32;          // columns of S per lane (lane, lane + 32)
+  constexpr int RB = CPL == 1 ? 5 : 6;         // bits of the row index in the pivot-search key
   const int w = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n = md.n;
   const int p0 = tid & 127, h = tid >> 7;  // orbital rows p0, p0 + 128 (norb <= 256)
   const bool overlay = md.nslab == 1 && n <= 128;  // G overwrites the walker copy
@@ -208,52 +210,74 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
     }
     __syncthreads();
     if (NH == 2) {
-      if (lane < o) {
 #pragma unroll
-        for (int m = 0; m < RPT; ++m) {
-          const int r = warp + NW * m;
-          if (r < o) Ssh[0][r][lane] = cadd(Ssh[0][r][lane], Ssh[1][r][lane]);
+      for (int cc = 0; cc < CPL; ++cc) {
+        const int col = lane + 32 * cc;
+        if (col < o) {
+#pragma unroll
+          for (int m = 0; m < RPT; ++m) {
+            const int r = warp + NW * m;
+            if (r < o) Ssh[0][r][col] = cadd(Ssh[0][r][col], Ssh[1][r][col]);
+          }
         }
       }
       __syncthreads();
     }
     // Gauss-Jordan, double-buffered in shared memory: step j reads Ssh[j & 1] and writes
     // Ssh[(j & 1) ^ 1], so one barrier per pivot; thread (warp, lane) updates rows
-    // warp, warp + 8, .. of column lane.
-    bool used = lane >= o;  // row `lane` already pivoted (the same in every warp)
+    // warp, warp + 8, .. of columns lane (and lane + 32 for more than 32 electrons).
+    bool used[CPL];  // row lane + 32 cc already pivoted (the same in every warp)
+#pragma unroll
+    for (int cc = 0; cc < CPL; ++cc) used[cc] = lane + 32 * cc >= o;
 #pragma unroll 1
     for (int j = 0; j < o; ++j) {
       const int b = j & 1;
       // loads that do not depend on the pivot first: column j (search), own elements, and
       // the column-j factors of the own rows
-      const float2 v = lane < o ? Ssh[b][lane][j] : make_float2(0.f, 0.f);
-      float2 own[RPT], fj[RPT];
+      float2 own[RPT][CPL], fj[RPT];
 #pragma unroll
       for (int m = 0; m < RPT; ++m) {
         const int r = warp + NW * m;
-        own[m] = (r < o && lane < o) ? Ssh[b][r][lane] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int cc = 0; cc < CPL; ++cc)
+          own[m][cc] = (r < o && lane + 32 * cc < o) ? Ssh[b][r][lane + 32 * cc] : make_float2(0.f, 0.f);
         fj[m] = r < o ? Ssh[b][r][j] : make_float2(0.f, 0.f);
       }
-      const float mag = fabsf(v.x) + fabsf(v.y);
-      const unsigned key = used ? 0u : ((__float_as_uint(mag) & ~31u) | (unsigned)(31 - lane));
-      const int pr = 31 - (int)(__reduce_max_sync(0xffffffffu, key) & 31u);
-      if (lane == pr) used = true;
+      unsigned key = 0u;  // |re| + |im| of the candidate rows with the row index in the low bits
+#pragma unroll
+      for (int cc = 0; cc < CPL; ++cc) {
+        const int row = lane + 32 * cc;
+        const float2 v = row < o ? Ssh[b][row][j] : make_float2(0.f, 0.f);
+        const float mag = fabsf(v.x) + fabsf(v.y);
+        const unsigned kc = used[cc] ? 0u
+                                     : ((__float_as_uint(mag) & ~((1u << RB) - 1u)) |
+                                        (unsigned)((1 << RB) - 1 - row));
+        key = kc > key ? kc : key;
+      }
+      const int pr = (1 << RB) - 1 - (int)(__reduce_max_sync(0xffffffffu, key) & ((1u << RB) - 1u));
+#pragma unroll
+      for (int cc = 0; cc < CPL; ++cc)
+        if (lane + 32 * cc == pr) used[cc] = true;
       const float2 pv = Ssh[b][pr][j];
-      const float2 ap = lane < o ? Ssh[b][pr][lane] : make_float2(0.f, 0.f);
       // 1 / pv = conj(pv) / |pv|^2 with pv scaled by a power of two first (no overflow)
       int ex;
       frexpf(fmaxf(fabsf(pv.x), fabsf(pv.y)), &ex);
       const float px = ldexpf(pv.x, -ex), py = ldexpf(pv.y, -ex);
       const float dd = ldexpf(__frcp_rn(fmaf(px, px, py * py)), -ex);
       const float2 inv = make_float2(px * dd, -py * dd);
-      if (lane < o) {
-        const float2 sp = (lane == j) ? inv : cmul(ap, inv);
 #pragma unroll
-        for (int m = 0; m < RPT; ++m) {
-          const int r = warp + NW * m;
-          if (r < o)
-            Ssh[b ^ 1][r][lane] =
-                (r == pr) ? sp : csub((lane == j) ? make_float2(0.f, 0.f) : own[m], cmul(fj[m], sp));
+      for (int cc = 0; cc < CPL; ++cc) {
+        const int col = lane + 32 * cc;
+        if (col < o) {
+          const float2 ap = Ssh[b][pr][col];
+          const float2 sp = (col == j) ? inv : cmul(ap, inv);
+#pragma unroll
+          for (int m = 0; m < RPT; ++m) {
+            const int r = warp + NW * m;
+            if (r < o)
+              Ssh[b ^ 1][r][col] =
+                  (r == pr) ? sp : csub((col == j) ? make_float2(0.f, 0.f) : own[m][cc], cmul(fj[m], sp));
+          }
         }
       }
       if (tid == 0) {
@@ -267,9 +291,13 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
     if (warp == 0) {  // det: FP64 product of the pivots (a shuffle tree), sign of the pivot order
       int cnt = 0;
       double2 pd = c2(1.0, 0.0);
-      if (lane < o) {
-        for (int y = lane + 1; y < o; ++y) cnt += piv_s[lane] > piv_s[y] ? 1 : 0;
-        pd = c2((double)pivv[lane].x, (double)pivv[lane].y);
+#pragma unroll
+      for (int cc = 0; cc < CPL; ++cc) {
+        const int x = lane + 32 * cc;
+        if (x < o) {
+          for (int y = x + 1; y < o; ++y) cnt += piv_s[x] > piv_s[y] ? 1 : 0;
+          pd = cmul(pd, c2((double)pivv[x].x, (double)pivv[x].y));
+        }
       }
       cnt = __reduce_add_sync(0xffffffffu, cnt);
 #pragma unroll
@@ -281,11 +309,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
       __syncthreads();  // the next slab rewrites Ws, Cs and Ssh
       continue;
     }
-    if (lane < o) {
 #pragma unroll
-      for (int m = 0; m < RPT; ++m) {
-        const int r = warp + NW * m;
-        if (r < o) Si[step_s[r] * kGreenMaxO + piv_s[lane]] = Ssh[fbuf][r][lane];
+    for (int cc = 0; cc < CPL; ++cc) {
+      const int col = lane + 32 * cc;
+      if (col < o) {
+#pragma unroll
+        for (int m = 0; m < RPT; ++m) {
+          const int r = warp + NW * m;
+          if (r < o) Si[step_s[r] * kGreenMaxO + piv_s[col]] = Ssh[fbuf][r][col];
+        }
       }
     }
     __syncthreads();

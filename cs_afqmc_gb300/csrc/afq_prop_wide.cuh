@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(128 * NP + 64, 1)
   constexpr int NT = 16 * NP, KQ = kWideKQ, S = kWideStages;
   constexpr uint32_t BT = (uint32_t)NT * 128;  // bytes per B K tile
   constexpr int kProd = 4 * NP, kCtrl = 4 * NP + 1;
+  constexpr uint32_t kCols = 4 * NT <= 256 ? 256 : 512;  // TMEM columns allocated
   unsigned char* ring = smem;  // unit s: A_hi tile, then A_lo tile
   unsigned char* Bh = ring + S * 2 * kPropTile;
   unsigned char* Bl = Bh + KQ * BT;
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(128 * NP + 64, 1)
     ptx::fence_mbar_init();
   }
   if (warp == kCtrl) {
-    ptx::tmem_alloc(tmem_holder, 256);  // D[mt][h] at (2 mt + h) NT
+    ptx::tmem_alloc(tmem_holder, kCols);  // D[mt][h] at (2 mt + h) NT
     ptx::tmem_relinquish();
   }
   ptx::tc_fence_before();
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(128 * NP + 64, 1)
   __syncthreads();
   if (warp == kCtrl) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, 256);
+    ptx::tmem_dealloc(tmem, kCols);
   }
 }
 

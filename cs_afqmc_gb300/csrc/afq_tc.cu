@@ -434,6 +434,77 @@ __global__ void k_split_u(const float* __restrict__ u, long n, const unsigned* _
   }
 }
 
+// ---- exchange matrix on the tensor cores (large systems) --------------------------------
+// U[(i,q),(k,p)] = sum_g rc[g][i,p] rc[g][k,q] is a permutation of X X^T with
+// X[(i,p)][g] = rc[g][i n + p]: X is split into fp16 hi / lo planes under one power-of-two
+// scale, X X^T runs on the persistent split GEMM (three products, drained FP32 accumulation)
+// and the epilogue writes U permuted and unscaled into the FP32 scratch with its max |U|.
+constexpr int kExchangeTensorMinKb = 4096;  // below this the FP64 build (k_prep_u) is kept
+
+// *amax <- max |src| as float bits (non-negative floats order like their bits)
+__global__ void k_amax_f64(const double* __restrict__ src, long n, unsigned* __restrict__ amax) {
+  float mx = 0.f;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    mx = fmaxf(mx, fabsf((float)src[i]));
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(amax, __float_as_uint(mx));
+}
+
+// X[(i,p)][g] (hi / lo, row stride ldg) from rc [nchol][kb] scaled by pow2_scale(*amax_x);
+// 32 x 32 tiles through shared memory
+__global__ void k_prep_xu(const double* __restrict__ rc, int nchol, int kb, int ldg, const unsigned* amax_x,
+                          int bf16, uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, g0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const float scl = pow2_scale(__uint_as_float(*amax_x));
+  for (int r = ty; r < 32; r += 8) {
+    const int g = g0 + r, k = r0 + tx;
+    tile[r][tx] = (g < nchol && k < kb) ? (float)(rc[(size_t)g * kb + k] * (double)scl) : 0.f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int k = r0 + r, g = g0 + tx;
+    if (k < kb && g < nchol) {
+      uint16_t h, l;
+      split16(tile[tx][r], bf16 != 0, h, l);
+      hi[(size_t)k * ldg + g] = h;
+      lo[(size_t)k * ldg + g] = l;
+    }
+  }
+}
+
+// split-GEMM epilogue for U: D[(i,p)][(k,q)] -> u[(i n + q) ldk + k n + p] / scale^2
+struct SplitStoreU {
+  static constexpr bool kWarpStore = false;
+  struct Params {
+    float* u;
+    int kb, n, ldk;
+    const unsigned* amax_x;
+    unsigned* amax_u;
+  };
+  __device__ __forceinline__ static void store(const Params& p, int row, int col0, const float* v, int) {
+    if (row >= p.kb) return;
+    const float s = pow2_scale(__uint_as_float(*p.amax_x)), unscale = 1.0f / (s * s);
+    const int i = row / p.n, pp = row - i * p.n;
+    int k = col0 / p.n, q = col0 - k * p.n;
+    float mx = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < 128; ++j) {
+      if (col0 + j < p.kb) {
+        const float val = v[j] * unscale;
+        p.u[(size_t)(i * p.n + q) * p.ldk + k * p.n + pp] = val;
+        mx = fmaxf(mx, fabsf(val));
+      }
+      if (++q == p.n) {
+        q = 0;
+        ++k;
+      }
+    }
+    atomicMax(p.amax_u, __float_as_uint(mx));
+  }
+};
+
 // vhs B operand: chol [nchol][n*n] -> lop[(p*nq + q)][g], 32x32 tiles through shared memory
 __global__ void k_prep_lop(const double* __restrict__ chol, int nchol, int n, int nq, int ldg, int bf16,
                            uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
@@ -679,7 +750,7 @@ struct Plan {
   size_t o_gfb[2], o_xt[2], o_vbuf[2], o_wt[2][2], o_acc[2][2], o_t0[2][2], o_gblk[2][2];
   size_t o_fbpart;
   size_t o_ginv, o_ene1, o_pshift, o_pfbt, o_cout, o_exc, o_status, o_amax, o_trial32[2], o_rh1[2];
-  size_t o_dchol;
+  size_t o_dchol, o_xu[2];
 };
 
 int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
@@ -715,8 +786,9 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
     walker_rows(t.o_slab[s], &t.R[s], &t.wpt[s]);
     t.bn_w[s] = t.R[s] * t.wpt[s];
     t.NT[s] = rup(2 * t.o_slab[s], 16);
-    if (t.NT[s] > 64) {
-      afq_set_error("mixed precision path: at most 32 electrons per spin");
+    if (t.NT[s] > (t.wide ? 80 : 64)) {
+      afq_set_error("mixed precision path: at most %d electrons per spin%s", t.wide ? 40 : 32,
+                    t.wide ? "" : " for norb <= 128");
       return -2;
     }
   }
@@ -786,6 +858,12 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
     }
   }
   P->o_utmp = L.take(umax * 4);
+  {  // X planes of the tensor-core exchange build (the largest block; blocks reuse them)
+    int kbmax = 0;
+    for (int b = 0; b < t.nblk; ++b) kbmax = t.kb[b] > kbmax ? t.kb[b] : kbmax;
+    for (int i = 0; i < 2; ++i)
+      P->o_xu[i] = L.take(kbmax > kExchangeTensorMinKb ? (size_t)kbmax * t.ldg * H : 256);
+  }
   for (int i = 0; i < 2; ++i) P->o_gfb[i] = L.take((size_t)2 * t.nw * t.ldfb * H);
   for (int i = 0; i < 2; ++i) P->o_xt[i] = L.take((size_t)2 * t.nw * t.ldg * H);
   for (int i = 0; i < 2; ++i) P->o_vbuf[i] = L.take((size_t)nwc * t.mr * 2 * t.nq * H);
@@ -921,10 +999,41 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
       k_prep_rows_scaled<<<c.nchol, 256, 0, st>>>(c.rot_chol[b], t.kb[b], t.ldkb[b], bf, t.rc_blk_inv[b],
                                                   t.rc_blk[b][0], t.rc_blk[b][1]);
     }
-    // exchange matrix of this block: FP64 accumulation, power-of-two scaling, hi/lo split
-    cudaMemsetAsync(amax, 0, 4, st);
-    k_prep_u<<<dim3((t.kb[b] + 31) / 32, (t.kb[b] + 31) / 32), 256, 0, st>>>(c.rot_chol[b], c.nchol, t.kb[b],
-                                                                           t.n, t.ldkb[b], t.u_tmp, amax);
+    // exchange matrix of this block: power-of-two scaling, hi/lo split; built in FP64 on the
+    // SIMT cores, or for large blocks as X X^T on the split tensor-core GEMM
+    cudaMemsetAsync(amax, 0, 8, st);
+    if (t.kb[b] > kExchangeTensorMinKb) {
+      uint16_t* xh = U(P.o_xu[0]);
+      uint16_t* xl = U(P.o_xu[1]);
+      k_amax_f64<<<1024, 256, 0, st>>>(c.rot_chol[b], (long)c.nchol * t.kb[b], amax + 1);
+      k_prep_xu<<<dim3((t.kb[b] + 31) / 32, (c.nchol + 31) / 32), 256, 0, st>>>(c.rot_chol[b], c.nchol, t.kb[b],
+                                                                               t.ldg, amax + 1, bf, xh, xl);
+      SplitMaps xm;
+      memset(&xm, 0, sizeof(xm));
+      TC_CHECK(make_tmap_16(&xm.a_hi, xh, t.kb[b], c.nchol, t.ldg, 128, t.bf16));
+      TC_CHECK(make_tmap_16(&xm.a_lo, xl, t.kb[b], c.nchol, t.ldg, 128, t.bf16));
+      TC_CHECK(make_tmap_16(&xm.b_hi, xh, t.kb[b], c.nchol, t.ldg, kSplitBBox, t.bf16));
+      TC_CHECK(make_tmap_16(&xm.b_lo, xl, t.kb[b], c.nchol, t.ldg, kSplitBBox, t.bf16));
+      SplitArgs ga;
+      ga.m_tiles = (t.kb[b] + 127) / 128;
+      ga.n_tiles = (t.kb[b] + kSplitBN - 1) / kSplitBN;
+      ga.k_tiles = (c.nchol + 63) / 64;
+      ga.k_splits = 1;
+      ga.a_row0 = 0;
+      ga.has_alo = 1;
+      ga.has_blo = 1;
+      ga.drain = t.drain > 0 ? t.drain : ga.k_tiles;
+      ga.idesc = ptx::idesc_f16(128, kSplitBN, t.bf16 ? 1 : 0);
+      int dev = 0, sms = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        sms = 148;
+      SplitStoreU::Params up{t.u_tmp, t.kb[b], t.n, t.ldkb[b], amax + 1, amax};
+      TC_CHECK(launch_split<SplitStoreU>(K_PREP, xm, ga, sms, up, t.status, st));
+    } else {
+      k_prep_u<<<dim3((t.kb[b] + 31) / 32, (t.kb[b] + 31) / 32), 256, 0, st>>>(c.rot_chol[b], c.nchol, t.kb[b],
+                                                                             t.n, t.ldkb[b], t.u_tmp, amax);
+    }
     const long ucount = (long)t.kb[b] * t.ldkb[b];
     k_split_u<<<1024, 256, 0, st>>>(t.u_tmp, ucount, amax, bf, t.u[b][0], t.u[b][1]);
     unsigned amax_h = 0;
@@ -1074,10 +1183,10 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
   const float2* w1 = static_cast<const float2*>(wd);
   // the walker operand of the exp_h1 GEMMs is needed only when they run as separate launches
   const int flags = (write_ops || for_propagation) ? ((t.fused || t.wide ? 0 : kGreenWT) | kGreenG) : 0;
-  const int om = omax <= 8 ? 8 : omax <= 16 ? 16 : omax <= 24 ? 24 : 32;
+  const int om = omax <= 8 ? 8 : omax <= 16 ? 16 : omax <= 24 ? 24 : omax <= 32 ? 32 : 40;
   const size_t smem =
       green_fused_smem(t.n, omax, om, md.o_blk[0] + md.o_blk[1], (flags & kGreenG) != 0, md.nslab);
-  if (int rc = check_smem_optin(smem + sizeof(float2) * 2 * 32 * 33 + 1024,
+  if (int rc = check_smem_optin(smem + sizeof(float2) * 2 * om * (om + 1) + 1024,
                                 "mixed Green's-function kernel (norb x electrons too large for one CTA)"))
     return rc;
   {
@@ -1085,7 +1194,8 @@ int tc_green(TcState& t, const afq_ctx_dev& c, const void* wu, const void* wd, d
     if (om == 8) launch_green_fused<8>(md, smem, w0, w1, ovl, flags, st);
     else if (om == 16) launch_green_fused<16>(md, smem, w0, w1, ovl, flags, st);
     else if (om == 24) launch_green_fused<24>(md, smem, w0, w1, ovl, flags, st);
-    else launch_green_fused<32>(md, smem, w0, w1, ovl, flags, st);
+    else if (om == 32) launch_green_fused<32>(md, smem, w0, w1, ovl, flags, st);
+    else launch_green_fused<40>(md, smem, w0, w1, ovl, flags, st);
   }
   return launch_check("green_fused");
 }
@@ -1279,7 +1389,8 @@ static int propagate_fused(TcState& t, const afq_ctx_dev& c, float2* const* W, c
         if (np == 1) TC_CHECK(launch_prop_wide<1>(t, s, pd, st));
         else if (np == 2) TC_CHECK(launch_prop_wide<2>(t, s, pd, st));
         else if (np == 3) TC_CHECK(launch_prop_wide<3>(t, s, pd, st));
-        else TC_CHECK(launch_prop_wide<4>(t, s, pd, st));
+        else if (np == 4) TC_CHECK(launch_prop_wide<4>(t, s, pd, st));
+        else TC_CHECK(launch_prop_wide<5>(t, s, pd, st));
         continue;
       }
       if (np == 1) TC_CHECK(launch_prop_fused<1>(t, s, pd, st));

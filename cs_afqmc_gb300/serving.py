@@ -283,7 +283,7 @@ class AfqmcServer:
         return results, time.perf_counter() - t0
 
 
-def poisson_requests(rate: float, duration: float, seed: int = 0, norb_range=(20, 128),
+def poisson_requests(rate: float, duration: float, seed: int = 0, norb_range=(20, 200),
                      walkers=(64, 256, 1024), n_steps: int = 100, precision: str = "mixed"):
     """The serving workload: a Poisson stream (rate jobs/s over `duration` s) of independent
     jobs, norb uniform in norb_range, nocc = norb // 6, nchol = 5 norb, walkers drawn from

@@ -30,8 +30,10 @@ CASES = [
     dict(kind="rhf", restricted=True, norb=150, nelec=(25, 25), nchol=300, nw=6),
     dict(kind="uhf", restricted=False, norb=140, nelec=(12, 9), nchol=200, nw=5),
     dict(kind="rhf", restricted=True, norb=200, nelec=(32, 32), nchol=400, nw=4),
+    dict(kind="rhf", restricted=True, norb=198, nelec=(33, 33), nchol=396, nw=4),  # S 33 x 33
 ]
-IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40", "rhf-120", "uhf-60", "rhf-150", "uhf-140", "rhf-200"]
+IDS = ["rhf-r", "rhf-u", "uhf", "tiny", "rhf-40", "rhf-120", "uhf-60", "rhf-150", "uhf-140", "rhf-200",
+       "rhf-198-o33"]
 
 
 @pytest.fixture(params=list(range(len(CASES))), ids=IDS)
