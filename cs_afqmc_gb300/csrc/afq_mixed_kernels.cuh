@@ -101,7 +101,7 @@ constexpr int kGfThreads = 128;  // threads per walker CTA (128 or 256; 128 meas
 // owns two orbital rows); with one slab and norb <= 128 it overwrites the walker copy once
 // G's inputs are in registers
 __host__ __device__ constexpr size_t green_fused_smem(int n, int omax, int om, int gtot, bool g, int nslab) {
-  return (((size_t)n * green_s_ld(omax) * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15) +
+  return (((size_t)n * green_s_ld(omax) * 8 + 15) & ~(size_t)15) +
          (size_t)om * kGreenMaxO * 8 + ((g && (nslab == 2 || n > 128)) ? (size_t)gtot * n * 8 : 0);
 }
 
@@ -133,7 +133,7 @@ __device__ __forceinline__ void copy_rows(float2* dst, const float2* __restrict_
 }
 
 template <int OM, int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md, const float2* __restrict__ wu,
+__global__ void __launch_bounds__(NT, (OM <= 24 ? 640 : 512) / NT) k_green_fused(const MixedDev md, const float2* __restrict__ wu,
                                                                const float2* __restrict__ wd,
                                                                double2* __restrict__ ovl, int flags) {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -149,9 +149,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   const bool do_g = (flags & kGreenG) != 0;
   const int gtot = md.o_blk[0] + md.o_blk[1];
   float2* Ws = reinterpret_cast<float2*>(sm);                    // [n][ld] (columns >= o zero)
-  float* Cs = reinterpret_cast<float*>(Ws + (size_t)n * ldmax);  // [n][o]
-  float2* Si = reinterpret_cast<float2*>(
-      sm + (((size_t)n * ldmax * 8 + (size_t)n * omax * 4 + 15) & ~(size_t)15));  // [OM][kGreenMaxO]
+  float2* Si = reinterpret_cast<float2*>(sm + (((size_t)n * ldmax * 8 + 15) & ~(size_t)15));  // [OM][kGreenMaxO]
   // [gtot][n]: after the walker copy's last use when it overlays it (ld >= o = gtot)
   float2* Gs = overlay ? Ws : Si + OM * kGreenMaxO;
   __shared__ float2 Ssh[2][OM][OM + 1];  // S (partials), then the double-buffered working matrix
@@ -164,11 +162,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
   for (int s = 0; s < md.nslab; ++s) {
     const int o = md.o_slab[s], o4 = (o + 3) & ~3, ld = green_s_ld(o);
     const float2* W = (s == 0 ? wu : wd) + (size_t)w * n * o;
+    const float* __restrict__ Ct = md.trial32[s];  // [n][o] trial in FP32
     if (o4 != o)
       for (int pp = tid; pp < n; pp += NT)
         for (int k = o; k < o4; ++k) Ws[pp * ld + k] = make_float2(0.f, 0.f);
     copy_rows<NT>(Ws, W, n, o, ld);
-    copy_batched<NT>(Cs, md.trial32[s], n * o, [](int e) { return e; });
     __syncthreads();
     for (int p = p0; (flags & kGreenWT) && p < n; p += 128) {  // walker operand of the exp_h1 products: row (w, 2k + c), column p
       uint16_t* hi = md.wt[s][0] + (size_t)w * md.R[s] * md.nk + p;
@@ -194,7 +192,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
       const int p1 = hh + 1 == NH ? n : (hh + 1) * nh;
 #pragma unroll 4
       for (int pp = hh * nh; pp < p1; ++pp) {
-        const float cv = Cs[pp * o + i];
+        const float cv = __ldg(&Ct[pp * o + i]);  // the trial: the same for every walker (L1)
         const float4 x = *reinterpret_cast<const float4*>(&Ws[pp * ld + k0]);
         const float4 y = *reinterpret_cast<const float4*>(&Ws[pp * ld + k0 + 2]);
         a0.x = fmaf(cv, x.x, a0.x); a0.y = fmaf(cv, x.y, a0.y);
@@ -306,7 +304,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
       if (lane == 0) det = cmul(det, (cnt & 1) ? c2(-pd.x, -pd.y) : pd);
     }
     if (!do_g) {
-      __syncthreads();  // the next slab rewrites Ws, Cs and Ssh
+      __syncthreads();  // the next slab rewrites Ws and Ssh
       continue;
     }
 #pragma unroll
@@ -359,7 +357,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_green_fused(const MixedDev md,
         }
       }
     }
-    __syncthreads();  // Ws, Cs, Ssh and Si are rewritten by the next slab
+    __syncthreads();  // Ws, Ssh and Si are rewritten by the next slab
   }
   if (tid == 0 && ovl) ovl[w] = md.restricted_square ? cmul(det, det) : det;
   if (!do_g) return;
@@ -520,7 +518,7 @@ struct FbReduce {
   double2* fb_out;      // non-null: write the force bias instead
 };
 
-__global__ void __launch_bounds__(256) k_fb_reduce(const FbReduce r) {
+__global__ void __launch_bounds__(256, 3) k_fb_reduce(const FbReduce r) {
   __shared__ double red[32];
   const int w = blockIdx.x;
   const float gi = r.g_inv[w];
