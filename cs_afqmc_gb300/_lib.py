@@ -138,6 +138,7 @@ _TEST_SIGS = {
     "afq_test_gemm_split": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, _vp, _vp]),
+    "afq_test_split_pairs": (ctypes.c_int, [ctypes.c_int]),
 }
 _SIGS.update(_TEST_SIGS)
 

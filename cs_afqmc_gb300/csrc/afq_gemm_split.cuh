@@ -1,15 +1,16 @@
 // Persistent split-precision tcgen05 GEMM: D[M x N] = A_hi B_hi^T + A_lo B_hi^T + A_hi B_lo^T
 // (x ~ hi + lo, 16-bit planes; the lo terms are optional), for the large contractions whose
-// operands are both dense planes (vhs = i sqrt(dt) x~ . chol).
+// operands are both dense planes (vhs = i sqrt(dt) x~ . chol, force bias, exchange matrix).
 //
 // Against the tile-per-CTA core (afq_gemm.cuh) it changes three things:
 //  * each K tile loads the four planes once (A_hi, A_lo, B_hi, B_lo) and issues the three
 //    products from them, instead of re-loading A_hi and B_hi for every term;
 //  * 128 x 256 output tiles (131 flop per loaded byte with both lo terms);
-//  * one CTA per SM loops over tiles. The TMA warp runs ahead across tile boundaries, the
-//    MMA warp alternates between two 256-column TMEM accumulators, and eight epilogue warps
-//    keep the running FP32 sums in registers, so a tile's stores overlap the next tile's
-//    main loop.
+//  * one CTA (or CTA pair) per SM loops over tiles. The TMA warp runs ahead across tile
+//    boundaries, the MMA warp alternates between two 256-column TMEM accumulators, and eight
+//    epilogue warps keep the running FP32 sums in registers, so a tile's stores overlap the
+//    next tile's main loop for two accumulation runs. (A tcgen05.mma costs about the same
+//    for N = 128 as for N = 256, so narrower tiles with more accumulators run slower.)
 //
 // Accumulation: the tensor core truncates when it adds into its FP32 accumulator (about
 // 6e-9 * K relative bias over a long sum). The MMAs of every `drain` K tiles go into a fresh
@@ -17,11 +18,20 @@
 // K tile the small correction products are issued before hi*hi so that they meet a small
 // accumulator.
 //
-// Warp roles (320 threads): warp 0 lane 0 issues TMA loads into a two-deep ring of K-tile
-// units; warp 1 owns the TMEM allocation (512 columns) and lane 0 issues the MMAs; warps
-// 2..9 drain the accumulators: warp w reads TMEM lanes 32*(w%4).. and columns
-// 128*((w-2)/4).. (thread = output row, 128 columns per thread). Every wait is bounded: on a
-// timeout the CTA records a nonzero word in *status, stops, and still frees its TMEM.
+// Warp roles (320 threads): warp 0 lane 0 issues TMA loads into a ring of K-tile units; warp
+// 1 owns the TMEM allocation (512 columns) and lane 0 issues the MMAs; warps 2..9 drain the
+// accumulators: warp w reads TMEM lanes 32*(w%4).. and columns 128*((w-2)/4).. (thread =
+// output row, 128 columns per thread). Every wait is bounded: on a timeout the CTA records a
+// nonzero word in *status, stops, and still frees its TMEM.
+//
+// CTA pairs (CG = 2, clusters of two CTAs): a tile is 256 rows x 256 columns and one
+// tcgen05.mma.cta_group::2 (M = 256) issued by the even CTA covers both SMs. Each CTA loads
+// its own 128 A rows and its own half (128 rows) of the B tile with plain TMA loads into its
+// own shared memory (64 KB per K tile instead of 96 KB; three-deep ring). The loads of both
+// CTAs complete on the even CTA's `full` barrier; the even CTA's MMA thread releases stages
+// and accumulators with one commit per CTA; the odd CTA's epilogue warps arrive remotely on
+// the even CTA's `accempty` barriers. Each CTA drains and stores its own 128 accumulator rows
+// from its own TMEM.
 #pragma once
 #include "afq_ptx.cuh"
 
@@ -32,15 +42,20 @@ struct SplitMaps {
 };
 
 constexpr int kSplitThreads = 320;
-constexpr int kSplitBN = 256;
-constexpr int kSplitStages = 2;
-constexpr int kSplitA = 128 * 128;                      // bytes of one A plane per K tile
-constexpr int kSplitB = kSplitBN * 128;                 // bytes of one B plane per K tile
-constexpr int kSplitBBox = 128;                         // rows per B TMA box (half a tile)
-constexpr int kSplitUnit = 2 * kSplitA + 2 * kSplitB;   // one K tile, four planes
-constexpr int kSplitStageRow = 80;                      // bytes per row of an epilogue staging buffer
+constexpr int kSplitBN = 256;                            // output columns per tile
+constexpr int kSplitBBox = 128;                          // rows per B TMA box
+constexpr int kSplitA = 128 * 128;                       // bytes of one A plane per K tile
+constexpr int kSplitB = kSplitBN * 128;                  // bytes of one B plane (all tile rows) per K tile
+constexpr int kSplitRing = 3 * 65536;                    // K-tile ring in shared memory
+constexpr int kSplitStages = 2;                          // single CTA: 96 KB units
+constexpr int kSplitUnit = 2 * kSplitA + 2 * kSplitB;
+constexpr int kSplitStages2 = 3;                         // CTA pair: 64 KB units (half of B)
+constexpr int kSplitUnit2 = 2 * kSplitA + 2 * (kSplitB / 2);
+constexpr int kSplitStageRow = 80;                       // bytes per row of an epilogue staging buffer
 constexpr int kSplitStageWarp = 32 * kSplitStageRow;     // one buffer per epilogue warp
-constexpr int kSplitSmem = 1024 + kSplitStages * kSplitUnit + 256 + 8 * kSplitStageWarp;
+constexpr int kSplitSmem = 1024 + kSplitRing + 256 + 8 * kSplitStageWarp;
+static_assert(kSplitStages * kSplitUnit <= kSplitRing && kSplitStages2 * kSplitUnit2 <= kSplitRing,
+              "K-tile ring");
 
 struct SplitArgs {
   int m_tiles, n_tiles, k_tiles;
@@ -49,7 +64,7 @@ struct SplitArgs {
   int has_alo;     // A_lo * B_hi term
   int has_blo;     // B_lo * A_hi term
   int drain;       // K tiles per accumulation run (>= 1)
-  uint32_t idesc;  // M = 128, N = 256
+  uint32_t idesc;  // M = 128 (256 for CTA pairs), N = kSplitBN
 };
 
 // Epi::store(params, row, col0, v, ks): row of D (global row index without a_row0), 128
@@ -58,45 +73,61 @@ struct SplitArgs {
 // kWarpStore provides store_warp(params, row0, lane, col0, v, ks, stage) instead, called by
 // all 32 lanes of the warp (rows row0 + lane) with a kSplitStageWarp-byte shared-memory
 // buffer of its own.
-template <class Epi>
+template <class Epi, int CG = 1>
 __global__ void __launch_bounds__(kSplitThreads, 1)
     k_gemm_split(const __grid_constant__ SplitMaps maps, const SplitArgs g,
                  const __grid_constant__ typename Epi::Params ep, int* status) {
+  static_assert(CG == 1 || CG == 2, "one CTA or a CTA pair per tile");
+  constexpr int STAGES = CG == 2 ? kSplitStages2 : kSplitStages;
+  constexpr int UNIT = CG == 2 ? kSplitUnit2 : kSplitUnit;
+  constexpr int BPL = kSplitB / CG;  // bytes of one B plane per CTA and K tile
+  constexpr int NBOX = kSplitBN / CG / kSplitBBox;  // B boxes per plane per CTA
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kSplitStages * kSplitUnit);
-  uint64_t* empty = full + kSplitStages;
-  uint64_t* accfull = empty + kSplitStages;  // [2]
-  uint64_t* accempty = accfull + 2;          // [2]
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kSplitRing);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accfull = empty + STAGES;  // [2]
+  uint64_t* accempty = accfull + 2;    // [2]
   uint64_t* done = accempty + 2;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(done + 1);
+  unsigned char* stage_base = smem + kSplitRing + 256;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cid = blockIdx.x, ncl = gridDim.x;
-  const int mt = g.m_tiles;
+  const uint32_t rank = CG == 2 ? ptx::cluster_ctarank() : 0u;
+  const bool leader = rank == 0;
+  const int cid = blockIdx.x / CG, ncl = gridDim.x / CG;
+  const int mt = (g.m_tiles + CG - 1) / CG;  // row blocks of 128 * CG rows
   const int ntiles = mt * g.n_tiles * g.k_splits;
   const int kps = (g.k_tiles + g.k_splits - 1) / g.k_splits;  // K tiles per split
-  const uint32_t tx_bytes = kSplitA * (g.has_alo ? 2 : 1) + kSplitB * (g.has_blo ? 2 : 1);
+  const uint32_t tx_cta = kSplitA * (g.has_alo ? 2 : 1) + BPL * (g.has_blo ? 2 : 1);
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kSplitStages; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       ptx::mbar_init(&full[s], 1);
       ptx::mbar_init(&empty[s], 1);
     }
     for (int a = 0; a < 2; ++a) {
       ptx::mbar_init(&accfull[a], 1);
-      ptx::mbar_init(&accempty[a], 8);  // one arrival per epilogue warp
+      ptx::mbar_init(&accempty[a], 8 * CG);  // one arrival per epilogue warp of the pair
     }
     ptx::mbar_init(done, 1);
     ptx::fence_mbar_init();
   }
   if (warp == 1) {
-    ptx::tmem_alloc(tmem_holder, 512);
-    ptx::tmem_relinquish();
+    if constexpr (CG == 2) {
+      ptx::tmem_alloc_pair(tmem_holder, 512);
+      ptx::tmem_relinquish_pair();
+    } else {
+      ptx::tmem_alloc(tmem_holder, 512);
+      ptx::tmem_relinquish();
+    }
   }
   ptx::tc_fence_before();
-  __syncthreads();
+  if constexpr (CG == 2)
+    ptx::cluster_sync();  // the peer's barriers are initialised before any remote arrival
+  else
+    __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
   bool ok = true;
@@ -109,96 +140,143 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       if (g.has_blo) ptx::prefetch_tmap(&maps.b_lo);
       int it = 0;
       for (int tile = cid; tile < ntiles && ok; tile += ncl) {
-        const int m0 = (tile % mt) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
+        const int m0 = (tile % mt) * 128 * CG + (int)rank * 128;
+        const int nb = ((tile / mt) % g.n_tiles) * kSplitBN + (int)rank * (kSplitBN / CG);
         const int ks = tile / (mt * g.n_tiles);
         const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
         for (int kt = ka; kt < kb; ++kt, ++it) {
-          const int s = it % kSplitStages, r = it / kSplitStages;
-          if (r > 0 && !ptx::mbar_wait(&empty[s], (r - 1) & 1)) {
-            ok = false;
-            break;
+          const int s = it % STAGES, r = it / STAGES;
+          if (r > 0) {
+            const bool got = CG == 2 ? ptx::mbar_wait_cluster(&empty[s], (r - 1) & 1)
+                                     : ptx::mbar_wait(&empty[s], (r - 1) & 1);
+            if (!got) {
+              ok = false;
+              break;
+            }
           }
-          unsigned char* u = smem + s * kSplitUnit;
-          ptx::mbar_expect_tx(&full[s], tx_bytes);
-          ptx::tma_load_2d(u, &maps.a_hi, &full[s], kt * 64, g.a_row0 + m0);
-          if (g.has_alo) ptx::tma_load_2d(u + kSplitA, &maps.a_lo, &full[s], kt * 64, g.a_row0 + m0);
+          unsigned char* u = smem + s * UNIT;
+          if constexpr (CG == 2) {
+            // both CTAs' loads complete on the even CTA's barrier, which expects the pair's bytes
+            const uint32_t fb = ptx::mapa_shared(&full[s], 0);
+            if (leader) ptx::mbar_expect_tx(&full[s], 2 * tx_cta);
+            ptx::tma_load_2d_pair(u, &maps.a_hi, fb, kt * 64, g.a_row0 + m0);
+            if (g.has_alo) ptx::tma_load_2d_pair(u + kSplitA, &maps.a_lo, fb, kt * 64, g.a_row0 + m0);
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {
-            const int hb = hh * kSplitBBox * 128;
-            ptx::tma_load_2d(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, n0 + hh * kSplitBBox);
-            if (g.has_blo)
-              ptx::tma_load_2d(u + 2 * kSplitA + kSplitB + hb, &maps.b_lo, &full[s], kt * 64, n0 + hh * kSplitBBox);
+            for (int hh = 0; hh < NBOX; ++hh) {
+              const int hb = hh * kSplitBBox * 128;
+              ptx::tma_load_2d_pair(u + 2 * kSplitA + hb, &maps.b_hi, fb, kt * 64, nb + hh * kSplitBBox);
+              if (g.has_blo)
+                ptx::tma_load_2d_pair(u + 2 * kSplitA + BPL + hb, &maps.b_lo, fb, kt * 64, nb + hh * kSplitBBox);
+            }
+          } else {
+            ptx::mbar_expect_tx(&full[s], tx_cta);
+            ptx::tma_load_2d(u, &maps.a_hi, &full[s], kt * 64, g.a_row0 + m0);
+            if (g.has_alo) ptx::tma_load_2d(u + kSplitA, &maps.a_lo, &full[s], kt * 64, g.a_row0 + m0);
+#pragma unroll
+            for (int hh = 0; hh < NBOX; ++hh) {
+              const int hb = hh * kSplitBBox * 128;
+              ptx::tma_load_2d(u + 2 * kSplitA + hb, &maps.b_hi, &full[s], kt * 64, nb + hh * kSplitBBox);
+              if (g.has_blo)
+                ptx::tma_load_2d(u + 2 * kSplitA + BPL + hb, &maps.b_lo, &full[s], kt * 64, nb + hh * kSplitBBox);
+            }
           }
         }
       }
-      // never leave a copy in flight: wait for the last round issued on each stage
-      for (int j = it - 1; j >= 0 && j >= it - kSplitStages; --j)
-        if (!ptx::mbar_wait(&full[j % kSplitStages], (j / kSplitStages) & 1)) ok = false;
+      // never leave a copy in flight: wait for the last round issued on each stage (the even
+      // CTA's barrier counts the odd CTA's bytes too; the odd CTA cannot leave before the
+      // closing cluster barrier, which the even CTA reaches after this wait)
+      if (leader)
+        for (int j = it - 1; j >= 0 && j >= it - STAGES; --j) {
+          const bool got = CG == 2 ? ptx::mbar_wait_cluster(&full[j % STAGES], (j / STAGES) & 1)
+                                   : ptx::mbar_wait(&full[j % STAGES], (j / STAGES) & 1);
+          if (!got) ok = false;
+        }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
+    if (lane == 0 && leader) {
       int it = 0, grun = 0;
+      uint32_t peer_empty = 0, peer_accfull = 0;
+      if constexpr (CG == 2) {
+        peer_empty = ptx::mapa_shared(empty, 1);
+        peer_accfull = ptx::mapa_shared(accfull, 1);
+      }
       for (int tile = cid; tile < ntiles && ok; tile += ncl) {
         const int ks = tile / (mt * g.n_tiles);
         const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
         const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
         for (int run = 0; run < runs_per_tile && ok; ++run, ++grun) {
           const int a = grun & 1;
-          if (grun >= 2 && !ptx::mbar_wait(&accempty[a], ((grun - 2) >> 1) & 1)) {
-            ok = false;
-            break;
+          if (grun >= 2) {
+            const bool got = CG == 2 ? ptx::mbar_wait_cluster(&accempty[a], ((grun - 2) >> 1) & 1)
+                                     : ptx::mbar_wait(&accempty[a], ((grun - 2) >> 1) & 1);
+            if (!got) {
+              ok = false;
+              break;
+            }
           }
           ptx::tc_fence_after();
           const uint32_t dacc = tmem + (uint32_t)(a * kSplitBN);
           const int kt0 = ka + run * g.drain, kt1 = min(kb, kt0 + g.drain);
           for (int kt = kt0; kt < kt1; ++kt, ++it) {
-            const int s = it % kSplitStages, r = it / kSplitStages;
-            if (!ptx::mbar_wait(&full[s], r & 1)) {
+            const int s = it % STAGES, r = it / STAGES;
+            const bool got = CG == 2 ? ptx::mbar_wait_cluster(&full[s], r & 1) : ptx::mbar_wait(&full[s], r & 1);
+            if (!got) {
               ok = false;
               break;
             }
             ptx::tc_fence_after();
-            const uint32_t ua = ptx::smem_u32(smem + s * kSplitUnit);
-            const uint32_t ahi = ua, alo = ua + kSplitA, bhi = ua + 2 * kSplitA, blo = bhi + kSplitB;
+            const uint32_t ua = ptx::smem_u32(smem + s * UNIT);
+            const uint32_t ahi = ua, alo = ua + kSplitA, bhi = ua + 2 * kSplitA, blo = bhi + BPL;
             bool first = kt == kt0;
+            auto mma = [&](uint32_t ad, uint32_t bd) {
+              const uint64_t da = ptx::desc_kmajor_sw128(ad), db = ptx::desc_kmajor_sw128(bd);
+              if constexpr (CG == 2)
+                ptx::mma_f16_pair(dacc, da, db, g.idesc, first ? 0u : 1u);
+              else
+                ptx::mma_f16(dacc, da, db, g.idesc, first ? 0u : 1u);
+              first = false;
+            };
             // correction products first, then hi * hi
             if (g.has_alo) {
 #pragma unroll
-              for (int kk = 0; kk < 4; ++kk) {
-                ptx::mma_f16(dacc, ptx::desc_kmajor_sw128(alo + kk * 32), ptx::desc_kmajor_sw128(bhi + kk * 32),
-                             g.idesc, first ? 0u : 1u);
-                first = false;
-              }
+              for (int kk = 0; kk < 4; ++kk) mma(alo + kk * 32, bhi + kk * 32);
             }
             if (g.has_blo) {
 #pragma unroll
-              for (int kk = 0; kk < 4; ++kk) {
-                ptx::mma_f16(dacc, ptx::desc_kmajor_sw128(ahi + kk * 32), ptx::desc_kmajor_sw128(blo + kk * 32),
-                             g.idesc, first ? 0u : 1u);
-                first = false;
-              }
+              for (int kk = 0; kk < 4; ++kk) mma(ahi + kk * 32, blo + kk * 32);
             }
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              ptx::mma_f16(dacc, ptx::desc_kmajor_sw128(ahi + kk * 32), ptx::desc_kmajor_sw128(bhi + kk * 32),
-                           g.idesc, first ? 0u : 1u);
-              first = false;
+            for (int kk = 0; kk < 4; ++kk) mma(ahi + kk * 32, bhi + kk * 32);
+            if constexpr (CG == 2) {
+              ptx::mma_commit_pair(ptx::smem_u32(&empty[s]));
+              ptx::mma_commit_pair(peer_empty + (uint32_t)(s * 8));
+            } else {
+              ptx::mma_commit(&empty[s]);
             }
-            ptx::mma_commit(&empty[s]);
           }
-          ptx::mma_commit(&accfull[a]);
+          if constexpr (CG == 2) {
+            ptx::mma_commit_pair(ptx::smem_u32(&accfull[a]));
+            ptx::mma_commit_pair(peer_accfull + (uint32_t)(a * 8));
+          } else {
+            ptx::mma_commit(&accfull[a]);
+          }
         }
       }
       // every MMA issued has completed before TMEM is released
-      ptx::mma_commit(done);
+      if constexpr (CG == 2)
+        ptx::mma_commit_pair(ptx::smem_u32(done));
+      else
+        ptx::mma_commit(done);
       if (!ptx::mbar_wait(done, 0)) ok = false;
     }
   } else {
     const int q = warp & 3, half = (warp - 2) >> 2;
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+    uint32_t acc_empty_bar = 0;
+    if constexpr (CG == 2) acc_empty_bar = ptx::mapa_shared(accempty, 0);
     int grun = 0;
     for (int tile = cid; tile < ntiles && ok; tile += ncl) {
-      const int m0 = (tile % mt) * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
+      const int m0 = (tile % mt) * 128 * CG + (int)rank * 128, n0 = ((tile / mt) % g.n_tiles) * kSplitBN;
       const int ks = tile / (mt * g.n_tiles);
       const int ka = ks * kps, kb = min(g.k_tiles, ka + kps);
       const int runs_per_tile = kb > ka ? (kb - ka + g.drain - 1) / g.drain : 0;
@@ -208,7 +286,9 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       for (int run = 0; run < runs_per_tile; ++run, ++grun) {
         const int a = grun & 1;
         // warp-uniform outcome: the TMEM loads below are .sync.aligned
-        if (!__all_sync(0xffffffffu, ptx::mbar_wait(&accfull[a], (grun >> 1) & 1))) {
+        const bool got = CG == 2 ? ptx::mbar_wait_cluster(&accfull[a], (grun >> 1) & 1)
+                                 : ptx::mbar_wait(&accfull[a], (grun >> 1) & 1);
+        if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
         }
@@ -225,22 +305,32 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
         }
         ptx::tc_fence_before();
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(&accempty[a]);
+        if (lane == 0) {
+          if constexpr (CG == 2)
+            ptx::mbar_arrive_cluster(acc_empty_bar + (uint32_t)(a * 8));
+          else
+            ptx::mbar_arrive(&accempty[a]);
+        }
       }
       if (!ok) break;
       if constexpr (Epi::kWarpStore)
-        Epi::store_warp(ep, m0 + q * 32, lane, n0 + half * 128, sum, ks,
-                        smem + kSplitStages * kSplitUnit + 256 + (warp - 2) * kSplitStageWarp);
+        Epi::store_warp(ep, m0 + q * 32, lane, n0 + half * 128, sum, ks, stage_base + (warp - 2) * kSplitStageWarp);
       else
         Epi::store(ep, m0 + q * 32 + lane, n0 + half * 128, sum, ks);
     }
   }
   if (!ok) atomicOr(status, 4);
   ptx::tc_fence_before();
-  __syncthreads();
+  if constexpr (CG == 2)
+    ptx::cluster_sync();  // the even CTA's MMAs into this CTA's TMEM and shared memory are done
+  else
+    __syncthreads();
   if (warp == 1) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, 512);
+    if constexpr (CG == 2)
+      ptx::tmem_dealloc_pair(tmem, 512);
+    else
+      ptx::tmem_dealloc(tmem, 512);
   }
 }
 

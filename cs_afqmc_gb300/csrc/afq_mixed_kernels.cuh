@@ -661,33 +661,44 @@ struct EpiVHSSplit {
   static constexpr bool kWarpStore = true;
   // Rows R0 + lane (walker R / 2, real (even R) or imaginary part) and 128 columns col0.. of
   // vhs, i.e. (orbital pr, q) pairs, into the Taylor operand V = [Vr | Vi] per walker. Per 32
-  // columns each lane converts its row to fp16 hi / lo and stages one plane at a time in
-  // shared memory (80-byte rows), then four lanes store each row's 64 contiguous bytes: a
-  // warp's stores cover 8 rows x 64 B instead of 32 separate 16-byte pieces.
+  // columns each lane converts its row to fp16 hi / lo (two values per conversion
+  // instruction) and stages one plane at a time in shared memory (80-byte rows), then four
+  // lanes store each row's 64 contiguous bytes: a warp's stores cover 8 rows x 64 B instead of
+  // 32 separate 16-byte pieces. A 32-column group never crosses a row run (runs are multiples
+  // of 32 long and start at multiples of 32), so (pr, q0) is decoded once per tile and then
+  // advanced.
   __device__ __forceinline__ static void store_warp(const Params& p, int R0, int lane, int col0, const float* v, int,
                                                     unsigned char* stage) {
     const int R = R0 + lane;
     const bool bf = p.bf16 != 0;
     const float scale = (R & 1) == 0 ? p.sqdt : -p.sqdt;
+    int pr, q0;
+    if (p.sym)
+      sym_decode(p.n, p.nq, col0, pr, q0);
+    else {
+      pr = col0 / p.nq;
+      q0 = col0 % p.nq;
+    }
 #pragma unroll
     for (int c32 = 0; c32 < 128; c32 += 32) {
-      const int col = col0 + c32;
-      int pr, q0;
-      if (p.sym)
-        sym_decode(p.n, p.nq, col, pr, q0);  // the 32 columns stay inside one row run
-      else {
-        pr = col / p.nq;
-        q0 = col % p.nq;
-      }
-      if (pr >= p.n) continue;  // warp-uniform
+      if (pr >= p.n) break;  // warp-uniform
       uint32_t hw[16], lw[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        uint16_t h0, l0, h1, l1;
-        split16(v[c32 + 2 * j] * scale, bf, h0, l0);
-        split16(v[c32 + 2 * j + 1] * scale, bf, h1, l1);
-        hw[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        lw[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        const float a = v[c32 + 2 * j] * scale, b = v[c32 + 2 * j + 1] * scale;
+        if (bf) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+          const float2 hf = __bfloat1622float2(h);
+          const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+          hw[j] = *reinterpret_cast<const uint32_t*>(&h);
+          lw[j] = *reinterpret_cast<const uint32_t*>(&l);
+        } else {
+          const __half2 h = __floats2half2_rn(a, b);
+          const float2 hf = __half22float2(h);
+          const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+          hw[j] = *reinterpret_cast<const uint32_t*>(&h);
+          lw[j] = *reinterpret_cast<const uint32_t*>(&l);
+        }
       }
 #pragma unroll
       for (int plane = 0; plane < 2; ++plane) {
@@ -709,6 +720,12 @@ struct EpiVHSSplit {
           }
         }
         __syncwarp();
+      }
+      // next 32 columns: same row run, or the start of the next row's run
+      q0 += 32;
+      if (q0 >= p.nq) {
+        ++pr;
+        q0 = p.sym ? 32 * (pr >> 5) : 0;
       }
     }
   }

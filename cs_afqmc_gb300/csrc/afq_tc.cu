@@ -94,6 +94,11 @@ static int launch_gemm(int cls, const GemmMaps& maps, int nterms, int k_tiles, i
 }
 
 // persistent split-precision GEMM (afq_gemm_split.cuh): one CTA per SM, at most one per tile.
+// With two or more M tiles the tiles go to CTA pairs (clusters of two, one 256-row MMA over
+// both SMs, each CTA loading its own half of B); the grid is then twice the number of
+// co-resident pairs, or of tiles if fewer. split_pairs(0) keeps the single-CTA kernel.
+static int g_split_pairs = 1;
+
 template <class Epi>
 static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms,
                         const typename Epi::Params& ep, int* status, cudaStream_t st) {
@@ -102,7 +107,43 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
     afq_set_error("split gemm: bad sizes");
     return -1;
   }
-  auto kfn = k_gemm_split<Epi>;
+  const bool bf16 = ((g.idesc >> 7) & 1u) != 0;
+  if (g_split_pairs && g.m_tiles >= 2) {
+    auto kfn = k_gemm_split<Epi, 2>;
+    cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
+    g.idesc = ptx::idesc_f16(256, kSplitBN, bf16 ? 1 : 0);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kSplitThreads);
+    cfg.dynamicSmemBytes = kSplitSmem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(num_sms - (num_sms & 1));
+    int maxc = 0;
+    if (cudaOccupancyMaxActiveClusters(&maxc, kfn, &cfg) != cudaSuccess || maxc < 1) {
+      cudaGetLastError();
+      maxc = num_sms / 2;
+    }
+    const int pair_tiles = (g.m_tiles + 1) / 2 * g.n_tiles * g.k_splits;
+    const int npairs = pair_tiles < maxc ? pair_tiles : maxc;
+    cfg.gridDim = dim3(2 * npairs);
+    cudaError_t e;
+    {
+      ProfScope _ps(cls, st);
+      e = cudaLaunchKernelEx(&cfg, kfn, maps, g, ep, status);
+    }
+    if (e != cudaSuccess) {
+      afq_set_error("gemm_split (CTA pairs): %s", cudaGetErrorString(e));
+      return (int)e;
+    }
+    return launch_check("gemm_split");
+  }
+  auto kfn = k_gemm_split<Epi, 1>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSplitSmem);
   const int grid = ntiles < num_sms ? ntiles : num_sms;
   {
@@ -829,9 +870,20 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
     cudaGetLastError();  // a host without a device leaves an error behind
     const int mt2 = (2 * c.nw + 127) / 128, nt2 = (c.nchol + kSplitBN - 1) / kSplitBN;
     const int kt = (t.kfb + 63) / 64;
-    int ks = (sms + mt2 * nt2 - 1) / (mt2 * nt2);
-    if (ks > kt / 4) ks = kt / 4;
-    t.fb_ks = ks < 1 ? 1 : ks;
+    const bool pairs = g_split_pairs && mt2 >= 2;  // the launch's form (CTA pairs share an M tile pair)
+    const int workers = pairs ? sms / 2 : sms, units = (pairs ? (mt2 + 1) / 2 : mt2) * nt2;
+    // K splits minimising (tile rounds) x (K tiles per split); ties to fewer partials
+    int best = 1;
+    long best_cost = -1;
+    for (int ks = 1; ks <= (kt / 4 > 1 ? kt / 4 : 1); ++ks) {
+      const long rounds = ((long)units * ks + workers - 1) / workers;
+      const long cost = rounds * ((kt + ks - 1) / ks);
+      if (best_cost < 0 || cost < best_cost) {
+        best_cost = cost;
+        best = ks;
+      }
+    }
+    t.fb_ks = best;
     t.fb_npad = nt2 * kSplitBN;
   }
   t.n_fb_terms = 1 + ((cfg & kFbDyn) ? 1 : 0) + ((cfg & kFbStat) ? 1 : 0);
@@ -1594,6 +1646,12 @@ extern "C" int afq_test_gemm_split(const void* a_hi, const void* a_lo, const voi
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 148;
   SplitStoreF32::Params ep{d, M, N, (long)N};
   return launch_split<SplitStoreF32>(K_PREP, maps, g, sms, ep, status, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int afq_test_split_pairs(int enable) {
+  const int prev = afq::g_split_pairs;
+  if (enable >= 0) afq::g_split_pairs = enable ? 1 : 0;
+  return prev;
 }
 
 extern "C" int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stride,

@@ -26,12 +26,18 @@ int afq_test_gemm_f16(const void* a, const void* b, int nterms, long a_term_stri
                       int bf16, int bn, int drain, int* status, void* stream);
 
 /* D[M,N] (fp32) = A_hi B_hi^T + A_lo B_hi^T + A_hi B_lo^T with the persistent split GEMM
- * (128 x 256 tiles, one CTA per SM). a_lo / b_lo may be NULL (term left out). All planes
- * K-major with leading dimensions lda / ldb (multiples of 8). drain: K tiles per
- * accumulation run, 0 = one run over all of K. */
+ * (128 x 256 tiles per CTA; with M > 128, 256 x 256 tiles per CTA pair unless pairs are
+ * switched off). a_lo / b_lo may be NULL (term left out). All planes K-major with leading
+ * dimensions lda / ldb (multiples of 8). drain: K tiles per accumulation run, 0 = one run
+ * over all of K. */
 int afq_test_gemm_split(const void* a_hi, const void* a_lo, const void* b_hi, const void* b_lo,
                         float* d, int M, int N, int K, int lda, int ldb, int bf16, int drain,
                         int* status, void* stream);
+
+/* Library-wide choice of the split GEMM's form for every later launch (library GEMMs
+ * included): enable = 1 CTA pairs (the default), 0 one CTA per tile, < 0 no change.
+ * Returns the previous setting. Not thread-safe: for tests and timing comparisons. */
+int afq_test_split_pairs(int enable);
 
 #ifdef __cplusplus
 }

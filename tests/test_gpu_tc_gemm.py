@@ -45,12 +45,23 @@ SPLIT_SHAPES = [(128, 256, 64), (300, 700, 600), (2048, 15360, 600), (130, 250, 
                 (512, 1024, 2400)]
 
 
+@pytest.fixture(params=["pairs", "single"])
+def split_form(request):
+    """Run a split-GEMM test with CTA pairs (the default form for M > 128) and with one CTA
+    per tile, restoring the library's setting afterwards."""
+    lib = _lib.load()
+    prev = lib.afq_test_split_pairs(1 if request.param == "pairs" else 0)
+    yield request.param
+    lib.afq_test_split_pairs(prev)
+
+
 @pytest.mark.parametrize("M,N,K", SPLIT_SHAPES)
 @pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
 @pytest.mark.parametrize("terms", ["hi", "hi+alo", "all"])
 @pytest.mark.parametrize("drain", [0, 1, 2])
-def test_split_gemm_matches_fp32(M, N, K, dtype, terms, drain):
-    """Persistent split GEMM: A_hi B_hi^T (+ A_lo B_hi^T) (+ A_hi B_lo^T) against torch FP32."""
+def test_split_gemm_matches_fp32(M, N, K, dtype, terms, drain, split_form):
+    """Persistent split GEMM: A_hi B_hi^T (+ A_lo B_hi^T) (+ A_hi B_lo^T) against torch FP32,
+    on CTA pairs (odd M tile counts included: 300 rows) and on single CTAs."""
     g = torch.Generator(device="cuda").manual_seed(M + 3 * N + K)
     lda = (K + 7) // 8 * 8
     ah = torch.randn(M, lda, device="cuda", generator=g).to(dtype)
@@ -76,7 +87,7 @@ def test_split_gemm_matches_fp32(M, N, K, dtype, terms, drain):
 
 
 @pytest.mark.parametrize("drain", [0, 1, 2])
-def test_split_accumulation_bias(drain):
+def test_split_accumulation_bias(drain, split_form):
     """Drained runs of the split GEMM remove the tensor core's truncation bias (K = 2400)."""
     M, N, K = 256, 512, 2400
     g = torch.Generator(device="cuda").manual_seed(6)
