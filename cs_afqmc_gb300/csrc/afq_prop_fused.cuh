@@ -9,7 +9,7 @@
 //   A (in tensor memory, row p in lane p, K packed two per column): E - I [128][nq] (loaded
 //     once), Vr and Vi [128][nq] of the current walker. Keeping A in TMEM leaves the tensor
 //     core only the small B operand to read from shared memory per instruction.
-//   B (shared memory, K-major, 128-byte swizzle): [NT rows][nq] written by the epilogue
+//   B (shared memory, K-major, 128-byte swizzle): [2 NT rows][nq] written by the epilogue
 //     threads, row 2k + c = part c (re / im) of column k of the current term, K = orbital q.
 // The complex product V T is two real products, D0 = Vr B and D1 = Vi B, combined in the
 // epilogue: Re(VT) = D0[2k] - D1[2k+1], Im(VT) = D0[2k+1] + D1[2k]; (E - I) T is D0 alone.
@@ -23,6 +23,12 @@
 // propagated; four loader warps move it into TMEM once the current walker's last Taylor
 // products have completed, which overlaps the final exp_h1 product and the next walker's
 // first one.
+//
+// Those two exp_h1 products are independent and share the A operand (E - I), so with a
+// Taylor series (nterms > 1) they are one MMA chain of N = 2 NT: B rows 0 .. NT-1 hold this
+// walker's Taylor sum, rows NT .. 2 NT-1 the next walker's slab, and the products land in D0
+// and D1. Each output element is the same K sum as in two separate chains; per walker this
+// saves one exp_h1 chain and one epilogue round trip.
 //
 // Precision: every product accumulates its correction terms (lo * hi, hi * lo) first, then
 // hi * hi, in one FP32 accumulator over K <= 128 (two K tiles); the Taylor sum, W1 and W'
@@ -52,7 +58,7 @@ constexpr uint32_t kPropTile = 16384;  // one 128-row x 64-column 16-bit operand
 
 __host__ __device__ constexpr size_t prop_fused_smem(int nq, int NT) {
   return 1024 + (size_t)(nq / 64) * kPropTile * 4  // V staging: hi / lo, Vr and Vi tiles
-         + (size_t)(nq / 64) * NT * 128 * 2       // B hi / lo
+         + (size_t)(nq / 64) * 2 * NT * 128 * 2   // B hi / lo (2 NT rows: the merged exp_h1 chain)
          + 256;                                   // barriers, TMEM address
 }
 
@@ -69,7 +75,7 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int KQ = pd.nq / 64, kw = pd.nq / 2;
-  const uint32_t BT = (uint32_t)pd.NT * 128;  // bytes per B K tile
+  const uint32_t BT = (uint32_t)pd.NT * 2 * 128;  // bytes per B K tile (2 NT rows)
   unsigned char* Sv = smem;                   // staging: [plane][part][kt] tiles
   unsigned char* Bh = Sv + 4 * KQ * kPropTile;
   unsigned char* Bl = Bh + KQ * BT;
@@ -89,6 +95,7 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
   constexpr int kLoad = 4 * NP, kCtrl = 4 * NP + 4;  // loader warps, control warp
   const bool bf = pd.bf16 != 0;
   const bool need_v = pd.nterms > 1;
+  const bool merge = need_v;  // final exp_h1 chain of a walker merged with the next walker's first
   const bool v_lo = pd.split > 0;
   const int nsteps = pd.nterms + 1;  // exp_h1, nterms - 1 Taylor products, exp_h1
   // V_lo is last used by Taylor product `split`: when that is not the last product, the next
@@ -120,7 +127,8 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
   if (warp == kCtrl) {
     if (lane == 0) {
       const uint32_t sBh = ptx::smem_u32(Bh), sBl = ptx::smem_u32(Bl);
-      const uint32_t idesc = ptx::idesc_f16(128, NT, bf ? 1 : 0);
+      const uint32_t idesc1 = ptx::idesc_f16(128, NT, bf ? 1 : 0), idesc2 = ptx::idesc_f16(128, 2 * NT, bf ? 1 : 0);
+      uint32_t idesc = idesc1;
       const uint32_t vbytes = 2 * KQ * kPropTile * (v_lo ? 2 : 1);
       auto load_v = [&](int wl) {
         ptx::mbar_expect_tx(v_bar, vbytes);
@@ -149,8 +157,11 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
       uint32_t sc = 0;  // steps issued so far (phase of ready / done)
       int it = 0;       // walkers started
       for (int wl = blockIdx.x; wl < pd.nwc && ok; wl += gridDim.x, ++it) {
-        for (int st = 0; st < nsteps && ok; ++st, ++sc) {
+        const bool has_next = wl + (int)gridDim.x < pd.nwc;
+        // after the first walker, a walker's first exp_h1 product ran in the previous one's last chain
+        for (int st = (merge && it > 0) ? 1 : 0; st < nsteps && ok; ++st, ++sc) {
           const bool expo = st == 0 || st == nsteps - 1;
+          idesc = (merge && has_next && st == nsteps - 1) ? idesc2 : idesc1;
           if (!ptx::mbar_wait(ready, sc & 1)) {
             ok = false;
             break;
@@ -302,11 +313,12 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
     const uint32_t b_row0 = (uint32_t)(kt_p * BT + 2048 * g) + ((uint32_t)(kc_p & 7) << 1);
     const uint32_t sBh_e = ptx::smem_u32(Bh) + b_row0, sBl_e = ptx::smem_u32(Bl) + b_row0;
     const int c8 = kc_p >> 3;
-    auto put = [&](const float* val, bool lo) {
+    // rows0: 0 for this walker's rows, NT for the next walker's rows of the merged exp_h1 chain
+    auto put = [&](const float* val, bool lo, int rows0) {
       if (!pk) return;
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
-        const uint32_t off = (uint32_t)(128 * r) + ((uint32_t)(c8 ^ (r & 7)) << 4);
+        const uint32_t off = (uint32_t)(128 * (rows0 + r)) + ((uint32_t)(c8 ^ (r & 7)) << 4);
         const float x = (prow && k0 + (r >> 1) < pd.o) ? val[r] : 0.f;
         uint16_t h, l;
         split16(x, bf, h, l);
@@ -333,29 +345,34 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
       }
     };
     uint32_t sc = 0;
-    float wv[16];
+    float wv[16], acc[16];
+    bool have_w1 = false;  // acc holds W1 of the walker (its first exp_h1 product ran merged)
     if (blockIdx.x < pd.nwc) load_w(blockIdx.x, wv);
     for (int wl = blockIdx.x; wl < pd.nwc && ok; wl += gridDim.x) {
-      float acc[16];
-      // ---- W1 = W + (E - I) W
-      put(wv, pd.w_lo != 0);
-      signal();
-      if (!wait_done(sc++)) {
-        ok = false;
-        break;
-      }
-      ptx::tc_fence_after();
-      {
+      const int wn = wl + gridDim.x;
+      const bool next = merge && wn < pd.nwc;
+      if (!have_w1) {
+        // ---- W1 = W + (E - I) W
+        put(wv, pd.w_lo != 0, 0);
+        signal();
+        if (!wait_done(sc++)) {
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
         float d0[16];
         ptx::tmem_ld16p(lane_base, d0);
         ptx::tmem_ld_wait();
 #pragma unroll
         for (int j = 0; j < 16; ++j) acc[j] = wv[j] + d0[j];
+        put(acc, pd.nterms > 1 ? pd.split >= 1 : pd.w_lo != 0, 0);
+        signal();
       }
-      put(acc, pd.nterms > 1 ? pd.split >= 1 : pd.w_lo != 0);
-      signal();
       // ---- T_m = V T_{m-1} / m, acc += T_m
       for (int m = 1; m < pd.nterms; ++m) {
+        // the next walker's slab rows (B rows of the merged chain), loaded while the last
+        // Taylor product runs
+        if (next && m + 1 == pd.nterms) load_w(wn, wv);
         if (!wait_done(sc++)) {
           ok = false;
           break;
@@ -374,30 +391,43 @@ __global__ void __launch_bounds__(128 * NP + 160, 1)
           acc[2 * kk] += tr;
           acc[2 * kk + 1] += ti;
         }
-        if (m + 1 < pd.nterms)
-          put(d0, m + 1 <= pd.split);
-        else
-          put(acc, pd.w_lo != 0);  // operand of the final exp_h1 product
+        if (m + 1 < pd.nterms) {
+          put(d0, m + 1 <= pd.split, 0);
+        } else {
+          put(acc, pd.w_lo != 0, 0);            // operand of the final exp_h1 product
+          if (next) put(wv, pd.w_lo != 0, NT);  // and of the next walker's first
+        }
         signal();
       }
       if (!ok) break;
-      // next walker's slab rows: loads issued before this walker's results are stored
-      const int wn = wl + gridDim.x;
-      if (wn < pd.nwc) load_w(wn, wv);
-      // ---- W' = acc + (E - I) acc
+      // without the merge: the next walker's slab rows, loaded before this walker's results are stored
+      if (!merge && wn < pd.nwc) load_w(wn, wv);
+      // ---- W' = acc + (E - I) acc (merged: and the next walker's W1 = W + (E - I) W)
       if (!wait_done(sc++)) {
         ok = false;
         break;
       }
       ptx::tc_fence_after();
-      float d0[16];
-      ptx::tmem_ld16p(lane_base, d0);
-      ptx::tmem_ld_wait();
-      if (prow) {
-        float2* dst = pd.w + ((size_t)wl * pd.n + p) * pd.o;
+      {
+        float d0[16];
+        ptx::tmem_ld16p(lane_base, d0);
+        ptx::tmem_ld_wait();
+        if (prow) {
+          float2* dst = pd.w + ((size_t)wl * pd.n + p) * pd.o;
 #pragma unroll
-        for (int kk = 0; kk < 8; ++kk)
-          if (k0 + kk < pd.o) dst[k0 + kk] = make_float2(acc[2 * kk] + d0[2 * kk], acc[2 * kk + 1] + d0[2 * kk + 1]);
+          for (int kk = 0; kk < 8; ++kk)
+            if (k0 + kk < pd.o) dst[k0 + kk] = make_float2(acc[2 * kk] + d0[2 * kk], acc[2 * kk + 1] + d0[2 * kk + 1]);
+        }
+      }
+      have_w1 = next;
+      if (next) {
+        float d1[16];
+        ptx::tmem_ld16p(lane_base + NT, d1);
+        ptx::tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j] = wv[j] + d1[j];
+        put(acc, pd.split >= 1, 0);
+        signal();
       }
     }
   }
