@@ -8,9 +8,11 @@ resident in HBM and runs the jobs concurrently:
   library's workspace size plus the Hamiltonian, walker and field buffers) fits in the
   memory budget next to the jobs already resident, and a slot is free; otherwise it waits
   in arrival order;
-* continuous batching: each job owns a CUDA stream; the loop keeps one block of every
-  active job in flight, so blocks of different jobs overlap on the device, and a job that
-  arrives while others run starts as soon as it is admitted;
+* continuous batching: each job owns a CUDA stream and, at admission, all of its blocks
+  are enqueued on it (a job's blocks are ordered on its stream, and its draws come from a
+  host-side counter, so nothing waits for the device). Blocks of different jobs overlap on
+  the device, a job that arrives while others run starts as soon as it is admitted, and
+  the host's set-up of a new job never leaves the device without queued work;
 * CUDA graphs: after its first (eager) block a job's block - propagate_phaseless plus the
   block end - is captured once and replayed; only the field and SR draws (counter-based
   Philox, so identical to an eager run) are launched outside the graph.
@@ -97,7 +99,8 @@ def footprint_bytes(spec: JobSpec) -> int:
 
 
 class _Job:
-    """One admitted job: its stream, device state, captured block graph and progress."""
+    """One admitted job: its stream, device state and captured block graph. Construction
+    sets the job up and enqueues every block and the result copy on the job's stream."""
 
     def __init__(self, spec: JobSpec, system: synthetic.SyntheticSystem, t_arrival: float,
                  use_graph: bool):
@@ -105,13 +108,22 @@ class _Job:
         self.t_admitted = time.perf_counter()
         self.stream = torch.cuda.Stream()
         self.n_blocks = max(1, spec.n_steps // spec.n_prop_steps)
-        self.done_blocks = 0
         self.graph: Optional[torch.cuda.CUDAGraph] = None
-        self.event = torch.cuda.Event()
-        self.finished_event: Optional[torch.cuda.Event] = None
         with torch.cuda.stream(self.stream):
             self._setup(system)
-            self._launch_eager()
+            for b in range(self.n_blocks):
+                self._draw()
+                if b > 0 and self.use_graph and self.graph is None:
+                    self._capture()
+                if self.graph is not None:
+                    self.graph.replay()
+                else:
+                    self._block_body()
+                self._record(b)
+            self.host_e.copy_(self.hist_e, non_blocking=True)
+            self.host_w.copy_(self.hist_w, non_blocking=True)
+            self.finished_event = torch.cuda.Event()
+            self.finished_event.record(self.stream)
 
     def _setup(self, s: synthetic.SyntheticSystem):
         sp = self.spec
@@ -164,16 +176,9 @@ class _Job:
         _lib.call("afq_block_end", self.eng.ctx, ctypes.byref(state), self.energy.data_ptr(),
                   self.zeta_global.data_ptr(), self.wsum.data_ptr(), st)
 
-    def _record(self):
-        b = self.done_blocks
+    def _record(self, b: int):
         self.hist_e[b].copy_(self.energy[0])
         self.hist_w[b].copy_(self.wsum[0])
-
-    def _launch_eager(self):
-        self._draw()
-        self._block_body()
-        self._record()
-        self.event.record(self.stream)
 
     def _capture(self):
         g = torch.cuda.CUDAGraph()
@@ -188,28 +193,6 @@ class _Job:
         except Exception:  # noqa: BLE001 - a context that cannot be captured runs eagerly
             self.graph = None
             self.use_graph = False
-
-    def advance(self) -> bool:
-        """Called when the previous block finished: launch the next block or the result
-        copy. Returns True once the job's result copy has been enqueued."""
-        self.done_blocks += 1
-        with torch.cuda.stream(self.stream):
-            if self.done_blocks >= self.n_blocks:
-                self.host_e.copy_(self.hist_e, non_blocking=True)
-                self.host_w.copy_(self.hist_w, non_blocking=True)
-                self.finished_event = torch.cuda.Event()
-                self.finished_event.record(self.stream)
-                return True
-            if self.use_graph and self.graph is None:
-                self._capture()
-            self._draw()
-            if self.graph is not None:
-                self.graph.replay()
-            else:
-                self._block_body()
-            self._record()
-            self.event.record(self.stream)
-        return False
 
     def result(self) -> JobResult:
         return JobResult(self.spec.job_id, self.spec, self.host_e.numpy().copy(), self.host_w.numpy().copy(),
@@ -238,20 +221,19 @@ class AfqmcServer:
         pending = sorted(requests, key=lambda r: r[0])
         queue: List[Tuple[float, JobSpec, synthetic.SyntheticSystem]] = []
         active: List[_Job] = []
-        finishing: List[_Job] = []
         used = 0
         held: Dict[int, int] = {}
         results: List[JobResult] = []
         t0 = time.perf_counter()
         i = 0
-        while i < len(pending) or queue or active or finishing:
+        while i < len(pending) or queue or active:
             now = time.perf_counter() - t0
             while i < len(pending) and pending[i][0] <= now:
                 off, spec, payload = pending[i]
                 queue.append((t0 + off, spec, payload))
                 i += 1
             # admission in arrival order by footprint
-            while queue and len(active) + len(finishing) < self.max_active:
+            while queue and len(active) < self.max_active:
                 t_arr, spec, payload = queue[0]
                 need = footprint_bytes(spec)
                 if need > self.budget:
@@ -262,18 +244,12 @@ class AfqmcServer:
                 active.append(_Job(spec, payload, t_arr, self.use_graphs))
                 held[spec.job_id] = need
                 used += need
-            # progress: every active job whose block finished gets its next block
+            # completions: a job's blocks and result copy were enqueued at admission
             progressed = False
             for job in list(active):
-                if job.event.query():
-                    progressed = True
-                    if job.advance():
-                        active.remove(job)
-                        finishing.append(job)
-            for job in list(finishing):
                 if job.finished_event.query():
                     progressed = True
-                    finishing.remove(job)
+                    active.remove(job)
                     results.append(job.result())
                     used -= held.pop(job.spec.job_id)
                     del job
