@@ -991,67 +991,78 @@ struct EpiExp {
 };
 
 // ======================================================================================
-// Exchange epilogue. D[(i,q)][(w, re/im)] = Z_w[(i,q)] = sum_(k,p) U[(i,q),(k,p)] G_w[k,p] with
+// Exchange epilogue of the split GEMM, on the transposed product D = G U (U symmetric):
+// D[(w, re/im)][(i,q)] = Z_w[(i,q)] = sum_(k,p) U[(i,q),(k,p)] G_w[k,p] with
 // U[(i,q),(k,p)] = sum_g rot_chol_g[i,p] rot_chol_g[k,q], so that the exchange sum of
 // wavefunctions.py:539 (and 737-738), exc = sum_g sum_ik f_g[i,k] f_g[k,i] with
-// f_g = rot_chol_g G^T, equals sum_(i,q) Z_w[(i,q)] G_w[i,q]. Writes the tile's partial sum
-// of exc per walker (rows of the tile summed), unscaled.
+// f_g = rot_chol_g G^T, equals sum_(i,q) Z_w[(i,q)] G_w[i,q]. A thread holds row (w, part)
+// of D over 128 consecutive (i,q): it reads the same 128 entries of G_w's re and im rows
+// (contiguous 16-byte loads, hi + lo) and forms Z_part . G_re and Z_part . G_im; the
+// neighbouring lane (the other part of the same walker) completes the complex product. The
+// walker's partial of exc for these 128 columns and this K range goes, scaled, to slot
+// ks * n128 + col0 / 128 of its row of partials: exc is linear in Z, so K-split partials
+// need no separate reduction, and the final energy kernel sums the slots in a fixed order.
 // ======================================================================================
 
-struct EpiExc {
+struct EpiExcSplit {
+  static constexpr bool kWarpStore = true;
   struct Params {
     const uint16_t* g_hi;  // [2 nw][ldk] Green operand (rows 2w, 2w+1 = re, im)
     const uint16_t* g_lo;
     const float* g_inv;    // [nw]
     float u_inv;
-    int kb, ldk, nw, mt, bf16;
-    double2* exc_part;     // [nw][mt]
+    int kb, ldk, nw, bf16;
+    int n128, slots;       // 128-column groups of kb; partial slots per walker (K splits * n128)
+    double2* exc_part;     // [nw][slots]
   };
-  static constexpr int kSmemBytes = 4 * 128 * 8;
-  __device__ static void run(const Params& p, int m0, int n0, int bn, uint32_t tmem, int q, int lane,
-                             unsigned char* smem, bool) {
-    float2* part = reinterpret_cast<float2*>(smem);  // [4][128]
-    const int r = m0 + q * 32 + lane;
-    const bool rv = r < p.kb;
-    const bool bf = p.bf16 != 0;
-#pragma unroll 1
-    for (int c0 = 0; c0 < bn; c0 += 16) {
-      float v[16];
-      ptx::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + c0, v);
-      ptx::tmem_ld_wait();
+  __device__ __forceinline__ static void store_warp(const Params& p, int row0, int lane, int col0, const float* v,
+                                                    int ks, unsigned char*) {
+    if (row0 >= 2 * p.nw || col0 >= p.kb) return;  // warp-uniform: padding rows / columns of the last tiles
+    const int R = row0 + lane, w = R >> 1;
+    const bool rv = R < 2 * p.nw, bf = p.bf16 != 0;
+    // Z_part . G_re and Z_part . G_im: 8-column chunk sums added with Kahan compensation
+    float a_re = 0.f, a_im = 0.f, k_re = 0.f, k_im = 0.f;
+    if (rv) {
+      const uint16_t* gr_h = p.g_hi + (size_t)(2 * w) * p.ldk;
+      const uint16_t* gr_l = p.g_lo + (size_t)(2 * w) * p.ldk;
+      const uint16_t* gi_h = gr_h + p.ldk;
+      const uint16_t* gi_l = gr_l + p.ldk;
 #pragma unroll
-      for (int jj = 0; jj < 8; ++jj) {
-        const int w = (n0 + c0) / 2 + jj;
-        float px = 0.f, py = 0.f;
-        if (rv && w < p.nw) {
-          const size_t ir = (size_t)(2 * w) * p.ldk + r, ii = ir + p.ldk;
-          const float gr = h2f(p.g_hi[ir], bf) + h2f(p.g_lo[ir], bf);
-          const float gi = h2f(p.g_hi[ii], bf) + h2f(p.g_lo[ii], bf);
-          const float zr = v[2 * jj], zi = v[2 * jj + 1];
-          px = zr * gr - zi * gi;
-          py = zr * gi + zi * gr;
-        }
+      for (int c8 = 0; c8 < 128; c8 += 8) {
+        const int c = col0 + c8;
+        if (c < p.kb) {  // 8 columns at a time (c + 8 <= ldk: rows padded to multiples of 8)
+          const uint4 rh = *reinterpret_cast<const uint4*>(gr_h + c), rl = *reinterpret_cast<const uint4*>(gr_l + c);
+          const uint4 ih = *reinterpret_cast<const uint4*>(gi_h + c), il = *reinterpret_cast<const uint4*>(gi_l + c);
+          const uint32_t rhw[4] = {rh.x, rh.y, rh.z, rh.w}, rlw[4] = {rl.x, rl.y, rl.z, rl.w};
+          const uint32_t ihw[4] = {ih.x, ih.y, ih.z, ih.w}, ilw[4] = {il.x, il.y, il.z, il.w};
+          float s_re = 0.f, s_im = 0.f;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          px += __shfl_xor_sync(0xffffffffu, px, off);
-          py += __shfl_xor_sync(0xffffffffu, py, off);
+          for (int e = 0; e < 8; ++e) {
+            const int sh = 16 * (e & 1);
+            const float gre = h2f((uint16_t)(rhw[e >> 1] >> sh), bf) + h2f((uint16_t)(rlw[e >> 1] >> sh), bf);
+            const float gim = h2f((uint16_t)(ihw[e >> 1] >> sh), bf) + h2f((uint16_t)(ilw[e >> 1] >> sh), bf);
+            if (c + e < p.kb) {  // the row's padding columns are never written
+              s_re = fmaf(v[c8 + e], gre, s_re);
+              s_im = fmaf(v[c8 + e], gim, s_im);
+            }
+          }
+          const float y_re = s_re - k_re, t_re = a_re + y_re;
+          k_re = (t_re - a_re) - y_re;
+          a_re = t_re;
+          const float y_im = s_im - k_im, t_im = a_im + y_im;
+          k_im = (t_im - a_im) - y_im;
+          a_im = t_im;
         }
-        if (lane == 0) part[q * 128 + c0 / 2 + jj] = make_float2(px, py);
       }
+      a_re -= k_re;
+      a_im -= k_im;
     }
-    ptx::named_bar_sync(1, 128);
-    const int t = q * 32 + lane;
-    if (t < bn / 2) {
-      const int w = n0 / 2 + t;
-      if (w < p.nw) {
-        double sx = 0.0, sy = 0.0;
-        for (int qq = 0; qq < 4; ++qq) {
-          sx += part[qq * 128 + t].x;
-          sy += part[qq * 128 + t].y;
-        }
-        const double s = (double)p.g_inv[w] * (double)p.g_inv[w] * (double)p.u_inv;
-        p.exc_part[(size_t)w * p.mt + m0 / 128] = c2(sx * s, sy * s);
-      }
+    // lane 2k: Z_re . G (part 0), lane 2k + 1: Z_im . G (part 1)
+    const float o_re = __shfl_xor_sync(0xffffffffu, a_re, 1), o_im = __shfl_xor_sync(0xffffffffu, a_im, 1);
+    if (rv && (R & 1) == 0) {
+      const double sc = (double)p.g_inv[w] * (double)p.g_inv[w] * (double)p.u_inv;
+      const double ex = (double)a_re - (double)o_im, ey = (double)a_im + (double)o_re;
+      p.exc_part[(size_t)w * p.slots + ks * p.n128 + col0 / 128] = c2(ex * sc, ey * sc);
     }
   }
 };

@@ -153,6 +153,25 @@ static int launch_split(int cls, const SplitMaps& maps, SplitArgs g, int num_sms
   return launch_check("gemm_split");
 }
 
+// K splits of a split GEMM over m_tiles x n_tiles output tiles (128 x 256) and k_tiles K
+// tiles: the count minimising (tile rounds) x (K tiles per split) over the CTAs, or CTA
+// pairs when the launch takes that form; ties go to fewer partials
+static int choose_ksplit(int m_tiles, int n_tiles, int k_tiles, int sms) {
+  const bool pairs = g_split_pairs && m_tiles >= 2;
+  const int workers = pairs ? sms / 2 : sms, units = (pairs ? (m_tiles + 1) / 2 : m_tiles) * n_tiles;
+  int best = 1;
+  long best_cost = -1;
+  for (int ks = 1; ks <= (k_tiles / 4 > 1 ? k_tiles / 4 : 1); ++ks) {
+    const long rounds = ((long)units * ks + workers - 1) / workers;
+    const long cost = rounds * ((k_tiles + ks - 1) / ks);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = ks;
+    }
+  }
+  return best;
+}
+
 // ======================================================================================
 // Taylor kernel (propagation.py:76-90): per walker slab, T_0 = W1 (B operand from the
 // first exp_h1 product), T_m = V T_{m-1} / m on the tensor cores with V = [Vr | Vi] held in
@@ -847,7 +866,6 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
     t.o_blk[b] = c.gocc[b];
     t.kb[b] = t.o_blk[b] * t.n;
     t.ldkb[b] = rup(t.kb[b], 8);
-    t.mt_z[b] = (t.kb[b] + 127) / 128;
     const size_t ub = (size_t)t.kb[b] * t.ldkb[b];
     if (ub > umax) umax = ub;
   }
@@ -870,20 +888,11 @@ int make_plan(const afq_ctx_dev& c, int nwc, int32_t cfg, Plan* P) {
     cudaGetLastError();  // a host without a device leaves an error behind
     const int mt2 = (2 * c.nw + 127) / 128, nt2 = (c.nchol + kSplitBN - 1) / kSplitBN;
     const int kt = (t.kfb + 63) / 64;
-    const bool pairs = g_split_pairs && mt2 >= 2;  // the launch's form (CTA pairs share an M tile pair)
-    const int workers = pairs ? sms / 2 : sms, units = (pairs ? (mt2 + 1) / 2 : mt2) * nt2;
-    // K splits minimising (tile rounds) x (K tiles per split); ties to fewer partials
-    int best = 1;
-    long best_cost = -1;
-    for (int ks = 1; ks <= (kt / 4 > 1 ? kt / 4 : 1); ++ks) {
-      const long rounds = ((long)units * ks + workers - 1) / workers;
-      const long cost = rounds * ((kt + ks - 1) / ks);
-      if (best_cost < 0 || cost < best_cost) {
-        best_cost = cost;
-        best = ks;
-      }
+    t.fb_ks = choose_ksplit(mt2, nt2, kt, sms);
+    for (int b = 0; b < t.nblk; ++b) {  // exchange: Z = U . G on the split GEMM, K-split partials of exc
+      t.z_ks[b] = choose_ksplit(mt2, (t.kb[b] + kSplitBN - 1) / kSplitBN, (t.kb[b] + 63) / 64, sms);
+      t.mt_z[b] = t.z_ks[b] * ((t.kb[b] + 127) / 128);
     }
-    t.fb_ks = best;
     t.fb_npad = nt2 * kSplitBN;
   }
   t.n_fb_terms = 1 + ((cfg & kFbDyn) ? 1 : 0) + ((cfg & kFbStat) ? 1 : 0);
@@ -1195,20 +1204,12 @@ int tc_init(TcState* out, const afq_ctx_dev& c, const afq_hamiltonian& h, const 
         TC_CHECK(mk(&t.m_c[b].b[i++], t.rc_blk[b][1], c.nchol, t.kb[b], t.ldkb[b], t.fb_bn));
       }
     }
-    // exchange: Z = U_b . G_b (A = U, B = Green operand)
-    {
-      int i = 0;
-      TC_CHECK(mk(&t.m_z[b].a[i], t.u[b][0], t.kb[b], t.kb[b], t.ldkb[b], 128));
-      TC_CHECK(mk(&t.m_z[b].b[i++], t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
-      if (t.cfg & kEneDyn) {
-        TC_CHECK(mk(&t.m_z[b].a[i], t.u[b][0], t.kb[b], t.kb[b], t.ldkb[b], 128));
-        TC_CHECK(mk(&t.m_z[b].b[i++], t.g_blk[b][1], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
-      }
-      if (t.cfg & kEneStat) {
-        TC_CHECK(mk(&t.m_z[b].a[i], t.u[b][1], t.kb[b], t.kb[b], t.ldkb[b], 128));
-        TC_CHECK(mk(&t.m_z[b].b[i++], t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
-      }
-    }
+    // exchange: Z^T = G_b . U_b (U symmetric) on the split GEMM (A = Green operand planes, B = U planes)
+    memset(&t.m_zs[b], 0, sizeof(SplitMaps));
+    TC_CHECK(mk(&t.m_zs[b].a_hi, t.g_blk[b][0], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+    if (t.cfg & kEneDyn) TC_CHECK(mk(&t.m_zs[b].a_lo, t.g_blk[b][1], 2 * t.nw, t.kb[b], t.ldkb[b], 128));
+    TC_CHECK(mk(&t.m_zs[b].b_hi, t.u[b][0], t.kb[b], t.kb[b], t.ldkb[b], kSplitBBox));
+    if (t.cfg & kEneStat) TC_CHECK(mk(&t.m_zs[b].b_lo, t.u[b][1], t.kb[b], t.kb[b], t.ldkb[b], kSplitBBox));
   }
   t.ready = 1;
   *out = t;
@@ -1571,7 +1572,7 @@ int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
     else
       TC_CHECK(fb_gemm(t, c, nullptr, t.c_out + (size_t)b * t.nw * c.nchol, st, &t.m_c[b], t.rc_blk_inv[b], 1.0f,
                        t.kb[b]));
-    EpiExc::Params ep;
+    EpiExcSplit::Params ep;
     ep.g_hi = t.g_blk[b][0];
     ep.g_lo = t.g_blk[b][1];
     ep.g_inv = t.g_inv;
@@ -1579,12 +1580,21 @@ int tc_energy(TcState& t, const afq_ctx_dev& c, double2* out, cudaStream_t st) {
     ep.kb = t.kb[b];
     ep.ldk = t.ldkb[b];
     ep.nw = t.nw;
-    ep.mt = t.mt_z[b];
     ep.bf16 = t.bf16 ? 1 : 0;
+    ep.n128 = (t.kb[b] + 127) / 128;
+    ep.slots = t.mt_z[b];
     ep.exc_part = t.exc_part + (b == 0 ? 0 : (size_t)t.nw * t.mt_z[0]);
-    const int kt = (t.kb[b] + 63) / 64, nt = (2 * t.nw + 127) / 128;
-    TC_CHECK((launch_gemm<128, 4, EpiExc>(K_ENERGY, t.m_z[b], t.n_en_terms, kt, t.mt_z[b], nt, 128, t.bf16, ep,
-                                         t.status, st, 0, t.drain)));
+    SplitArgs sa;
+    sa.m_tiles = (2 * t.nw + 127) / 128;
+    sa.n_tiles = (t.kb[b] + kSplitBN - 1) / kSplitBN;
+    sa.k_tiles = (t.kb[b] + 63) / 64;
+    sa.k_splits = t.z_ks[b];
+    sa.a_row0 = 0;
+    sa.has_alo = (t.cfg & kEneDyn) ? 1 : 0;   // G_lo * U_hi
+    sa.has_blo = (t.cfg & kEneStat) ? 1 : 0;  // G_hi * U_lo
+    sa.drain = t.drain > 0 ? t.drain : sa.k_tiles;
+    sa.idesc = ptx::idesc_f16(128, kSplitBN, t.bf16 ? 1 : 0);
+    TC_CHECK(launch_split<EpiExcSplit>(K_ENERGY, t.m_zs[b], sa, t.num_sms, ep, t.status, st));
   }
   {
     ProfScope _ps(K_ENERGY_FIN, st);

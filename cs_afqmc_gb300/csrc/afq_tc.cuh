@@ -81,7 +81,8 @@ struct TcState {
   int nw, nwc;
   int nslab, nblk;          // walker slabs, Green blocks
   int o_slab[2], R[2], wpt[2], bn_w[2], NT[2];
-  int o_blk[2], kb[2], ldkb[2], mt_z[2];
+  int o_blk[2], kb[2], ldkb[2], mt_z[2];  // mt_z: exchange partial slots per walker (K splits x 32-row groups)
+  int z_ks[2];                              // exchange GEMM K splits per spin block
   int fb_bn, fb_ntiles;
   int fb_ks, fb_npad;       // force bias on the split GEMM: K splits, padded N of the partials
   float* fb_part;           // [fb_ks][2 nw][fb_npad] K-split partials of the force bias
@@ -106,7 +107,8 @@ struct TcState {
                             // non-diagonal Cholesky vector under kDiagChol (4)
   float* dchol;             // kDiagChol: [nchol][n] diagonals of the Cholesky vectors
   // tensor maps
-  GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2], m_z[2];
+  GemmMaps m_fb, m_vhs, m_e1[2], m_e2[2], m_c[2];
+  SplitMaps m_zs[2];  // exchange: A = U planes, B = Green operand planes
   CUtensorMap m_vt[2][2];   // Taylor: vbuf hi/lo (unused index for slab)
   CUtensorMap m_t0[2][2];   // Taylor: t0[s] hi/lo
   bool fused;               // fused propagation kernel (norb <= 128, <= 32 orbitals per slab)
