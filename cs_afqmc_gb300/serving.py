@@ -8,7 +8,8 @@ resident in HBM and runs the jobs concurrently:
   library's workspace size plus the Hamiltonian, walker and field buffers) fits in the
   memory budget next to the jobs already resident, and a slot is free; otherwise it waits
   in arrival order;
-* continuous batching: each job owns a CUDA stream and, at admission, all of its blocks
+* continuous batching: each job owns a CUDA stream (one per server slot, created with the
+  server, so that no two resident jobs share a stream) and, at admission, all of its blocks
   are enqueued on it (a job's blocks are ordered on its stream, and its draws come from a
   host-side counter, so nothing waits for the device). Blocks of different jobs overlap on
   the device, a job that arrives while others run starts as soon as it is admitted, and
@@ -103,10 +104,10 @@ class _Job:
     sets the job up and enqueues every block and the result copy on the job's stream."""
 
     def __init__(self, spec: JobSpec, system: synthetic.SyntheticSystem, t_arrival: float,
-                 use_graph: bool):
+                 use_graph: bool, stream: torch.cuda.Stream):
         self.spec, self.t_arrival, self.use_graph = spec, t_arrival, use_graph
         self.t_admitted = time.perf_counter()
-        self.stream = torch.cuda.Stream()
+        self.stream = stream
         self.n_blocks = max(1, spec.n_steps // spec.n_prop_steps)
         self.graph: Optional[torch.cuda.CUDAGraph] = None
         with torch.cuda.stream(self.stream):
@@ -203,12 +204,19 @@ class AfqmcServer:
     """Continuous-batching server for independent jobs on the current GPU.
 
     hbm_budget: bytes the resident jobs may hold (default: 85 % of the free memory at
-    construction). max_active: most jobs resident at once."""
+    construction). max_active: most jobs resident at once (at most 32: one stream per slot
+    from PyTorch's per-device pool of 32, taken in a row so that they are distinct)."""
 
     def __init__(self, hbm_budget: Optional[int] = None, max_active: int = 16, use_graphs: bool = True):
         if not torch.cuda.is_available():
             raise _lib.AfqError("the serving loop needs a CUDA device")
+        if not 1 <= max_active <= 32:
+            raise _lib.AfqError("max_active must be in [1, 32]")
         _lib.load()
+        # a job's blocks are all enqueued at admission: resident jobs must not share a stream
+        self.streams = [torch.cuda.Stream() for _ in range(max_active)]
+        if len({st.cuda_stream for st in self.streams}) != max_active:
+            raise _lib.AfqError("could not obtain distinct CUDA streams for the serving slots")
         free, _ = torch.cuda.mem_get_info()
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
         self.max_active = max_active
@@ -221,6 +229,7 @@ class AfqmcServer:
         pending = sorted(requests, key=lambda r: r[0])
         queue: List[Tuple[float, JobSpec, synthetic.SyntheticSystem]] = []
         active: List[_Job] = []
+        free_streams = list(self.streams)
         used = 0
         held: Dict[int, int] = {}
         results: List[JobResult] = []
@@ -241,7 +250,7 @@ class AfqmcServer:
                 if used + need > self.budget:
                     break
                 queue.pop(0)
-                active.append(_Job(spec, payload, t_arr, self.use_graphs))
+                active.append(_Job(spec, payload, t_arr, self.use_graphs, free_streams.pop()))
                 held[spec.job_id] = need
                 used += need
             # completions: a job's blocks and result copy were enqueued at admission
@@ -252,6 +261,7 @@ class AfqmcServer:
                     active.remove(job)
                     results.append(job.result())
                     used -= held.pop(job.spec.job_id)
+                    free_streams.append(job.stream)
                     del job
             if not progressed:
                 time.sleep(poll_s)
