@@ -156,6 +156,31 @@ def flops_per_launch(cls: str, w: dict, n_batch: int) -> float:
     return table.get(cls, 0.0)
 
 
+def flops_per_walker_step(w: dict, meas_every: int) -> dict:
+    """Dense algorithmic work (real flops) of one walker through one propagation step, with
+    the measurement (QR, overlap, Green's function, local energy) amortised over the
+    `meas_every` steps between measurements:
+      step = 4 G n^2 (vhs) + 40 n^2 Nc (five Taylor products) + 8 n^2 Nc (two exp_h1
+             products) + sum over spins [12 n m^2 + 8 m^3 (Green) + 4 G m n (force bias)
+             + 4 n m^2 + 8 m^3 / 3 (overlap)]
+      measurement = sum over spins [12 n m^2 + 8 m^3 + 4 G n m^2 + 8 G m^2 (Coulomb and
+             exchange) + 8 n m^2 - 8 m^3 / 3]
+    with n orbitals, G vectors, m electrons of a spin and Nc the walker columns (one spin
+    for restricted walkers, both for two-slab walkers), the dense formulas whatever the
+    structure of the vectors (diagonal or symmetric)."""
+    n, G = w["norb"], w["nchol"]
+    two = w.get("kind", "rhf") == "uhf"
+    spins = [w["nelec"][0], w["nelec"][1]] if two else [w["nelec"][0]]
+    nc = sum(spins)
+    step = 4.0 * G * n * n + 40.0 * n * n * nc + 8.0 * n * n * nc
+    meas = 0.0
+    for m in spins:
+        step += 12.0 * n * m * m + 8.0 * m ** 3 + 4.0 * G * m * n + 4.0 * n * m * m + 8.0 * m ** 3 / 3
+        meas += 12.0 * n * m * m + 8.0 * m ** 3 + 4.0 * G * n * m * m + 8.0 * G * m * m + 8.0 * n * m * m \
+            - 8.0 * m ** 3 / 3
+    return {"step": step, "measurement": meas, "per_walker_step": step + meas / meas_every}
+
+
 def bytes_per_launch(cls: str, w: dict, n_batch: int) -> float:
     """Algorithmic HBM bytes per launch of the memory/latency-bound kernels (mixed path):
     green = the fused Green's-function kernel as the propagation chain calls it (walker slabs
@@ -564,6 +589,17 @@ def run_ours(args, rank, world, local):
                 "note": "small per-walker linear algebra (S, Gauss-Jordan, G): latency-bound, "
                         "HBM is the bound it is measured against"}
 
+    # ---- whole-step roofline: dense work per walker-step at the measured rate ----
+    fw = flops_per_walker_step(w, N_PROP)
+    step_peak = peaks["bf16_tflops"] if args.precision == "mixed" else 1.04
+    step_ach = fw["per_walker_step"] * value / 1e12
+    step_roof = {"flops_per_walker_step": round(fw["per_walker_step"]),
+                 "flops_per_step_part": round(fw["step"]), "flops_per_measurement": round(fw["measurement"]),
+                 "measurement_every_steps": N_PROP, "achieved": round(step_ach, 2), "peak": step_peak,
+                 "unit": "TFLOP/s", "frac": round(step_ach / step_peak, 4),
+                 "note": "dense formulas (vhs, Taylor, exp_h1, force bias, Green, overlap per step; "
+                         "Coulomb and exchange per measurement), flops x walker-steps/s"}
+
     # ---- CPU baseline (FP64 oracle, one process per core) ----
     cpu = None
     if cpu_pool is not None:
@@ -603,7 +639,7 @@ def run_ours(args, rank, world, local):
         "data": "synthetic",
         "config": bench_config(w, args, world),
         "precision": args.precision, "last_block_energy": block_energy,
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "roofline": roof, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
         "clocks": clocks, "kernels": kernels,
         "kernels_timing": ("second pass of the same steps with a CUDA-event pair around every launch on "
                            "its stream (value above is timed without them)"),
